@@ -1,0 +1,219 @@
+"""Test infrastructure only: ctypes driver of the reference's own C++ ERT
+modelling code (oracle/_ref/libgimli_ref.so, built by oracle/Makefile from
+the reference sources with the project's entry shim oracle/ref_shim.cpp).
+
+The reference normally factors each system matrix with CHOLMOD
+(core/src/bert/dcfemmodelling.cpp:2199-2210), which is not available here.
+``RefModelling`` injects an FP64 sparse LU (scipy SuperLU, partial pivoting
+off-diagonal threshold 0 so the symmetric matrix is factored like a
+Cholesky) through the reference's own solver hook
+(core/src/bert/dcfemmodelling.h:266 setSolver).  Each captured system matrix
+is kept so tests can compare the assembled CSR with the product's.
+
+Only tests and the fixture generator use this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_ref", "libgimli_ref.so")
+
+_FACTOR = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                           ctypes.c_void_p, ctypes.c_void_p)
+_SOLVE = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p)
+
+_lib = None
+
+
+def available():
+    return os.path.exists(LIB_PATH)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = ctypes.CDLL(LIB_PATH)
+        vp = ctypes.c_void_p
+        L.ref_create.restype = vp
+        L.ref_create.argtypes = [ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int, vp, vp,
+                                 ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, vp, ctypes.c_int, vp,
+                                 vp, ctypes.c_int]
+        L.ref_destroy.argtypes = [vp]
+        L.ref_last_error.restype = ctypes.c_char_p
+        L.ref_set_solver.argtypes = [vp, _FACTOR, _SOLVE]
+        L.ref_set_threads.argtypes = [vp, ctypes.c_int]
+        L.ref_set_kw.argtypes = [vp, ctypes.c_int, vp, vp]
+        L.ref_kw_count.argtypes = [vp]
+        L.ref_get_kw.argtypes = [vp, vp, vp]
+        L.ref_electrode_nodes.argtypes = [vp, vp]
+        L.ref_geometric_factors.argtypes = [vp, vp]
+        L.ref_response.argtypes = [vp, vp, ctypes.c_int, vp]
+        L.ref_subpot_shape.argtypes = [vp, vp, vp]
+        L.ref_subpotentials.argtypes = [vp, vp]
+        L.ref_jacobian.argtypes = [vp, vp, ctypes.c_int, vp, vp, vp]
+        L.ref_assemble.argtypes = [vp, vp, ctypes.c_double, vp, vp, vp, vp, vp, vp]
+        L.ref_primary.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, vp]
+        L.ref_besselK0.restype = ctypes.c_double
+        L.ref_besselK0.argtypes = [ctypes.c_double]
+        L.ref_besselK1.restype = ctypes.c_double
+        L.ref_besselK1.argtypes = [ctypes.c_double]
+        L.ref_gauss_legendre.argtypes = [ctypes.c_int, vp, vp]
+        L.ref_gauss_laguerre.argtypes = [ctypes.c_int, vp, vp]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _check(rc):
+    if rc != 0:
+        raise RuntimeError("reference call failed: " + lib().ref_last_error().decode())
+
+
+class RefModelling:
+    """The reference's DCSRMultiElectrodeModelling on a given mesh/scheme."""
+
+    def __init__(self, mesh, sensors, abmn, kfac=None, threads=1, keep_matrices=False):
+        L = lib()
+        self.mesh = mesh
+        self._keep = [np.ascontiguousarray(mesh.nodes, np.float64),
+                      np.ascontiguousarray(mesh.node_markers, np.int32),
+                      np.ascontiguousarray(mesh.cells, np.int32),
+                      np.ascontiguousarray(mesh.cell_markers, np.int32),
+                      np.ascontiguousarray(mesh.boundaries, np.int32),
+                      np.ascontiguousarray(mesh.boundary_markers, np.int32),
+                      np.ascontiguousarray(sensors, np.float64).reshape(-1, 3),
+                      np.ascontiguousarray(abmn, np.int32).reshape(-1, 4)]
+        kf = None if kfac is None else np.ascontiguousarray(kfac, np.float64)
+        self._keep.append(kf)
+        nodes, nm, cells, cm, bnd, bm, sens, ab = self._keep[:8]
+        self.nData = len(ab)
+        self.nE = len(sens)
+        h = L.ref_create(mesh.dim(), len(nodes), _p(nodes), _p(nm), len(cells), cells.shape[1], _p(cells),
+                         _p(cm), len(bnd), bnd.shape[1], _p(bnd), _p(bm), len(sens), _p(sens), len(ab),
+                         _p(ab), None if kf is None else _p(kf), 0)
+        if not h:
+            raise RuntimeError("ref_create failed: " + L.ref_last_error().decode())
+        self.h = h
+        self.keep_matrices = keep_matrices
+        self.matrices = []
+        self._lu = None
+
+        def factor(n, nnz, rowptr, colidx, vals):
+            try:
+                rp = np.ctypeslib.as_array(ctypes.cast(rowptr, ctypes.POINTER(ctypes.c_int)), (n + 1,)).copy()
+                ci = np.ctypeslib.as_array(ctypes.cast(colidx, ctypes.POINTER(ctypes.c_int)), (nnz,)).copy()
+                va = np.ctypeslib.as_array(ctypes.cast(vals, ctypes.POINTER(ctypes.c_double)), (nnz,)).copy()
+                A = sp.csr_matrix((va, ci, rp), shape=(n, n))
+                if self.keep_matrices:
+                    self.matrices.append((rp, ci, va))
+                self._lu = spla.splu(A.tocsc(), permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=0.0)
+                return 0
+            except Exception:  # pragma: no cover - reported through the C layer
+                return 1
+
+        def solve(n, rhs, x):
+            try:
+                b = np.ctypeslib.as_array(ctypes.cast(rhs, ctypes.POINTER(ctypes.c_double)), (n,))
+                out = np.ctypeslib.as_array(ctypes.cast(x, ctypes.POINTER(ctypes.c_double)), (n,))
+                out[:] = self._lu.solve(np.array(b))
+                return 0
+            except Exception:  # pragma: no cover
+                return 1
+
+        self._cb = (_FACTOR(factor), _SOLVE(solve))
+        _check(L.ref_set_solver(h, self._cb[0], self._cb[1]))
+        _check(L.ref_set_threads(h, int(threads)))
+
+    def close(self):
+        if self.h:
+            lib().ref_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_kw(self, k, w):
+        k = np.ascontiguousarray(k, np.float64)
+        w = np.ascontiguousarray(w, np.float64)
+        _check(lib().ref_set_kw(self.h, len(k), _p(k), _p(w)))
+
+    def kw(self):
+        n = lib().ref_kw_count(self.h)
+        k = np.zeros(n)
+        w = np.zeros(n)
+        _check(lib().ref_get_kw(self.h, _p(k), _p(w)))
+        return k, w
+
+    def electrode_nodes(self):
+        out = np.zeros(self.nE, np.int32)
+        _check(lib().ref_electrode_nodes(self.h, _p(out)))
+        return out
+
+    def geometric_factors(self):
+        out = np.zeros(self.nData)
+        _check(lib().ref_geometric_factors(self.h, _p(out)))
+        return out
+
+    def response(self, model):
+        m = np.ascontiguousarray(model, np.float64)
+        out = np.zeros(self.nData)
+        self.matrices = []
+        _check(lib().ref_response(self.h, _p(m), len(m), _p(out)))
+        return out
+
+    def subpotentials(self):
+        r = ctypes.c_int()
+        c = ctypes.c_int()
+        lib().ref_subpot_shape(self.h, ctypes.byref(r), ctypes.byref(c))
+        out = np.zeros((r.value, c.value))
+        _check(lib().ref_subpotentials(self.h, _p(out)))
+        return out
+
+    def jacobian(self, model):
+        m = np.ascontiguousarray(model, np.float64)
+        r = ctypes.c_int()
+        c = ctypes.c_int()
+        _check(lib().ref_jacobian(self.h, _p(m), len(m), None, ctypes.byref(r), ctypes.byref(c)))
+        J = np.zeros((r.value, c.value))
+        _check(lib().ref_jacobian(self.h, _p(m), len(m), _p(J), ctypes.byref(r), ctypes.byref(c)))
+        return J
+
+    def assemble(self, rho_cell, k, src_center):
+        """System matrix as the SR calculateK builds it (CSR tuple)."""
+        rho = np.ascontiguousarray(rho_cell, np.float64)
+        sc = np.ascontiguousarray(src_center, np.float64)
+        n = ctypes.c_int()
+        nnz = ctypes.c_int()
+        _check(lib().ref_assemble(self.h, _p(rho), float(k), _p(sc), ctypes.byref(n), ctypes.byref(nnz),
+                                  None, None, None))
+        rp = np.zeros(n.value + 1, np.int32)
+        ci = np.zeros(nnz.value, np.int32)
+        va = np.zeros(nnz.value)
+        _check(lib().ref_assemble(self.h, _p(rho), float(k), _p(sc), ctypes.byref(n), ctypes.byref(nnz),
+                                  _p(rp), _p(ci), _p(va)))
+        return rp, ci, va
+
+    def primary(self, e, k, surface_z=0.0):
+        out = np.zeros(self.mesh.nodeCount())
+        _check(lib().ref_primary(self.h, int(e), float(k), float(surface_z), _p(out)))
+        return out
+
+
+def besselK0(x):
+    return lib().ref_besselK0(float(x))
+
+
+def besselK1(x):
+    return lib().ref_besselK1(float(x))

@@ -1,0 +1,316 @@
+// Test infrastructure only: a C entry layer over the reference's own C++
+// ERT modelling code, compiled from the reference sources into
+// oracle/_ref/libgimli_ref.so by oracle/Makefile.  Nothing in the product
+// links or loads this file; tests and fixture generation call it through
+// ctypes (oracle/ref_driver.py) to obtain reference outputs.
+//
+// What it drives (reference file:line):
+//   mesh construction      core/src/mesh.h:183-217 (createNode/createTriangle/
+//                          createTetrahedron/createEdge/createTriangleFace),
+//                          mesh.h:457 createNeighborInfos
+//   data container         core/src/bert/bertDataContainer.h:62 addFourPointData
+//   forward operator       core/src/bert/dcfemmodelling.h:344 DCSRMultiElectrodeModelling
+//   response / Jacobian    core/src/bert/dcfemmodelling.cpp:1085-1197, 1446-1476
+//   solver injection       core/src/bert/dcfemmodelling.h:266 setSolver,
+//                          core/src/solverWrapper.h:26-56 SolverWrapper
+// The reference's default direct solver (CHOLMOD/UMFPACK) is not available,
+// so the solve is delegated to a host callback (an FP64 sparse direct solver
+// supplied by the caller).  Every other step is the reference's own code.
+
+#include <gimli.h>
+#include <mesh.h>
+#include <node.h>
+#include <meshentities.h>
+#include <sparsematrix.h>
+#include <solverWrapper.h>
+#include <bert/dcfemmodelling.h>
+#include <bert/bertDataContainer.h>
+#include <bert/bertMisc.h>
+#include <bert/bertJacobian.h>
+
+#include <cstring>
+#include <exception>
+#include <string>
+#include <vector>
+
+namespace GIMLI {
+// Defined (not declared in a header) in core/src/bert/dcfemmodelling.cpp:300-304.
+void dcfemBoundaryAssembleStiffnessMatrix(RSparseMatrix &S, const Mesh &mesh,
+                                          const RVector3 &source, double k);
+}
+
+using namespace GIMLI;
+
+extern "C" {
+// factor(n, nnz, rowptr, colidx, vals): called once per system matrix.
+typedef int (*ref_factor_fn)(int n, int nnz, const int *rowptr,
+                             const int *colidx, const double *vals);
+// solve(n, rhs, x): x = A^{-1} rhs for the last factored matrix.
+typedef int (*ref_solve_fn)(int n, const double *rhs, double *x);
+}
+
+namespace {
+
+std::string g_last_error;
+
+class CallbackSolver : public SolverWrapper {
+public:
+    CallbackSolver(ref_factor_fn f, ref_solve_fn s) : SolverWrapper(false), f_(f), s_(s) {}
+    void setMatrix(const RSparseMatrix &S) override {
+        const std::vector<int> &cp = S.vecColPtr();
+        const std::vector<int> &ri = S.vecRowIdx();
+        const RVector &v = S.vecVals();
+        n_ = (int)S.rows();
+        int rc = f_(n_, (int)ri.size(), cp.data(), ri.data(), &v[0]);
+        if (rc != 0) throwError("oracle factor callback failed");
+    }
+    void solve(const RVector &rhs, RVector &sol) override {
+        if ((int)sol.size() != n_) sol.resize(n_);
+        int rc = s_(n_, &rhs[0], &sol[0]);
+        if (rc != 0) throwError("oracle solve callback failed");
+    }
+private:
+    ref_factor_fn f_;
+    ref_solve_fn s_;
+    int n_ = 0;
+};
+
+struct RefHandle {
+    Mesh mesh;
+    DataContainerERT data;
+    DCSRMultiElectrodeModelling *fop = nullptr;
+    CallbackSolver *solver = nullptr;
+    RMatrix subpots;          // collected sub-potentials (nE*nK x nNodes)
+    RefHandle(int dim) : mesh(dim) {}
+    ~RefHandle() { delete fop; delete solver; }
+};
+
+template <class F> int guarded(F &&f) {
+    try {
+        f();
+        return 0;
+    } catch (std::exception &e) {
+        g_last_error = e.what();
+        return 1;
+    } catch (...) {
+        g_last_error = "unknown exception";
+        return 1;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *ref_last_error() { return g_last_error.c_str(); }
+
+// Build mesh + data container + SR forward operator.
+// cellNodes: nCells*nv (nv=3 triangle, 4 tetrahedron), bndNodes: nBnd*nvb.
+// abmn: nData*4 with -1 for an electrode at infinity.  kfac may be NULL.
+void *ref_create(int dim, int nNodes, const double *xyz, const int *nodeMarker,
+                 int nCells, int nv, const int *cellNodes, const int *cellMarker,
+                 int nBnd, int nvb, const int *bndNodes, const int *bndMarker,
+                 int nSensors, const double *sensorXyz, int nData, const int *abmn,
+                 const double *kfac, int verbose) {
+    RefHandle *h = nullptr;
+    int rc = guarded([&] {
+        h = new RefHandle(dim);
+        Mesh &m = h->mesh;
+        for (int i = 0; i < nNodes; i++)
+            m.createNode(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], nodeMarker[i]);
+        for (int c = 0; c < nCells; c++) {
+            const int *cn = cellNodes + (size_t)c * nv;
+            if (nv == 3) m.createTriangle(m.node(cn[0]), m.node(cn[1]), m.node(cn[2]), cellMarker[c]);
+            else if (nv == 4) m.createTetrahedron(m.node(cn[0]), m.node(cn[1]), m.node(cn[2]), m.node(cn[3]), cellMarker[c]);
+            else throwError("unsupported cell node count");
+        }
+        for (int b = 0; b < nBnd; b++) {
+            const int *bn = bndNodes + (size_t)b * nvb;
+            if (nvb == 2) m.createEdge(m.node(bn[0]), m.node(bn[1]), bndMarker[b]);
+            else if (nvb == 3) m.createTriangleFace(m.node(bn[0]), m.node(bn[1]), m.node(bn[2]), bndMarker[b]);
+            else throwError("unsupported boundary node count");
+        }
+        m.createNeighborInfos();
+        for (int s = 0; s < nSensors; s++)
+            h->data.createSensor(RVector3(sensorXyz[3 * s], sensorXyz[3 * s + 1], sensorXyz[3 * s + 2]), 1e-9);
+        for (int d = 0; d < nData; d++)
+            h->data.addFourPointData(abmn[4 * d], abmn[4 * d + 1], abmn[4 * d + 2], abmn[4 * d + 3]);
+        if (kfac) {
+            RVector k(nData);
+            for (int d = 0; d < nData; d++) k[d] = kfac[d];
+            h->data.set("k", k);
+        }
+        h->fop = new DCSRMultiElectrodeModelling(verbose != 0);
+        h->fop->setData(h->data);
+        h->fop->setMesh(h->mesh, true);
+        h->fop->collectSubPotentials(h->subpots);
+        h->fop->initJacobian();
+    });
+    if (rc) { delete h; return nullptr; }
+    return h;
+}
+
+void ref_destroy(void *hp) { delete (RefHandle *)hp; }
+
+int ref_set_solver(void *hp, ref_factor_fn f, ref_solve_fn s) {
+    RefHandle *h = (RefHandle *)hp;
+    return guarded([&] {
+        delete h->solver;
+        h->solver = new CallbackSolver(f, s);
+        h->fop->setSolver(h->solver);
+    });
+}
+
+int ref_set_threads(void *hp, int n) {
+    RefHandle *h = (RefHandle *)hp;
+    return guarded([&] { h->fop->setThreadCount(n); });
+}
+
+int ref_set_kw(void *hp, int nK, const double *k, const double *w) {
+    RefHandle *h = (RefHandle *)hp;
+    return guarded([&] {
+        RVector kv(nK), wv(nK);
+        for (int i = 0; i < nK; i++) { kv[i] = k[i]; wv[i] = w[i]; }
+        h->fop->setkValues(kv);
+        h->fop->setWeights(wv);
+    });
+}
+
+// Number of wavenumbers chosen by the reference (initKWaveList) or set.
+int ref_kw_count(void *hp) { return (int)((RefHandle *)hp)->fop->kValues().size(); }
+
+int ref_get_kw(void *hp, double *k, double *w) {
+    RefHandle *h = (RefHandle *)hp;
+    return guarded([&] {
+        const RVector &kv = h->fop->kValues();
+        const RVector &wv = h->fop->weights();
+        for (Index i = 0; i < kv.size(); i++) { k[i] = kv[i]; w[i] = wv[i]; }
+    });
+}
+
+// Electrode node ids as matched by searchElectrodes_ (-1 if not a node electrode),
+// plus sourceCenterPos_-equivalent and surfaceZ are not exposed by the reference.
+int ref_electrode_nodes(void *hp, int *nodeIds) {
+    RefHandle *h = (RefHandle *)hp;
+    return guarded([&] {
+        const std::vector<ElectrodeShape *> &el = h->fop->electrodes();
+        for (size_t i = 0; i < el.size(); i++) nodeIds[i] = el[i]->mID();
+    });
+}
+
+int ref_geometric_factors(void *hp, double *kout) {
+    RefHandle *h = (RefHandle *)hp;
+    return guarded([&] {
+        RVector k(geometricFactors(h->data, h->mesh.dim(), false));
+        for (Index i = 0; i < k.size(); i++) kout[i] = k[i];
+    });
+}
+
+int ref_response(void *hp, const double *model, int nModel, double *rhoa) {
+    RefHandle *h = (RefHandle *)hp;
+    return guarded([&] {
+        RVector m(nModel);
+        for (int i = 0; i < nModel; i++) m[i] = model[i];
+        RVector r(h->fop->response(m));
+        for (Index i = 0; i < r.size(); i++) rhoa[i] = r[i];
+    });
+}
+
+// Sub-potentials of the last response: rows (i + kIdx*nE), cols nodes.
+int ref_subpot_shape(void *hp, int *rows, int *cols) {
+    RefHandle *h = (RefHandle *)hp;
+    *rows = (int)h->subpots.rows();
+    *cols = h->subpots.rows() ? (int)h->subpots[0].size() : 0;
+    return 0;
+}
+
+int ref_subpotentials(void *hp, double *out) {
+    RefHandle *h = (RefHandle *)hp;
+    return guarded([&] {
+        Index r = h->subpots.rows();
+        for (Index i = 0; i < r; i++) {
+            const RVector &row = h->subpots[i];
+            std::memcpy(out + i * row.size(), &row[0], row.size() * sizeof(double));
+        }
+    });
+}
+
+// createJacobian(model) then copy J (rows x cols, row-major).
+int ref_jacobian(void *hp, const double *model, int nModel, double *J, int *rows, int *cols) {
+    RefHandle *h = (RefHandle *)hp;
+    return guarded([&] {
+        RVector m(nModel);
+        for (int i = 0; i < nModel; i++) m[i] = model[i];
+        h->fop->createJacobian(m);
+        RMatrix *Jm = dynamic_cast<RMatrix *>(h->fop->jacobian());
+        if (!Jm) throwError("no real Jacobian");
+        *rows = (int)Jm->rows();
+        *cols = (int)Jm->cols();
+        if (J) {
+            for (Index i = 0; i < Jm->rows(); i++)
+                std::memcpy(J + i * Jm->cols(), &(*Jm)[i][0], Jm->cols() * sizeof(double));
+        }
+    });
+}
+
+// The system matrix exactly as the SR calculateK builds it
+// (dcfemmodelling.cpp:2174-2182): pattern, domain assembly with the given
+// per-cell resistivity, mixed boundary terms at the mean electrode position,
+// calibration Dirichlet rows.  srcCenter is the mean electrode position.
+// Call once with vals == NULL to get nnz, then with buffers of that size.
+int ref_assemble(void *hp, const double *rho, double k, const double *srcCenter,
+                 int *n, int *nnz, int *rowptr, int *colidx, double *vals) {
+    RefHandle *h = (RefHandle *)hp;
+    return guarded([&] {
+        Mesh &m = h->mesh;
+        RVector att(m.cellCount());
+        for (Index c = 0; c < m.cellCount(); c++) att[c] = rho[c];
+        Mesh mm(m);
+        mm.setCellAttributes(att);
+        RSparseMatrix S;
+        S.buildSparsityPattern(mm);
+        dcfemDomainAssembleStiffnessMatrix(S, mm, k);
+        dcfemBoundaryAssembleStiffnessMatrix(S, mm, RVector3(srcCenter[0], srcCenter[1], srcCenter[2]), k);
+        *n = (int)S.rows();
+        *nnz = (int)S.nVals();
+        if (vals) {
+            const std::vector<int> &cp = S.vecColPtr();
+            const std::vector<int> &ri = S.vecRowIdx();
+            for (size_t i = 0; i < cp.size(); i++) rowptr[i] = cp[i];
+            for (size_t i = 0; i < ri.size(); i++) colidx[i] = ri[i];
+            for (Index i = 0; i < S.nVals(); i++) vals[i] = S.vecVals()[i];
+        }
+    });
+}
+
+// Analytic primary potential of the reference (bertMisc.cpp:186-271) at all
+// nodes for electrode index e (singular value set as in the SR path).
+int ref_primary(void *hp, int e, double k, double surfaceZ, double *out) {
+    RefHandle *h = (RefHandle *)hp;
+    return guarded([&] {
+        const std::vector<ElectrodeShape *> &el = h->fop->electrodes();
+        RVector u(exactDCSolution(h->mesh, el[e], k, surfaceZ, true));
+        for (Index i = 0; i < u.size(); i++) out[i] = u[i];
+    });
+}
+
+double ref_besselK0(double x) { return besselK0(x); }
+double ref_besselK1(double x) { return besselK1(x); }
+
+int ref_gauss_legendre(int n, double *x, double *w) {
+    return guarded([&] {
+        RVector xv, wv;
+        GaussLegendre(0.0, 1.0, n, xv, wv);
+        for (int i = 0; i < n; i++) { x[i] = xv[i]; w[i] = wv[i]; }
+    });
+}
+
+int ref_gauss_laguerre(int n, double *x, double *w) {
+    return guarded([&] {
+        RVector xv, wv;
+        GaussLaguerre(n, xv, wv);
+        for (int i = 0; i < n; i++) { x[i] = xv[i]; w[i] = wv[i]; }
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,240 @@
+"""ERT data container, measurement-scheme generators and analytic geometric
+factors.
+
+``DataContainerERT`` keeps what the forward operator reads from the
+reference's ``GIMLI::DataContainerERT`` (core/src/bert/bertDataContainer.h:32,
+addFourPointData at :62): sensor positions and the four electrode index
+columns ``a b m n`` (-1 = electrode at infinity) plus the data fields
+``k`` (geometric factor) and ``rhoa``.
+
+The scheme generators restate the loops of pyGIMLi's scheme classes
+(pygimli/physics/ert/ertScheme.py: dipole-dipole 476-527, pole-dipole
+554-578, Wenner-alpha 652-672) and ``createData`` mirrors
+``pg.physics.ert.createData(elecs, schemeName)``.
+
+``geometricFactors`` restates core/src/bert/bertMisc.cpp:131-176 with the
+half-space mirror potential of bertMisc.cpp:186-230 (k = 1 / (u_AM - u_BM -
+u_AN + u_BN), 2-D sensor positions (x, y) are moved to (x, 0, y) first).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+class DataContainerERT:
+    """Sensors + four-point configurations + data fields."""
+
+    def __init__(self, sensors=None, abmn=None):
+        self._sensors = np.zeros((0, 3))
+        self._abmn = np.zeros((0, 4), np.int32)
+        self._fields = {}
+        if sensors is not None:
+            self.setSensorPositions(sensors)
+        if abmn is not None:
+            ab = np.asarray(abmn, dtype=np.int32).reshape(-1, 4)
+            self._abmn = ab.copy()
+
+    # -- sensors ------------------------------------------------------------
+    def setSensorPositions(self, pos):
+        p = np.asarray(pos, dtype=np.float64)
+        if p.ndim == 1:
+            p = np.column_stack([p, np.zeros(len(p)), np.zeros(len(p))])
+        if p.shape[1] == 2:
+            p = np.column_stack([p, np.zeros(len(p))])
+        self._sensors = np.ascontiguousarray(p)
+
+    def sensorPositions(self):
+        return self._sensors.copy()
+
+    def sensorPosition(self, i):
+        return self._sensors[i].copy()
+
+    def sensorCount(self):
+        return len(self._sensors)
+
+    def createSensor(self, pos, tolerance=1e-3):
+        p = np.zeros(3)
+        p[:len(pos)] = pos
+        if len(self._sensors):
+            d = np.linalg.norm(self._sensors - p, axis=1)
+            i = int(np.argmin(d))
+            if d[i] < tolerance:
+                return i
+        self._sensors = np.vstack([self._sensors, p])
+        return len(self._sensors) - 1
+
+    # -- data -------------------------------------------------------------
+    def addFourPointData(self, a, b, m, n):
+        self._abmn = np.vstack([self._abmn, np.array([[a, b, m, n]], np.int32)])
+        for k, v in self._fields.items():
+            self._fields[k] = np.append(v, 0.0)
+        return len(self._abmn) - 1
+
+    def size(self):
+        return len(self._abmn)
+
+    def __len__(self):
+        return self.size()
+
+    def abmn(self):
+        return self._abmn.copy()
+
+    def __getitem__(self, token):
+        if token in ("a", "b", "m", "n"):
+            return self._abmn[:, "abmn".index(token)].astype(np.float64)
+        if token in self._fields:
+            return self._fields[token].copy()
+        if token in ("k", "rhoa", "u", "i", "r", "err", "ip"):
+            return np.zeros(self.size())
+        raise KeyError(token)
+
+    def __call__(self, token):
+        return self[token]
+
+    def get(self, token):
+        return self[token]
+
+    def __setitem__(self, token, values):
+        self.set(token, values)
+
+    def set(self, token, values):
+        v = np.asarray(values, dtype=np.float64)
+        if v.shape != (self.size(),):
+            raise ValueError(f"field '{token}' needs {self.size()} values")
+        if token in ("a", "b", "m", "n"):
+            self._abmn[:, "abmn".index(token)] = v.astype(np.int32)
+        else:
+            self._fields[token] = v.copy()
+
+    def exists(self, token):
+        return token in self._fields
+
+    def allNonZero(self, token):
+        return token in self._fields and bool(np.all(self._fields[token] != 0))
+
+    def copy(self):
+        d = DataContainerERT(self._sensors, self._abmn)
+        d._fields = {k: v.copy() for k, v in self._fields.items()}
+        return d
+
+    def __repr__(self):
+        return f"DataContainerERT(sensors={self.sensorCount()}, data={self.size()}, fields={sorted(self._fields)})"
+
+
+# -- measurement schemes (pygimli/physics/ert/ertScheme.py) -----------------
+
+def _scheme_dd(nE, spacings=(1,), max_separation=999):
+    out = []
+    for space in spacings:
+        max_sep = nE - space
+        max_inj = nE - space
+        if max_separation < max_sep:
+            max_sep = max_separation
+        for sep in range(1, max_sep + 1):
+            for i in range(max_inj - sep):
+                a = i
+                b = (a + space) % nE
+                m = (b + sep) % nE
+                n = (m + space) % nE
+                if m + space < nE:
+                    out.append((a, b, m, n))
+    return out
+
+
+def _scheme_pd(nE, max_separation=999):
+    out = []
+    b = -1
+    for a in range(nE):
+        for m in range(a + 1, nE - 1):
+            n = m + 1
+            if m - a > max_separation:
+                break
+            out.append((a, b, m, n))
+    return out
+
+
+def _scheme_wa(nE, max_separation=999):
+    out = []
+    max_sep = nE - 2
+    if max_separation < max_sep:
+        max_sep = max_separation
+    for sep in range(1, max_sep + 1):
+        for i in range((nE - 2) - sep):
+            a = i
+            m = a + sep
+            n = m + sep
+            b = n + sep
+            if max(a, b, m, n) < nE:
+                out.append((a, b, m, n))
+    return out
+
+
+def createData(elecs, schemeName="dd", **kwargs):
+    """Create a data container for the electrode positions ``elecs``
+    (array of x, or (N, 2|3) positions) and a scheme name
+    (``dd`` dipole-dipole, ``pd`` pole-dipole, ``wa`` Wenner-alpha)."""
+    e = np.asarray(elecs, dtype=np.float64)
+    if e.ndim == 1:
+        e = np.column_stack([e, np.zeros(len(e)), np.zeros(len(e))])
+    nE = len(e)
+    max_sep = kwargs.pop("maxSeparation", 999)
+    if schemeName == "dd":
+        rows = _scheme_dd(nE, kwargs.pop("spacings", (1,)), max_sep)
+    elif schemeName == "pd":
+        rows = _scheme_pd(nE, max_sep)
+    elif schemeName == "wa":
+        rows = _scheme_wa(nE, max_sep)
+    else:
+        raise ValueError(f"unknown scheme '{schemeName}'")
+    d = DataContainerERT(e, np.array(rows, np.int32).reshape(-1, 4))
+    return d
+
+
+def grid_line_scheme(electrode_grid, kind="dd", max_separation=999):
+    """Dipole-dipole / pole-dipole lines along x and along y of a rectangular
+    surface electrode grid ``electrode_grid`` (nx, ny) whose electrode index
+    is ``ix * ny + iy``."""
+    nx, ny = electrode_grid
+    rows = []
+    lines = [[ix * ny + iy for ix in range(nx)] for iy in range(ny)]
+    lines += [[ix * ny + iy for iy in range(ny)] for ix in range(nx)]
+    gen = _scheme_dd if kind == "dd" else _scheme_pd
+    for line in lines:
+        loc = gen(len(line), max_separation=max_separation) if kind == "pd" else \
+            gen(len(line), (1,), max_separation)
+        for (a, b, m, n) in loc:
+            rows.append(tuple(line[i] if i >= 0 else -1 for i in (a, b, m, n)))
+    return np.array(rows, np.int32).reshape(-1, 4)
+
+
+# -- geometric factors (core/src/bert/bertMisc.cpp:131-230) ---------------
+
+def _u_half(p, s):
+    """3-D half-space potential of a unit source at ``s`` observed at ``p``
+    with the mirror source above z=0 (bertMisc.cpp:186-230 with k = 0,
+    surfaceZ = 0): (1/r + 1/r') / (4 pi)."""
+    r = np.linalg.norm(p - s, axis=-1)
+    sm = s.copy()
+    sm[..., 2] = -s[..., 2]
+    rm = np.linalg.norm(p - sm, axis=-1)
+    with np.errstate(divide="ignore"):
+        return (1.0 / r + 1.0 / rm) / (4.0 * np.pi)
+
+
+def geometricFactors(data, dim=3):
+    """Analytic half-space geometric factors for every datum."""
+    pos = data.sensorPositions().copy()
+    if dim == 2:
+        # (x, y) -> (x, 0, y) when y differs from 0 (bertMisc.cpp:134-145)
+        mv = pos[:, 1] != 0.0
+        pos[mv, 2] = pos[mv, 1]
+        pos[mv, 1] = 0.0
+    ab = data.abmn()
+    k = np.empty(len(ab))
+    for i, (a, b, m, n) in enumerate(ab):
+        uam = _u_half(pos[m], pos[a]) if (a > -1 and m > -1) else 0.0
+        ubm = _u_half(pos[m], pos[b]) if (b > -1 and m > -1) else 0.0
+        uan = _u_half(pos[n], pos[a]) if (a > -1 and n > -1) else 0.0
+        ubn = _u_half(pos[n], pos[b]) if (b > -1 and n > -1) else 0.0
+        k[i] = 1.0 / (uam - ubm - uan + ubn)
+    return k
