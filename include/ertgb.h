@@ -1,0 +1,135 @@
+/* ertgb — GB300-native ERT (DC resistivity) forward operator and Jacobian.
+ *
+ * C ABI of libertgb.so.  Plain pointers and sizes only; every function
+ * returns an ertgb_status and never throws.  Arrays named *_host live in host
+ * memory, arrays named *_dev in device memory of the context's GPU.  A
+ * ``stream`` argument is a cudaStream_t passed as void* (NULL = the
+ * context's own stream); device-buffer calls are stream-ordered and return
+ * before the work finishes, host-buffer calls synchronise.
+ *
+ * The operator is the singularity-removal (SR) DC forward operator of
+ * pyGIMLi: pg.physics.ert.ERTModelling(sr=True) -> C++
+ * GIMLI::DCSRMultiElectrodeModelling.  Each entry point below names the
+ * reference interface it replaces (paths inside the pyGIMLi tree).
+ */
+#ifndef ERTGB_H
+#define ERTGB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ertgb_ctx ertgb_ctx;
+
+typedef enum {
+    ERTGB_OK = 0,
+    ERTGB_BAD_INPUT = 1,     /* sizes, indices, non-positive resistivity ... */
+    ERTGB_NOT_CONVERGED = 2, /* PCG hit max_iter before the tolerance      */
+    ERTGB_OOM = 3,           /* device allocation failed                     */
+    ERTGB_CUDA_ERROR = 4,    /* a CUDA runtime call failed                   */
+    ERTGB_STATE = 5          /* call order (e.g. jacobian before response)   */
+} ertgb_status;
+
+/* Preconditioners of the block PCG. */
+typedef enum { ERTGB_PRECOND_JACOBI = 0 } ertgb_precond;
+
+/* Solver statistics of the last response. */
+typedef struct {
+    int32_t iterations;       /* PCG iterations until every column converged */
+    int32_t n_rhs;            /* right-hand sides = electrodes x wavenumbers */
+    double max_rel_residual;  /* max_j ||b_j - A x_j|| / ||b_j|| (recursive)  */
+    double ms_assemble;       /* device time of the last response's phases   */
+    double ms_rhs;
+    double ms_solve;
+    double ms_collect;
+    double ms_jacobian;       /* device time of the last jacobian            */
+} ertgb_stats;
+
+/* Create a context on CUDA device ``device``.  Replaces the construction of
+ * DCSRMultiElectrodeModelling (core/src/bert/dcfemmodelling.h:346-359,
+ * pygimli/physics/ert/ertModelling.py:87-122). */
+int ertgb_create(ertgb_ctx **ctx, int device);
+int ertgb_destroy(ertgb_ctx *ctx);
+/* Message of the last failing call on this context ("" if none). */
+const char *ertgb_last_error(const ertgb_ctx *ctx);
+
+/* Mesh: replaces ModellingBase::setMesh (core/src/modellingbase.cpp:179-206)
+ * with DCMultiElectrodeModelling::updateMeshDependency_
+ * (core/src/bert/dcfemmodelling.cpp:711-773).  dim 2 (triangles, y = depth,
+ * 2.5-D) or 3 (tetrahedra).  xyz: n_nodes x 3.  cell_nodes: n_cells x
+ * (dim+1).  bnd_nodes: n_bnd x dim, bnd_marker -1 Neumann / -2 mixed,
+ * bnd_cell: adjacent cell of each boundary.  Builds the CSR pattern
+ * (core/src/sparsematrix.h:966-1024), the per-slot assembly map and the
+ * element matrices (core/src/elementmatrix.cpp:683-1122). */
+int ertgb_set_mesh(ertgb_ctx *ctx, int dim, int n_nodes, const double *xyz_host,
+                   int n_cells, const int32_t *cell_nodes_host, const int32_t *cell_marker_host,
+                   int n_bnd, const int32_t *bnd_nodes_host, const int32_t *bnd_marker_host,
+                   const int32_t *bnd_cell_host);
+
+/* Node electrodes as matched by DCMultiElectrodeModelling::searchElectrodes_
+ * (core/src/bert/dcfemmodelling.cpp:790-1030): node id of each electrode,
+ * the surface coordinate on axis dim-1 of the Neumann boundary
+ * (updateMeshDependency_, :727-745).  Replaces that search's results; the
+ * mean electrode position (sourceCenterPos_, :1026-1030), the singular
+ * radii (core/src/bert/electrode.cpp:154-197) and the incident cells
+ * (electrode.cpp:102-127) are derived here. */
+int ertgb_set_electrodes(ertgb_ctx *ctx, int n_elec, const int32_t *elec_node_host,
+                         double surface_z);
+
+/* Wavenumbers and weights: DCMultiElectrodeModelling::setkValues/setWeights
+ * (core/src/bert/dcfemmodelling.h:239-243). */
+int ertgb_set_kw(ertgb_ctx *ctx, int n_k, const double *k_host, const double *w_host);
+
+/* Measurement scheme: the a b m n columns (-1 = at infinity) and geometric
+ * factors k of DataContainerERT (core/src/bert/bertDataContainer.h:62),
+ * as read by DataMap::data (core/src/bert/datamap.cpp:159-231). */
+int ertgb_set_scheme(ertgb_ctx *ctx, int n_data, const int32_t *abmn_host, const double *kfac_host);
+
+/* Solver controls: relative residual tolerance, iteration cap, preconditioner. */
+int ertgb_set_solver(ertgb_ctx *ctx, double rtol, int max_iter, int precond);
+
+/* Forward response: DCMultiElectrodeModelling::response
+ * (core/src/bert/dcfemmodelling.cpp:1085-1197) for a per-cell resistivity
+ * (the result of mapERTModel, :1199-1218).  Writes n_data apparent
+ * resistivities sqrt(|rhoa * rhoa_reciprocal|).  Keeps the sub-potentials
+ * on the device for ertgb_jacobian (the reference keeps subSolutions_). */
+int ertgb_response(ertgb_ctx *ctx, const double *rho_cell_dev, double *rhoa_dev, void *stream);
+/* Same with host buffers (copies included). */
+int ertgb_response_host(ertgb_ctx *ctx, const double *rho_cell_host, double *rhoa_host);
+
+/* Jacobian: DCMultiElectrodeModelling::createJacobian
+ * (core/src/bert/dcfemmodelling.cpp:1446-1476, createSensitivityCol
+ * core/src/bert/bertJacobian.cpp:267-421, calc2 :70-119) from the
+ * sub-potentials of the last response.  J is n_data x n_param row-major,
+ * n_param = max(cell marker) + 1, FP64 (dtype 0) or FP32 (dtype 1).  When
+ * n_model == n_param the rows are scaled by k_i / model_j^2
+ * (dcfemmodelling.cpp:1377-1384). */
+int ertgb_jacobian(ertgb_ctx *ctx, const double *model_dev, int n_model, void *J_dev, int dtype,
+                   void *stream);
+/* Same with host buffers (model and J on the host). */
+int ertgb_jacobian_host(ertgb_ctx *ctx, const double *model_host, int n_model, void *J_host,
+                        int dtype);
+
+/* Sizes after set_mesh/set_electrodes/set_kw/set_scheme. */
+int ertgb_sizes(const ertgb_ctx *ctx, int64_t *n_nodes, int64_t *nnz, int64_t *n_param,
+                int64_t *n_rhs);
+
+/* Parity accessors (host outputs). */
+int ertgb_get_pattern(ertgb_ctx *ctx, int32_t *rowptr_host, int32_t *colidx_host);
+/* System matrix values of wavenumber k_index from the last response:
+ * which 0 = S (model), 1 = S1 (unit resistivity). */
+int ertgb_get_matrix(ertgb_ctx *ctx, int k_index, int which, double *vals_host);
+/* Sub-potentials of the last response, laid out [k][electrode][node]
+ * like the reference's subSolutions_ rows (i + k*nElecs). */
+int ertgb_get_potentials(ertgb_ctx *ctx, double *pot_host);
+/* Unit-current primary potentials [k][electrode][node]. */
+int ertgb_get_primary(ertgb_ctx *ctx, double *prim_host);
+int ertgb_get_stats(const ertgb_ctx *ctx, ertgb_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ERTGB_H */

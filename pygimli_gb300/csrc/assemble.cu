@@ -1,0 +1,515 @@
+// FP64 kernels of the ERT forward operator around the solve:
+//   element matrices      per cell gradient (K) and mass (M) matrices
+//   boundary coefficients mixed (Robin) boundary alpha per wavenumber
+//   primary potentials    analytic unit-current potentials per (k, electrode)
+//   assembly              S = sum_cells (M k^2 + K)/rho + sum_bnd u2 alpha/rho
+//                         as a gather over the per-slot contribution lists
+//   source resistivity    geometric mean of the cells at each electrode
+//   SR right-hand side    b = S1 prim / rho_s - S prim, prim = rho_s u_p
+//   potentials            u = x + prim
+//   collect / response    electrode potential matrix, ABMN voltages,
+//                         reciprocity mean apparent resistivity
+//
+// Reference (paths in pyGIMLi):
+//   core/src/elementmatrix.cpp:683-796, 798-870, 1036-1041
+//   core/src/bert/dcfemmodelling.cpp:163-228 (domain), 243-299 and 430-506
+//   (mixed boundary), 2152-2296 (SR calculateK), 1697-1729 (k-sum),
+//   1139-1196 (response); core/src/bert/bertMisc.cpp:186-271
+//   (exactDCSolution); core/src/bert/electrode.cpp:102-197;
+//   core/src/bert/datamap.cpp:57-98, 159-231.
+#include <cfloat>
+#include <cmath>
+
+#include "bessel.cuh"
+#include "ertgb_internal.cuh"
+
+namespace ertgb {
+
+namespace {
+
+constexpr double kTol = 1e-12;  // TOLERANCE of the reference (gimli.h)
+constexpr double kPi = 3.141592653589793238462643383279502884;
+constexpr int kThreads = 256;
+
+inline unsigned grid1(int64_t n, int threads = kThreads, int64_t cap = 1 << 20) {
+    int64_t g = ceil_div(n, threads);
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return (unsigned)g;
+}
+
+// ---------------------------------------------------------------- geometry
+__global__ void k_element_matrices(int64_t C, int dim, const double *__restrict__ xyz,
+                                   const int32_t *__restrict__ cells, double *__restrict__ K,
+                                   double *__restrict__ M) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C;
+         c += (int64_t)gridDim.x * blockDim.x) {
+        if (dim == 2) {
+            const int32_t *cn = cells + c * 3;
+            const double x1 = xyz[3 * cn[0]], y1 = xyz[3 * cn[0] + 1];
+            const double x2 = xyz[3 * cn[1]], y2 = xyz[3 * cn[1] + 1];
+            const double x3 = xyz[3 * cn[2]], y3 = xyz[3 * cn[2] + 1];
+            // closed form of the reference's triangle gradient matrix, J = 2 * area
+            const double J = fabs((x2 - x1) * (y3 - y1) - (x3 - x1) * (y2 - y1));
+            const double a = ((x3 - x1) * (x3 - x1) + (y3 - y1) * (y3 - y1)) / J;
+            const double b = -((x3 - x1) * (x2 - x1) + (y3 - y1) * (y2 - y1)) / J;
+            const double cc = ((x2 - x1) * (x2 - x1) + (y2 - y1) * (y2 - y1)) / J;
+            double *k = K + c * 9;
+            k[0] = a * 0.5 + b + cc * 0.5;
+            k[3] = a * -0.5 + b * -0.5;
+            k[6] = b * -0.5 + cc * -0.5;
+            k[4] = a * 0.5;
+            k[7] = b * 0.5;
+            k[8] = cc * 0.5;
+            k[1] = k[3];
+            k[2] = k[6];
+            k[5] = k[7];
+            const double m0 = (J / 2.0) / 12.0;
+            double *m = M + c * 9;
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) m[i * 3 + j] = (i == j) ? 2.0 * m0 : m0;
+        } else {
+            const int32_t *cn = cells + c * 4;
+            double p[4][3];
+            for (int i = 0; i < 4; i++)
+                for (int d = 0; d < 3; d++) p[i][d] = xyz[3 * cn[i] + d];
+            double e1[3], e2[3], e3[3];
+            for (int d = 0; d < 3; d++) {
+                e1[d] = p[1][d] - p[0][d];
+                e2[d] = p[2][d] - p[0][d];
+                e3[d] = p[3][d] - p[0][d];
+            }
+            // gradients of the barycentric coordinates: rows of inv([e1 e2 e3])
+            double g[4][3];
+            const double c23[3] = {e2[1] * e3[2] - e2[2] * e3[1], e2[2] * e3[0] - e2[0] * e3[2],
+                                   e2[0] * e3[1] - e2[1] * e3[0]};
+            const double c31[3] = {e3[1] * e1[2] - e3[2] * e1[1], e3[2] * e1[0] - e3[0] * e1[2],
+                                   e3[0] * e1[1] - e3[1] * e1[0]};
+            const double c12[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                                   e1[0] * e2[1] - e1[1] * e2[0]};
+            const double det = e1[0] * c23[0] + e1[1] * c23[1] + e1[2] * c23[2];
+            for (int d = 0; d < 3; d++) {
+                g[1][d] = c23[d] / det;
+                g[2][d] = c31[d] / det;
+                g[3][d] = c12[d] / det;
+                g[0][d] = -(g[1][d] + g[2][d] + g[3][d]);
+            }
+            const double V = fabs(det) / 6.0;
+            double *k = K + c * 16;
+            double *m = M + c * 16;
+            for (int i = 0; i < 4; i++)
+                for (int j = 0; j < 4; j++) {
+                    k[i * 4 + j] = V * (g[i][0] * g[j][0] + g[i][1] * g[j][1] + g[i][2] * g[j][2]);
+                    m[i * 4 + j] = (i == j) ? 2.0 * (V / 20.0) : (V / 20.0);
+                }
+        }
+    }
+}
+
+__global__ void k_boundary_geometry(int64_t B, int dim, const double *__restrict__ xyz,
+                                    const int32_t *__restrict__ bnd, double *__restrict__ mass,
+                                    double *__restrict__ center, double *__restrict__ normal) {
+    for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < B;
+         b += (int64_t)gridDim.x * blockDim.x) {
+        if (dim == 2) {
+            const int32_t *bn = bnd + b * 2;
+            const double x0 = xyz[3 * bn[0]], y0 = xyz[3 * bn[0] + 1], z0 = xyz[3 * bn[0] + 2];
+            const double x1 = xyz[3 * bn[1]], y1 = xyz[3 * bn[1] + 1], z1 = xyz[3 * bn[1] + 2];
+            const double tx = x1 - x0, ty = y1 - y0;
+            const double L = sqrt(tx * tx + ty * ty + (z1 - z0) * (z1 - z0));
+            const double m0 = L / 6.0;
+            mass[b * 4 + 0] = 2.0 * m0;
+            mass[b * 4 + 1] = m0;
+            mass[b * 4 + 2] = m0;
+            mass[b * 4 + 3] = 2.0 * m0;
+            center[b * 3 + 0] = (x0 + x1) / 2.0;
+            center[b * 3 + 1] = (y0 + y1) / 2.0;
+            center[b * 3 + 2] = (z0 + z1) / 2.0;
+            const double tl = sqrt(tx * tx + ty * ty);
+            normal[b * 3 + 0] = ty / tl;
+            normal[b * 3 + 1] = -tx / tl;
+            normal[b * 3 + 2] = 0.0;
+        } else {
+            const int32_t *bn = bnd + b * 3;
+            double p[3][3];
+            for (int i = 0; i < 3; i++)
+                for (int d = 0; d < 3; d++) p[i][d] = xyz[3 * bn[i] + d];
+            const double u[3] = {p[1][0] - p[0][0], p[1][1] - p[0][1], p[1][2] - p[0][2]};
+            const double v[3] = {p[2][0] - p[0][0], p[2][1] - p[0][1], p[2][2] - p[0][2]};
+            const double n[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]};
+            const double nl = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+            const double m0 = (0.5 * nl) / 12.0;
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) mass[b * 9 + i * 3 + j] = (i == j) ? 2.0 * m0 : m0;
+            for (int d = 0; d < 3; d++) {
+                center[b * 3 + d] = (p[0][d] + p[1][d] + p[2][d]) / 3.0;
+                normal[b * 3 + d] = n[d] / nl;
+            }
+        }
+    }
+}
+
+// mixedBoundaryCondition: mirror source through the plane 0 on axis dim-1
+// (y for k > 0, z for k == 0), source = mean electrode position.
+__global__ void k_boundary_alpha(int64_t B, int nK, const double *__restrict__ kv, double sx, double sy,
+                                 double sz, const double *__restrict__ center,
+                                 const double *__restrict__ normal, double *__restrict__ alpha) {
+    const int64_t total = B * nK;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int ki = (int)(t / B);
+        const int64_t b = t - (int64_t)ki * B;
+        const double k = kv[ki];
+        double src[3] = {sx, sy, sz};
+        double mir[3] = {sx, sy, sz};
+        const int ax = (k > 0.0) ? 1 : 2;
+        mir[ax] = 2.0 * 0.0 - src[ax];
+        double r[3], rm[3];
+        for (int d = 0; d < 3; d++) {
+            r[d] = src[d] - center[b * 3 + d];
+            rm[d] = mir[d] - center[b * 3 + d];
+        }
+        const double ra = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+        const double rma = sqrt(rm[0] * rm[0] + rm[1] * rm[1] + rm[2] * rm[2]);
+        const double *n = normal + b * 3;
+        const double rn = fabs(r[0] * n[0] + r[1] * n[1] + r[2] * n[2]);
+        const double rmn = fabs(rm[0] * n[0] + rm[1] * n[1] + rm[2] * n[2]);
+        double res;
+        if (k == 0.0) {
+            res = ((rma * rma) * rn / ra + (ra * ra) * rmn / rma) / (rma * ra * (ra + rma));
+        } else {
+            const double k0a = as_k0(ra * k), k0m = as_k0(rma * k);
+            if (fabs(k0a) < kTol || fabs(k0m) < kTol) {
+                res = 0.0;
+            } else {
+                res = k * (rn / ra * as_k1(ra * k) + rmn / rma * as_k1(rma * k)) / (k0a + k0m);
+            }
+        }
+        alpha[(int64_t)ki * B + b] = res;
+    }
+}
+
+// Unit-current primary potential at every node for column t = k*nE + e
+// (exactDCSolution with the singular value at the source node).
+__global__ void k_primary(int64_t n, int nE, int nK, int64_t Rpad, const double *__restrict__ xyz,
+                          const double *__restrict__ epos, const int32_t *__restrict__ enode,
+                          const double *__restrict__ emin_r, const double *__restrict__ kv,
+                          double surface_z, int fullspace, double *__restrict__ up) {
+    const int64_t R = (int64_t)nE * nK;
+    const int64_t total = n * Rpad;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t node = idx / Rpad;
+        const int64_t t = idx - node * Rpad;
+        if (t >= R) {
+            up[idx] = 0.0;
+            continue;
+        }
+        const int ki = (int)(t / nE);
+        const int e = (int)(t - (int64_t)ki * nE);
+        const double k = kv[ki];
+        const double *s = epos + 3 * e;
+        const double vx = xyz[3 * node], vy = xyz[3 * node + 1], vz = xyz[3 * node + 2];
+        double val;
+        if (node == enode[e]) {
+            const double mr = emin_r[e];
+            val = (k > 0.0) ? as_k0(mr / 6.0 * k) / kPi : 1.0 / (2.0 * kPi * mr / 2.0);
+        } else {
+            const double dx = vx - s[0], dy = vy - s[1], dz = vz - s[2];
+            const double r = sqrt(dx * dx + dy * dy + dz * dz);
+            if (r < kTol) {
+                val = 0.0;
+            } else {
+                const int ax = (k > 0.0) ? 1 : 2;
+                double m[3] = {s[0], s[1], s[2]};
+                m[ax] = 2.0 * surface_z - s[ax];
+                if (fullspace) {
+                    val = (k == 0.0) ? 1.0 / (4.0 * kPi * r) : as_k0(r * k) / (2.0 * kPi);
+                } else {
+                    const double mx = vx - m[0], my = vy - m[1], mz = vz - m[2];
+                    const double rm = sqrt(mx * mx + my * my + mz * mz);
+                    if (k == 0.0) {
+                        val = (1.0 / r + 1.0 / rm) / (4.0 * kPi);
+                    } else if (m[0] == s[0] && m[1] == s[1] && m[2] == s[2]) {
+                        val = as_k0(r * k) / kPi;
+                    } else {
+                        val = (as_k0(r * k) + as_k0(rm * k)) / (2.0 * kPi);
+                    }
+                }
+            }
+        }
+        up[idx] = val;
+    }
+}
+
+// ---------------------------------------------------------------- assembly
+// One thread per (slot, wavenumber).  Contributions are summed in the
+// reference's order: cells ascending, then mixed boundaries ascending.
+__global__ void k_assemble(int64_t nnz, const int32_t *__restrict__ cptr, const int32_t *__restrict__ centry,
+                           const double *__restrict__ K, const double *__restrict__ M,
+                           const double *__restrict__ bmass, const double *__restrict__ alpha,
+                           const int32_t *__restrict__ bcell, const double *__restrict__ rho,
+                           const double *__restrict__ kv, int nv2, int nvb2, int64_t C, int64_t B,
+                           double *__restrict__ vals) {
+    const int ki = blockIdx.y;
+    const double k = kv[ki];
+    const double kk = k * k;
+    const int64_t cbase = C * nv2;
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < nnz;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        const int32_t q1 = cptr[s + 1];
+        for (int32_t q = cptr[s]; q < q1; q++) {
+            const int64_t e = centry[q];
+            if (e < cbase) {
+                const int64_t c = e / nv2;
+                const double r = rho ? rho[c] : 1.0;
+                if (fabs(r) > kTol) {
+                    const double se = (k > 0.0) ? M[e] * kk + K[e] : K[e];
+                    acc += (1.0 / r) * se;
+                }
+            } else {
+                const int64_t eb = e - cbase;
+                const int64_t b = eb / nvb2;
+                const double r = rho ? rho[bcell[b]] : 1.0;
+                acc += (alpha[(int64_t)ki * B + b] / r) * bmass[eb];
+            }
+        }
+        vals[(int64_t)ki * nnz + s] = acc;
+    }
+}
+
+__global__ void k_dinv(int64_t n, int nK, int64_t nnz, const int32_t *__restrict__ diag,
+                       const double *__restrict__ vals, double *__restrict__ dinv) {
+    const int64_t total = n * nK;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t ki = t / n, r = t - ki * n;
+        dinv[t] = 1.0 / vals[ki * nnz + diag[r]];
+    }
+}
+
+__global__ void k_source_rho(int nE, const int32_t *__restrict__ ptr, const int32_t *__restrict__ ecell,
+                             const double *__restrict__ rho, double *__restrict__ out) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nE) return;
+    double s = 0.0;
+    const int a = ptr[e], b = ptr[e + 1];
+    for (int q = a; q < b; q++) s += log(rho[ecell[q]]);
+    s /= (double)(b - a);
+    out[e] = exp(s);
+}
+
+__global__ void k_check_rho(int64_t C, const double *__restrict__ rho, int32_t *__restrict__ bad) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C;
+         c += (int64_t)gridDim.x * blockDim.x) {
+        const double r = rho[c];
+        if (!(r >= kTol) || isinf(r)) atomicAdd(bad, 1);
+    }
+}
+
+// SR right-hand side, one warp per row, lanes over columns t = k*nE + e:
+// b = (S1 prim) / rho_s - S prim with prim = rho_s * u_p.
+__global__ void k_rhs(int64_t n, int64_t nnz, int nE, int64_t R, int64_t Rpad,
+                      const int32_t *__restrict__ rowptr, const int32_t *__restrict__ colidx,
+                      const double *__restrict__ S, const double *__restrict__ S1,
+                      const double *__restrict__ up, const double *__restrict__ rhos,
+                      double *__restrict__ b) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t row = warp; row < n; row += nwarps) {
+        const int32_t s0 = rowptr[row], s1 = rowptr[row + 1];
+        for (int64_t t = lane; t < Rpad; t += 32) {
+            double out = 0.0;
+            if (t < R) {
+                const int64_t ki = t / nE;
+                const int e = (int)(t - ki * nE);
+                const double rs = rhos[e];
+                const double *Sk = S + ki * nnz;
+                const double *S1k = S1 + ki * nnz;
+                double a1 = 0.0, a2 = 0.0;
+                for (int32_t s = s0; s < s1; s++) {
+                    const double prim = up[(int64_t)colidx[s] * Rpad + t] * rs;
+                    a1 += S1k[s] * prim;
+                    a2 += Sk[s] * prim;
+                }
+                out = a1 / rs - a2;
+            }
+            b[row * Rpad + t] = out;
+        }
+    }
+}
+
+__global__ void k_finish_pot(int64_t n, int nE, int64_t R, int64_t Rpad, const double *__restrict__ up,
+                             const double *__restrict__ rhos, double *__restrict__ x) {
+    const int64_t total = n * Rpad;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t t = idx % Rpad;
+        if (t < R) {
+            const int e = (int)(t % nE);
+            x[idx] += up[idx] * rhos[e];
+        }
+    }
+}
+
+// U[e][f] = sum_k w_k u_k[e](node of electrode f), summed like the
+// reference's k loop (first term a product, then accumulate).
+__global__ void k_collect(int nE, int nK, int64_t Rpad, const int32_t *__restrict__ enode,
+                          const double *__restrict__ w, const double *__restrict__ x,
+                          double *__restrict__ U) {
+    const int64_t total = (int64_t)nE * nE;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int e = (int)(t / nE), f = (int)(t % nE);
+        const double *row = x + (int64_t)enode[f] * Rpad;
+        double acc = row[e] * w[0];
+        for (int ki = 1; ki < nK; ki++) acc += row[(int64_t)ki * nE + e] * w[ki];
+        U[t] = acc;
+    }
+}
+
+__device__ inline double abmn_u(const double *U, int nE, int a, int b, int m, int n) {
+    double uAM = 0.0, uAN = 0.0, uBM = 0.0, uBN = 0.0;
+    if (a != -1 && m != -1) uAM = U[(int64_t)a * nE + m];
+    if (a != -1 && n != -1) uAN = U[(int64_t)a * nE + n];
+    if (b != -1 && m != -1) uBM = U[(int64_t)b * nE + m];
+    if (b != -1 && n != -1) uBN = U[(int64_t)b * nE + n];
+    return (uAM - uAN) - (uBM - uBN);
+}
+
+__global__ void k_response(int64_t D, int nE, const int32_t *__restrict__ abmn, const double *__restrict__ kfac,
+                           const double *__restrict__ U, double *__restrict__ rhoa) {
+    for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < D;
+         d += (int64_t)gridDim.x * blockDim.x) {
+        const int a = abmn[4 * d], b = abmn[4 * d + 1], m = abmn[4 * d + 2], n = abmn[4 * d + 3];
+        double r = abmn_u(U, nE, a, b, m, n);
+        double rr = abmn_u(U, nE, m, n, a, b);
+        r = rint(r / 1e-10) * 1e-10;
+        rr = rint(rr / 1e-10) * 1e-10;
+        r *= kfac[d];
+        rr *= kfac[d];
+        rhoa[d] = sqrt(fabs(r * rr));
+    }
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------- drivers
+void build_mesh_device(Context &c) {
+    MeshData &m = c.mesh;
+    cudaStream_t s = c.stream;
+    m.d_xyz.upload(m.xyz, s);
+    m.d_cells.upload(m.cells, s);
+    m.d_rowptr.upload(m.rowptr, s);
+    m.d_colidx.upload(m.colidx, s);
+    std::vector<int32_t> cptr, centry, diag;
+    build_assembly_map(m, cptr, centry, diag);
+    m.d_cptr.upload(cptr, s);
+    m.d_centry.upload(centry, s);
+    m.d_diag.upload(diag, s);
+    m.d_K.alloc((size_t)m.C * m.nv * m.nv);
+    m.d_M.alloc((size_t)m.C * m.nv * m.nv);
+    k_element_matrices<<<grid1(m.C), kThreads, 0, s>>>(m.C, m.dim, m.d_xyz.p, m.d_cells.p, m.d_K.p, m.d_M.p);
+    ERTGB_CUDA(cudaGetLastError());
+    m.d_bnd_nodes.upload(m.bnd_nodes, s);
+    m.d_bnd_cell.upload(m.bnd_cell, s);
+    m.d_bnd_mass.alloc((size_t)m.B * m.nvb * m.nvb);
+    m.d_bnd_center.alloc((size_t)m.B * 3);
+    m.d_bnd_normal.alloc((size_t)m.B * 3);
+    if (m.B) {
+        k_boundary_geometry<<<grid1(m.B), kThreads, 0, s>>>(m.B, m.dim, m.d_xyz.p, m.d_bnd_nodes.p,
+                                                             m.d_bnd_mass.p, m.d_bnd_center.p,
+                                                             m.d_bnd_normal.p);
+        ERTGB_CUDA(cudaGetLastError());
+    }
+    // host copies of large maps are not kept
+    ERTGB_CUDA(cudaStreamSynchronize(s));
+}
+
+void compute_boundary_alpha(Context &c) {
+    MeshData &m = c.mesh;
+    c.d_alpha.alloc((size_t)std::max<int64_t>(m.B, 1) * c.nK);
+    if (m.B) {
+        k_boundary_alpha<<<grid1(m.B * c.nK), kThreads, 0, c.stream>>>(
+            m.B, c.nK, c.d_k.p, c.src_center[0], c.src_center[1], c.src_center[2], m.d_bnd_center.p,
+            m.d_bnd_normal.p, c.d_alpha.p);
+        ERTGB_CUDA(cudaGetLastError());
+    }
+}
+
+void compute_primary(Context &c) {
+    MeshData &m = c.mesh;
+    c.d_up.alloc((size_t)m.n * c.Rpad);
+    const int fullspace = (c.surface_z == -DBL_MAX || std::isnan(c.surface_z)) ? 1 : 0;
+    k_primary<<<grid1(m.n * c.Rpad, kThreads, 1 << 16), kThreads, 0, c.stream>>>(
+        m.n, c.nE, c.nK, c.Rpad, m.d_xyz.p, c.d_epos.p, c.d_enode.p, c.d_emin_r.p, c.d_k.p, c.surface_z,
+        fullspace, c.d_up.p);
+    ERTGB_CUDA(cudaGetLastError());
+}
+
+void assemble_all(Context &c, const double *rho_cell, double *vals, cudaStream_t s) {
+    MeshData &m = c.mesh;
+    dim3 grid(grid1(m.nnz, kThreads, 1 << 16), c.nK);
+    k_assemble<<<grid, kThreads, 0, s>>>(m.nnz, m.d_cptr.p, m.d_centry.p, m.d_K.p, m.d_M.p, m.d_bnd_mass.p,
+                                         c.d_alpha.p, m.d_bnd_cell.p, rho_cell, c.d_k.p, m.nv * m.nv,
+                                         m.nvb * m.nvb, m.C, m.B, vals);
+    ERTGB_CUDA(cudaGetLastError());
+    if (rho_cell) {
+        c.d_dinv.alloc((size_t)m.n * c.nK);
+        k_dinv<<<grid1(m.n * c.nK), kThreads, 0, s>>>(m.n, c.nK, m.nnz, m.d_diag.p, vals, c.d_dinv.p);
+        ERTGB_CUDA(cudaGetLastError());
+    }
+}
+
+void assemble_unit(Context &c, cudaStream_t s) {
+    c.d_S1.alloc((size_t)c.nK * c.mesh.nnz);
+    assemble_all(c, nullptr, c.d_S1.p, s);
+}
+
+void check_rho(Context &c, const double *rho_cell, cudaStream_t s) {
+    DBuf<int32_t> bad;
+    bad.alloc(1);
+    bad.zero(s);
+    k_check_rho<<<grid1(c.mesh.C, kThreads, 4096), kThreads, 0, s>>>(c.mesh.C, rho_cell, bad.p);
+    ERTGB_CUDA(cudaGetLastError());
+    int32_t h = 0;
+    ERTGB_CUDA(cudaMemcpyAsync(&h, bad.p, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    ERTGB_CUDA(cudaStreamSynchronize(s));
+    if (h) throw Error(ERTGB_BAD_INPUT, "response for model with negative or zero resistivity is not defined (" +
+                                            std::to_string(h) + " cells)");
+}
+
+void compute_source_rho(Context &c, const double *rho_cell, cudaStream_t s) {
+    c.d_rhos.alloc(c.nE);
+    k_source_rho<<<(unsigned)ceil_div(c.nE, 128), 128, 0, s>>>(c.nE, c.d_ecell_ptr.p, c.d_ecell.p, rho_cell,
+                                                              c.d_rhos.p);
+    ERTGB_CUDA(cudaGetLastError());
+}
+
+void build_rhs(Context &c, cudaStream_t s) {
+    MeshData &m = c.mesh;
+    k_rhs<<<grid1(m.n * 32, kThreads, 1 << 16), kThreads, 0, s>>>(m.n, m.nnz, c.nE, c.R, c.Rpad, m.d_rowptr.p,
+                                                                  m.d_colidx.p, c.d_S.p, c.d_S1.p, c.d_up.p,
+                                                                  c.d_rhos.p, c.d_r.p);
+    ERTGB_CUDA(cudaGetLastError());
+}
+
+void finish_potentials(Context &c, cudaStream_t s) {
+    MeshData &m = c.mesh;
+    k_finish_pot<<<grid1(m.n * c.Rpad, kThreads, 1 << 16), kThreads, 0, s>>>(m.n, c.nE, c.R, c.Rpad, c.d_up.p,
+                                                                             c.d_rhos.p, c.d_x.p);
+    ERTGB_CUDA(cudaGetLastError());
+}
+
+void collect_response(Context &c, double *rhoa, cudaStream_t s) {
+    c.d_U.alloc((size_t)c.nE * c.nE);
+    k_collect<<<grid1((int64_t)c.nE * c.nE), kThreads, 0, s>>>(c.nE, c.nK, c.Rpad, c.d_enode.p, c.d_w.p, c.d_x.p,
+                                                               c.d_U.p);
+    ERTGB_CUDA(cudaGetLastError());
+    k_response<<<grid1(c.D), kThreads, 0, s>>>(c.D, c.nE, c.d_abmn.p, c.d_kfac.p, c.d_U.p, rhoa);
+    ERTGB_CUDA(cudaGetLastError());
+}
+
+}  // namespace ertgb

@@ -1,0 +1,459 @@
+// C ABI of libertgb (declared in include/ertgb.h).  Every entry point
+// catches all exceptions and returns a status; messages are kept per context.
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <set>
+
+#include "ertgb_internal.cuh"
+
+using namespace ertgb;
+
+namespace {
+
+std::string g_create_error;
+
+template <class F> int guard(Context *c, F &&f) {
+    if (!c) return ERTGB_BAD_INPUT;
+    try {
+        f();
+        c->last_error.clear();
+        return ERTGB_OK;
+    } catch (Error &e) {
+        c->last_error = e.what();
+        return e.code;
+    } catch (std::exception &e) {
+        c->last_error = e.what();
+        return ERTGB_BAD_INPUT;
+    } catch (...) {
+        c->last_error = "unknown error";
+        return ERTGB_BAD_INPUT;
+    }
+}
+
+void invalidate_derived(Context &c) {
+    c.prim_ready = false;
+    c.s1_ready = false;
+    c.have_pot = false;
+}
+
+// Join the caller's stream into the context stream and back.
+struct StreamJoin {
+    Context &c;
+    cudaStream_t user;
+    StreamJoin(Context &ctx, void *stream) : c(ctx), user((cudaStream_t)stream) {
+        if (user && user != c.stream) {
+            ERTGB_CUDA(cudaEventRecord(c.ev[6], user));
+            ERTGB_CUDA(cudaStreamWaitEvent(c.stream, c.ev[6], 0));
+        }
+    }
+    void done() {
+        if (user && user != c.stream) {
+            ERTGB_CUDA(cudaEventRecord(c.ev[7], c.stream));
+            ERTGB_CUDA(cudaStreamWaitEvent(user, c.ev[7], 0));
+        }
+    }
+};
+
+void ensure_derived(Context &c) {
+    if (!c.have_mesh) throw Error(ERTGB_STATE, "no mesh set");
+    if (!c.have_elec) throw Error(ERTGB_STATE, "no electrodes set");
+    if (!c.have_kw) throw Error(ERTGB_STATE, "no wavenumbers set");
+    if (!c.have_scheme) throw Error(ERTGB_STATE, "no measurement scheme set");
+    ERTGB_CUDA(cudaSetDevice(c.device));
+    if (!c.prim_ready) {
+        c.R = (int64_t)c.nE * c.nK;
+        c.Rpad = ceil_div(c.R, 32) * 32;
+        compute_boundary_alpha(c);
+        compute_primary(c);
+        build_jacobian_tiles(c);
+        MeshData &m = c.mesh;
+        m.d_pcell_ptr.upload(m.pcell_ptr, c.stream);
+        m.d_pcell.upload(m.pcell, c.stream);
+        m.d_jtile_p.upload(m.jtile_p, c.stream);
+        c.prim_ready = true;
+        c.s1_ready = false;
+    }
+    if (!c.s1_ready) {
+        assemble_unit(c, c.stream);
+        c.s1_ready = true;
+    }
+}
+
+float elapsed(Context &c, int a, int b) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c.ev[a], c.ev[b]);
+    return ms;
+}
+
+int do_response(Context &c, const double *rho, double *rhoa, void *stream) {
+    int status = ERTGB_OK;
+    StreamJoin j(c, stream);
+    ensure_derived(c);
+    cudaStream_t s = c.stream;
+    c.have_pot = false;
+    check_rho(c, rho, s);
+    MeshData &m = c.mesh;
+    ERTGB_CUDA(cudaEventRecord(c.ev[0], s));
+    c.d_S.alloc((size_t)c.nK * m.nnz);
+    assemble_all(c, rho, c.d_S.p, s);
+    compute_source_rho(c, rho, s);
+    ERTGB_CUDA(cudaEventRecord(c.ev[1], s));
+    c.d_r.alloc((size_t)m.n * c.Rpad);
+    build_rhs(c, s);
+    ERTGB_CUDA(cudaEventRecord(c.ev[2], s));
+    status = pcg_solve(c, s);
+    ERTGB_CUDA(cudaEventRecord(c.ev[3], s));
+    finish_potentials(c, s);
+    collect_response(c, rhoa, s);
+    ERTGB_CUDA(cudaEventRecord(c.ev[4], s));
+    ERTGB_CUDA(cudaEventSynchronize(c.ev[4]));
+    c.stats.ms_assemble = elapsed(c, 0, 1);
+    c.stats.ms_rhs = elapsed(c, 1, 2);
+    c.stats.ms_solve = elapsed(c, 2, 3);
+    c.stats.ms_collect = elapsed(c, 3, 4);
+    c.have_pot = true;
+    j.done();
+    return status;
+}
+
+void do_jacobian(Context &c, const double *model, int n_model, void *J, int dtype, void *stream) {
+    if (!c.have_pot) throw Error(ERTGB_STATE, "createJacobian needs the potentials of a response first");
+    if (dtype != 0 && dtype != 1) throw Error(ERTGB_BAD_INPUT, "dtype must be 0 (FP64) or 1 (FP32)");
+    StreamJoin j(c, stream);
+    cudaStream_t s = c.stream;
+    ERTGB_CUDA(cudaEventRecord(c.ev[4], s));
+    jacobian(c, model, n_model, J, dtype, s);
+    ERTGB_CUDA(cudaEventRecord(c.ev[5], s));
+    ERTGB_CUDA(cudaEventSynchronize(c.ev[5]));
+    c.stats.ms_jacobian = elapsed(c, 4, 5);
+    j.done();
+}
+
+}  // namespace
+
+extern "C" {
+
+int ertgb_create(ertgb_ctx **out, int device) {
+    if (!out) return ERTGB_BAD_INPUT;
+    *out = nullptr;
+    Context *c = new Context();
+    int rc = guard(c, [&] {
+        c->device = device;
+        ERTGB_CUDA(cudaSetDevice(device));
+        ERTGB_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        for (auto &e : c->ev) ERTGB_CUDA(cudaEventCreate(&e));
+    });
+    if (rc != ERTGB_OK) {
+        g_create_error = c->last_error;
+        delete c;
+        return rc;
+    }
+    *out = reinterpret_cast<ertgb_ctx *>(c);
+    return ERTGB_OK;
+}
+
+int ertgb_destroy(ertgb_ctx *ctx) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    if (!c) return ERTGB_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto &e : c->ev)
+        if (e) cudaEventDestroy(e);
+    cudaStream_t s = c->stream;
+    delete c;
+    if (s) cudaStreamDestroy(s);
+    return ERTGB_OK;
+}
+
+const char *ertgb_last_error(const ertgb_ctx *ctx) {
+    const Context *c = reinterpret_cast<const Context *>(ctx);
+    if (!c) return g_create_error.c_str();
+    return c->last_error.c_str();
+}
+
+int ertgb_set_mesh(ertgb_ctx *ctx, int dim, int n_nodes, const double *xyz, int n_cells,
+                   const int32_t *cell_nodes, const int32_t *cell_marker, int n_bnd, const int32_t *bnd_nodes,
+                   const int32_t *bnd_marker, const int32_t *bnd_cell) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        ERTGB_REQUIRE(dim == 2 || dim == 3, "dim must be 2 or 3");
+        ERTGB_REQUIRE(n_nodes > 0 && n_cells > 0 && n_bnd >= 0, "empty mesh");
+        ERTGB_REQUIRE(xyz && cell_nodes && cell_marker, "null mesh array");
+        ERTGB_CUDA(cudaSetDevice(c->device));
+        c->mesh.~MeshData();  // release the previous mesh's device buffers
+        new (&c->mesh) MeshData();
+        MeshData &m = c->mesh;
+        m.dim = dim;
+        m.nv = dim + 1;
+        m.nvb = dim;
+        m.n = n_nodes;
+        m.C = n_cells;
+        m.xyz.assign(xyz, xyz + (size_t)n_nodes * 3);
+        m.cells.assign(cell_nodes, cell_nodes + (size_t)n_cells * m.nv);
+        m.marker.assign(cell_marker, cell_marker + n_cells);
+        for (int32_t v : m.cells) ERTGB_REQUIRE(v >= 0 && v < n_nodes, "cell node index out of range");
+        int32_t pmax = -1;
+        for (int32_t v : m.marker) pmax = std::max(pmax, v);
+        m.P = (int64_t)pmax + 1;
+        bool have_mixed = false;
+        for (int b = 0; b < n_bnd; b++) {
+            const int mk = bnd_marker[b];
+            if (mk == -3 || mk == -4)
+                throw Error(ERTGB_BAD_INPUT, "Dirichlet boundary markers (-3, -4) are not supported");
+            if (mk != -2) continue;
+            have_mixed = true;
+            for (int i = 0; i < m.nvb; i++) {
+                const int32_t v = bnd_nodes[(size_t)b * m.nvb + i];
+                ERTGB_REQUIRE(v >= 0 && v < n_nodes, "boundary node index out of range");
+                m.bnd_nodes.push_back(v);
+            }
+            ERTGB_REQUIRE(bnd_cell && bnd_cell[b] >= 0 && bnd_cell[b] < n_cells,
+                          "mixed boundary without an adjacent cell");
+            m.bnd_cell.push_back(bnd_cell[b]);
+        }
+        if (!have_mixed && dim == 3)
+            throw Error(ERTGB_BAD_INPUT, "Neumann-only domains (no mixed boundary) are not supported");
+        m.B = (int64_t)m.bnd_cell.size();
+        build_pattern(m);
+        build_mesh_device(*c);
+        c->have_mesh = true;
+        c->have_elec = false;
+        invalidate_derived(*c);
+    });
+}
+
+int ertgb_set_electrodes(ertgb_ctx *ctx, int n_elec, const int32_t *elec_node, double surface_z) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        if (!c->have_mesh) throw Error(ERTGB_STATE, "set the mesh before the electrodes");
+        ERTGB_REQUIRE(n_elec > 0 && elec_node, "no electrodes");
+        MeshData &m = c->mesh;
+        c->nE = n_elec;
+        c->enode.assign(elec_node, elec_node + n_elec);
+        std::set<int32_t> uniq;
+        for (int32_t v : c->enode) {
+            ERTGB_REQUIRE(v >= 0 && v < m.n, "electrode node index out of range");
+            ERTGB_REQUIRE(uniq.insert(v).second, "two electrodes on the same node");
+        }
+        c->surface_z = surface_z;
+        // source centre = mean electrode position
+        double sc[3] = {0, 0, 0};
+        std::vector<double> epos((size_t)n_elec * 3);
+        for (int e = 0; e < n_elec; e++)
+            for (int d = 0; d < 3; d++) {
+                epos[3 * e + d] = m.xyz[3 * (size_t)c->enode[e] + d];
+                sc[d] += epos[3 * e + d];
+            }
+        for (int d = 0; d < 3; d++) c->src_center[d] = sc[d] / (double)n_elec;
+        // incident cells and smallest neighbour distance per electrode node
+        std::vector<std::vector<int32_t>> inc(n_elec);
+        std::vector<int> slot(m.n, -1);
+        for (int e = 0; e < n_elec; e++) slot[c->enode[e]] = e;
+        for (int64_t cc = 0; cc < m.C; cc++)
+            for (int i = 0; i < m.nv; i++) {
+                const int e = slot[m.cells[cc * m.nv + i]];
+                if (e >= 0) inc[e].push_back((int32_t)cc);
+            }
+        c->ecell_ptr.assign(n_elec + 1, 0);
+        c->ecell.clear();
+        c->emin_r.assign(n_elec, DBL_MAX);
+        for (int e = 0; e < n_elec; e++) {
+            ERTGB_REQUIRE(!inc[e].empty(), "electrode node belongs to no cell");
+            const int32_t nd = c->enode[e];
+            for (int32_t cc : inc[e]) {
+                c->ecell.push_back(cc);
+                for (int i = 0; i < m.nv; i++) {
+                    const int32_t o = m.cells[(size_t)cc * m.nv + i];
+                    if (o == nd) continue;
+                    double d2 = 0;
+                    for (int d = 0; d < 3; d++) {
+                        const double dd = m.xyz[3 * (size_t)nd + d] - m.xyz[3 * (size_t)o + d];
+                        d2 += dd * dd;
+                    }
+                    c->emin_r[e] = std::min(c->emin_r[e], std::sqrt(d2));
+                }
+            }
+            c->ecell_ptr[e + 1] = (int32_t)c->ecell.size();
+        }
+        cudaStream_t s = c->stream;
+        c->d_enode.upload(c->enode, s);
+        c->d_epos.upload(epos, s);
+        c->d_emin_r.upload(c->emin_r, s);
+        c->d_ecell_ptr.upload(c->ecell_ptr, s);
+        c->d_ecell.upload(c->ecell, s);
+        ERTGB_CUDA(cudaStreamSynchronize(s));
+        c->have_elec = true;
+        invalidate_derived(*c);
+    });
+}
+
+int ertgb_set_kw(ertgb_ctx *ctx, int n_k, const double *k, const double *w) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        ERTGB_REQUIRE(n_k > 0 && k && w, "no wavenumbers");
+        for (int i = 0; i < n_k; i++) ERTGB_REQUIRE(k[i] >= 0.0 && std::isfinite(k[i]) && std::isfinite(w[i]),
+                                                    "wavenumbers must be finite and non-negative");
+        c->nK = n_k;
+        c->k.assign(k, k + n_k);
+        c->w.assign(w, w + n_k);
+        c->d_k.upload(c->k, c->stream);
+        c->d_w.upload(c->w, c->stream);
+        ERTGB_CUDA(cudaStreamSynchronize(c->stream));
+        c->have_kw = true;
+        invalidate_derived(*c);
+    });
+}
+
+int ertgb_set_scheme(ertgb_ctx *ctx, int n_data, const int32_t *abmn, const double *kfac) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        ERTGB_REQUIRE(n_data > 0 && abmn && kfac, "empty scheme");
+        if (!c->have_elec) throw Error(ERTGB_STATE, "set the electrodes before the scheme");
+        for (int64_t i = 0; i < 4 * (int64_t)n_data; i++)
+            ERTGB_REQUIRE(abmn[i] >= -1 && abmn[i] < c->nE, "electrode index out of range in scheme");
+        c->D = n_data;
+        c->d_abmn.upload(abmn, (size_t)4 * n_data, c->stream);
+        c->d_kfac.upload(kfac, (size_t)n_data, c->stream);
+        ERTGB_CUDA(cudaStreamSynchronize(c->stream));
+        c->have_scheme = true;
+        c->have_pot = false;
+    });
+}
+
+int ertgb_set_solver(ertgb_ctx *ctx, double rtol, int max_iter, int precond) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        ERTGB_REQUIRE(rtol > 0.0 && rtol < 1.0, "rtol must be in (0, 1)");
+        ERTGB_REQUIRE(max_iter > 0, "max_iter must be positive");
+        ERTGB_REQUIRE(precond == ERTGB_PRECOND_JACOBI, "unknown preconditioner");
+        c->rtol = rtol;
+        c->max_iter = max_iter;
+        c->precond = precond;
+    });
+}
+
+int ertgb_response(ertgb_ctx *ctx, const double *rho_cell_dev, double *rhoa_dev, void *stream) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    int status = ERTGB_OK;
+    int rc = guard(c, [&] {
+        ERTGB_REQUIRE(rho_cell_dev && rhoa_dev, "null buffer");
+        status = do_response(*c, rho_cell_dev, rhoa_dev, stream);
+        if (status == ERTGB_NOT_CONVERGED) throw Error(ERTGB_NOT_CONVERGED, "PCG did not converge");
+    });
+    return rc;
+}
+
+int ertgb_response_host(ertgb_ctx *ctx, const double *rho_cell, double *rhoa) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        ERTGB_REQUIRE(rho_cell && rhoa, "null buffer");
+        if (!c->have_mesh || !c->have_scheme) throw Error(ERTGB_STATE, "mesh and scheme needed");
+        ERTGB_CUDA(cudaSetDevice(c->device));
+        c->d_rho_tmp.upload(rho_cell, (size_t)c->mesh.C, c->stream);
+        c->d_rhoa.alloc((size_t)c->D);
+        int st = do_response(*c, c->d_rho_tmp.p, c->d_rhoa.p, nullptr);
+        ERTGB_CUDA(cudaMemcpyAsync(rhoa, c->d_rhoa.p, sizeof(double) * c->D, cudaMemcpyDeviceToHost, c->stream));
+        ERTGB_CUDA(cudaStreamSynchronize(c->stream));
+        if (st == ERTGB_NOT_CONVERGED) throw Error(ERTGB_NOT_CONVERGED, "PCG did not converge");
+    });
+}
+
+int ertgb_jacobian(ertgb_ctx *ctx, const double *model_dev, int n_model, void *J_dev, int dtype, void *stream) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        ERTGB_REQUIRE(J_dev, "null buffer");
+        ERTGB_REQUIRE(n_model == 0 || model_dev, "null model");
+        do_jacobian(*c, model_dev, n_model, J_dev, dtype, stream);
+    });
+}
+
+int ertgb_jacobian_host(ertgb_ctx *ctx, const double *model, int n_model, void *J, int dtype) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        ERTGB_REQUIRE(J, "null buffer");
+        ERTGB_CUDA(cudaSetDevice(c->device));
+        const double *md = nullptr;
+        if (n_model > 0) {
+            ERTGB_REQUIRE(model, "null model");
+            c->d_model_tmp.upload(model, (size_t)n_model, c->stream);
+            md = c->d_model_tmp.p;
+        }
+        const size_t bytes = (size_t)c->D * c->mesh.P * (dtype == 0 ? 8 : 4);
+        c->d_J_tmp.alloc(bytes);
+        do_jacobian(*c, md, n_model, c->d_J_tmp.p, dtype, nullptr);
+        ERTGB_CUDA(cudaMemcpyAsync(J, c->d_J_tmp.p, bytes, cudaMemcpyDeviceToHost, c->stream));
+        ERTGB_CUDA(cudaStreamSynchronize(c->stream));
+    });
+}
+
+int ertgb_sizes(const ertgb_ctx *ctx, int64_t *n_nodes, int64_t *nnz, int64_t *n_param, int64_t *n_rhs) {
+    const Context *c = reinterpret_cast<const Context *>(ctx);
+    if (!c) return ERTGB_BAD_INPUT;
+    if (n_nodes) *n_nodes = c->mesh.n;
+    if (nnz) *nnz = c->mesh.nnz;
+    if (n_param) *n_param = c->mesh.P;
+    if (n_rhs) *n_rhs = (int64_t)c->nE * c->nK;
+    return ERTGB_OK;
+}
+
+int ertgb_get_pattern(ertgb_ctx *ctx, int32_t *rowptr, int32_t *colidx) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        if (!c->have_mesh) throw Error(ERTGB_STATE, "no mesh");
+        if (rowptr) std::memcpy(rowptr, c->mesh.rowptr.data(), sizeof(int32_t) * c->mesh.rowptr.size());
+        if (colidx) std::memcpy(colidx, c->mesh.colidx.data(), sizeof(int32_t) * c->mesh.colidx.size());
+    });
+}
+
+int ertgb_get_matrix(ertgb_ctx *ctx, int k_index, int which, double *vals) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        ERTGB_REQUIRE(k_index >= 0 && k_index < c->nK && vals, "bad k index");
+        const DBuf<double> &src = which == 0 ? c->d_S : c->d_S1;
+        if (src.n < (size_t)c->nK * c->mesh.nnz) throw Error(ERTGB_STATE, "matrix not assembled yet");
+        ERTGB_CUDA(cudaMemcpy(vals, src.p + (size_t)k_index * c->mesh.nnz, sizeof(double) * c->mesh.nnz,
+                              cudaMemcpyDeviceToHost));
+    });
+}
+
+static void copy_blocked(Context &c, const double *dev, double *host) {
+    const int64_t n = c.mesh.n;
+    std::vector<double> tmp((size_t)n * c.Rpad);
+    ERTGB_CUDA(cudaMemcpy(tmp.data(), dev, sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost));
+    for (int ki = 0; ki < c.nK; ki++)
+        for (int e = 0; e < c.nE; e++) {
+            double *o = host + ((size_t)ki * c.nE + e) * n;
+            const int64_t t = (int64_t)ki * c.nE + e;
+            for (int64_t i = 0; i < n; i++) o[i] = tmp[(size_t)i * c.Rpad + t];
+        }
+}
+
+int ertgb_get_potentials(ertgb_ctx *ctx, double *pot) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        if (!c->have_pot) throw Error(ERTGB_STATE, "no potentials yet");
+        ERTGB_REQUIRE(pot, "null buffer");
+        copy_blocked(*c, c->d_x.p, pot);
+    });
+}
+
+int ertgb_get_primary(ertgb_ctx *ctx, double *prim) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        ERTGB_REQUIRE(prim, "null buffer");
+        ensure_derived(*c);
+        ERTGB_CUDA(cudaStreamSynchronize(c->stream));
+        copy_blocked(*c, c->d_up.p, prim);
+    });
+}
+
+int ertgb_get_stats(const ertgb_ctx *ctx, ertgb_stats *stats) {
+    const Context *c = reinterpret_cast<const Context *>(ctx);
+    if (!c || !stats) return ERTGB_BAD_INPUT;
+    *stats = c->stats;
+    return ERTGB_OK;
+}
+
+}  // extern "C"

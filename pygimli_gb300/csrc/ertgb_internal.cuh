@@ -1,0 +1,171 @@
+// Internal definitions of libertgb: the context, device buffers and the
+// kernel launchers shared between translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/ertgb.h"
+
+namespace ertgb {
+
+// Error carried across the C ABI as a status code plus message.
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+#define ERTGB_CUDA(call)                                                                   \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess) {                                                           \
+            if (e_ == cudaErrorMemoryAllocation)                                           \
+                throw ::ertgb::Error(ERTGB_OOM, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+            throw ::ertgb::Error(ERTGB_CUDA_ERROR, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+        }                                                                                  \
+    } while (0)
+
+#define ERTGB_REQUIRE(cond, msg)                                                           \
+    do {                                                                                   \
+        if (!(cond)) throw ::ertgb::Error(ERTGB_BAD_INPUT, msg);                           \
+    } while (0)
+
+// Owning device buffer (raw cudaMalloc; the library's own workspaces).
+template <class T> struct DBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf &) = delete;
+    DBuf &operator=(const DBuf &) = delete;
+    ~DBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void alloc(size_t count) {
+        if (count == n && p) return;
+        release();
+        if (count == 0) return;
+        ERTGB_CUDA(cudaMalloc(&p, count * sizeof(T)));
+        n = count;
+    }
+    void upload(const T *h, size_t count, cudaStream_t s) {
+        alloc(count);
+        if (count) ERTGB_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+    void upload(const std::vector<T> &h, cudaStream_t s) { upload(h.data(), h.size(), s); }
+    void zero(cudaStream_t s) {
+        if (n) ERTGB_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+    }
+};
+
+// Mesh-dependent structures.
+struct MeshData {
+    int dim = 0, nv = 0, nvb = 0;
+    int64_t n = 0, C = 0, B = 0;  // nodes, cells, mixed boundaries
+    int64_t nnz = 0;
+    int64_t P = 0;                // parameters = max(cell marker) + 1
+    std::vector<double> xyz;      // host copy (n x 3)
+    std::vector<int32_t> cells;   // C x nv
+    std::vector<int32_t> marker;  // C
+    std::vector<int32_t> rowptr, colidx;
+    std::vector<int32_t> bnd_nodes, bnd_cell;  // mixed boundaries only
+    // device
+    DBuf<double> d_xyz;
+    DBuf<int32_t> d_cells, d_rowptr, d_colidx, d_diag;
+    DBuf<int32_t> d_cptr, d_centry;  // per-slot contribution lists
+    DBuf<double> d_K, d_M;           // per-cell element matrices (C x nv*nv)
+    DBuf<int32_t> d_bnd_nodes, d_bnd_cell;
+    DBuf<double> d_bnd_mass, d_bnd_center, d_bnd_normal;  // B x nvb^2, B x 3, B x 3
+    // parameter -> cells (sorted by parameter), for the Jacobian
+    std::vector<int32_t> pcell_ptr, pcell;
+    DBuf<int32_t> d_pcell_ptr, d_pcell;
+    std::vector<int32_t> jtile_p;  // Jacobian tiles: parameter boundaries
+    DBuf<int32_t> d_jtile_p;
+    int jtile_cells_max = 0;
+};
+
+struct Context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[8];
+    std::string last_error;
+    MeshData mesh;
+    bool have_mesh = false;
+    // electrodes
+    int nE = 0;
+    std::vector<int32_t> enode;
+    double surface_z = 0.0;
+    double src_center[3] = {0, 0, 0};
+    std::vector<double> emin_r;              // singular radius per electrode
+    std::vector<int32_t> ecell_ptr, ecell;   // incident cells per electrode
+    DBuf<int32_t> d_enode, d_ecell_ptr, d_ecell;
+    DBuf<double> d_emin_r, d_epos;
+    bool have_elec = false;
+    // wavenumbers
+    int nK = 0;
+    std::vector<double> k, w;
+    DBuf<double> d_k, d_w;
+    bool have_kw = false;
+    // scheme
+    int64_t D = 0;
+    DBuf<int32_t> d_abmn;
+    DBuf<double> d_kfac;
+    bool have_scheme = false;
+    // solver
+    double rtol = 1e-10;
+    int max_iter = 20000;
+    int precond = ERTGB_PRECOND_JACOBI;
+    // derived per (mesh, electrodes, kw)
+    int64_t R = 0, Rpad = 0;     // right-hand sides nK*nE, padded to 32
+    bool prim_ready = false;
+    DBuf<double> d_alpha;         // nK x B mixed-boundary coefficients
+    DBuf<double> d_up;            // unit primary potential  n x Rpad
+    DBuf<double> d_S1;            // nK x nnz (unit resistivity)
+    bool s1_ready = false;
+    // per response
+    DBuf<double> d_S;             // nK x nnz
+    DBuf<double> d_dinv;          // nK x n  (1 / diag)
+    DBuf<double> d_rhos;          // nE source resistivity
+    DBuf<double> d_x, d_r, d_p, d_q, d_b;  // n x Rpad
+    DBuf<double> d_part;          // reduction partials
+    DBuf<double> d_col;           // per-column scalars (see pcg.cu)
+    DBuf<int32_t> d_active;
+    DBuf<double> d_U;             // nE x nE collected electrode potentials
+    DBuf<double> d_rhoa;
+    bool have_pot = false;
+    DBuf<double> d_rho_tmp, d_model_tmp;
+    DBuf<char> d_J_tmp;
+    ertgb_stats stats{};
+};
+
+// --- launchers (defined in the .cu files) -----------------------------------
+// assemble.cu
+void build_mesh_device(Context &c);
+void compute_boundary_alpha(Context &c);
+void compute_primary(Context &c);
+void assemble_all(Context &c, const double *rho_cell, double *vals_out, cudaStream_t s);
+void assemble_unit(Context &c, cudaStream_t s);
+void compute_source_rho(Context &c, const double *rho_cell, cudaStream_t s);
+void build_rhs(Context &c, cudaStream_t s);
+void finish_potentials(Context &c, cudaStream_t s);
+void collect_response(Context &c, double *rhoa, cudaStream_t s);
+void check_rho(Context &c, const double *rho_cell, cudaStream_t s);
+// pcg.cu
+int pcg_solve(Context &c, cudaStream_t s);
+// jacobian.cu
+void jacobian(Context &c, const double *model, int n_model, void *J, int dtype, cudaStream_t s);
+// setup.cpp
+void build_pattern(MeshData &m);
+void build_assembly_map(MeshData &m, std::vector<int32_t> &cptr, std::vector<int32_t> &centry,
+                        std::vector<int32_t> &diag);
+void build_jacobian_tiles(Context &c);
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+}  // namespace ertgb

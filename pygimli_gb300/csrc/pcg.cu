@@ -1,0 +1,350 @@
+// Multi-right-hand-side preconditioned conjugate gradients (FP64).
+//
+// Replaces the reference's direct solve (CHOLMOD factor per wavenumber, one
+// triangular solve per current source: core/src/bert/dcfemmodelling.cpp:
+// 2199-2210 and 2285; core/src/cholmodWrapper.cpp:309-420).  All sources of
+// all wavenumbers are solved together: the iterate blocks are n x Rpad,
+// node-major, column t = k*nE + e uses the matrix of wavenumber k.  Every
+// column runs its own CG recurrence (own alpha, beta) and stops when
+// ||r_t|| <= rtol ||b_t||; reductions are deterministic (fixed-order block
+// partials, no atomics on values).
+//
+// One iteration = 5 kernels:
+//   spmm_dot      q = A p (warp per row, lanes over columns) + partial p.q
+//   finish_alpha  alpha_t = rho_t / (p.q)_t
+//   update_xr     x += alpha p, r -= alpha q, partial r.z and r.r (z = D^-1 r)
+//   finish_beta   convergence test, beta_t = (r.z)_t / rho_t
+//   update_p      p = D^-1 r + beta p
+// A chunk of iterations is captured once into a CUDA graph and replayed; the
+// host reads the count of active columns after each replay.  The iteration
+// cap bounds the loop, so the solve never waits on the device indefinitely.
+#include <algorithm>
+#include <cmath>
+
+#include "ertgb_internal.cuh"
+
+namespace ertgb {
+
+namespace {
+
+constexpr int kRowsPerBlock = 8;  // warps per block in spmm, rows per block in vector kernels
+constexpr int kGraphIters = 16;
+
+// per-column scalar slots in Context::d_col
+enum Col { RHO = 0, ALPHA, BETA, BNORM2, RNORM2, PQ, NCOL };
+
+template <int CH>
+__global__ void __launch_bounds__(256) k_spmm_dot(int64_t n, int64_t nnz, int nE, int nK, int64_t Rpad,
+                                                  const int32_t *__restrict__ rowptr,
+                                                  const int32_t *__restrict__ colidx,
+                                                  const double *__restrict__ vals,
+                                                  const double *__restrict__ p, double *__restrict__ q,
+                                                  double *__restrict__ part) {
+    __shared__ double red[kRowsPerBlock][32 * CH];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t t0 = (int64_t)blockIdx.y * 32 * CH + lane;
+    int64_t kofs[CH];  // value-array offset of each column's wavenumber (padding -> last)
+#pragma unroll
+    for (int j = 0; j < CH; j++) kofs[j] = min((t0 + 32 * j) / nE, (int64_t)nK - 1) * nnz;
+    double dot[CH];
+#pragma unroll
+    for (int j = 0; j < CH; j++) dot[j] = 0.0;
+    for (int64_t row = (int64_t)blockIdx.x * kRowsPerBlock + wid; row < n;
+         row += (int64_t)gridDim.x * kRowsPerBlock) {
+        double acc[CH];
+#pragma unroll
+        for (int j = 0; j < CH; j++) acc[j] = 0.0;
+        const int32_t s1 = rowptr[row + 1];
+        for (int32_t s = rowptr[row]; s < s1; s++) {
+            const int64_t col = colidx[s];
+            const double *pc = p + col * Rpad + t0;
+#pragma unroll
+            for (int j = 0; j < CH; j++) acc[j] = fma(vals[kofs[j] + s], pc[32 * j], acc[j]);
+        }
+        double *qr = q + row * Rpad + t0;
+        const double *pr = p + row * Rpad + t0;
+#pragma unroll
+        for (int j = 0; j < CH; j++) {
+            qr[32 * j] = acc[j];
+            dot[j] = fma(pr[32 * j], acc[j], dot[j]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < CH; j++) red[wid][lane + 32 * j] = dot[j];
+    __syncthreads();
+    for (int c = threadIdx.x; c < 32 * CH; c += blockDim.x) {
+        double s = 0.0;
+#pragma unroll
+        for (int w = 0; w < kRowsPerBlock; w++) s += red[w][c];
+        part[(int64_t)blockIdx.x * Rpad + (int64_t)blockIdx.y * 32 * CH + c] = s;
+    }
+}
+
+// Vector kernels: block (32, 8), grid (Rpad/32, NB); thread column t, rows
+// strided by 8*NB.  part_a / part_b receive per-block column partials.
+__global__ void k_init(int64_t n, int nE, int nK, int64_t R, int64_t Rpad, const double *__restrict__ dinv,
+                       const double *__restrict__ r, double *__restrict__ p, double *__restrict__ part_a,
+                       double *__restrict__ part_b) {
+    __shared__ double sa[kRowsPerBlock][32], sb[kRowsPerBlock][32];
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    const int64_t ki = t < R ? t / nE : 0;
+    const double *dk = dinv + ki * n;
+    double a = 0.0, b = 0.0;
+    for (int64_t row = (int64_t)blockIdx.y * kRowsPerBlock + threadIdx.y; row < n;
+         row += (int64_t)gridDim.y * kRowsPerBlock) {
+        const int64_t i = row * Rpad + t;
+        const double rv = r[i];
+        const double z = t < R ? rv * dk[row] : 0.0;
+        p[i] = z;
+        a = fma(rv, z, a);
+        b = fma(rv, rv, b);
+    }
+    sa[threadIdx.y][threadIdx.x] = a;
+    sb[threadIdx.y][threadIdx.x] = b;
+    __syncthreads();
+    if (threadIdx.y == 0) {
+        double s1 = 0.0, s2 = 0.0;
+        for (int w = 0; w < kRowsPerBlock; w++) {
+            s1 += sa[w][threadIdx.x];
+            s2 += sb[w][threadIdx.x];
+        }
+        part_a[(int64_t)blockIdx.y * Rpad + t] = s1;
+        part_b[(int64_t)blockIdx.y * Rpad + t] = s2;
+    }
+}
+
+__global__ void k_finish_init(int64_t Rpad, int64_t R, int NB, const double *__restrict__ part_a,
+                              const double *__restrict__ part_b, double *__restrict__ col,
+                              int32_t *__restrict__ active, int32_t *__restrict__ iters,
+                              int32_t *__restrict__ nactive) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < Rpad;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        double rz = 0.0, rr = 0.0;
+        for (int b = 0; b < NB; b++) {
+            rz += part_a[(int64_t)b * Rpad + t];
+            rr += part_b[(int64_t)b * Rpad + t];
+        }
+        col[RHO * Rpad + t] = rz;
+        col[BNORM2 * Rpad + t] = rr;
+        col[RNORM2 * Rpad + t] = rr;
+        col[ALPHA * Rpad + t] = 0.0;
+        col[BETA * Rpad + t] = 0.0;
+        const int a = (t < R && rr > 0.0) ? 1 : 0;
+        active[t] = a;
+        iters[t] = 0;
+        if (a) atomicAdd(nactive, 1);
+    }
+}
+
+__global__ void k_finish_alpha(int64_t Rpad, int NB, const double *__restrict__ part,
+                               double *__restrict__ col, const int32_t *__restrict__ active,
+                               int32_t *__restrict__ nactive) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *nactive = 0;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < Rpad;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        if (!active[t]) continue;
+        double pq = 0.0;
+        for (int b = 0; b < NB; b++) pq += part[(int64_t)b * Rpad + t];
+        col[PQ * Rpad + t] = pq;
+        col[ALPHA * Rpad + t] = (pq != 0.0) ? col[RHO * Rpad + t] / pq : 0.0;
+    }
+}
+
+__global__ void k_update_xr(int64_t n, int nE, int64_t R, int64_t Rpad, const double *__restrict__ dinv,
+                            const double *__restrict__ col, const int32_t *__restrict__ active,
+                            double *__restrict__ x, double *__restrict__ r, const double *__restrict__ p,
+                            const double *__restrict__ q, double *__restrict__ part_a,
+                            double *__restrict__ part_b) {
+    __shared__ double sa[kRowsPerBlock][32], sb[kRowsPerBlock][32];
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    const bool act = active[t] != 0;
+    const double alpha = col[ALPHA * Rpad + t];
+    const int64_t ki = t < R ? t / nE : 0;
+    const double *dk = dinv + ki * n;
+    double a = 0.0, b = 0.0;
+    if (act) {
+        for (int64_t row = (int64_t)blockIdx.y * kRowsPerBlock + threadIdx.y; row < n;
+             row += (int64_t)gridDim.y * kRowsPerBlock) {
+            const int64_t i = row * Rpad + t;
+            x[i] = fma(alpha, p[i], x[i]);
+            const double rv = fma(-alpha, q[i], r[i]);
+            r[i] = rv;
+            a = fma(rv, rv * dk[row], a);
+            b = fma(rv, rv, b);
+        }
+    }
+    sa[threadIdx.y][threadIdx.x] = a;
+    sb[threadIdx.y][threadIdx.x] = b;
+    __syncthreads();
+    if (threadIdx.y == 0) {
+        double s1 = 0.0, s2 = 0.0;
+        for (int w = 0; w < kRowsPerBlock; w++) {
+            s1 += sa[w][threadIdx.x];
+            s2 += sb[w][threadIdx.x];
+        }
+        part_a[(int64_t)blockIdx.y * Rpad + t] = s1;
+        part_b[(int64_t)blockIdx.y * Rpad + t] = s2;
+    }
+}
+
+__global__ void k_finish_beta(int64_t Rpad, int NB, double rtol2, const double *__restrict__ part_a,
+                              const double *__restrict__ part_b, double *__restrict__ col,
+                              int32_t *__restrict__ active, int32_t *__restrict__ iters,
+                              int32_t *__restrict__ nactive) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < Rpad;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        if (!active[t]) {
+            col[BETA * Rpad + t] = 0.0;
+            continue;
+        }
+        double rz = 0.0, rr = 0.0;
+        for (int b = 0; b < NB; b++) {
+            rz += part_a[(int64_t)b * Rpad + t];
+            rr += part_b[(int64_t)b * Rpad + t];
+        }
+        iters[t] += 1;
+        col[RNORM2 * Rpad + t] = rr;
+        const double rho = col[RHO * Rpad + t];
+        col[BETA * Rpad + t] = (rho != 0.0) ? rz / rho : 0.0;
+        col[RHO * Rpad + t] = rz;
+        if (rr <= rtol2 * col[BNORM2 * Rpad + t] || !(rr == rr)) {
+            active[t] = 0;
+        } else {
+            atomicAdd(nactive, 1);
+        }
+    }
+}
+
+__global__ void k_update_p(int64_t n, int nE, int64_t R, int64_t Rpad, const double *__restrict__ dinv,
+                           const double *__restrict__ col, const int32_t *__restrict__ active,
+                           const double *__restrict__ r, double *__restrict__ p) {
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    if (!active[t]) return;
+    const double beta = col[BETA * Rpad + t];
+    const int64_t ki = t < R ? t / nE : 0;
+    const double *dk = dinv + ki * n;
+    for (int64_t row = (int64_t)blockIdx.y * kRowsPerBlock + threadIdx.y; row < n;
+         row += (int64_t)gridDim.y * kRowsPerBlock) {
+        const int64_t i = row * Rpad + t;
+        p[i] = fma(beta, p[i], r[i] * dk[row]);
+    }
+}
+
+int choose_ch(int64_t Rpad) {
+    const int64_t w = Rpad / 32;
+    for (int ch : {4, 3, 2}) {
+        if (w % ch == 0) return ch;
+    }
+    return 1;
+}
+
+void launch_spmm(int ch, dim3 grid, cudaStream_t s, int64_t n, int64_t nnz, int nE, int nK, int64_t Rpad,
+                 const int32_t *rowptr, const int32_t *colidx, const double *vals, const double *p, double *q,
+                 double *part) {
+    switch (ch) {
+        case 4: k_spmm_dot<4><<<grid, 256, 0, s>>>(n, nnz, nE, nK, Rpad, rowptr, colidx, vals, p, q, part); break;
+        case 3: k_spmm_dot<3><<<grid, 256, 0, s>>>(n, nnz, nE, nK, Rpad, rowptr, colidx, vals, p, q, part); break;
+        case 2: k_spmm_dot<2><<<grid, 256, 0, s>>>(n, nnz, nE, nK, Rpad, rowptr, colidx, vals, p, q, part); break;
+        default: k_spmm_dot<1><<<grid, 256, 0, s>>>(n, nnz, nE, nK, Rpad, rowptr, colidx, vals, p, q, part); break;
+    }
+}
+
+}  // namespace
+
+int pcg_solve(Context &c, cudaStream_t s) {
+    MeshData &m = c.mesh;
+    const int64_t n = m.n, Rpad = c.Rpad, R = c.R;
+    const int NB = (int)std::min<int64_t>(ceil_div(n, kRowsPerBlock), 1184);
+    const int ch = choose_ch(Rpad);
+    const int nchunk = (int)(Rpad / (32 * ch));
+    // workspaces
+    c.d_x.alloc((size_t)n * Rpad);
+    c.d_p.alloc((size_t)n * Rpad);
+    c.d_q.alloc((size_t)n * Rpad);
+    c.d_part.alloc((size_t)NB * Rpad * 3);
+    c.d_col.alloc((size_t)NCOL * Rpad);
+    c.d_active.alloc((size_t)Rpad * 2 + 1);
+    double *part_a = c.d_part.p, *part_b = c.d_part.p + (size_t)NB * Rpad, *part_c = c.d_part.p + 2 * (size_t)NB * Rpad;
+    int32_t *active = c.d_active.p, *iters = c.d_active.p + Rpad, *nactive = c.d_active.p + 2 * Rpad;
+    ERTGB_CUDA(cudaMemsetAsync(c.d_x.p, 0, sizeof(double) * n * Rpad, s));
+    ERTGB_CUDA(cudaMemsetAsync(nactive, 0, sizeof(int32_t), s));
+    const dim3 vb(32, kRowsPerBlock), vg((unsigned)(Rpad / 32), (unsigned)NB);
+    const dim3 sg((unsigned)NB, (unsigned)nchunk);
+    const unsigned fg = (unsigned)ceil_div(Rpad, 256);
+    const double rtol2 = c.rtol * c.rtol;
+    k_init<<<vg, vb, 0, s>>>(n, c.nE, c.nK, R, Rpad, c.d_dinv.p, c.d_r.p, c.d_p.p, part_a, part_b);
+    k_finish_init<<<fg, 256, 0, s>>>(Rpad, R, NB, part_a, part_b, c.d_col.p, active, iters, nactive);
+    ERTGB_CUDA(cudaGetLastError());
+
+    // capture a chunk of iterations
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    ERTGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    for (int it = 0; it < kGraphIters; it++) {
+        launch_spmm(ch, sg, s, n, m.nnz, c.nE, c.nK, Rpad, m.d_rowptr.p, m.d_colidx.p, c.d_S.p, c.d_p.p, c.d_q.p,
+                    part_c);
+        k_finish_alpha<<<fg, 256, 0, s>>>(Rpad, NB, part_c, c.d_col.p, active, nactive);
+        k_update_xr<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, c.d_dinv.p, c.d_col.p, active, c.d_x.p, c.d_r.p,
+                                      c.d_p.p, c.d_q.p, part_a, part_b);
+        k_finish_beta<<<fg, 256, 0, s>>>(Rpad, NB, rtol2, part_a, part_b, c.d_col.p, active, iters, nactive);
+        k_update_p<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, c.d_dinv.p, c.d_col.p, active, c.d_r.p, c.d_p.p);
+    }
+    cudaError_t cap = cudaStreamEndCapture(s, &graph);
+    if (cap != cudaSuccess) ERTGB_CUDA(cap);
+    cudaError_t inst = cudaGraphInstantiate(&exec, graph, 0);
+    if (inst != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        ERTGB_CUDA(inst);
+    }
+    int32_t h_active = 0;
+    int iterations = 0;
+    int status = ERTGB_OK;
+    ERTGB_CUDA(cudaMemcpyAsync(&h_active, nactive, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    ERTGB_CUDA(cudaStreamSynchronize(s));
+    try {
+        while (h_active > 0) {
+            if (iterations >= c.max_iter) {
+                status = ERTGB_NOT_CONVERGED;
+                break;
+            }
+            ERTGB_CUDA(cudaGraphLaunch(exec, s));
+            iterations += kGraphIters;
+            ERTGB_CUDA(cudaMemcpyAsync(&h_active, nactive, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+            ERTGB_CUDA(cudaStreamSynchronize(s));
+        }
+    } catch (...) {
+        cudaGraphExecDestroy(exec);
+        cudaGraphDestroy(graph);
+        throw;
+    }
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    // statistics: exact iteration count and final relative residual
+    std::vector<int32_t> it_h(Rpad);
+    std::vector<double> rn(Rpad), bn(Rpad);
+    ERTGB_CUDA(cudaMemcpyAsync(it_h.data(), iters, sizeof(int32_t) * Rpad, cudaMemcpyDeviceToHost, s));
+    ERTGB_CUDA(cudaMemcpyAsync(rn.data(), c.d_col.p + RNORM2 * Rpad, sizeof(double) * Rpad, cudaMemcpyDeviceToHost, s));
+    ERTGB_CUDA(cudaMemcpyAsync(bn.data(), c.d_col.p + BNORM2 * Rpad, sizeof(double) * Rpad, cudaMemcpyDeviceToHost, s));
+    ERTGB_CUDA(cudaStreamSynchronize(s));
+    int maxit = 0;
+    double maxres = 0.0;
+    bool finite = true;
+    for (int64_t t = 0; t < R; t++) {
+        maxit = std::max(maxit, it_h[t]);
+        if (bn[t] > 0) {
+            const double rel = std::sqrt(rn[t] / bn[t]);
+            if (!std::isfinite(rel)) finite = false;
+            else maxres = std::max(maxres, rel);
+        }
+    }
+    if (!finite) {
+        status = ERTGB_NOT_CONVERGED;
+        maxres = NAN;
+    }
+    c.stats.iterations = maxit;
+    c.stats.n_rhs = (int32_t)R;
+    c.stats.max_rel_residual = maxres;
+    return status;
+}
+
+}  // namespace ertgb

@@ -1,0 +1,141 @@
+// Host-side setup of libertgb: CSR sparsity pattern, the conflict-free
+// per-slot assembly map and the Jacobian parameter tiles.
+//
+// Pattern: same content and order as SparseMatrix::buildSparsityPattern
+// (core/src/sparsematrix.h:966-1024): for every node the set of nodes that
+// share a cell with it, diagonal included, rows and columns ascending, int32.
+//
+// Assembly map: for every CSR slot the list of element-matrix entries that
+// land on it, cell entries first in ascending cell order, then mixed-boundary
+// entries in ascending boundary order.  A gather over this list sums in the
+// same order as the reference's scatter (SparseMatrix::add over cells,
+// core/src/sparsematrix.cpp:247-266, then over boundaries), with no atomics.
+#include <algorithm>
+#include <cstring>
+
+#include "ertgb_internal.cuh"
+
+namespace ertgb {
+
+void build_pattern(MeshData &m) {
+    const int64_t n = m.n, C = m.C;
+    const int nv = m.nv;
+    // node -> cells
+    std::vector<int64_t> nc_ptr(n + 1, 0);
+    for (int64_t c = 0; c < C; c++)
+        for (int i = 0; i < nv; i++) nc_ptr[m.cells[c * nv + i] + 1]++;
+    for (int64_t i = 0; i < n; i++) nc_ptr[i + 1] += nc_ptr[i];
+    std::vector<int32_t> nc(nc_ptr[n]);
+    {
+        std::vector<int64_t> pos(nc_ptr.begin(), nc_ptr.end() - 1);
+        for (int64_t c = 0; c < C; c++)
+            for (int i = 0; i < nv; i++) nc[pos[m.cells[c * nv + i]]++] = (int32_t)c;
+    }
+    // rows
+    m.rowptr.assign(n + 1, 0);
+    std::vector<int32_t> mark(n, -1);
+    std::vector<int32_t> row;
+    std::vector<int32_t> cols;
+    cols.reserve((size_t)C * nv * 4);
+    for (int64_t r = 0; r < n; r++) {
+        row.clear();
+        for (int64_t q = nc_ptr[r]; q < nc_ptr[r + 1]; q++) {
+            const int32_t *cn = &m.cells[(int64_t)nc[q] * nv];
+            for (int i = 0; i < nv; i++) {
+                if (mark[cn[i]] != (int32_t)r) {
+                    mark[cn[i]] = (int32_t)r;
+                    row.push_back(cn[i]);
+                }
+            }
+        }
+        if (row.empty()) throw Error(ERTGB_BAD_INPUT, "mesh has a node that belongs to no cell");
+        std::sort(row.begin(), row.end());
+        cols.insert(cols.end(), row.begin(), row.end());
+        if (cols.size() > (size_t)INT32_MAX) throw Error(ERTGB_BAD_INPUT, "matrix too large for int32 indices");
+        m.rowptr[r + 1] = (int32_t)cols.size();
+    }
+    m.colidx.swap(cols);
+    m.nnz = (int64_t)m.colidx.size();
+}
+
+namespace {
+inline int32_t find_slot(const MeshData &m, int32_t r, int32_t c) {
+    const int32_t *b = m.colidx.data() + m.rowptr[r];
+    const int32_t *e = m.colidx.data() + m.rowptr[r + 1];
+    const int32_t *it = std::lower_bound(b, e, c);
+    if (it == e || *it != c) throw Error(ERTGB_BAD_INPUT, "boundary facet not part of any cell");
+    return (int32_t)(it - m.colidx.data());
+}
+}  // namespace
+
+// Per-slot contribution lists (host) -> cptr (nnz+1), centry.
+void build_assembly_map(MeshData &m, std::vector<int32_t> &cptr, std::vector<int32_t> &centry,
+                        std::vector<int32_t> &diag) {
+    const int nv = m.nv, nvb = m.nvb;
+    const int64_t C = m.C, B = m.B;
+    if ((double)C * nv * nv + (double)B * nvb * nvb > (double)INT32_MAX)
+        throw Error(ERTGB_BAD_INPUT, "mesh too large for int32 assembly entries");
+    std::vector<int32_t> cell_slot((size_t)C * nv * nv);
+    for (int64_t c = 0; c < C; c++) {
+        const int32_t *cn = &m.cells[c * nv];
+        for (int i = 0; i < nv; i++)
+            for (int j = 0; j < nv; j++) cell_slot[(c * nv + i) * nv + j] = find_slot(m, cn[i], cn[j]);
+    }
+    std::vector<int32_t> bnd_slot((size_t)B * nvb * nvb);
+    for (int64_t b = 0; b < B; b++) {
+        const int32_t *bn = &m.bnd_nodes[b * nvb];
+        for (int i = 0; i < nvb; i++)
+            for (int j = 0; j < nvb; j++) bnd_slot[(b * nvb + i) * nvb + j] = find_slot(m, bn[i], bn[j]);
+    }
+    cptr.assign(m.nnz + 1, 0);
+    for (int32_t s : cell_slot) cptr[s + 1]++;
+    for (int32_t s : bnd_slot) cptr[s + 1]++;
+    for (int64_t i = 0; i < m.nnz; i++) cptr[i + 1] += cptr[i];
+    centry.assign(cptr[m.nnz], 0);
+    std::vector<int32_t> pos(cptr.begin(), cptr.end() - 1);
+    const int32_t nv2 = nv * nv, nvb2 = nvb * nvb;
+    for (int64_t e = 0; e < C * nv2; e++) centry[pos[cell_slot[e]]++] = (int32_t)e;
+    const int32_t base = (int32_t)(C * nv2);
+    for (int64_t e = 0; e < B * nvb2; e++) centry[pos[bnd_slot[e]]++] = base + (int32_t)e;
+    diag.resize(m.n);
+    for (int64_t r = 0; r < m.n; r++) diag[r] = find_slot(m, (int32_t)r, (int32_t)r);
+}
+
+// Parameters -> cells and the Jacobian tiles (consecutive parameters whose
+// cells fit the shared-memory staging budget of jacobian.cu).
+void build_jacobian_tiles(Context &c) {
+    MeshData &m = c.mesh;
+    const int64_t P = m.P;
+    m.pcell_ptr.assign(P + 1, 0);
+    for (int64_t i = 0; i < m.C; i++)
+        if (m.marker[i] >= 0) m.pcell_ptr[m.marker[i] + 1]++;
+    for (int64_t p = 0; p < P; p++) m.pcell_ptr[p + 1] += m.pcell_ptr[p];
+    m.pcell.assign(m.pcell_ptr[P], 0);
+    std::vector<int32_t> pos(m.pcell_ptr.begin(), m.pcell_ptr.end() - 1);
+    for (int64_t i = 0; i < m.C; i++)
+        if (m.marker[i] >= 0) m.pcell[pos[m.marker[i]]++] = (int32_t)i;
+    // staging bytes per cell: U and V for nv nodes x nK x (nE + 1) doubles
+    const size_t per_cell = (size_t)m.nv * c.nK * (c.nE + 1) * 2 * sizeof(double);
+    const size_t budget = 200 * 1024;
+    int max_cells = (int)std::max<size_t>(1, budget / std::max<size_t>(per_cell, 1));
+    if (per_cell > budget) max_cells = 1;  // staged in chunks of one cell
+    max_cells = std::min(max_cells, 32);
+    m.jtile_cells_max = max_cells;
+    m.jtile_p.clear();
+    m.jtile_p.push_back(0);
+    int64_t p = 0;
+    while (p < P) {
+        int64_t q = p, cells = 0;
+        while (q < P && q - p < 32) {
+            int64_t cq = m.pcell_ptr[q + 1] - m.pcell_ptr[q];
+            if (q > p && cells + cq > max_cells) break;
+            cells += cq;
+            q++;
+        }
+        if (q == p) q = p + 1;
+        m.jtile_p.push_back((int32_t)q);
+        p = q;
+    }
+}
+
+}  // namespace ertgb

@@ -207,6 +207,34 @@ def grid_line_scheme(electrode_grid, kind="dd", max_separation=999):
     return np.array(rows, np.int32).reshape(-1, 4)
 
 
+def grid_scheme_3d(nx, ny, max_line_offset=3):
+    """Surface-grid scheme for an (nx, ny) electrode grid (electrode index
+    ``ix * ny + iy``): inline dipole-dipole along every x and y line,
+    pole-dipole along the x lines, and cross-line dipole-dipole (current
+    dipole on one x line, potential dipoles of unit length on the x lines
+    up to ``max_line_offset`` lines away).  For 12 x 8 electrodes and offset
+    3 this gives 5336 configurations."""
+    def idx(ix, iy):
+        return ix * ny + iy
+    rows = []
+    xl = [[idx(ix, iy) for ix in range(nx)] for iy in range(ny)]
+    yl = [[idx(ix, iy) for iy in range(ny)] for ix in range(nx)]
+    for line in xl + yl:
+        for (a, b, m, n) in _scheme_dd(len(line)):
+            rows.append((line[a], line[b], line[m], line[n]))
+    for line in xl:
+        for (a, _, m, n) in _scheme_pd(len(line)):
+            rows.append((line[a], -1, line[m], line[n]))
+    for iy in range(ny):
+        for jy in range(ny):
+            if jy == iy or abs(jy - iy) > max_line_offset:
+                continue
+            for a in range(nx - 1):
+                for m in range(nx - 1):
+                    rows.append((idx(a, iy), idx(a + 1, iy), idx(m, jy), idx(m + 1, jy)))
+    return np.array(rows, np.int32).reshape(-1, 4)
+
+
 # -- geometric factors (core/src/bert/bertMisc.cpp:131-230) ---------------
 
 def _u_half(p, s):

@@ -1,0 +1,348 @@
+"""Drop-in ERT forward operator on one GB300: ``ERTModelling``.
+
+Mirrors the method surface of pyGIMLi's ``pg.physics.ert.ERTModelling``
+(pygimli/physics/ert/ertModelling.py:73-246) over the singularity-removal
+operator ``DCSRMultiElectrodeModelling`` (core/src/bert/dcfemmodelling.h:344):
+``setMesh``, ``setData``, ``response(model)``, ``createJacobian(model)``,
+``jacobian()``, ``mesh()``, ``parameterCount``, ``solution()``,
+``calcGeometricFactor``, ``mapERTModel``, ``setkValues/setWeights``.
+Every numerical step runs in libertgb.so (hand-written sm_103a CUDA behind
+the C ABI of include/ertgb.h); this module only does setup bookkeeping
+(electrode search, wavenumbers, model mapping) and moves buffers.
+
+Scope (raises otherwise): real resistivity, node electrodes (marker -99),
+flat surface with mixed far-field boundaries, pole current pattern (the
+reference's default when there is no reference electrode).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native
+from .data import DataContainerERT, geometricFactors
+from .kwave import init_kwave_list
+from .mesh import MARKER_BOUND_HOMOGEN_NEUMANN, MARKER_BOUND_MIXED, MARKER_NODE_ELECTRODE, Mesh
+from .modelmap import map_model
+
+TOLERANCE = 1e-12
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def search_electrodes(mesh, sensors):
+    """Node electrodes as DCMultiElectrodeModelling::searchElectrodes_ finds
+    them (core/src/bert/dcfemmodelling.cpp:790-1030): sensor i takes the first
+    still-unused node with marker -99 within 1 cm.  2-D sensors given as
+    (x, 0, z) are swapped to (x, z) first (:859-867)."""
+    ePos = np.asarray(sensors, dtype=np.float64).reshape(-1, 3).copy()
+    if mesh.dim() == 2:
+        zvar = np.ptp(ePos[:, 2]) > 0 or np.max(np.abs(ePos[:, 2])) > 0
+        yvar = np.ptp(ePos[:, 1]) > 0
+        if zvar and not yvar and np.max(np.abs(ePos[:, 1])) < 1e-8:
+            ePos[:, [1, 2]] = ePos[:, [2, 1]]
+    cand = np.nonzero(mesh.node_markers == MARKER_NODE_ELECTRODE)[0]
+    used = np.zeros(len(cand), bool)
+    out = np.empty(len(ePos), np.int32)
+    cpos = mesh.nodes[cand]
+    for i, p in enumerate(ePos):
+        d = np.linalg.norm(cpos - p, axis=1)
+        ok = np.nonzero((d < 0.01) & ~used)[0]
+        if len(ok) == 0:
+            raise ValueError(f"There is a requested electrode that does not match the given mesh: {p}")
+        used[ok[0]] = True
+        out[i] = cand[ok[0]]
+    return out
+
+
+def surface_info(mesh):
+    """surfaceZ and topography flag of updateMeshDependency_
+    (core/src/bert/dcfemmodelling.cpp:711-773)."""
+    bm = mesh.boundary_markers
+    neu = np.nonzero(bm == MARKER_BOUND_HOMOGEN_NEUMANN)[0]
+    if len(neu) == 0:
+        return -np.finfo(np.float64).max, False
+    c = mesh.nodes[mesh.boundaries[neu]].mean(axis=1)[:, mesh.dim() - 1]
+    return float(c[0]), bool(np.any(c != c[0]))
+
+
+class ERTModelling:
+    """ERT forward operator (singularity removal) on one GB300."""
+
+    def __init__(self, sr=True, verbose=False, device=0, rtol=1e-10, maxIter=20000):
+        if not sr:
+            raise NotImplementedError("only the singularity-removal operator (sr=True) is provided")
+        self.verbose = verbose
+        self._lib = _native.load()
+        self._ctx = ctypes.c_void_p()
+        _native.check(None, self._lib.ertgb_create(ctypes.byref(self._ctx), int(device)))
+        self.device = int(device)
+        self._mesh = None
+        self._data = None
+        self._k = None
+        self._w = None
+        self._kw_user = False
+        self._J = None
+        self._elec_nodes = None
+        self._last_model = None
+        self.setSolverTolerance(rtol, maxIter)
+
+    def __del__(self):
+        try:
+            if getattr(self, "_ctx", None) and self._ctx.value:
+                self._lib.ertgb_destroy(self._ctx)
+                self._ctx = ctypes.c_void_p()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        return _native.check(self._ctx, rc)
+
+    # -------------------------------------------------------------- setup
+    def setVerbose(self, v):
+        self.verbose = bool(v)
+
+    def setThreadCount(self, n):
+        """No-op: the work runs on the GPU."""
+
+    def setSolver(self, solver):
+        raise NotImplementedError("the linear solver is the built-in GPU block PCG")
+
+    def setSolverTolerance(self, rtol=1e-10, maxIter=20000):
+        self._check(self._lib.ertgb_set_solver(self._ctx, float(rtol), int(maxIter), 0))
+
+    def setComplex(self, c):
+        if c:
+            raise NotImplementedError("complex resistivity is not supported")
+
+    def complex(self):
+        return False
+
+    def setMesh(self, mesh, ignoreRegionManager=True):
+        if not isinstance(mesh, Mesh):
+            raise TypeError("mesh must be a pygimli_gb300.mesh.Mesh")
+        surf, topo = surface_info(mesh)
+        if topo:
+            raise NotImplementedError("meshes with topography need numerical primary potentials (not supported)")
+        bm = mesh.boundary_markers
+        if mesh.dim() == 3 and not np.any(bm == MARKER_BOUND_MIXED):
+            raise NotImplementedError("Neumann-only domains are not supported")
+        b = np.ascontiguousarray(mesh.boundaries, np.int32)
+        self._check(self._lib.ertgb_set_mesh(
+            self._ctx, mesh.dim(), mesh.nodeCount(), _ptr(mesh.nodes), mesh.cellCount(),
+            _ptr(mesh.cells), _ptr(mesh.cell_markers), len(b), _ptr(b),
+            _ptr(mesh.boundary_markers), _ptr(mesh.boundary_cells)))
+        self._mesh = mesh
+        self._surface_z = surf
+        self._J = None
+        if self._data is not None:
+            self._update_data()
+
+    def mesh(self):
+        return self._mesh
+
+    def setData(self, data):
+        if not isinstance(data, DataContainerERT):
+            raise TypeError("data must be a pygimli_gb300.data.DataContainerERT")
+        self._data = data
+        self._J = None
+        if self._mesh is not None:
+            self._update_data()
+
+    @property
+    def data(self):
+        return self._data
+
+    def _update_data(self):
+        mesh, data = self._mesh, self._data
+        self._elec_nodes = search_electrodes(mesh, data.sensorPositions())
+        self._check(self._lib.ertgb_set_electrodes(self._ctx, len(self._elec_nodes),
+                                                   _ptr(self._elec_nodes), float(self._surface_z)))
+        if not self._kw_user:
+            self._k, self._w = init_kwave_list(mesh.dim(), data.sensorPositions())
+        self._push_kw()
+        self._push_scheme()
+
+    def _push_kw(self):
+        k = np.ascontiguousarray(self._k, np.float64)
+        w = np.ascontiguousarray(self._w, np.float64)
+        self._check(self._lib.ertgb_set_kw(self._ctx, len(k), _ptr(k), _ptr(w)))
+
+    def _push_scheme(self):
+        data = self._data
+        kf = data["k"]
+        if data.size() == 0:
+            raise ValueError("data container is empty")
+        if np.min(np.abs(kf)) < TOLERANCE:
+            kf = self.calcGeometricFactor(data)
+            data.set("k", kf)
+        ab = np.ascontiguousarray(data.abmn(), np.int32)
+        kf = np.ascontiguousarray(kf, np.float64)
+        self._check(self._lib.ertgb_set_scheme(self._ctx, len(ab), _ptr(ab), _ptr(kf)))
+
+    def setkValues(self, k):
+        self._k = np.asarray(k, np.float64).copy()
+        self._kw_user = True
+        if self._w is not None and len(self._w) == len(self._k) and self._elec_nodes is not None:
+            self._push_kw()
+
+    def setWeights(self, w):
+        self._w = np.asarray(w, np.float64).copy()
+        self._kw_user = True
+        if self._k is not None and len(self._w) == len(self._k) and self._elec_nodes is not None:
+            self._push_kw()
+
+    def kValues(self):
+        return None if self._k is None else self._k.copy()
+
+    def weights(self):
+        return None if self._w is None else self._w.copy()
+
+    @property
+    def parameterCount(self):
+        return int(self._mesh.cell_markers.max()) + 1
+
+    def calcGeometricFactor(self, data=None):
+        """Analytic geometric factors (flat surface, calcGeometricFactor,
+        core/src/bert/dcfemmodelling.cpp:1527-1557)."""
+        data = self._data if data is None else data
+        return geometricFactors(data, self._mesh.dim())
+
+    def mapERTModel(self, model, background=-9e99):
+        return map_model(self._mesh, model, background)
+
+    # ---------------------------------------------------------- forward
+    def _ready(self):
+        if self._mesh is None or self._data is None:
+            raise RuntimeError("mesh and data must be set")
+        if self._data.exists("k") and np.min(np.abs(self._data["k"])) >= TOLERANCE:
+            return
+        self._push_scheme()
+
+    def response(self, model):
+        """Apparent resistivities for ``model`` (numpy in -> numpy out, or a
+        CUDA tensor of per-cell resistivities -> CUDA tensor)."""
+        self._ready()
+        torch = _torch()
+        if isinstance(model, torch.Tensor) and model.is_cuda:
+            rho = model.to(torch.float64).contiguous()
+            if rho.numel() != self._mesh.cellCount():
+                raise ValueError("device models must be per-cell resistivities")
+            out = torch.empty(self._data.size(), dtype=torch.float64, device=rho.device)
+            self._response_dev(rho, out)
+            self._last_model = rho
+            return out
+        m = np.asarray(model, np.float64)
+        if np.min(m) < TOLERANCE:
+            raise ValueError(f"response for model with negative or zero resistivity is not defined: "
+                             f"min={m.min()}")
+        rho = np.ascontiguousarray(self.mapERTModel(m), np.float64)
+        dev = torch.device("cuda", self.device)
+        rho_d = torch.from_numpy(rho).pin_memory().to(dev, non_blocking=True)
+        out = torch.empty(self._data.size(), dtype=torch.float64, device=dev)
+        self._response_dev(rho_d, out)
+        self._last_model = m
+        return out.cpu().numpy()
+
+    def _response_dev(self, rho, out):
+        torch = _torch()
+        stream = torch.cuda.current_stream(rho.device).cuda_stream
+        self._check(self._lib.ertgb_response(self._ctx, ctypes.c_void_p(rho.data_ptr()),
+                                             ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream)))
+
+    def createJacobian(self, model, dtype="float64"):
+        """Jacobian d rhoa / d model from the potentials of the last response
+        (like the reference, which reuses its stored sub-potentials).  Stored
+        on the device; ``jacobian()`` returns it."""
+        torch = _torch()
+        if self._mesh is None:
+            raise RuntimeError("no mesh")
+        P = self.parameterCount
+        D = self._data.size()
+        tdt = torch.float64 if dtype in ("float64", torch.float64) else torch.float32
+        dev = torch.device("cuda", self.device)
+        if isinstance(model, torch.Tensor):
+            md = model.to(device=dev, dtype=torch.float64).contiguous()
+        else:
+            md = torch.from_numpy(np.ascontiguousarray(model, np.float64)).to(dev)
+        J = torch.empty((D, P), dtype=tdt, device=dev)
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        self._check(self._lib.ertgb_jacobian(self._ctx, ctypes.c_void_p(md.data_ptr()), int(md.numel()),
+                                             ctypes.c_void_p(J.data_ptr()), 0 if tdt == torch.float64 else 1,
+                                             ctypes.c_void_p(stream)))
+        self._J = J
+        return J
+
+    def jacobian(self):
+        return self._J
+
+    # ---------------------------------------------------- inspection
+    def sizes(self):
+        n = ctypes.c_int64()
+        nnz = ctypes.c_int64()
+        p = ctypes.c_int64()
+        r = ctypes.c_int64()
+        self._check(self._lib.ertgb_sizes(self._ctx, ctypes.byref(n), ctypes.byref(nnz), ctypes.byref(p),
+                                          ctypes.byref(r)))
+        return n.value, nnz.value, p.value, r.value
+
+    def pattern(self):
+        n, nnz, _, _ = self.sizes()
+        rp = np.zeros(n + 1, np.int32)
+        ci = np.zeros(nnz, np.int32)
+        self._check(self._lib.ertgb_get_pattern(self._ctx, _ptr(rp), _ptr(ci)))
+        return rp, ci
+
+    def matrix(self, k_index=0, which=0):
+        _, nnz, _, _ = self.sizes()
+        v = np.zeros(nnz)
+        self._check(self._lib.ertgb_get_matrix(self._ctx, int(k_index), int(which), _ptr(v)))
+        return v
+
+    def subPotentials(self):
+        """[k][electrode][node] total potentials of the last response."""
+        n, _, _, _ = self.sizes()
+        out = np.zeros((len(self._k), len(self._elec_nodes), n))
+        self._check(self._lib.ertgb_get_potentials(self._ctx, _ptr(out)))
+        return out
+
+    def primaryPotentials(self):
+        n, _, _, _ = self.sizes()
+        out = np.zeros((len(self._k), len(self._elec_nodes), n))
+        self._check(self._lib.ertgb_get_primary(self._ctx, _ptr(out)))
+        return out
+
+    def solution(self):
+        """k-summed potentials per electrode source (nE x nodes), the
+        reference's solutions_ (dcfemmodelling.cpp:1707-1729)."""
+        u = self.subPotentials()
+        return np.einsum("k,ken->en", self._w, u)
+
+    def stats(self):
+        s = _native.Stats()
+        self._check(self._lib.ertgb_get_stats(self._ctx, ctypes.byref(s)))
+        return {f: getattr(s, f) for f, _ in s._fields_}
+
+    def electrodeNodes(self):
+        return None if self._elec_nodes is None else self._elec_nodes.copy()
+
+
+def simulate(mesh, scheme, res, sr=True, **kwargs):
+    """Noise-free apparent resistivities of ``res`` (per cell) for ``scheme``,
+    like pg.physics.ert.simulate without noise (pygimli/physics/ert/ert.py:12-285)."""
+    fop = ERTModelling(sr=sr, **kwargs)
+    data = scheme.copy()
+    if not data.exists("k") or np.min(np.abs(data["k"])) < TOLERANCE:
+        data.set("k", geometricFactors(data, mesh.dim()))
+    fop.setData(data)
+    fop.setMesh(mesh, ignoreRegionManager=True)
+    data.set("rhoa", fop.response(res))
+    return data

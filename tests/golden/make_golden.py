@@ -1,0 +1,117 @@
+"""Generate the golden fixtures of tests/golden/ by running the reference's own
+C++ ERT modelling code (built from the reference sources by oracle/Makefile
+into oracle/_ref/libgimli_ref.so and driven through oracle/ref_driver.py).
+
+Run from the repository root after ``make -C oracle``:
+
+    python tests/golden/make_golden.py
+
+Each fixture holds the inputs (mesh arrays, sensors, ABMN, geometric
+factors, resistivity) and the reference outputs: wavenumbers/weights, the
+assembled system matrices (CSR), primary potentials, sub-potentials,
+apparent resistivities and the Jacobian.  Sizes are kept small so the
+fixtures stay a few hundred KB.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle.ref_driver import RefModelling, besselK0, besselK1, lib  # noqa: E402
+from pygimli_gb300.data import DataContainerERT, createData, geometricFactors, grid_line_scheme  # noqa: E402
+from pygimli_gb300.mesh import create_box_mesh_3d, create_para_mesh_2d  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def _resistivity(mesh, seed):
+    rng = np.random.default_rng(seed)
+    rho = np.exp(rng.uniform(np.log(50.0), np.log(200.0), mesh.cellCount()))
+    c = mesh.cellCenters()
+    d = mesh.dim() - 1
+    box = (np.abs(c[:, 0] - c[:, 0].mean() * 0.5) < 2.0) & (c[:, d] > -2.0)
+    rho[box] = 10.0
+    return rho
+
+
+def case(name, mesh, data, seed, threads=1):
+    R = RefModelling(mesh, data.sensorPositions(), data.abmn(), data["k"], threads=threads,
+                     keep_matrices=True)
+    k, w = R.kw()
+    rho = _resistivity(mesh, seed)
+    rhoa = R.response(rho)
+    mats = R.matrices
+    sub = R.subpotentials().reshape(len(k), data.sensorCount(), mesh.nodeCount())
+    J = R.jacobian(rho)
+    kidx = np.unique([0, len(k) // 2, len(k) - 1])
+    prim = np.stack([np.stack([R.primary(e, k[i], 0.0) for e in range(data.sensorCount())]) for i in kidx])
+    rp = np.stack([mats[i][0] for i in kidx])
+    ci = np.stack([mats[i][1] for i in kidx])
+    va = np.stack([mats[i][2] for i in kidx])
+    rho1 = np.ones(mesh.cellCount())
+    src_center = mesh.nodes[R.electrode_nodes()].mean(axis=0)
+    S1 = np.stack([R.assemble(rho1, k[i], src_center)[2] for i in kidx])
+    np.savez_compressed(
+        os.path.join(OUT, name + ".npz"),
+        dim=mesh.dim(), nodes=mesh.nodes, cells=mesh.cells, cell_markers=mesh.cell_markers,
+        node_markers=mesh.node_markers, boundaries=mesh.boundaries,
+        boundary_markers=mesh.boundary_markers, boundary_cells=mesh.boundary_cells,
+        sensors=data.sensorPositions(), abmn=data.abmn(), kfac=data["k"],
+        kfac_ref=R.geometric_factors(), rho=rho, k=k, w=w, rhoa=rhoa,
+        electrode_nodes=R.electrode_nodes(), kidx=kidx, rowptr=rp[0], colidx=ci[0], S=va, S1=S1,
+        primary=prim, subpot=sub, J=J)
+    R.close()
+    print(name, mesh, len(data), "k:", len(k), "J:", J.shape)
+
+
+def bessel_table():
+    x = np.concatenate([np.geomspace(1e-6, 2.0, 60), np.linspace(2.0, 40.0, 60), [2.0, 3.75, 50.0]])
+    k0 = np.array([besselK0(v) for v in x])
+    k1 = np.array([besselK1(v) for v in x])
+    gl, gw, lx, lw = {}, {}, {}, {}
+    import ctypes
+    out = {}
+    for n in (4, 5, 8, 12, 17, 21):
+        a = np.zeros(n)
+        b = np.zeros(n)
+        lib().ref_gauss_legendre(n, a.ctypes.data_as(ctypes.c_void_p), b.ctypes.data_as(ctypes.c_void_p))
+        out[f"leg_x_{n}"] = a.copy()
+        out[f"leg_w_{n}"] = b.copy()
+        lib().ref_gauss_laguerre(n, a.ctypes.data_as(ctypes.c_void_p), b.ctypes.data_as(ctypes.c_void_p))
+        out[f"lag_x_{n}"] = a.copy()
+        out[f"lag_w_{n}"] = b.copy()
+    np.savez_compressed(os.path.join(OUT, "bessel_quadrature.npz"), x=x, k0=k0, k1=k1, **out)
+    print("bessel_quadrature", len(x))
+
+
+def main():
+    bessel_table()
+    # 2.5-D: 11 electrodes, dipole-dipole
+    xs = np.arange(11.0)
+    m2 = create_para_mesh_2d(xs, para_dx=0.5, para_depth=4.0)
+    d2 = createData(xs, "dd")
+    d2["k"] = geometricFactors(d2, 2)
+    case("ert2d_small", m2, d2, seed=11)
+    # 2.5-D with pole-dipole (electrode at infinity) and Wenner
+    d2b = createData(xs, "pd")
+    wa = createData(xs, "wa").abmn()
+    d2b = DataContainerERT(d2b.sensorPositions(), np.vstack([d2b.abmn(), wa]))
+    d2b["k"] = geometricFactors(d2b, 2)
+    case("ert2d_pd_wa", m2, d2b, seed=12)
+    # 3-D: 4 x 3 electrode grid, dipole-dipole + pole-dipole lines
+    e = np.array([(x, y) for x in np.arange(4) * 4.0 for y in np.arange(3) * 4.0])
+    m3 = create_box_mesh_3d(e, h=2.0, para_margin=(2, 2), para_depth=6.0, outer=60.0,
+                            growth=2.0, depth_growth=1.5)
+    ab = np.vstack([grid_line_scheme((4, 3), "dd"), grid_line_scheme((4, 3), "pd")])
+    d3 = DataContainerERT(np.column_stack([e, np.zeros(len(e))]), ab)
+    d3["k"] = geometricFactors(d3, 3)
+    case("ert3d_small", m3, d3, seed=13)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,243 @@
+"""GPU parity of the CUDA path (libertgb.so through ERTModelling and the C ABI)
+against the reference's own outputs (tests/golden/) and the FP64 oracle.
+
+Tolerances (relative): CSR indices bit-exact; matrix values <= 1e-12;
+primary potentials <= 1e-12; potentials and apparent resistivities <= 1e-6;
+Jacobian <= 1e-5 in the Frobenius norm.  Full-size workloads are checked
+through size-independent properties (linearity in the resistivity scale,
+the half-space value, Jacobian rows recomputed from the GPU potentials)."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+from oracle import ert_oracle as O
+from pygimli_gb300.data import DataContainerERT, createData, geometricFactors, grid_scheme_3d
+from pygimli_gb300.mesh import Mesh, create_box_mesh_3d, create_para_mesh_2d
+
+pytestmark = pytest.mark.gpu
+
+TOL_MAT = 1e-12
+TOL_POT = 1e-6
+TOL_J = 1e-5
+
+
+@pytest.fixture(scope="module")
+def torch():
+    t = pytest.importorskip("torch")
+    if not t.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from pygimli_gb300 import build
+    build.build()
+    return t
+
+
+def fop_for(mesh, data, k=None, w=None, **kw):
+    from pygimli_gb300 import ERTModelling
+    fop = ERTModelling(**kw)
+    if k is not None:
+        fop.setkValues(k)
+        fop.setWeights(w)
+    fop.setData(data)
+    fop.setMesh(mesh)
+    return fop
+
+
+def load_case(golden_dir, name):
+    z = np.load(os.path.join(golden_dir, name + ".npz"))
+    mesh = Mesh(int(z["dim"]), z["nodes"], z["cells"], z["cell_markers"], z["node_markers"],
+                z["boundaries"], z["boundary_markers"], z["boundary_cells"])
+    data = DataContainerERT(z["sensors"], z["abmn"])
+    data.set("k", z["kfac"])
+    return z, mesh, data
+
+
+def rel(a, b):
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+@pytest.mark.parametrize("name", ["ert2d_small", "ert2d_pd_wa", "ert3d_small"])
+def test_golden_parity(torch, golden_dir, name):
+    z, mesh, data = load_case(golden_dir, name)
+    fop = fop_for(mesh, data)
+    assert np.array_equal(fop.kValues(), z["k"]) and np.array_equal(fop.weights(), z["w"])
+    rp, ci = fop.pattern()
+    assert np.array_equal(rp, z["rowptr"]) and np.array_equal(ci, z["colidx"])
+    rhoa = fop.response(z["rho"])
+    e_rhoa = float(np.max(np.abs(rhoa - z["rhoa"]) / z["rhoa"]))
+    for j, ki in enumerate(z["kidx"]):
+        assert rel(fop.matrix(ki, 0), z["S"][j]) <= TOL_MAT
+        assert rel(fop.matrix(ki, 1), z["S1"][j]) <= TOL_MAT
+    prim = fop.primaryPotentials()
+    for j, ki in enumerate(z["kidx"]):
+        assert rel(prim[ki], z["primary"][j]) <= TOL_MAT
+    e_pot = rel(fop.subPotentials(), z["subpot"])
+    J = fop.createJacobian(z["rho"]).cpu().numpy()
+    e_J = float(np.linalg.norm(J - z["J"]) / np.linalg.norm(z["J"]))
+    print(f"{name}: rhoa {e_rhoa:.2e} potentials {e_pot:.2e} J {e_J:.2e} iters {fop.stats()['iterations']}")
+    assert e_rhoa <= TOL_POT and e_pot <= TOL_POT and e_J <= TOL_J
+
+
+def _c1_case(seed=1):
+    xs = np.arange(41.0)
+    mesh = create_para_mesh_2d(xs, para_dx=0.25, para_depth=10.0)
+    data = createData(xs, "dd")
+    data.set("k", geometricFactors(data, 2))
+    rng = np.random.default_rng(seed)
+    rho = np.exp(rng.uniform(np.log(50.0), np.log(200.0), mesh.cellCount()))
+    c = mesh.cellCenters()
+    rho[(np.abs(c[:, 0] - 12.0) < 3.0) & (c[:, 1] > -4.0) & (c[:, 1] < -1.0)] = 10.0
+    rho[(np.abs(c[:, 0] - 28.0) < 3.0) & (c[:, 1] > -6.0) & (c[:, 1] < -2.0)] = 1000.0
+    return mesh, data, rho
+
+
+def test_2d_config_vs_oracle(torch):
+    """41 electrodes, 741 dipole-dipole data, ~3.6k nodes, 17 wavenumbers."""
+    mesh, data, rho = _c1_case()
+    fop = fop_for(mesh, data)
+    assert len(fop.kValues()) == 17
+    rhoa = fop.response(rho)
+    J = fop.createJacobian(rho).cpu().numpy()
+    P = O.Problem(mesh, data.sensorPositions(), data.abmn(), data["k"], fop.kValues(), fop.weights())
+    rhoa_o, u = P.response(rho)
+    J_o = P.jacobian(u, rho)
+    e_r = float(np.max(np.abs(rhoa - rhoa_o) / rhoa_o))
+    e_J = float(np.linalg.norm(J - J_o) / np.linalg.norm(J_o))
+    print(f"2d config: rhoa {e_r:.2e} J {e_J:.2e} iters {fop.stats()['iterations']}")
+    assert e_r <= TOL_POT and e_J <= TOL_J
+
+
+def _small_3d(nx=5, ny=4):
+    e = np.array([(x, y) for x in np.arange(nx) * 4.0 for y in np.arange(ny) * 4.0])
+    mesh = create_box_mesh_3d(e, h=2.0, para_margin=(2, 2), para_depth=8.0, outer=80.0, growth=1.8,
+                              depth_growth=1.3)
+    data = DataContainerERT(np.column_stack([e, np.zeros(len(e))]), grid_scheme_3d(nx, ny, 2))
+    data.set("k", geometricFactors(data, 3))
+    rng = np.random.default_rng(3)
+    rho = np.exp(rng.normal(np.log(100.0), 1.0, mesh.cellCount()))
+    return mesh, data, rho
+
+
+def test_3d_vs_oracle(torch):
+    mesh, data, rho = _small_3d()
+    fop = fop_for(mesh, data)
+    rhoa = fop.response(rho)
+    J = fop.createJacobian(rho).cpu().numpy()
+    P = O.Problem(mesh, data.sensorPositions(), data.abmn(), data["k"], fop.kValues(), fop.weights())
+    rhoa_o, u = P.response(rho)
+    J_o = P.jacobian(u, rho)
+    e_r = float(np.max(np.abs(rhoa - rhoa_o) / rhoa_o))
+    e_J = float(np.linalg.norm(J - J_o) / np.linalg.norm(J_o))
+    print(f"3d small ({mesh.nodeCount()} nodes): rhoa {e_r:.2e} J {e_J:.2e} iters {fop.stats()['iterations']}")
+    assert e_r <= TOL_POT and e_J <= TOL_J
+
+
+def test_markers_shared_by_cells(torch):
+    """Parameters spanning several cells and marker -1 cells prolongated."""
+    mesh, data, rho = _c1_case(seed=2)
+    mk = np.arange(mesh.cellCount()) // 4
+    mk[::11] = -1
+    mk[mk >= 0] = np.unique(mk[mk >= 0], return_inverse=True)[1]
+    mesh.setCellMarkers(mk)
+    model = np.exp(np.random.default_rng(4).uniform(np.log(30.0), np.log(300.0), int(mk.max()) + 1))
+    fop = fop_for(mesh, data)
+    rhoa = fop.response(model)
+    J = fop.createJacobian(model).cpu().numpy()
+    assert J.shape == (data.size(), int(mk.max()) + 1)
+    rho_cell = O.map_model(mesh, model)
+    P = O.Problem(mesh, data.sensorPositions(), data.abmn(), data["k"], fop.kValues(), fop.weights())
+    rhoa_o, u = P.response(rho_cell)
+    J_o = P.jacobian(u, model)
+    assert float(np.max(np.abs(rhoa - rhoa_o) / rhoa_o)) <= TOL_POT
+    assert float(np.linalg.norm(J - J_o) / np.linalg.norm(J_o)) <= TOL_J
+
+
+def test_fp32_jacobian_and_host_abi(torch, golden_dir):
+    from pygimli_gb300 import _native
+    z, mesh, data = load_case(golden_dir, "ert2d_small")
+    fop = fop_for(mesh, data)
+    r_dev = fop.response(z["rho"])
+    J64 = fop.createJacobian(z["rho"]).cpu().numpy()
+    J32 = fop.createJacobian(z["rho"], dtype="float32").cpu().numpy()
+    assert np.linalg.norm(J32 - J64) <= 1e-6 * np.linalg.norm(J64)
+    L = _native.load()
+    rho = np.ascontiguousarray(z["rho"])
+    out = np.zeros(data.size())
+    _native.check(fop._ctx, L.ertgb_response_host(fop._ctx, rho.ctypes.data_as(ctypes.c_void_p),
+                                                  out.ctypes.data_as(ctypes.c_void_p)))
+    assert np.array_equal(out, r_dev)
+    Jh = np.zeros_like(J64)
+    _native.check(fop._ctx, L.ertgb_jacobian_host(fop._ctx, rho.ctypes.data_as(ctypes.c_void_p), len(rho),
+                                                  Jh.ctypes.data_as(ctypes.c_void_p), 0))
+    assert np.array_equal(Jh, J64)
+
+
+def test_error_paths(torch, golden_dir):
+    from pygimli_gb300._native import NOT_CONVERGED, STATE, BAD_INPUT, ErtgbError
+    z, mesh, data = load_case(golden_dir, "ert2d_small")
+    fop = fop_for(mesh, data)
+    with pytest.raises(ErtgbError) as e:
+        fop.createJacobian(z["rho"])
+    assert e.value.code == STATE
+    bad = z["rho"].copy()
+    bad[5] = 0.0
+    with pytest.raises(ValueError):
+        fop.response(bad)
+    dev = torch.tensor(bad, device="cuda")
+    dev[7] = -1.0
+    with pytest.raises(ErtgbError) as e:
+        fop.response(dev)
+    assert e.value.code == BAD_INPUT
+    fop.setSolverTolerance(1e-10, 1)
+    with pytest.raises(ErtgbError) as e:
+        fop.response(z["rho"])
+    assert e.value.code == NOT_CONVERGED
+    fop.setSolverTolerance(1e-10, 20000)
+    r = fop.response(z["rho"])
+    assert np.max(np.abs(r - z["rhoa"]) / z["rhoa"]) <= TOL_POT
+
+
+def _jacobian_rows_from_potentials(mesh, data, k, w, u, model, rows):
+    K, M = O.element_matrices(mesh.dim(), mesh.nodes, mesh.cells)
+    ab = data.abmn()[rows]
+    out = np.zeros((len(rows), mesh.cellCount()))
+    cells = mesh.cells
+    for ki in range(len(k)):
+        S = M * (k[ki] ** 2) + K
+        Uc = np.transpose(u[ki][:, cells], (1, 2, 0))
+        Uc = np.concatenate([Uc, np.zeros(Uc.shape[:2] + (1,))], axis=2)
+        V = np.einsum("cij,cje->cie", S, Uc)
+        dab = V[:, :, ab[:, 0]] - V[:, :, ab[:, 1]]
+        dmn = Uc[:, :, ab[:, 2]] - Uc[:, :, ab[:, 3]]
+        out += w[ki] * np.einsum("cid,cid->dc", dab, dmn)
+    kf = data["k"][rows]
+    return out / ((model ** 2)[None, :] / kf[:, None])
+
+
+def test_3d_config_properties(torch):
+    """96 electrodes on 12 x 8, ~88k nodes, ~486k tetrahedra, 5336 data."""
+    e = np.array([(x, y) for x in np.arange(12) * 4.0 for y in np.arange(8) * 4.0])
+    mesh = create_box_mesh_3d(e)
+    data = DataContainerERT(np.column_stack([e, np.zeros(len(e))]), grid_scheme_3d(12, 8))
+    data.set("k", geometricFactors(data, 3))
+    rng = np.random.default_rng(7)
+    rho = np.exp(rng.normal(np.log(100.0), 1.0, mesh.cellCount()))
+    fop = fop_for(mesh, data)
+    r1 = fop.response(rho)
+    st = fop.stats()
+    # linearity in the resistivity scale
+    r2 = fop.response(2.0 * rho)
+    assert float(np.max(np.abs(r2 - 2.0 * r1) / (2.0 * r1))) <= TOL_POT
+    # Jacobian rows against a recomputation from the GPU potentials
+    J = fop.createJacobian(2.0 * rho)
+    rows = np.array([0, 17, 600, 1500, 2500, 4000, 5300])
+    Jr = J[torch.as_tensor(rows, device=J.device)].cpu().numpy()
+    u = fop.subPotentials()
+    Jo = _jacobian_rows_from_potentials(mesh, data, fop.kValues(), fop.weights(), u, 2.0 * rho, rows)
+    assert float(np.linalg.norm(Jr - Jo) / np.linalg.norm(Jo)) <= TOL_J
+    # homogeneous half-space: apparent resistivity equals the resistivity
+    rh = fop.response(np.full(mesh.cellCount(), 100.0))
+    assert float(np.max(np.abs(rh - 100.0) / 100.0)) < 0.05
+    print(f"3d config: iters {st['iterations']} solve {st['ms_solve']:.1f} ms, homogeneous "
+          f"max dev {np.max(np.abs(rh - 100.0)):.3f}")

@@ -1,0 +1,90 @@
+"""Host-side logic (no GPU): scheme generators, synthetic meshes, the C ABI
+library build, its exported symbols and its error path without a device."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from pygimli_gb300.data import createData, grid_line_scheme, grid_scheme_3d
+from pygimli_gb300.mesh import create_box_mesh_3d, create_para_mesh_2d
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_dipole_dipole_count():
+    # 41 electrodes, default dipole-dipole: 741 configurations
+    d = createData(np.arange(41.0), "dd")
+    assert d.size() == 741
+    ab = d.abmn()
+    assert np.all(ab[:, 1] == ab[:, 0] + 1) and np.all(ab[:, 3] == ab[:, 2] + 1)
+    assert np.all(ab[:, 2] > ab[:, 1])
+
+
+def test_pole_dipole_and_wenner():
+    pd = createData(np.arange(11.0), "pd").abmn()
+    assert np.all(pd[:, 1] == -1) and np.all(pd[:, 3] == pd[:, 2] + 1)
+    wa = createData(np.arange(11.0), "wa").abmn()
+    s = wa[:, 2] - wa[:, 0]
+    assert np.all(wa[:, 3] - wa[:, 2] == s) and np.all(wa[:, 1] - wa[:, 3] == s)
+
+
+def test_grid_scheme_indices():
+    ab = grid_line_scheme((12, 8), "dd")
+    assert ab.min() >= 0 and ab.max() < 96 and len(ab) == 540
+    ab = grid_scheme_3d(12, 8)
+    assert len(ab) == 5336 and ab.max() < 96 and len(np.unique(ab, axis=0)) == len(ab)
+    assert np.all((ab[:, 1] == -1) | (ab[:, 1] != ab[:, 0]))
+
+
+def test_para_mesh_2d_config():
+    m = create_para_mesh_2d(np.arange(41.0), para_dx=0.25, para_depth=10.0)
+    assert 3000 <= m.nodeCount() <= 4500 and 5500 <= m.cellCount() <= 8000
+    assert np.sum(m.node_markers == -99) == 41
+    assert set(np.unique(m.boundary_markers)) == {-1, -2}
+    assert np.all(m.boundary_cells >= 0)
+    assert np.all(m.cellSizes() > 0)
+
+
+def test_box_mesh_3d_config():
+    e = np.array([(x, y) for x in np.arange(12) * 4.0 for y in np.arange(8) * 4.0])
+    m = create_box_mesh_3d(e)
+    assert 80000 <= m.nodeCount() <= 100000 and 450000 <= m.cellCount() <= 560000
+    assert np.sum(m.node_markers == -99) == 96
+    assert np.all(m.boundary_cells >= 0)
+    lo, hi = m.nodes.min(0), m.nodes.max(0)
+    assert np.allclose(lo, [-500, -500, -500]) and np.allclose(hi, [500, 500, 0])
+
+
+def _header_symbols():
+    txt = open(os.path.join(ROOT, "include", "ertgb.h")).read()
+    return sorted(set(re.findall(r"\b(ertgb_[a-z_]+)\s*\(", txt)))
+
+
+@pytest.fixture(scope="module")
+def built_lib():
+    from pygimli_gb300 import build
+    return build.build()
+
+
+def test_library_exports_every_header_symbol(built_lib):
+    L = ctypes.CDLL(built_lib)
+    syms = _header_symbols()
+    assert len(syms) >= 15
+    for s in syms:
+        assert hasattr(L, s), s
+    from pygimli_gb300 import _native
+    assert set(_native.SIGNATURES) == set(syms)
+
+
+def test_library_fails_loudly_without_device(built_lib):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from pygimli_gb300 import _native
+    L = _native.load()
+    ctx = ctypes.c_void_p()
+    rc = L.ertgb_create(ctypes.byref(ctx), 0)
+    assert rc == _native.CUDA_ERROR
+    assert b"cuda" in L.ertgb_last_error(None).lower()
