@@ -1,0 +1,319 @@
+#!/usr/bin/env python3
+"""Benchmark of the ERT forward operator + Jacobian on GB300.
+
+One step = one Gauss-Newton iteration's operator work: ``response(model)``
+(assembly, SR right-hand sides, multi-RHS PCG over all current sources,
+collect, apparent resistivities) followed by ``createJacobian(model)``
+(dense D x P Jacobian), on a seeded synthetic workload (default ``box_3d``:
+96 electrodes, 5336 data, ~486k tetrahedra, ~88k nodes, FP64 block PCG to a
+relative residual of 1e-10).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``value`` is device time per step with the inputs resident in HBM (CUDA
+events around K steps on the launching stream).  ``e2e`` is the same step
+through the public Python API with host numpy inputs and the apparent
+resistivities and the full Jacobian copied back to pinned host memory.
+``--impl reference`` times the CPU oracle port (the reference's algorithm
+restated in numpy/scipy with a SuperLU direct solve) on a bounded,
+extrapolated sample.  With N > 1 ranks (torchrun) every rank runs an
+independent replica of the workload (the operator uses one GPU).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "fwd+Jacobian s/GN-iter: learned-precond vs plain GPU PCG @1e-6; %HBM peak"
+UNIT = "s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["box_3d", "box_3d_probe", "line_2d"], default="box_3d")
+    ap.add_argument("--rtol", type=float, default=1e-10)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def workload(name):
+    from pygimli_gb300 import synthetic
+    if name == "line_2d":
+        mesh, data, rho = synthetic.line_2d()
+        cfg = {"workload": "line_2d: 2.5-D, 41 electrodes, 741 dipole-dipole, "
+                           f"{mesh.nodeCount()} nodes, {mesh.cellCount()} triangles, 17 wavenumbers"}
+    else:
+        mesh, data, rho = synthetic.box_3d(scheme="inline" if name == "box_3d_probe" else "full")
+        cfg = {"workload": f"{name}: 3-D, 96 electrodes (12x8 @4 m), {data.size()} ABMN, "
+                           f"{mesh.nodeCount()} nodes, {mesh.cellCount()} tetrahedra, P1"}
+    return mesh, data, rho, cfg
+
+
+def dist_init(n):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if n > 0 else "gloo")
+    return world, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return float("nan")
+
+        sm = np.array([num(r[1]) for r in rows])
+        mx = np.array([num(r[2]) for r in rows])
+        power = np.array([num(r[3]) for r in rows])
+        loaded = power >= np.nanpercentile(power, 50) if np.isfinite(power).any() else np.ones(len(rows), bool)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = [nm for i, nm in enumerate(names) if any(r[5 + i].lower().startswith("active") for r in rows)]
+        return {"sm_mhz": float(np.nanmedian(sm[loaded])), "sm_max_mhz": float(np.nanmax(mx)),
+                "samples": len(rows), "reasons": reasons}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel_file):
+    """DRAM bytes per launch from a committed ncu summary (profiles/*.txt,
+    line ``dram_bytes_per_launch = <bytes>``), else None."""
+    p = os.path.join(ROOT, "profiles", kernel_file)
+    if not os.path.exists(p):
+        return None
+    with open(p) as fh:
+        for line in fh:
+            if line.strip().startswith("dram_bytes_per_launch"):
+                try:
+                    return float(line.split("=")[1].split()[0])
+                except (IndexError, ValueError):
+                    return None
+    return None
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    from oracle.cpu_baseline import SampledBaseline, host_threads
+    from pygimli_gb300.kwave import init_kwave_list
+    mesh, data, rho, cfg = workload(args.workload)
+    k, w = init_kwave_list(mesh.dim(), data.sensorPositions())
+    base = SampledBaseline(mesh, data, k, w)
+    threads = host_threads()
+    # light warm-up: assembly only (the timed steps each factor the full matrix)
+    for _ in range(max(1, min(args.warmup, 1))):
+        base.P.assemble(rho, 0)
+    steps = args.steps
+    times, desc = [], ""
+    t_start = time.perf_counter()
+    for i in range(steps):
+        t, desc = base.step(rho, n_src=8, n_rows=64, threads=threads, seed=i)
+        times.append(t)
+        if time.perf_counter() - t_start > 150.0 and i >= 0:
+            break
+    value = float(np.mean(times))
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": len(times),
+           "steps_requested": steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
+           "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded)", "impl": "reference",
+           "config": dict(cfg, parallelism="cpu", solver="SuperLU direct (CHOLMOD stand-in)"),
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                            "sample": desc},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    from pygimli_gb300 import _native
+    from pygimli_gb300 import build as _build
+    from pygimli_gb300.ert import ERTModelling
+    _build.build()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    mesh, data, rho, cfg = workload(args.workload)
+    t_setup = time.perf_counter()
+    fop = ERTModelling(device=local, rtol=args.rtol)
+    fop.setData(data)
+    fop.setMesh(mesh)
+    setup_s = time.perf_counter() - t_setup
+    L = _native.load()
+    D, P, C = data.size(), fop.parameterCount, mesh.cellCount()
+    rho_d = torch.from_numpy(rho).to(dev)
+    rhoa_d = torch.empty(D, dtype=torch.float64, device=dev)
+    J_d = torch.empty((D, P), dtype=torch.float64, device=dev)
+    import ctypes
+
+    def step():
+        fop._response_dev(rho_d, rhoa_d)
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        fop._check(L.ertgb_jacobian(fop._ctx, ctypes.c_void_p(rho_d.data_ptr()), C,
+                                    ctypes.c_void_p(J_d.data_ptr()), 0, ctypes.c_void_p(stream)))
+
+    for _ in range(max(args.warmup, 0)):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    clocks = Clocks(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0])
+                    if os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].isdigit() else local)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    total_ms = e0.elapsed_time(e1)
+    st = fop.stats()
+    launches = int(st["launches_response"] + st["launches_jacobian"]) * args.steps
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = total_ms / 1e3 / (args.steps * world)
+
+    # roofline of the dominant kernel (CUDA events on the context stream)
+    ms = ctypes.c_double()
+    by = ctypes.c_double()
+    fl = ctypes.c_double()
+    prof = {}
+    for name, kid, reps in (("spmm", 0, 20), ("jacobian", 1, 2), ("assemble", 2, 10)):
+        fop._check(L.ertgb_profile_kernel(fop._ctx, kid, reps, ctypes.c_void_p(J_d.data_ptr()),
+                                          ctypes.byref(ms), ctypes.byref(by), ctypes.byref(fl)))
+        prof[name] = (ms.value, by.value, fl.value)
+    per_step = {"spmm": prof["spmm"][0] * st["iterations"], "jacobian": prof["jacobian"][0],
+                "assemble": prof["assemble"][0]}
+    dom = max(per_step, key=per_step.get)
+    peak, peak_kind = measured_peaks()
+    d_ms, d_bytes, d_flops = prof[dom]
+    achieved = d_bytes / (d_ms * 1e-3) / 1e9
+    traffic = ncu_traffic(f"{dom}_fp64_{args.workload}.txt")
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                "algorithmic_bytes": d_bytes, "ms_per_launch": d_ms,
+                "fp64_tflops": d_flops / (d_ms * 1e-3) / 1e12,
+                "share_of_step": per_step[dom] / (total_ms / args.steps)}
+
+    # end to end through the public API, host buffers
+    e2e = None
+    if not args.no_e2e:
+        Jh = torch.empty((D, P), dtype=torch.float64, pin_memory=True)
+        model = rho.copy()
+        tt = []
+        for i in range(max(1, min(args.steps, 3)) + 1):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r = fop.response(model)
+            J = fop.createJacobian(model)
+            Jh.copy_(J, non_blocking=True)
+            torch.cuda.synchronize()
+            if i > 0:
+                tt.append(time.perf_counter() - t0)
+            del J
+        e2e = {"value": float(np.mean(tt)), "unit": UNIT, "h2d_bytes_per_step": int(C * 8 + P * 8),
+               "d2h_bytes_per_step": int(D * 8 + D * P * 8), "steps": len(tt),
+               "check_rhoa_vs_device": float(np.max(np.abs(r - rhoa_d.cpu().numpy()) / r))}
+        del Jh
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle.cpu_baseline import SampledBaseline
+        base = SampledBaseline(mesh, data, fop.kValues(), fop.weights())
+        t, desc = base.step(rho, n_src=4, n_rows=32, threads=1)
+        cpu = {"value": t, "unit": UNIT, "cores": 1, "kind": "port", "sample": desc}
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": value * 1e3 * world, "higher_is_better": False,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+               "config": dict(cfg, parallelism=f"replicas x{world}", solver="block PCG (Jacobi), FP64",
+                              rtol=args.rtol, l2="working set > L2: PCG blocks 4 x "
+                              f"{mesh.nodeCount() * 96 * 8 / 1e6:.0f} MB, J {D * P * 8 / 1e9:.1f} GB"),
+               "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+               "clocks": clk,
+               "breakdown_ms": {"assemble": st["ms_assemble"], "rhs": st["ms_rhs"], "solve": st["ms_solve"],
+                                "collect": st["ms_collect"], "jacobian": st["ms_jacobian"],
+                                "pcg_iterations": st["iterations"], "n_rhs": st["n_rhs"],
+                                "max_rel_residual": st["max_rel_residual"], "setup_s": setup_s}}
+        print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_init(args.gpus if args.impl == "ours" else 0)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -4,8 +4,10 @@
  * returns an ertgb_status and never throws.  Arrays named *_host live in host
  * memory, arrays named *_dev in device memory of the context's GPU.  A
  * ``stream`` argument is a cudaStream_t passed as void* (NULL = the
- * context's own stream); device-buffer calls are stream-ordered and return
- * before the work finishes, host-buffer calls synchronise.
+ * context's own stream): the call's work is ordered after the work already
+ * queued on that stream, and later work on it is ordered after the call.
+ * Compute calls also return only after their work is done, because the
+ * solver decides on the host when to stop.
  *
  * The operator is the singularity-removal (SR) DC forward operator of
  * pyGIMLi: pg.physics.ert.ERTModelling(sr=True) -> C++
@@ -45,7 +47,16 @@ typedef struct {
     double ms_solve;
     double ms_collect;
     double ms_jacobian;       /* device time of the last jacobian            */
+    int64_t launches_response; /* kernels launched by the last response       */
+    int64_t launches_jacobian; /* kernels launched by the last jacobian       */
 } ertgb_stats;
+
+/* Kernels that ertgb_profile_kernel can time. */
+typedef enum {
+    ERTGB_KERNEL_SPMM = 0,     /* PCG operator q = A p with column dots       */
+    ERTGB_KERNEL_JACOBIAN = 1, /* Jacobian of the last response (FP64 J)      */
+    ERTGB_KERNEL_ASSEMBLE = 2  /* system matrices of the last response        */
+} ertgb_kernel;
 
 /* Create a context on CUDA device ``device``.  Replaces the construction of
  * DCSRMultiElectrodeModelling (core/src/bert/dcfemmodelling.h:346-359,
@@ -127,6 +138,14 @@ int ertgb_get_potentials(ertgb_ctx *ctx, double *pot_host);
 /* Unit-current primary potentials [k][electrode][node]. */
 int ertgb_get_primary(ertgb_ctx *ctx, double *prim_host);
 int ertgb_get_stats(const ertgb_ctx *ctx, ertgb_stats *stats);
+
+/* Measurement helper with no counterpart in the reference: launches one
+ * kernel ``reps`` times on the context stream (on the state of the last
+ * response) and returns the mean launch time from CUDA events, with the
+ * algorithmic DRAM bytes and FLOPs of one launch.  J_scratch_dev must hold
+ * n_data x n_param doubles for ERTGB_KERNEL_JACOBIAN (else unused). */
+int ertgb_profile_kernel(ertgb_ctx *ctx, int kernel, int reps, void *J_scratch_dev, double *ms_per_launch,
+                         double *bytes_per_launch, double *flops_per_launch);
 
 #ifdef __cplusplus
 }

@@ -26,7 +26,8 @@ class Stats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int32), ("n_rhs", ctypes.c_int32),
                 ("max_rel_residual", ctypes.c_double), ("ms_assemble", ctypes.c_double),
                 ("ms_rhs", ctypes.c_double), ("ms_solve", ctypes.c_double),
-                ("ms_collect", ctypes.c_double), ("ms_jacobian", ctypes.c_double)]
+                ("ms_collect", ctypes.c_double), ("ms_jacobian", ctypes.c_double),
+                ("launches_response", ctypes.c_int64), ("launches_jacobian", ctypes.c_int64)]
 
 
 # name -> (restype, argtypes)
@@ -52,6 +53,8 @@ SIGNATURES = {
     "ertgb_get_potentials": (_ci, [_vp, _vp]),
     "ertgb_get_primary": (_ci, [_vp, _vp]),
     "ertgb_get_stats": (_ci, [_vp, ctypes.POINTER(Stats)]),
+    "ertgb_profile_kernel": (_ci, [_vp, _ci, _ci, _vp, ctypes.POINTER(_d), ctypes.POINTER(_d),
+                                   ctypes.POINTER(_d)]),
 }
 
 _lib = None

@@ -512,4 +512,30 @@ void collect_response(Context &c, double *rhoa, cudaStream_t s) {
     ERTGB_CUDA(cudaGetLastError());
 }
 
+void profile_assemble(Context &c, int reps, double *ms, double *bytes, double *flops) {
+    MeshData &m = c.mesh;
+    if (c.d_S.n < (size_t)c.nK * m.nnz || !c.d_rho_last) throw Error(ERTGB_STATE, "profile needs a completed response");
+    cudaStream_t s = c.stream;
+    dim3 grid(grid1(m.nnz, kThreads, 1 << 16), c.nK);
+    auto go = [&] {
+        k_assemble<<<grid, kThreads, 0, s>>>(m.nnz, m.d_cptr.p, m.d_centry.p, m.d_K.p, m.d_M.p, m.d_bnd_mass.p,
+                                             c.d_alpha.p, m.d_bnd_cell.p, c.d_rho_last, c.d_k.p, m.nv * m.nv,
+                                             m.nvb * m.nvb, m.C, m.B, c.d_S.p);
+    };
+    go();
+    ERTGB_CUDA(cudaEventRecord(c.ev[0], s));
+    for (int r = 0; r < reps; r++) go();
+    ERTGB_CUDA(cudaEventRecord(c.ev[1], s));
+    ERTGB_CUDA(cudaEventSynchronize(c.ev[1]));
+    float t = 0.f;
+    ERTGB_CUDA(cudaEventElapsedTime(&t, c.ev[0], c.ev[1]));
+    *ms = (double)t / reps;
+    const double entries = (double)m.C * m.nv * m.nv + (double)m.B * m.nvb * m.nvb;
+    // slot lists, element values (K and M), resistivity per cell, boundary
+    // terms, matrix values written per wavenumber
+    *bytes = (double)(m.nnz + 1) * 4.0 + entries * 4.0 + (double)m.C * m.nv * m.nv * 16.0 + m.C * 8.0 +
+             (double)m.B * (m.nvb * m.nvb * 8.0 + c.nK * 8.0 + 4.0) + (double)c.nK * m.nnz * 8.0;
+    *flops = entries * c.nK * 3.0;
+}
+
 }  // namespace ertgb

@@ -93,7 +93,9 @@ int do_response(Context &c, const double *rho, double *rhoa, void *stream) {
     ensure_derived(c);
     cudaStream_t s = c.stream;
     c.have_pot = false;
+    c.stats.launches_response = 0;
     check_rho(c, rho, s);
+    c.d_rho_last = rho;
     MeshData &m = c.mesh;
     ERTGB_CUDA(cudaEventRecord(c.ev[0], s));
     c.d_S.alloc((size_t)c.nK * m.nnz);
@@ -113,6 +115,8 @@ int do_response(Context &c, const double *rho, double *rhoa, void *stream) {
     c.stats.ms_rhs = elapsed(c, 1, 2);
     c.stats.ms_solve = elapsed(c, 2, 3);
     c.stats.ms_collect = elapsed(c, 3, 4);
+    // check_rho, assemble, dinv, source_rho, rhs, finish_pot, collect, response
+    c.stats.launches_response += 8;
     c.have_pot = true;
     j.done();
     return status;
@@ -128,6 +132,7 @@ void do_jacobian(Context &c, const double *model, int n_model, void *J, int dtyp
     ERTGB_CUDA(cudaEventRecord(c.ev[5], s));
     ERTGB_CUDA(cudaEventSynchronize(c.ev[5]));
     c.stats.ms_jacobian = elapsed(c, 4, 5);
+    c.stats.launches_jacobian = 1;
     j.done();
 }
 
@@ -454,6 +459,25 @@ int ertgb_get_stats(const ertgb_ctx *ctx, ertgb_stats *stats) {
     if (!c || !stats) return ERTGB_BAD_INPUT;
     *stats = c->stats;
     return ERTGB_OK;
+}
+
+int ertgb_profile_kernel(ertgb_ctx *ctx, int kernel, int reps, void *J_scratch, double *ms, double *bytes,
+                         double *flops) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        ERTGB_REQUIRE(reps > 0 && ms && bytes && flops, "bad profile arguments");
+        if (!c->have_pot) throw Error(ERTGB_STATE, "profile needs a completed response");
+        ERTGB_CUDA(cudaSetDevice(c->device));
+        switch (kernel) {
+            case ERTGB_KERNEL_SPMM: profile_spmm(*c, reps, ms, bytes, flops); break;
+            case ERTGB_KERNEL_JACOBIAN:
+                ERTGB_REQUIRE(J_scratch, "Jacobian profile needs a scratch J");
+                profile_jacobian(*c, reps, (double *)J_scratch, ms, bytes, flops);
+                break;
+            case ERTGB_KERNEL_ASSEMBLE: profile_assemble(*c, reps, ms, bytes, flops); break;
+            default: throw Error(ERTGB_BAD_INPUT, "unknown kernel id");
+        }
+    });
 }
 
 }  // extern "C"

@@ -139,6 +139,7 @@ struct Context {
     DBuf<double> d_U;             // nE x nE collected electrode potentials
     DBuf<double> d_rhoa;
     bool have_pot = false;
+    const double *d_rho_last = nullptr;  // resistivity of the last response (caller's buffer)
     DBuf<double> d_rho_tmp, d_model_tmp;
     DBuf<char> d_J_tmp;
     ertgb_stats stats{};
@@ -158,6 +159,9 @@ void collect_response(Context &c, double *rhoa, cudaStream_t s);
 void check_rho(Context &c, const double *rho_cell, cudaStream_t s);
 // pcg.cu
 int pcg_solve(Context &c, cudaStream_t s);
+void profile_spmm(Context &c, int reps, double *ms, double *bytes, double *flops);
+void profile_assemble(Context &c, int reps, double *ms, double *bytes, double *flops);
+void profile_jacobian(Context &c, int reps, double *J, double *ms, double *bytes, double *flops);
 // jacobian.cu
 void jacobian(Context &c, const double *model, int n_model, void *J, int dtype, cudaStream_t s);
 // setup.cpp

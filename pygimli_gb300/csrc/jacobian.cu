@@ -171,4 +171,25 @@ void jacobian(Context &c, const double *model, int n_model, void *J, int dtype, 
     else launch<float>(c, mdl, (float *)J, s);
 }
 
+void profile_jacobian(Context &c, int reps, double *J, double *ms, double *bytes, double *flops) {
+    if (!c.have_pot) throw Error(ERTGB_STATE, "profile needs a completed response");
+    MeshData &m = c.mesh;
+    cudaStream_t s = c.stream;
+    launch<double>(c, nullptr, J, s);
+    ERTGB_CUDA(cudaEventRecord(c.ev[0], s));
+    for (int r = 0; r < reps; r++) launch<double>(c, nullptr, J, s);
+    ERTGB_CUDA(cudaEventRecord(c.ev[1], s));
+    ERTGB_CUDA(cudaEventSynchronize(c.ev[1]));
+    float t = 0.f;
+    ERTGB_CUDA(cudaEventElapsedTime(&t, c.ev[0], c.ev[1]));
+    *ms = (double)t / reps;
+    const double Ca = (double)m.pcell.size();
+    // J written once, potentials read once, cell nodes + element matrices,
+    // parameter->cell map, scheme
+    *bytes = (double)c.D * m.P * 8.0 + (double)m.n * c.Rpad * 8.0 + Ca * (m.nv * 4.0 + 2.0 * m.nv * m.nv * 8.0 + 4.0) +
+             (double)(m.P + 1) * 4.0 + (double)c.D * (16.0 + 8.0);
+    // V = S U per (cell, k, electrode) and the (datum, cell, k) products
+    *flops = Ca * c.nK * (c.nE + 1) * m.nv * (2.0 * m.nv + 2.0) + (double)c.D * Ca * c.nK * (m.nv * 4.0 + 2.0);
+}
+
 }  // namespace ertgb

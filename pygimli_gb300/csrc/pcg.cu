@@ -296,6 +296,7 @@ int pcg_solve(Context &c, cudaStream_t s) {
         cudaGraphDestroy(graph);
         ERTGB_CUDA(inst);
     }
+    c.stats.launches_response += 2;
     int32_t h_active = 0;
     int iterations = 0;
     int status = ERTGB_OK;
@@ -309,6 +310,7 @@ int pcg_solve(Context &c, cudaStream_t s) {
             }
             ERTGB_CUDA(cudaGraphLaunch(exec, s));
             iterations += kGraphIters;
+            c.stats.launches_response += 5 * kGraphIters;
             ERTGB_CUDA(cudaMemcpyAsync(&h_active, nactive, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
             ERTGB_CUDA(cudaStreamSynchronize(s));
         }
@@ -345,6 +347,33 @@ int pcg_solve(Context &c, cudaStream_t s) {
     c.stats.n_rhs = (int32_t)R;
     c.stats.max_rel_residual = maxres;
     return status;
+}
+
+void profile_spmm(Context &c, int reps, double *ms, double *bytes, double *flops) {
+    MeshData &m = c.mesh;
+    const int64_t n = m.n, Rpad = c.Rpad;
+    const int NB = (int)std::min<int64_t>(ceil_div(n, kRowsPerBlock), 1184);
+    const int ch = choose_ch(Rpad);
+    const dim3 sg((unsigned)NB, (unsigned)(Rpad / (32 * ch)));
+    if (c.d_q.n < (size_t)n * Rpad || c.d_part.n < (size_t)NB * Rpad * 3 || c.d_S.n < (size_t)c.nK * m.nnz)
+        throw Error(ERTGB_STATE, "profile needs a completed response");
+    cudaStream_t s = c.stream;
+    double *part_c = c.d_part.p + 2 * (size_t)NB * Rpad;
+    launch_spmm(ch, sg, s, n, m.nnz, c.nE, c.nK, Rpad, m.d_rowptr.p, m.d_colidx.p, c.d_S.p, c.d_x.p, c.d_q.p, part_c);
+    ERTGB_CUDA(cudaEventRecord(c.ev[0], s));
+    for (int r = 0; r < reps; r++)
+        launch_spmm(ch, sg, s, n, m.nnz, c.nE, c.nK, Rpad, m.d_rowptr.p, m.d_colidx.p, c.d_S.p, c.d_x.p, c.d_q.p,
+                    part_c);
+    ERTGB_CUDA(cudaEventRecord(c.ev[1], s));
+    ERTGB_CUDA(cudaEventSynchronize(c.ev[1]));
+    float t = 0.f;
+    ERTGB_CUDA(cudaEventElapsedTime(&t, c.ev[0], c.ev[1]));
+    *ms = (double)t / reps;
+    // matrix (column indices + every wavenumber's values), row pointers,
+    // p read once, q written once, block partials written
+    *bytes = (double)m.nnz * (4.0 + 8.0 * c.nK) + (double)(n + 1) * 4.0 + 2.0 * n * Rpad * 8.0 +
+             (double)NB * Rpad * 8.0;
+    *flops = 2.0 * (double)m.nnz * Rpad + 2.0 * (double)n * Rpad;
 }
 
 }  // namespace ertgb

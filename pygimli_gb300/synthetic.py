@@ -1,0 +1,54 @@
+"""Seeded synthetic ERT workloads with the shapes of the benchmark
+configurations (no field data is used anywhere):
+
+``line_2d``  2.5-D, 41 surface electrodes at 1 m, dipole-dipole (741 data),
+             para mesh paraDX 0.25 / paraDepth 10 m (~3.6k nodes, ~6.8k
+             triangles), resistivity log-uniform in [50, 200] Ohm m with a
+             10 and a 1000 Ohm m rectangle.
+``box_3d``   3-D, 96 electrodes on a 12 x 8 grid at 4 m, 5336 dipole-dipole /
+             pole-dipole / cross-line data, tetrahedral mesh of the para box
+             padded to +-500 m (~88k nodes, ~486k tetrahedra), resistivity
+             log-normal (mu = ln 100, sigma = 1) with three ellipsoids.
+             ``scheme="inline"`` keeps only the 540 inline dipole-dipole
+             data (same mesh and sources; a 2 GB instead of a 21 GB
+             Jacobian, used for profiler captures).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .data import DataContainerERT, createData, geometricFactors, grid_line_scheme, grid_scheme_3d
+from .mesh import create_box_mesh_3d, create_para_mesh_2d
+
+
+def line_2d(seed=1):
+    xs = np.arange(41.0)
+    mesh = create_para_mesh_2d(xs, para_dx=0.25, para_depth=10.0)
+    data = createData(xs, "dd")
+    data.set("k", geometricFactors(data, 2))
+    rng = np.random.default_rng(seed)
+    rho = np.exp(rng.uniform(np.log(50.0), np.log(200.0), mesh.cellCount()))
+    c = mesh.cellCenters()
+    x1, x2 = rng.uniform(5.0, 17.0), rng.uniform(23.0, 35.0)
+    rho[(np.abs(c[:, 0] - x1) < 3.0) & (c[:, 1] > -4.0) & (c[:, 1] < -1.0)] = 10.0
+    rho[(np.abs(c[:, 0] - x2) < 3.0) & (c[:, 1] > -6.0) & (c[:, 1] < -2.0)] = 1000.0
+    return mesh, data, rho
+
+
+def box_3d(seed=7, nx=12, ny=8, spacing=4.0, scheme="full", **mesh_kw):
+    e = np.array([(x, y) for x in np.arange(nx) * spacing for y in np.arange(ny) * spacing])
+    mesh = create_box_mesh_3d(e, **mesh_kw)
+    ab = grid_scheme_3d(nx, ny) if scheme == "full" else grid_line_scheme((nx, ny), "dd")
+    data = DataContainerERT(np.column_stack([e, np.zeros(len(e))]), ab)
+    data.set("k", geometricFactors(data, 3))
+    rng = np.random.default_rng(seed)
+    rho = np.exp(rng.normal(np.log(100.0), 1.0, mesh.cellCount()))
+    c = mesh.cellCenters()
+    span = np.array([(nx - 1) * spacing, (ny - 1) * spacing])
+    for val in (10.0, 1000.0, 30.0):
+        ctr = np.array([rng.uniform(0.1, 0.9) * span[0], rng.uniform(0.1, 0.9) * span[1],
+                        -rng.uniform(3.0, 12.0)])
+        ax = rng.uniform([3.0, 3.0, 1.5], [8.0, 6.0, 4.0])
+        inside = np.sum(((c - ctr) / ax) ** 2, axis=1) <= 1.0
+        rho[inside] = val
+    return mesh, data, rho
