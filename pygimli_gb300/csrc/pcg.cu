@@ -29,6 +29,7 @@ namespace {
 
 constexpr int kRowsPerBlock = 8;  // warps per block in spmm, rows per block in vector kernels
 constexpr int kGraphIters = 16;
+constexpr int kPartRows = 608;  // block partial rows of every column reduction (4 x 152 SMs)
 
 // per-column scalar slots in Context::d_col
 enum Col { RHO = 0, ALPHA, BETA, BNORM2, RNORM2, PQ, NCOL };
@@ -113,41 +114,51 @@ __global__ void k_init(int64_t n, int nE, int nK, int64_t R, int64_t Rpad, const
     }
 }
 
+// Column reductions: block (32, 32), grid Rpad/32; thread (tx, ty) sums the
+// partial rows ty, ty+32, ... of column t, then the 32 sums are added in a
+// fixed order (deterministic).
+__device__ inline double col_sum(const double *__restrict__ part, int NB, int64_t Rpad, int64_t t,
+                                 double (*red)[33]) {
+    double s = 0.0;
+    for (int b = threadIdx.y; b < NB; b += 32) s += part[(int64_t)b * Rpad + t];
+    red[threadIdx.y][threadIdx.x] = s;
+    __syncthreads();
+    double tot = 0.0;
+    if (threadIdx.y == 0)
+        for (int w = 0; w < 32; w++) tot += red[w][threadIdx.x];
+    return tot;
+}
+
 __global__ void k_finish_init(int64_t Rpad, int64_t R, int NB, const double *__restrict__ part_a,
                               const double *__restrict__ part_b, double *__restrict__ col,
                               int32_t *__restrict__ active, int32_t *__restrict__ iters,
                               int32_t *__restrict__ nactive) {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < Rpad;
-         t += (int64_t)gridDim.x * blockDim.x) {
-        double rz = 0.0, rr = 0.0;
-        for (int b = 0; b < NB; b++) {
-            rz += part_a[(int64_t)b * Rpad + t];
-            rr += part_b[(int64_t)b * Rpad + t];
-        }
-        col[RHO * Rpad + t] = rz;
-        col[BNORM2 * Rpad + t] = rr;
-        col[RNORM2 * Rpad + t] = rr;
-        col[ALPHA * Rpad + t] = 0.0;
-        col[BETA * Rpad + t] = 0.0;
-        const int a = (t < R && rr > 0.0) ? 1 : 0;
-        active[t] = a;
-        iters[t] = 0;
-        if (a) atomicAdd(nactive, 1);
-    }
+    __shared__ double ra[32][33], rb[32][33];
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    const double rz = col_sum(part_a, NB, Rpad, t, ra);
+    const double rr = col_sum(part_b, NB, Rpad, t, rb);
+    if (threadIdx.y != 0) return;
+    col[RHO * Rpad + t] = rz;
+    col[BNORM2 * Rpad + t] = rr;
+    col[RNORM2 * Rpad + t] = rr;
+    col[ALPHA * Rpad + t] = 0.0;
+    col[BETA * Rpad + t] = 0.0;
+    const int a = (t < R && rr > 0.0) ? 1 : 0;
+    active[t] = a;
+    iters[t] = 0;
+    if (a) atomicAdd(nactive, 1);
 }
 
 __global__ void k_finish_alpha(int64_t Rpad, int NB, const double *__restrict__ part,
                                double *__restrict__ col, const int32_t *__restrict__ active,
                                int32_t *__restrict__ nactive) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) *nactive = 0;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < Rpad;
-         t += (int64_t)gridDim.x * blockDim.x) {
-        if (!active[t]) continue;
-        double pq = 0.0;
-        for (int b = 0; b < NB; b++) pq += part[(int64_t)b * Rpad + t];
-        col[PQ * Rpad + t] = pq;
-        col[ALPHA * Rpad + t] = (pq != 0.0) ? col[RHO * Rpad + t] / pq : 0.0;
-    }
+    __shared__ double red[32][33];
+    if (blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) *nactive = 0;
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    const double pq = col_sum(part, NB, Rpad, t, red);
+    if (threadIdx.y != 0 || !active[t]) return;
+    col[PQ * Rpad + t] = pq;
+    col[ALPHA * Rpad + t] = (pq != 0.0) ? col[RHO * Rpad + t] / pq : 0.0;
 }
 
 __global__ void k_update_xr(int64_t n, int nE, int64_t R, int64_t Rpad, const double *__restrict__ dinv,
@@ -191,27 +202,24 @@ __global__ void k_finish_beta(int64_t Rpad, int NB, double rtol2, const double *
                               const double *__restrict__ part_b, double *__restrict__ col,
                               int32_t *__restrict__ active, int32_t *__restrict__ iters,
                               int32_t *__restrict__ nactive) {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < Rpad;
-         t += (int64_t)gridDim.x * blockDim.x) {
-        if (!active[t]) {
-            col[BETA * Rpad + t] = 0.0;
-            continue;
-        }
-        double rz = 0.0, rr = 0.0;
-        for (int b = 0; b < NB; b++) {
-            rz += part_a[(int64_t)b * Rpad + t];
-            rr += part_b[(int64_t)b * Rpad + t];
-        }
-        iters[t] += 1;
-        col[RNORM2 * Rpad + t] = rr;
-        const double rho = col[RHO * Rpad + t];
-        col[BETA * Rpad + t] = (rho != 0.0) ? rz / rho : 0.0;
-        col[RHO * Rpad + t] = rz;
-        if (rr <= rtol2 * col[BNORM2 * Rpad + t] || !(rr == rr)) {
-            active[t] = 0;
-        } else {
-            atomicAdd(nactive, 1);
-        }
+    __shared__ double ra[32][33], rb[32][33];
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    const double rz = col_sum(part_a, NB, Rpad, t, ra);
+    const double rr = col_sum(part_b, NB, Rpad, t, rb);
+    if (threadIdx.y != 0) return;
+    if (!active[t]) {
+        col[BETA * Rpad + t] = 0.0;
+        return;
+    }
+    iters[t] += 1;
+    col[RNORM2 * Rpad + t] = rr;
+    const double rho = col[RHO * Rpad + t];
+    col[BETA * Rpad + t] = (rho != 0.0) ? rz / rho : 0.0;
+    col[RHO * Rpad + t] = rz;
+    if (rr <= rtol2 * col[BNORM2 * Rpad + t] || !(rr == rr)) {
+        active[t] = 0;
+    } else {
+        atomicAdd(nactive, 1);
     }
 }
 
@@ -254,7 +262,7 @@ void launch_spmm(int ch, dim3 grid, cudaStream_t s, int64_t n, int64_t nnz, int 
 int pcg_solve(Context &c, cudaStream_t s) {
     MeshData &m = c.mesh;
     const int64_t n = m.n, Rpad = c.Rpad, R = c.R;
-    const int NB = (int)std::min<int64_t>(ceil_div(n, kRowsPerBlock), 1184);
+    const int NB = (int)std::min<int64_t>(ceil_div(n, kRowsPerBlock), kPartRows);
     const int ch = choose_ch(Rpad);
     const int nchunk = (int)(Rpad / (32 * ch));
     // workspaces
@@ -270,10 +278,11 @@ int pcg_solve(Context &c, cudaStream_t s) {
     ERTGB_CUDA(cudaMemsetAsync(nactive, 0, sizeof(int32_t), s));
     const dim3 vb(32, kRowsPerBlock), vg((unsigned)(Rpad / 32), (unsigned)NB);
     const dim3 sg((unsigned)NB, (unsigned)nchunk);
-    const unsigned fg = (unsigned)ceil_div(Rpad, 256);
+    const unsigned fg = (unsigned)(Rpad / 32);
+    const dim3 fb(32, 32);
     const double rtol2 = c.rtol * c.rtol;
     k_init<<<vg, vb, 0, s>>>(n, c.nE, c.nK, R, Rpad, c.d_dinv.p, c.d_r.p, c.d_p.p, part_a, part_b);
-    k_finish_init<<<fg, 256, 0, s>>>(Rpad, R, NB, part_a, part_b, c.d_col.p, active, iters, nactive);
+    k_finish_init<<<fg, fb, 0, s>>>(Rpad, R, NB, part_a, part_b, c.d_col.p, active, iters, nactive);
     ERTGB_CUDA(cudaGetLastError());
 
     // capture a chunk of iterations
@@ -283,10 +292,10 @@ int pcg_solve(Context &c, cudaStream_t s) {
     for (int it = 0; it < kGraphIters; it++) {
         launch_spmm(ch, sg, s, n, m.nnz, c.nE, c.nK, Rpad, m.d_rowptr.p, m.d_colidx.p, c.d_S.p, c.d_p.p, c.d_q.p,
                     part_c);
-        k_finish_alpha<<<fg, 256, 0, s>>>(Rpad, NB, part_c, c.d_col.p, active, nactive);
+        k_finish_alpha<<<fg, fb, 0, s>>>(Rpad, NB, part_c, c.d_col.p, active, nactive);
         k_update_xr<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, c.d_dinv.p, c.d_col.p, active, c.d_x.p, c.d_r.p,
                                       c.d_p.p, c.d_q.p, part_a, part_b);
-        k_finish_beta<<<fg, 256, 0, s>>>(Rpad, NB, rtol2, part_a, part_b, c.d_col.p, active, iters, nactive);
+        k_finish_beta<<<fg, fb, 0, s>>>(Rpad, NB, rtol2, part_a, part_b, c.d_col.p, active, iters, nactive);
         k_update_p<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, c.d_dinv.p, c.d_col.p, active, c.d_r.p, c.d_p.p);
     }
     cudaError_t cap = cudaStreamEndCapture(s, &graph);
@@ -352,7 +361,7 @@ int pcg_solve(Context &c, cudaStream_t s) {
 void profile_spmm(Context &c, int reps, double *ms, double *bytes, double *flops) {
     MeshData &m = c.mesh;
     const int64_t n = m.n, Rpad = c.Rpad;
-    const int NB = (int)std::min<int64_t>(ceil_div(n, kRowsPerBlock), 1184);
+    const int NB = (int)std::min<int64_t>(ceil_div(n, kRowsPerBlock), kPartRows);
     const int ch = choose_ch(Rpad);
     const dim3 sg((unsigned)NB, (unsigned)(Rpad / (32 * ch)));
     if (c.d_q.n < (size_t)n * Rpad || c.d_part.n < (size_t)NB * Rpad * 3 || c.d_S.n < (size_t)c.nK * m.nnz)
