@@ -139,6 +139,19 @@ int ertgb_get_potentials(ertgb_ctx *ctx, double *pot_host);
 int ertgb_get_primary(ertgb_ctx *ctx, double *prim_host);
 int ertgb_get_stats(const ertgb_ctx *ctx, ertgb_stats *stats);
 
+/* Multi-right-hand-side CSR product with column dot products, the block
+ * PCG's operator kernel, for callers that run their own Krylov iterations
+ * on device arrays:  Y[:, t] = A_{k(t)} X[:, t] and dots[t] = X[:, t] . Y[:, t],
+ * k(t) = min(t / n_per_k, n_k - 1).  CSR int32 (rowptr n+1, colidx nnz),
+ * vals n_k x nnz, X and Y n x ld row-major (ld a multiple of 32), dots ld.
+ * Replaces the reference's SparseMatrix::mult (core/src/sparsematrix.h:
+ * 825-876) applied column by column.  Context free; scratch for the block
+ * partials is taken from the stream-ordered allocator.  Errors are reported
+ * through ertgb_last_error(NULL). */
+int ertgb_csr_spmm_dot(int64_t n, int64_t nnz, const int32_t *rowptr_dev, const int32_t *colidx_dev,
+                       const double *vals_dev, int n_k, int n_per_k, int64_t ld, const double *X_dev,
+                       double *Y_dev, double *dots_dev, void *stream);
+
 /* Measurement helper with no counterpart in the reference: launches one
  * kernel ``reps`` times on the context stream (on the state of the last
  * response) and returns the mean launch time from CUDA events, with the

@@ -13,6 +13,21 @@ using namespace ertgb;
 namespace {
 
 std::string g_create_error;
+thread_local std::string g_free_error;  // last error of the context-free entry points
+
+template <class F> int guard_free(F &&f) {
+    try {
+        f();
+        g_free_error.clear();
+        return ERTGB_OK;
+    } catch (Error &e) {
+        g_free_error = e.what();
+        return e.code;
+    } catch (std::exception &e) {
+        g_free_error = e.what();
+        return ERTGB_BAD_INPUT;
+    }
+}
 
 template <class F> int guard(Context *c, F &&f) {
     if (!c) return ERTGB_BAD_INPUT;
@@ -55,6 +70,18 @@ struct StreamJoin {
         }
     }
 };
+
+}  // namespace
+
+void ertgb::check_spmm_args(int64_t n, int64_t nnz, const void *rowptr, const void *colidx, const void *vals, int n_k,
+                            int n_per_k, int64_t ld, const void *X, const void *Y, const void *dots) {
+    ERTGB_REQUIRE(n > 0 && nnz > 0 && n_k > 0 && n_per_k > 0, "empty operator");
+    ERTGB_REQUIRE(ld > 0 && ld % 32 == 0, "ld must be a positive multiple of 32");
+    ERTGB_REQUIRE(rowptr && colidx && vals && X && Y && dots, "null device pointer");
+    ERTGB_REQUIRE(n <= INT32_MAX && nnz <= INT32_MAX, "int32 CSR indices");
+}
+
+namespace {
 
 void ensure_derived(Context &c) {
     if (!c.have_mesh) throw Error(ERTGB_STATE, "no mesh set");
@@ -174,7 +201,7 @@ int ertgb_destroy(ertgb_ctx *ctx) {
 
 const char *ertgb_last_error(const ertgb_ctx *ctx) {
     const Context *c = reinterpret_cast<const Context *>(ctx);
-    if (!c) return g_create_error.c_str();
+    if (!c) return g_free_error.empty() ? g_create_error.c_str() : g_free_error.c_str();
     return c->last_error.c_str();
 }
 
@@ -459,6 +486,24 @@ int ertgb_get_stats(const ertgb_ctx *ctx, ertgb_stats *stats) {
     if (!c || !stats) return ERTGB_BAD_INPUT;
     *stats = c->stats;
     return ERTGB_OK;
+}
+
+int ertgb_csr_spmm_dot(int64_t n, int64_t nnz, const int32_t *rowptr, const int32_t *colidx, const double *vals,
+                       int n_k, int n_per_k, int64_t ld, const double *X, double *Y, double *dots, void *stream) {
+    return guard_free([&] {
+        check_spmm_args(n, nnz, rowptr, colidx, vals, n_k, n_per_k, ld, X, Y, dots);
+        cudaStream_t s = (cudaStream_t)stream;
+        const int NB = spmm_partial_rows(n, 608);
+        double *part = nullptr;
+        ERTGB_CUDA(cudaMallocAsync((void **)&part, sizeof(double) * (size_t)NB * ld, s));
+        try {
+            spmm_dot_launch(n, nnz, rowptr, colidx, vals, n_k, n_per_k, ld, X, Y, dots, part, NB, s);
+        } catch (...) {
+            cudaFreeAsync(part, s);
+            throw;
+        }
+        ERTGB_CUDA(cudaFreeAsync(part, s));
+    });
 }
 
 int ertgb_profile_kernel(ertgb_ctx *ctx, int kernel, int reps, void *J_scratch, double *ms, double *bytes,

@@ -160,6 +160,15 @@ void check_rho(Context &c, const double *rho_cell, cudaStream_t s);
 // pcg.cu
 int pcg_solve(Context &c, cudaStream_t s);
 void profile_spmm(Context &c, int reps, double *ms, double *bytes, double *flops);
+// Y = A X with column dots (the PCG operator kernel) on raw CSR arrays; the
+// NB x ld block partials live in ``partials``.
+int spmm_partial_rows(int64_t n, int cap);
+void spmm_dot_launch(int64_t n, int64_t nnz, const int32_t *rowptr, const int32_t *colidx, const double *vals, int nK,
+                     int n_per_k, int64_t ld, const double *X, double *Y, double *dots, double *partials, int NB,
+                     cudaStream_t s);
+// Checks shared by the context-free operator entry points; throws Error.
+void check_spmm_args(int64_t n, int64_t nnz, const void *rowptr, const void *colidx, const void *vals, int n_k,
+                     int n_per_k, int64_t ld, const void *X, const void *Y, const void *dots);
 void profile_assemble(Context &c, int reps, double *ms, double *bytes, double *flops);
 void profile_jacobian(Context &c, int reps, double *J, double *ms, double *bytes, double *flops);
 // jacobian.cu

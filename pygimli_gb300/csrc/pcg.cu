@@ -358,6 +358,28 @@ int pcg_solve(Context &c, cudaStream_t s) {
     return status;
 }
 
+namespace {
+__global__ void k_col_total(int64_t Rpad, int NB, const double *__restrict__ part, double *__restrict__ out) {
+    __shared__ double red[32][33];
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    const double s = col_sum(part, NB, Rpad, t, red);
+    if (threadIdx.y == 0) out[t] = s;
+}
+}  // namespace
+
+int spmm_partial_rows(int64_t n, int cap) { return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, kRowsPerBlock), cap)); }
+
+void spmm_dot_launch(int64_t n, int64_t nnz, const int32_t *rowptr, const int32_t *colidx, const double *vals, int nK,
+                     int n_per_k, int64_t ld, const double *X, double *Y, double *dots, double *partials, int NB,
+                     cudaStream_t s) {
+    const int ch = choose_ch(ld);
+    const dim3 sg((unsigned)NB, (unsigned)(ld / (32 * ch)));
+    launch_spmm(ch, sg, s, n, nnz, n_per_k, nK, ld, rowptr, colidx, vals, X, Y, partials);
+    ERTGB_CUDA(cudaGetLastError());
+    k_col_total<<<(unsigned)(ld / 32), dim3(32, 32), 0, s>>>(ld, NB, partials, dots);
+    ERTGB_CUDA(cudaGetLastError());
+}
+
 void profile_spmm(Context &c, int reps, double *ms, double *bytes, double *flops) {
     MeshData &m = c.mesh;
     const int64_t n = m.n, Rpad = c.Rpad;

@@ -241,3 +241,44 @@ def test_3d_config_properties(torch):
     assert float(np.max(np.abs(rh - 100.0) / 100.0)) < 0.05
     print(f"3d config: iters {st['iterations']} solve {st['ms_solve']:.1f} ms, homogeneous "
           f"max dev {np.max(np.abs(rh - 100.0)):.3f}")
+
+
+def _spmm_case(golden_dir, torch, seed=0, ld=64):
+    """Golden system matrices of three wavenumbers as one multi-matrix
+    operator, 11 columns per matrix (33 used, padded to 64)."""
+    z = np.load(os.path.join(golden_dir, "ert2d_small.npz"))
+    rp, ci, vals = z["rowptr"], z["colidx"], z["S"]
+    n, nnz = len(rp) - 1, len(ci)
+    rng = np.random.default_rng(seed)
+    X = rng.standard_normal((n, ld))
+    dev = torch.device("cuda")
+    t = {"rp": torch.from_numpy(rp.astype(np.int32)).to(dev), "ci": torch.from_numpy(ci.astype(np.int32)).to(dev),
+         "v": torch.from_numpy(np.ascontiguousarray(vals)).to(dev), "X": torch.from_numpy(X).to(dev)}
+    import scipy.sparse as sp
+    Y = np.zeros((n, ld))
+    for col in range(ld):
+        kk = min(col // 11, 2)
+        Y[:, col] = sp.csr_matrix((vals[kk], ci, rp), shape=(n, n)) @ X[:, col]
+    return n, nnz, t, X, Y, np.einsum("ij,ij->j", X, Y)
+
+
+def _call_spmm(fn, n, nnz, t, ld, torch):
+    Y = torch.empty((n, ld), dtype=torch.float64, device="cuda")
+    dots = torch.empty(ld, dtype=torch.float64, device="cuda")
+    vp = ctypes.c_void_p
+    rc = fn(n, nnz, vp(t["rp"].data_ptr()), vp(t["ci"].data_ptr()), vp(t["v"].data_ptr()), 3, 11, ld,
+            vp(t["X"].data_ptr()), vp(Y.data_ptr()), vp(dots.data_ptr()), vp(torch.cuda.current_stream().cuda_stream))
+    return rc, Y, dots
+
+
+def test_csr_spmm_dot_entry(torch, golden_dir):
+    from pygimli_gb300 import _native
+    L = _native.load()
+    n, nnz, t, X, Y_ref, d_ref = _spmm_case(golden_dir, torch)
+    rc, Y, dots = _call_spmm(L.ertgb_csr_spmm_dot, n, nnz, t, 64, torch)
+    _native.check(None, rc)
+    torch.cuda.synchronize()
+    assert rel(Y.cpu().numpy(), Y_ref) <= TOL_MAT
+    assert rel(dots.cpu().numpy(), d_ref) <= TOL_MAT
+    rc, _, _ = _call_spmm(L.ertgb_csr_spmm_dot, n, nnz, t, 48, torch)
+    assert rc == _native.BAD_INPUT and b"multiple of 32" in L.ertgb_last_error(None)
