@@ -152,6 +152,20 @@ int ertgb_csr_spmm_dot(int64_t n, int64_t nnz, const int32_t *rowptr_dev, const 
                        const double *vals_dev, int n_k, int n_per_k, int64_t ld, const double *X_dev,
                        double *Y_dev, double *dots_dev, void *stream);
 
+/* Allocation-free variant of ertgb_csr_spmm_dot, for callers that cannot
+ * allocate device memory at call time (a host framework that owns the device
+ * memory through its own pool, or a loop that must not allocate after
+ * start-up).  No counterpart in the reference.  Same arguments and results;
+ * the block partials live in a fixed 2 MiB device array of the library
+ * (every GPU that loads the library holds it until exit), so ld is limited
+ * to 1024 columns (larger ld: ERTGB_BAD_INPUT).  Calls no allocator.  The
+ * first call on a device looks up the array's address and should come
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU race and must be ordered by the caller. */
+int ertgb_csr_spmm_dot_noalloc(int64_t n, int64_t nnz, const int32_t *rowptr_dev, const int32_t *colidx_dev,
+                               const double *vals_dev, int n_k, int n_per_k, int64_t ld, const double *X_dev,
+                               double *Y_dev, double *dots_dev, void *stream);
+
 /* Measurement helper with no counterpart in the reference: launches one
  * kernel ``reps`` times on the context stream (on the state of the last
  * response) and returns the mean launch time from CUDA events, with the

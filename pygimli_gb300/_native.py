@@ -54,6 +54,7 @@ SIGNATURES = {
     "ertgb_get_primary": (_ci, [_vp, _vp]),
     "ertgb_get_stats": (_ci, [_vp, ctypes.POINTER(Stats)]),
     "ertgb_csr_spmm_dot": (_ci, [_i64, _i64, _vp, _vp, _vp, _ci, _ci, _i64, _vp, _vp, _vp, _vp]),
+    "ertgb_csr_spmm_dot_noalloc": (_ci, [_i64, _i64, _vp, _vp, _vp, _ci, _ci, _i64, _vp, _vp, _vp, _vp]),
     "ertgb_profile_kernel": (_ci, [_vp, _ci, _ci, _vp, ctypes.POINTER(_d), ctypes.POINTER(_d),
                                    ctypes.POINTER(_d)]),
 }

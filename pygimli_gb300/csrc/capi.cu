@@ -73,6 +73,8 @@ struct StreamJoin {
 
 }  // namespace
 
+void ertgb::set_free_error(const std::string &msg) { g_free_error = msg; }
+
 void ertgb::check_spmm_args(int64_t n, int64_t nnz, const void *rowptr, const void *colidx, const void *vals, int n_k,
                             int n_per_k, int64_t ld, const void *X, const void *Y, const void *dots) {
     ERTGB_REQUIRE(n > 0 && nnz > 0 && n_k > 0 && n_per_k > 0, "empty operator");

@@ -166,6 +166,8 @@ int spmm_partial_rows(int64_t n, int cap);
 void spmm_dot_launch(int64_t n, int64_t nnz, const int32_t *rowptr, const int32_t *colidx, const double *vals, int nK,
                      int n_per_k, int64_t ld, const double *X, double *Y, double *dots, double *partials, int NB,
                      cudaStream_t s);
+// Message returned by ertgb_last_error(NULL) for the context-free entry points.
+void set_free_error(const std::string &msg);
 // Checks shared by the context-free operator entry points; throws Error.
 void check_spmm_args(int64_t n, int64_t nnz, const void *rowptr, const void *colidx, const void *vals, int n_k,
                      int n_per_k, int64_t ld, const void *X, const void *Y, const void *dots);
