@@ -37,6 +37,13 @@ typedef enum {
 /* Preconditioners of the block PCG. */
 typedef enum { ERTGB_PRECOND_JACOBI = 0 } ertgb_precond;
 
+/* Arithmetic of the block PCG.  FP64: everything in FP64.  MIXED: FP32
+ * recurrence (operator, preconditioner, vectors) with FP64 reliable updates
+ * every 64 iterations (the FP64 solution accumulates the FP32 increments and
+ * the residual restarts from the FP64 true residual); convergence is tested
+ * on the FP64 true residual, so the tolerance means the same in both. */
+typedef enum { ERTGB_PRECISION_FP64 = 0, ERTGB_PRECISION_MIXED = 1 } ertgb_precision;
+
 /* Solver statistics of the last response. */
 typedef struct {
     int32_t iterations;       /* PCG iterations until every column converged */
@@ -55,7 +62,8 @@ typedef struct {
 typedef enum {
     ERTGB_KERNEL_SPMM = 0,     /* PCG operator q = A p with column dots       */
     ERTGB_KERNEL_JACOBIAN = 1, /* Jacobian of the last response (FP64 J)      */
-    ERTGB_KERNEL_ASSEMBLE = 2  /* system matrices of the last response        */
+    ERTGB_KERNEL_ASSEMBLE = 2, /* system matrices of the last response        */
+    ERTGB_KERNEL_SPMM32 = 3    /* FP32 operator of the mixed-precision PCG    */
 } ertgb_kernel;
 
 /* Create a context on CUDA device ``device``.  Replaces the construction of
@@ -100,6 +108,9 @@ int ertgb_set_scheme(ertgb_ctx *ctx, int n_data, const int32_t *abmn_host, const
 
 /* Solver controls: relative residual tolerance, iteration cap, preconditioner. */
 int ertgb_set_solver(ertgb_ctx *ctx, double rtol, int max_iter, int precond);
+/* Solver arithmetic (ertgb_precision).  No counterpart in the reference,
+ * whose direct solver is FP64. */
+int ertgb_set_precision(ertgb_ctx *ctx, int precision);
 
 /* Forward response: DCMultiElectrodeModelling::response
  * (core/src/bert/dcfemmodelling.cpp:1085-1197) for a per-cell resistivity

@@ -3,6 +3,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <new>
 #include <set>
 
@@ -96,13 +97,13 @@ void ensure_derived(Context &c) {
         c.Rpad = ceil_div(c.R, 32) * 32;
         compute_boundary_alpha(c);
         compute_primary(c);
-        build_jacobian_tiles(c);
-        MeshData &m = c.mesh;
-        m.d_pcell_ptr.upload(m.pcell_ptr, c.stream);
-        m.d_pcell.upload(m.pcell, c.stream);
-        m.d_jtile_p.upload(m.jtile_p, c.stream);
         c.prim_ready = true;
         c.s1_ready = false;
+        c.jac_ready = false;
+    }
+    if (!c.jac_ready) {
+        build_jacobian_tiles(c);
+        c.jac_ready = true;
     }
     if (!c.s1_ready) {
         assemble_unit(c, c.stream);
@@ -134,7 +135,7 @@ int do_response(Context &c, const double *rho, double *rhoa, void *stream) {
     c.d_r.alloc((size_t)m.n * c.Rpad);
     build_rhs(c, s);
     ERTGB_CUDA(cudaEventRecord(c.ev[2], s));
-    status = pcg_solve(c, s);
+    status = (c.precision == ERTGB_PRECISION_MIXED) ? pcg_solve_mixed(c, s) : pcg_solve(c, s);
     ERTGB_CUDA(cudaEventRecord(c.ev[3], s));
     finish_potentials(c, s);
     collect_response(c, rhoa, s);
@@ -350,9 +351,28 @@ int ertgb_set_scheme(ertgb_ctx *ctx, int n_data, const int32_t *abmn, const doub
         c->D = n_data;
         c->d_abmn.upload(abmn, (size_t)4 * n_data, c->stream);
         c->d_kfac.upload(kfac, (size_t)n_data, c->stream);
+        // distinct current and potential dipoles, in order of first use
+        std::map<std::pair<int32_t, int32_t>, int32_t> amap, mmap;
+        std::vector<int32_t> dip_a, dip_m, data_dip((size_t)2 * n_data);
+        for (int64_t d = 0; d < n_data; d++) {
+            const auto ka = std::make_pair(abmn[4 * d], abmn[4 * d + 1]);
+            const auto km = std::make_pair(abmn[4 * d + 2], abmn[4 * d + 3]);
+            auto ia = amap.emplace(ka, (int32_t)amap.size());
+            if (ia.second) { dip_a.push_back(ka.first); dip_a.push_back(ka.second); }
+            auto im = mmap.emplace(km, (int32_t)mmap.size());
+            if (im.second) { dip_m.push_back(km.first); dip_m.push_back(km.second); }
+            data_dip[2 * d] = ia.first->second;
+            data_dip[2 * d + 1] = im.first->second;
+        }
+        c->nA = (int)amap.size();
+        c->nM = (int)mmap.size();
+        c->d_dip_a.upload(dip_a, c->stream);
+        c->d_dip_m.upload(dip_m, c->stream);
+        c->d_data_dip.upload(data_dip, c->stream);
         ERTGB_CUDA(cudaStreamSynchronize(c->stream));
         c->have_scheme = true;
         c->have_pot = false;
+        c->jac_ready = false;
     });
 }
 
@@ -365,6 +385,14 @@ int ertgb_set_solver(ertgb_ctx *ctx, double rtol, int max_iter, int precond) {
         c->rtol = rtol;
         c->max_iter = max_iter;
         c->precond = precond;
+    });
+}
+
+int ertgb_set_precision(ertgb_ctx *ctx, int precision) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        ERTGB_REQUIRE(precision == ERTGB_PRECISION_FP64 || precision == ERTGB_PRECISION_MIXED, "unknown precision");
+        c->precision = precision;
     });
 }
 
@@ -522,6 +550,7 @@ int ertgb_profile_kernel(ertgb_ctx *ctx, int kernel, int reps, void *J_scratch, 
                 profile_jacobian(*c, reps, (double *)J_scratch, ms, bytes, flops);
                 break;
             case ERTGB_KERNEL_ASSEMBLE: profile_assemble(*c, reps, ms, bytes, flops); break;
+            case ERTGB_KERNEL_SPMM32: profile_spmm32(*c, reps, ms, bytes, flops); break;
             default: throw Error(ERTGB_BAD_INPUT, "unknown kernel id");
         }
     });

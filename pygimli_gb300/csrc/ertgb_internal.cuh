@@ -85,9 +85,14 @@ struct MeshData {
     // parameter -> cells (sorted by parameter), for the Jacobian
     std::vector<int32_t> pcell_ptr, pcell;
     DBuf<int32_t> d_pcell_ptr, d_pcell;
-    std::vector<int32_t> jtile_p;  // Jacobian tiles: parameter boundaries
-    DBuf<int32_t> d_jtile_p;
-    int jtile_cells_max = 0;
+};
+
+// Jacobian tiles for one table precision: parameter boundaries of each tile
+// and the cells one tile may stage.
+struct JacTiles {
+    std::vector<int32_t> tile_p;
+    DBuf<int32_t> d_tile_p;
+    int max_cells = 0;
 };
 
 struct Context {
@@ -117,10 +122,17 @@ struct Context {
     DBuf<int32_t> d_abmn;
     DBuf<double> d_kfac;
     bool have_scheme = false;
+    // distinct current (a, b) and potential (m, n) dipoles of the scheme
+    int nA = 0, nM = 0;
+    DBuf<int32_t> d_dip_a, d_dip_m, d_data_dip;  // nA x 2, nM x 2, D x 2 (ia, im)
+    JacTiles jtiles[2];                          // FP64 and FP32 tables
+    bool jac_ready = false;
+    DBuf<char> d_jscale;                         // per-datum / per-parameter scales
     // solver
     double rtol = 1e-10;
     int max_iter = 20000;
     int precond = ERTGB_PRECOND_JACOBI;
+    int precision = ERTGB_PRECISION_FP64;
     // derived per (mesh, electrodes, kw)
     int64_t R = 0, Rpad = 0;     // right-hand sides nK*nE, padded to 32
     bool prim_ready = false;
@@ -132,7 +144,9 @@ struct Context {
     DBuf<double> d_S;             // nK x nnz
     DBuf<double> d_dinv;          // nK x n  (1 / diag)
     DBuf<double> d_rhos;          // nE source resistivity
-    DBuf<double> d_x, d_r, d_p, d_q, d_b;  // n x Rpad
+    DBuf<double> d_x, d_r, d_p, d_q;  // n x Rpad (d_r holds the right-hand sides)
+    // mixed precision: FP32 matrix, Jacobi diagonal and recurrence vectors
+    DBuf<float> d_S32, d_dinv32, d_r32, d_p32, d_q32, d_y32;
     DBuf<double> d_part;          // reduction partials
     DBuf<double> d_col;           // per-column scalars (see pcg.cu)
     DBuf<int32_t> d_active;
@@ -159,6 +173,9 @@ void collect_response(Context &c, double *rhoa, cudaStream_t s);
 void check_rho(Context &c, const double *rho_cell, cudaStream_t s);
 // pcg.cu
 int pcg_solve(Context &c, cudaStream_t s);
+// pcg_mixed.cu
+int pcg_solve_mixed(Context &c, cudaStream_t s);
+void profile_spmm32(Context &c, int reps, double *ms, double *bytes, double *flops);
 void profile_spmm(Context &c, int reps, double *ms, double *bytes, double *flops);
 // Y = A X with column dots (the PCG operator kernel) on raw CSR arrays; the
 // NB x ld block partials live in ``partials``.

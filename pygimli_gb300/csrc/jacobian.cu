@@ -1,9 +1,9 @@
-// Reciprocity Jacobian of the DC forward operator (FP64).
+// Reciprocity Jacobian of the DC forward operator.
 //
 //   J[d, p] = sum_{cells c with marker p} sum_k w_k
 //             ((K_c + k^2 M_c)(u_a,k - u_b,k)) . (u_m,k - u_n,k)
-//   then J[d, p] /= (model_p^2 / kfac_d) when the model has one value per
-//   parameter.
+//   then J[d, p] *= kfac_d / model_p^2 when the model has one value per
+//   parameter (the reference divides by model_p^2 / kfac_d).
 // Reference: createSensitivityCol_ / CreateSensitivityColMT::calc2
 // (core/src/bert/bertJacobian.cpp:70-119, 267-421), ElementMatrix::mult
 // (core/src/elementmatrix.h:280-293), scaling in
@@ -11,12 +11,19 @@
 // sub-potentials of the last response (column k*nE + e of the n x Rpad
 // block); an electrode index -1 contributes a zero potential.
 //
-// Layout: one block per tile of consecutive parameters (at most 32, their
-// cells within the shared-memory budget).  The block stages, for each cell of
-// the tile and each wavenumber, the node potentials U[i][e] of every
-// electrode (plus a zero column for index -1) and V = S U, then threads walk
-// the (datum, parameter) pairs with the parameter fastest, so that each warp
-// writes contiguous runs of a J row.
+// Dipole tables: a scheme uses far fewer distinct current dipoles (a, b) and
+// potential dipoles (m, n) than data.  One block handles a tile of
+// consecutive parameters.  For each cell of the tile and each wavenumber it
+// stages the node potentials U[i][e] of every electrode, V = S U, and then
+// the FP64 differences
+//   TA[ia][i] = V[a][i] - V[b][i]   for every distinct current dipole,
+//   TM[im][i] = U[m][i] - U[n][i]   for every distinct potential dipole,
+// stored with the cell index fastest (conflict-free shared-memory reads).
+// Every (datum, parameter) pair is then an nv-term dot product of two table
+// rows.  The differences are formed in FP64 (they cancel); the FP32 form
+// rounds the differences to FP32 and accumulates and stores in FP32.
+// Threads walk (datum, parameter) pairs with the parameter fastest, so a
+// warp writes contiguous runs of a J row.
 #include <algorithm>
 
 #include "ertgb_internal.cuh"
@@ -25,19 +32,22 @@ namespace ertgb {
 
 namespace {
 
-template <int NV, typename OutT>
+template <int NV, typename CT>
 __global__ void __launch_bounds__(256)
     k_jacobian(const int32_t *__restrict__ tile_p, const int32_t *__restrict__ pcell_ptr,
                const int32_t *__restrict__ pcell, const int32_t *__restrict__ cells,
                const double *__restrict__ K, const double *__restrict__ M, const double *__restrict__ kv,
                const double *__restrict__ w, int nK, int nE, int64_t Rpad, const double *__restrict__ pot,
-               const int32_t *__restrict__ abmn, const double *__restrict__ kfac,
-               const double *__restrict__ model, int64_t P, int64_t D, int max_cells, OutT *__restrict__ J) {
+               int nA, const int32_t *__restrict__ dip_a, int nM, const int32_t *__restrict__ dip_m,
+               const int32_t *__restrict__ data_dip, const CT *__restrict__ scale_d,
+               const CT *__restrict__ scale_p, int64_t P, int64_t D, int max_cells, CT *__restrict__ J) {
     extern __shared__ double smem[];
     const int E1 = nE + 1;
-    const int per_cell = nK * NV * E1;  // doubles per cell for U (same for V)
+    const int uv_cell = nK * NV * E1;  // doubles per cell for U (same for V)
     double *U = smem;
-    double *V = smem + (size_t)max_cells * per_cell;
+    double *V = smem + (size_t)max_cells * uv_cell;
+    CT *TA = reinterpret_cast<CT *>(V + (size_t)max_cells * uv_cell);
+    CT *TM = TA + (size_t)nK * nA * NV * max_cells;
     const int64_t p0 = tile_p[blockIdx.x], p1 = tile_p[blockIdx.x + 1];
     const int TP = (int)(p1 - p0);
     const int cbeg = pcell_ptr[p0], cend = pcell_ptr[p1];
@@ -45,13 +55,13 @@ __global__ void __launch_bounds__(256)
     const int nchunks = (ncell + max_cells - 1) / max_cells;
     const int64_t pairs = D * TP;
     const int64_t nbatch = (pairs + blockDim.x - 1) / blockDim.x;
+    const int W = max_cells;  // row stride of the tables (cell fastest)
 
     auto stage = [&](int c0, int cn) {
-        // potentials at the cell nodes
-        const int total = cn * per_cell;
+        const int total = cn * uv_cell;
         for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-            const int lc = idx / per_cell;
-            int rem = idx - lc * per_cell;
+            const int lc = idx / uv_cell;
+            int rem = idx - lc * uv_cell;
             const int ki = rem / (NV * E1);
             rem -= ki * NV * E1;
             const int i = rem / E1;
@@ -62,8 +72,8 @@ __global__ void __launch_bounds__(256)
         }
         __syncthreads();
         for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-            const int lc = idx / per_cell;
-            int rem = idx - lc * per_cell;
+            const int lc = idx / uv_cell;
+            int rem = idx - lc * uv_cell;
             const int ki = rem / (NV * E1);
             rem -= ki * NV * E1;
             const int i = rem / E1;
@@ -73,59 +83,79 @@ __global__ void __launch_bounds__(256)
             const double kk = k * k;
             const double *Kc = K + (int64_t)cell * NV * NV + i * NV;
             const double *Mc = M + (int64_t)cell * NV * NV + i * NV;
-            const double *Uc = U + (size_t)lc * per_cell + (size_t)ki * NV * E1 + e;
+            const double *Uc = U + (size_t)lc * uv_cell + (size_t)ki * NV * E1 + e;
             double acc = 0.0;
 #pragma unroll
             for (int j = 0; j < NV; j++) acc = fma(Mc[j] * kk + Kc[j], Uc[j * E1], acc);
             V[idx] = acc;
         }
         __syncthreads();
+        // dipole tables, FP64 differences
+        const int ta = nK * nA * NV * cn;
+        for (int idx = threadIdx.x; idx < ta; idx += blockDim.x) {
+            const int lc = idx % cn;
+            int rem = idx / cn;
+            const int i = rem % NV;
+            rem /= NV;
+            const int ia = rem % nA;
+            const int ki = rem / nA;
+            int a = dip_a[2 * ia], b = dip_a[2 * ia + 1];
+            a = a < 0 ? nE : a;
+            b = b < 0 ? nE : b;
+            const double *Vc = V + (size_t)lc * uv_cell + ((size_t)ki * NV + i) * E1;
+            TA[(((size_t)ki * nA + ia) * NV + i) * W + lc] = (CT)(Vc[a] - Vc[b]);
+        }
+        const int tm = nK * nM * NV * cn;
+        for (int idx = threadIdx.x; idx < tm; idx += blockDim.x) {
+            const int lc = idx % cn;
+            int rem = idx / cn;
+            const int i = rem % NV;
+            rem /= NV;
+            const int im = rem % nM;
+            const int ki = rem / nM;
+            int m = dip_m[2 * im], n = dip_m[2 * im + 1];
+            m = m < 0 ? nE : m;
+            n = n < 0 ? nE : n;
+            const double *Uc = U + (size_t)lc * uv_cell + ((size_t)ki * NV + i) * E1;
+            TM[(((size_t)ki * nM + im) * NV + i) * W + lc] = (CT)(Uc[m] - Uc[n]);
+        }
+        __syncthreads();
     };
 
-    auto accumulate = [&](int64_t pr, int c0, int cn, double acc) -> double {
+    auto accumulate = [&](int64_t pr, int c0, int cn, CT acc) -> CT {
         const int pl = (int)(pr % TP);
         const int64_t d = pr / TP;
         const int64_t p = p0 + pl;
-        int a = abmn[4 * d], b = abmn[4 * d + 1], m = abmn[4 * d + 2], n = abmn[4 * d + 3];
-        a = a < 0 ? nE : a;
-        b = b < 0 ? nE : b;
-        m = m < 0 ? nE : m;
-        n = n < 0 ? nE : n;
+        const int ia = data_dip[2 * d], im = data_dip[2 * d + 1];
         const int lo = max(pcell_ptr[p] - cbeg, c0), hi = min(pcell_ptr[p + 1] - cbeg, c0 + cn);
-        for (int lc = lo; lc < hi; lc++) {
-            const double *Ub = U + (size_t)(lc - c0) * per_cell;
-            const double *Vb = V + (size_t)(lc - c0) * per_cell;
+        for (int lc = lo - c0; lc < hi - c0; lc++) {
             for (int ki = 0; ki < nK; ki++) {
-                const double *Uk = Ub + (size_t)ki * NV * E1;
-                const double *Vk = Vb + (size_t)ki * NV * E1;
-                double s = 0.0;
+                const CT *ta = TA + ((size_t)ki * nA + ia) * NV * W + lc;
+                const CT *tm = TM + ((size_t)ki * nM + im) * NV * W + lc;
+                CT s = 0;
 #pragma unroll
-                for (int i = 0; i < NV; i++)
-                    s = fma(Vk[i * E1 + a] - Vk[i * E1 + b], Uk[i * E1 + m] - Uk[i * E1 + n], s);
-                acc = fma(s, w[ki], acc);
+                for (int i = 0; i < NV; i++) s = fma(ta[i * W], tm[i * W], s);
+                acc = fma(s, (CT)w[ki], acc);
             }
         }
         return acc;
     };
 
-    auto store = [&](int64_t pr, double acc) {
+    auto store = [&](int64_t pr, CT acc) {
         const int pl = (int)(pr % TP);
         const int64_t d = pr / TP;
         const int64_t p = p0 + pl;
-        if (model) {
-            const double m = model[p];
-            acc = acc / ((m * m) / kfac[d]);
-        }
-        J[d * P + p] = (OutT)acc;
+        if (scale_p) acc = (acc * scale_d[d]) * scale_p[p];
+        J[d * P + p] = acc;
     };
 
     if (nchunks <= 1) {
         if (ncell > 0) stage(0, ncell);
-        for (int64_t pr = threadIdx.x; pr < pairs; pr += blockDim.x) store(pr, accumulate(pr, 0, ncell, 0.0));
+        for (int64_t pr = threadIdx.x; pr < pairs; pr += blockDim.x) store(pr, accumulate(pr, 0, ncell, (CT)0));
     } else {
         for (int64_t bt = 0; bt < nbatch; bt++) {
             const int64_t pr = bt * blockDim.x + threadIdx.x;
-            double acc = 0.0;
+            CT acc = 0;
             for (int ch = 0; ch < nchunks; ch++) {
                 const int c0 = ch * max_cells;
                 const int cn = min(max_cells, ncell - c0);
@@ -138,46 +168,113 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-template <typename OutT>
-void launch(Context &c, const double *model, OutT *J, cudaStream_t s) {
-    MeshData &m = c.mesh;
-    const int ntiles = (int)m.jtile_p.size() - 1;
-    if (ntiles <= 0) return;
-    const size_t per_cell = (size_t)c.nK * m.nv * (c.nE + 1);
-    const size_t smem = 2 * per_cell * m.jtile_cells_max * sizeof(double);
-    if (smem > 227 * 1024)
-        throw Error(ERTGB_BAD_INPUT, "Jacobian staging of one cell exceeds shared memory (too many electrodes x wavenumbers)");
-    if (m.nv == 3) {
-        auto kern = k_jacobian<3, OutT>;
-        ERTGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        kern<<<ntiles, 256, smem, s>>>(m.d_jtile_p.p, m.d_pcell_ptr.p, m.d_pcell.p, m.d_cells.p, m.d_K.p, m.d_M.p,
-                                       c.d_k.p, c.d_w.p, c.nK, c.nE, c.Rpad, c.d_x.p, c.d_abmn.p, c.d_kfac.p, model,
-                                       m.P, c.D, m.jtile_cells_max, J);
-    } else {
-        auto kern = k_jacobian<4, OutT>;
-        ERTGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        kern<<<ntiles, 256, smem, s>>>(m.d_jtile_p.p, m.d_pcell_ptr.p, m.d_pcell.p, m.d_cells.p, m.d_K.p, m.d_M.p,
-                                       c.d_k.p, c.d_w.p, c.nK, c.nE, c.Rpad, c.d_x.p, c.d_abmn.p, c.d_kfac.p, model,
-                                       m.P, c.D, m.jtile_cells_max, J);
+// scale_d[d] = kfac[d], scale_p[p] = 1 / model[p]^2 in the compute type
+template <typename CT>
+__global__ void k_jac_scales(int64_t D, int64_t P, const double *__restrict__ kfac,
+                             const double *__restrict__ model, CT *__restrict__ sd, CT *__restrict__ sp) {
+    const int64_t total = D + P;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        if (t < D) {
+            sd[t] = (CT)kfac[t];
+        } else {
+            const double m = model[t - D];
+            sp[t - D] = (CT)(1.0 / (m * m));
+        }
     }
-    ERTGB_CUDA(cudaGetLastError());
+}
+
+size_t jac_cell_bytes(const Context &c, int dtype) {
+    const size_t uv = 2 * (size_t)c.nK * c.mesh.nv * (c.nE + 1) * sizeof(double);
+    const size_t tab = (size_t)c.nK * (c.nA + c.nM) * c.mesh.nv * (dtype == 0 ? 8 : 4);
+    return uv + tab;
+}
+
+template <typename CT>
+void launch(Context &c, const double *model, CT *J, int dtype, cudaStream_t s) {
+    MeshData &m = c.mesh;
+    JacTiles &T = c.jtiles[dtype];
+    const int ntiles = (int)T.tile_p.size() - 1;
+    if (ntiles <= 0) return;
+    const size_t smem = jac_cell_bytes(c, dtype) * T.max_cells;
+    const CT *sd = nullptr, *sp = nullptr;
+    if (model) {
+        c.d_jscale.alloc((size_t)(c.D + m.P) * sizeof(CT));
+        CT *base = reinterpret_cast<CT *>(c.d_jscale.p);
+        k_jac_scales<CT><<<(unsigned)std::min<int64_t>(ceil_div(c.D + m.P, 256), 4096), 256, 0, s>>>(
+            c.D, m.P, c.d_kfac.p, model, base, base + c.D);
+        ERTGB_CUDA(cudaGetLastError());
+        sd = base;
+        sp = base + c.D;
+    }
+    auto go = [&](auto kern) {
+        ERTGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kern<<<ntiles, 256, smem, s>>>(T.d_tile_p.p, m.d_pcell_ptr.p, m.d_pcell.p, m.d_cells.p, m.d_K.p, m.d_M.p,
+                                       c.d_k.p, c.d_w.p, c.nK, c.nE, c.Rpad, c.d_x.p, c.nA, c.d_dip_a.p, c.nM,
+                                       c.d_dip_m.p, c.d_data_dip.p, sd, sp, m.P, c.D, T.max_cells, J);
+        ERTGB_CUDA(cudaGetLastError());
+    };
+    if (m.nv == 3) go(k_jacobian<3, CT>);
+    else go(k_jacobian<4, CT>);
 }
 
 }  // namespace
 
+// Parameter -> cells and the Jacobian tiles of both table precisions
+// (consecutive parameters whose cells fit the shared-memory budget).
+void build_jacobian_tiles(Context &c) {
+    MeshData &m = c.mesh;
+    const int64_t P = m.P;
+    m.pcell_ptr.assign(P + 1, 0);
+    for (int64_t i = 0; i < m.C; i++)
+        if (m.marker[i] >= 0) m.pcell_ptr[m.marker[i] + 1]++;
+    for (int64_t p = 0; p < P; p++) m.pcell_ptr[p + 1] += m.pcell_ptr[p];
+    m.pcell.assign(m.pcell_ptr[P], 0);
+    std::vector<int32_t> pos(m.pcell_ptr.begin(), m.pcell_ptr.end() - 1);
+    for (int64_t i = 0; i < m.C; i++)
+        if (m.marker[i] >= 0) m.pcell[pos[m.marker[i]]++] = (int32_t)i;
+    m.d_pcell_ptr.upload(m.pcell_ptr, c.stream);
+    m.d_pcell.upload(m.pcell, c.stream);
+    const size_t budget = 200 * 1024;
+    for (int dt = 0; dt < 2; dt++) {
+        JacTiles &T = c.jtiles[dt];
+        const size_t per_cell = jac_cell_bytes(c, dt);
+        T.max_cells = per_cell > budget ? 0 : (int)std::min<size_t>(32, budget / per_cell);
+        T.tile_p.assign(1, 0);
+        if (T.max_cells == 0) continue;
+        int64_t p = 0;
+        while (p < P) {
+            int64_t q = p, ncell = 0;
+            while (q < P && q - p < 32) {
+                const int64_t cq = m.pcell_ptr[q + 1] - m.pcell_ptr[q];
+                if (q > p && ncell + cq > T.max_cells) break;
+                ncell += cq;
+                q++;
+            }
+            if (q == p) q = p + 1;
+            T.tile_p.push_back((int32_t)q);
+            p = q;
+        }
+        T.d_tile_p.upload(T.tile_p, c.stream);
+    }
+}
+
 void jacobian(Context &c, const double *model, int n_model, void *J, int dtype, cudaStream_t s) {
+    if (c.jtiles[dtype].max_cells == 0)
+        throw Error(ERTGB_BAD_INPUT, "Jacobian staging of one cell exceeds shared memory "
+                                     "(too many electrodes x wavenumbers x dipoles)");
     const double *mdl = (n_model == c.mesh.P) ? model : nullptr;
-    if (dtype == 0) launch<double>(c, mdl, (double *)J, s);
-    else launch<float>(c, mdl, (float *)J, s);
+    if (dtype == 0) launch<double>(c, mdl, (double *)J, 0, s);
+    else launch<float>(c, mdl, (float *)J, 1, s);
 }
 
 void profile_jacobian(Context &c, int reps, double *J, double *ms, double *bytes, double *flops) {
     if (!c.have_pot) throw Error(ERTGB_STATE, "profile needs a completed response");
     MeshData &m = c.mesh;
     cudaStream_t s = c.stream;
-    launch<double>(c, nullptr, J, s);
+    launch<double>(c, nullptr, J, 0, s);
     ERTGB_CUDA(cudaEventRecord(c.ev[0], s));
-    for (int r = 0; r < reps; r++) launch<double>(c, nullptr, J, s);
+    for (int r = 0; r < reps; r++) launch<double>(c, nullptr, J, 0, s);
     ERTGB_CUDA(cudaEventRecord(c.ev[1], s));
     ERTGB_CUDA(cudaEventSynchronize(c.ev[1]));
     float t = 0.f;
@@ -185,11 +282,12 @@ void profile_jacobian(Context &c, int reps, double *J, double *ms, double *bytes
     *ms = (double)t / reps;
     const double Ca = (double)m.pcell.size();
     // J written once, potentials read once, cell nodes + element matrices,
-    // parameter->cell map, scheme
+    // parameter->cell map, scheme and its dipole indices
     *bytes = (double)c.D * m.P * 8.0 + (double)m.n * c.Rpad * 8.0 + Ca * (m.nv * 4.0 + 2.0 * m.nv * m.nv * 8.0 + 4.0) +
-             (double)(m.P + 1) * 4.0 + (double)c.D * (16.0 + 8.0);
-    // V = S U per (cell, k, electrode) and the (datum, cell, k) products
-    *flops = Ca * c.nK * (c.nE + 1) * m.nv * (2.0 * m.nv + 2.0) + (double)c.D * Ca * c.nK * (m.nv * 4.0 + 2.0);
+             (double)(m.P + 1) * 4.0 + (double)c.D * (8.0 + 8.0) + (double)(c.nA + c.nM) * 8.0;
+    // V = S U, the dipole differences, and one nv-term dot per (datum, cell, k)
+    *flops = Ca * c.nK * ((c.nE + 1) * m.nv * 2.0 * m.nv + (c.nA + c.nM) * m.nv) +
+             (double)c.D * Ca * c.nK * (m.nv * 2.0 + 2.0);
 }
 
 }  // namespace ertgb

@@ -22,6 +22,7 @@
 #include <cmath>
 
 #include "ertgb_internal.cuh"
+#include "reduce.cuh"
 
 namespace ertgb {
 
@@ -112,21 +113,6 @@ __global__ void k_init(int64_t n, int nE, int nK, int64_t R, int64_t Rpad, const
         part_a[(int64_t)blockIdx.y * Rpad + t] = s1;
         part_b[(int64_t)blockIdx.y * Rpad + t] = s2;
     }
-}
-
-// Column reductions: block (32, 32), grid Rpad/32; thread (tx, ty) sums the
-// partial rows ty, ty+32, ... of column t, then the 32 sums are added in a
-// fixed order (deterministic).
-__device__ inline double col_sum(const double *__restrict__ part, int NB, int64_t Rpad, int64_t t,
-                                 double (*red)[33]) {
-    double s = 0.0;
-    for (int b = threadIdx.y; b < NB; b += 32) s += part[(int64_t)b * Rpad + t];
-    red[threadIdx.y][threadIdx.x] = s;
-    __syncthreads();
-    double tot = 0.0;
-    if (threadIdx.y == 0)
-        for (int w = 0; w < 32; w++) tot += red[w][threadIdx.x];
-    return tot;
 }
 
 __global__ void k_finish_init(int64_t Rpad, int64_t R, int NB, const double *__restrict__ part_a,
@@ -366,6 +352,16 @@ __global__ void k_col_total(int64_t Rpad, int NB, const double *__restrict__ par
     if (threadIdx.y == 0) out[t] = s;
 }
 }  // namespace
+
+void pcg_finish_init(dim3 g, dim3 b, cudaStream_t s, int64_t Rpad, int64_t R, int NB, const double *pa, const double *pb,
+                     double *col, int32_t *active, int32_t *iters, int32_t *nactive) {
+    k_finish_init<<<g, b, 0, s>>>(Rpad, R, NB, pa, pb, col, active, iters, nactive);
+}
+
+void pcg_finish_alpha(dim3 g, dim3 b, cudaStream_t s, int64_t Rpad, int NB, const double *part, double *col,
+                      const int32_t *active, int32_t *nactive) {
+    k_finish_alpha<<<g, b, 0, s>>>(Rpad, NB, part, col, active, nactive);
+}
 
 int spmm_partial_rows(int64_t n, int cap) { return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, kRowsPerBlock), cap)); }
 

@@ -1,0 +1,454 @@
+// Mixed-precision multi-right-hand-side PCG: FP32 recurrence, FP64 accuracy.
+//
+// The CG recurrence (operator, Jacobi preconditioner, r, p, q and the
+// solution increment y) runs in FP32, where GB300 has 55x the FP64 rate and
+// the vector traffic halves.  Every kReliableEvery iterations a reliable
+// update (Sleijpen & van der Vorst, "Reliable updated residuals in hybrid
+// Bi-CG methods", Computing 56, 1996) folds the FP32 increment into the FP64
+// solution, x += y, recomputes the true residual r = b - A x with the FP64
+// matrix, and restarts the FP32 residual from it.  Convergence is decided
+// only on that FP64 true residual (||r_t|| <= rtol ||b_t||), the same test
+// as the FP64 solver, so the converged accuracy is unchanged.  Column dot
+// products are accumulated in FP32 per thread and in FP64 across threads;
+// the per-column scalars (alpha, beta, rho) stay FP64.
+#include <algorithm>
+#include <cmath>
+
+#include "ertgb_internal.cuh"
+#include "reduce.cuh"
+
+namespace ertgb {
+
+namespace {
+
+constexpr int kRows = 8;            // warps per block (spmm) / rows per block (vector kernels)
+constexpr int kGraphIters = 16;     // iterations per captured graph
+constexpr int kReliableEvery = 4;   // graphs between reliable updates (64 iterations)
+constexpr int kPartRows = 608;
+
+enum Col { RHO = 0, ALPHA, BETA, BNORM2, RNORM2, PQ, NCOL };
+
+__global__ void k_to_f32(int64_t n, const double *__restrict__ a, float *__restrict__ b) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
+// block reduction of two per-thread FP64 partials over threadIdx.y, written to
+// part rows blockIdx.y (vector kernels: block (32, kRows), grid (Rpad/32, NB))
+__device__ inline void block_partials2(double a, double b, double *part_a, double *part_b, int64_t Rpad, int64_t t) {
+    __shared__ double sa[kRows][32], sb[kRows][32];
+    sa[threadIdx.y][threadIdx.x] = a;
+    sb[threadIdx.y][threadIdx.x] = b;
+    __syncthreads();
+    if (threadIdx.y == 0) {
+        double s1 = 0.0, s2 = 0.0;
+        for (int w = 0; w < kRows; w++) {
+            s1 += sa[w][threadIdx.x];
+            s2 += sb[w][threadIdx.x];
+        }
+        part_a[(int64_t)blockIdx.y * Rpad + t] = s1;
+        part_b[(int64_t)blockIdx.y * Rpad + t] = s2;
+    }
+}
+
+__global__ void k_m_init(int64_t n, int nE, int64_t R, int64_t Rpad, const float *__restrict__ dinv,
+                         const double *__restrict__ b, float *__restrict__ r, float *__restrict__ p,
+                         float *__restrict__ y, double *__restrict__ part_a, double *__restrict__ part_b) {
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    const int64_t ki = t < R ? t / nE : 0;
+    const float *dk = dinv + ki * n;
+    float a = 0.f;
+    double bb = 0.0;
+    for (int64_t row = (int64_t)blockIdx.y * kRows + threadIdx.y; row < n; row += (int64_t)gridDim.y * kRows) {
+        const int64_t i = row * Rpad + t;
+        const double bv = b[i];
+        const float rv = (float)bv;
+        const float z = t < R ? rv * dk[row] : 0.f;
+        r[i] = rv;
+        p[i] = z;
+        y[i] = 0.f;
+        a = fmaf(rv, z, a);
+        bb = fma(bv, bv, bb);
+    }
+    block_partials2((double)a, bb, part_a, part_b, Rpad, t);
+}
+
+template <int CH>
+__global__ void __launch_bounds__(256) k_spmm32_dot(int64_t n, int64_t nnz, int nE, int nK, int64_t Rpad,
+                                                    const int32_t *__restrict__ rowptr,
+                                                    const int32_t *__restrict__ colidx,
+                                                    const float *__restrict__ vals, const float *__restrict__ p,
+                                                    float *__restrict__ q, double *__restrict__ part) {
+    __shared__ double red[kRows][32 * CH];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t t0 = (int64_t)blockIdx.y * 32 * CH + lane;
+    int64_t kofs[CH];
+#pragma unroll
+    for (int j = 0; j < CH; j++) kofs[j] = min((t0 + 32 * j) / nE, (int64_t)nK - 1) * nnz;
+    float dot[CH];
+#pragma unroll
+    for (int j = 0; j < CH; j++) dot[j] = 0.f;
+    for (int64_t row = (int64_t)blockIdx.x * kRows + wid; row < n; row += (int64_t)gridDim.x * kRows) {
+        float acc[CH];
+#pragma unroll
+        for (int j = 0; j < CH; j++) acc[j] = 0.f;
+        const int32_t s1 = rowptr[row + 1];
+        for (int32_t s = rowptr[row]; s < s1; s++) {
+            const int64_t col = colidx[s];
+            const float *pc = p + col * Rpad + t0;
+#pragma unroll
+            for (int j = 0; j < CH; j++) acc[j] = fmaf(vals[kofs[j] + s], pc[32 * j], acc[j]);
+        }
+        float *qr = q + row * Rpad + t0;
+        const float *pr = p + row * Rpad + t0;
+#pragma unroll
+        for (int j = 0; j < CH; j++) {
+            qr[32 * j] = acc[j];
+            dot[j] = fmaf(pr[32 * j], acc[j], dot[j]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < CH; j++) red[wid][lane + 32 * j] = (double)dot[j];
+    __syncthreads();
+    for (int c = threadIdx.x; c < 32 * CH; c += blockDim.x) {
+        double s = 0.0;
+#pragma unroll
+        for (int w = 0; w < kRows; w++) s += red[w][c];
+        part[(int64_t)blockIdx.x * Rpad + (int64_t)blockIdx.y * 32 * CH + c] = s;
+    }
+}
+
+__global__ void k_m_update_xr(int64_t n, int nE, int64_t R, int64_t Rpad, const float *__restrict__ dinv,
+                              const double *__restrict__ col, const int32_t *__restrict__ active,
+                              float *__restrict__ y, float *__restrict__ r, const float *__restrict__ p,
+                              const float *__restrict__ q, double *__restrict__ part_a, double *__restrict__ part_b) {
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    const bool act = active[t] != 0;
+    const float alpha = (float)col[ALPHA * Rpad + t];
+    const int64_t ki = t < R ? t / nE : 0;
+    const float *dk = dinv + ki * n;
+    float a = 0.f, b = 0.f;
+    if (act) {
+        for (int64_t row = (int64_t)blockIdx.y * kRows + threadIdx.y; row < n; row += (int64_t)gridDim.y * kRows) {
+            const int64_t i = row * Rpad + t;
+            y[i] = fmaf(alpha, p[i], y[i]);
+            const float rv = fmaf(-alpha, q[i], r[i]);
+            r[i] = rv;
+            a = fmaf(rv, rv * dk[row], a);
+            b = fmaf(rv, rv, b);
+        }
+    }
+    block_partials2((double)a, (double)b, part_a, part_b, Rpad, t);
+}
+
+// recursive beta; convergence is left to the reliable updates
+__global__ void k_m_finish_beta(int64_t Rpad, int NB, const double *__restrict__ part_a,
+                                const double *__restrict__ part_b, double *__restrict__ col,
+                                const int32_t *__restrict__ active, int32_t *__restrict__ iters) {
+    __shared__ double ra[32][33], rb[32][33];
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    const double rz = col_sum(part_a, NB, Rpad, t, ra);
+    const double rr = col_sum(part_b, NB, Rpad, t, rb);
+    if (threadIdx.y != 0) return;
+    if (!active[t]) {
+        col[BETA * Rpad + t] = 0.0;
+        return;
+    }
+    iters[t] += 1;
+    (void)rr;
+    const double rho = col[RHO * Rpad + t];
+    col[BETA * Rpad + t] = (rho != 0.0 && rz == rz) ? rz / rho : 0.0;
+    col[RHO * Rpad + t] = rz;
+}
+
+__global__ void k_m_update_p(int64_t n, int nE, int64_t R, int64_t Rpad, const float *__restrict__ dinv,
+                             const double *__restrict__ col, const int32_t *__restrict__ active,
+                             const float *__restrict__ r, float *__restrict__ p) {
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    if (!active[t]) return;
+    const float beta = (float)col[BETA * Rpad + t];
+    const int64_t ki = t < R ? t / nE : 0;
+    const float *dk = dinv + ki * n;
+    for (int64_t row = (int64_t)blockIdx.y * kRows + threadIdx.y; row < n; row += (int64_t)gridDim.y * kRows) {
+        const int64_t i = row * Rpad + t;
+        p[i] = fmaf(beta, p[i], r[i] * dk[row]);
+    }
+}
+
+// reliable update, part 1: x += y, y = 0 on active columns
+__global__ void k_m_accum(int64_t n, int64_t Rpad, const int32_t *__restrict__ active, double *__restrict__ x,
+                          float *__restrict__ y, int32_t *__restrict__ nactive) {
+    if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) *nactive = 0;
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    if (!active[t]) return;
+    for (int64_t row = (int64_t)blockIdx.y * kRows + threadIdx.y; row < n; row += (int64_t)gridDim.y * kRows) {
+        const int64_t i = row * Rpad + t;
+        x[i] += (double)y[i];
+        y[i] = 0.f;
+    }
+}
+
+// reliable update, part 2: true residual r = b - A x in FP64 (warp per row,
+// lanes over columns), restart r32 from it, partials of r32.z32 and ||r||^2
+template <int CH>
+__global__ void __launch_bounds__(256) k_m_residual(int64_t n, int64_t nnz, int nE, int nK, int64_t R, int64_t Rpad,
+                                                    const int32_t *__restrict__ rowptr,
+                                                    const int32_t *__restrict__ colidx,
+                                                    const double *__restrict__ vals, const double *__restrict__ x,
+                                                    const double *__restrict__ b, const float *__restrict__ dinv,
+                                                    const int32_t *__restrict__ active, float *__restrict__ r32,
+                                                    double *__restrict__ part_a, double *__restrict__ part_b) {
+    __shared__ double ra[kRows][32 * CH], rb[kRows][32 * CH];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t t0 = (int64_t)blockIdx.y * 32 * CH + lane;
+    int64_t kofs[CH], kdi[CH];
+    bool act[CH];
+#pragma unroll
+    for (int j = 0; j < CH; j++) {
+        const int64_t t = t0 + 32 * j;
+        const int64_t ki = min(t / nE, (int64_t)nK - 1);
+        kofs[j] = ki * nnz;
+        kdi[j] = ki * n;
+        act[j] = active[t] != 0;
+    }
+    double sa[CH], sb[CH];
+#pragma unroll
+    for (int j = 0; j < CH; j++) sa[j] = sb[j] = 0.0;
+    for (int64_t row = (int64_t)blockIdx.x * kRows + wid; row < n; row += (int64_t)gridDim.x * kRows) {
+        double acc[CH];
+#pragma unroll
+        for (int j = 0; j < CH; j++) acc[j] = 0.0;
+        const int32_t s1 = rowptr[row + 1];
+        for (int32_t s = rowptr[row]; s < s1; s++) {
+            const int64_t col = colidx[s];
+            const double *xc = x + col * Rpad + t0;
+#pragma unroll
+            for (int j = 0; j < CH; j++)
+                if (act[j]) acc[j] = fma(vals[kofs[j] + s], xc[32 * j], acc[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < CH; j++) {
+            if (!act[j]) continue;
+            const int64_t i = row * Rpad + t0 + 32 * j;
+            const double rv = b[i] - acc[j];
+            const float r = (float)rv;
+            r32[i] = r;
+            sa[j] += (double)(r * (r * dinv[kdi[j] + row]));
+            sb[j] = fma(rv, rv, sb[j]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < CH; j++) {
+        ra[wid][lane + 32 * j] = sa[j];
+        rb[wid][lane + 32 * j] = sb[j];
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < 32 * CH; c += blockDim.x) {
+        double s1 = 0.0, s2 = 0.0;
+#pragma unroll
+        for (int w = 0; w < kRows; w++) {
+            s1 += ra[w][c];
+            s2 += rb[w][c];
+        }
+        part_a[(int64_t)blockIdx.x * Rpad + (int64_t)blockIdx.y * 32 * CH + c] = s1;
+        part_b[(int64_t)blockIdx.x * Rpad + (int64_t)blockIdx.y * 32 * CH + c] = s2;
+    }
+}
+
+// reliable update, part 3: FP64 convergence test, rho of the restarted residual
+__global__ void k_m_finish_ru(int64_t Rpad, int NB, double rtol2, const double *__restrict__ part_a,
+                              const double *__restrict__ part_b, double *__restrict__ col,
+                              int32_t *__restrict__ active, int32_t *__restrict__ nactive) {
+    __shared__ double ra[32][33], rb[32][33];
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    const double rz = col_sum(part_a, NB, Rpad, t, ra);
+    const double rr = col_sum(part_b, NB, Rpad, t, rb);
+    if (threadIdx.y != 0 || !active[t]) return;
+    col[RNORM2 * Rpad + t] = rr;
+    col[RHO * Rpad + t] = rz;
+    if (rr <= rtol2 * col[BNORM2 * Rpad + t] || !(rr == rr)) {
+        active[t] = 0;
+    } else {
+        atomicAdd(nactive, 1);
+    }
+}
+
+int choose_ch(int64_t Rpad) {
+    const int64_t w = Rpad / 32;
+    for (int ch : {4, 3, 2})
+        if (w % ch == 0) return ch;
+    return 1;
+}
+
+template <template <int> class F, typename... A> void dispatch_ch(int ch, A &&...args) {
+    switch (ch) {
+        case 4: F<4>::go(args...); break;
+        case 3: F<3>::go(args...); break;
+        case 2: F<2>::go(args...); break;
+        default: F<1>::go(args...); break;
+    }
+}
+
+template <int CH> struct SpmmL {
+    static void go(dim3 g, cudaStream_t s, int64_t n, int64_t nnz, int nE, int nK, int64_t Rpad, const int32_t *rp,
+                   const int32_t *ci, const float *v, const float *p, float *q, double *part) {
+        k_spmm32_dot<CH><<<g, 256, 0, s>>>(n, nnz, nE, nK, Rpad, rp, ci, v, p, q, part);
+    }
+};
+
+template <int CH> struct ResidL {
+    static void go(dim3 g, cudaStream_t s, int64_t n, int64_t nnz, int nE, int nK, int64_t R, int64_t Rpad,
+                   const int32_t *rp, const int32_t *ci, const double *v, const double *x, const double *b,
+                   const float *dinv, const int32_t *active, float *r32, double *pa, double *pb) {
+        k_m_residual<CH><<<g, 256, 0, s>>>(n, nnz, nE, nK, R, Rpad, rp, ci, v, x, b, dinv, active, r32, pa, pb);
+    }
+};
+
+}  // namespace
+
+// kernels of pcg.cu reused here
+void pcg_finish_init(dim3 g, dim3 b, cudaStream_t s, int64_t Rpad, int64_t R, int NB, const double *pa, const double *pb,
+                     double *col, int32_t *active, int32_t *iters, int32_t *nactive);
+void pcg_finish_alpha(dim3 g, dim3 b, cudaStream_t s, int64_t Rpad, int NB, const double *part, double *col,
+                      const int32_t *active, int32_t *nactive);
+
+int pcg_solve_mixed(Context &c, cudaStream_t s) {
+    MeshData &m = c.mesh;
+    const int64_t n = m.n, Rpad = c.Rpad, R = c.R;
+    const int NB = (int)std::min<int64_t>(ceil_div(n, kRows), kPartRows);
+    const int ch = choose_ch(Rpad);
+    const int nchunk = (int)(Rpad / (32 * ch));
+    c.d_x.alloc((size_t)n * Rpad);
+    c.d_S32.alloc((size_t)c.nK * m.nnz);
+    c.d_dinv32.alloc((size_t)c.nK * n);
+    c.d_r32.alloc((size_t)n * Rpad);
+    c.d_p32.alloc((size_t)n * Rpad);
+    c.d_q32.alloc((size_t)n * Rpad);
+    c.d_y32.alloc((size_t)n * Rpad);
+    c.d_part.alloc((size_t)NB * Rpad * 3);
+    c.d_col.alloc((size_t)NCOL * Rpad);
+    c.d_active.alloc((size_t)Rpad * 2 + 1);
+    double *part_a = c.d_part.p, *part_b = c.d_part.p + (size_t)NB * Rpad, *part_c = c.d_part.p + 2 * (size_t)NB * Rpad;
+    int32_t *active = c.d_active.p, *iters = c.d_active.p + Rpad, *nactive = c.d_active.p + 2 * Rpad;
+    const double *b = c.d_r.p;  // the right-hand sides (FP64), kept for the true residual
+    ERTGB_CUDA(cudaMemsetAsync(c.d_x.p, 0, sizeof(double) * n * Rpad, s));
+    ERTGB_CUDA(cudaMemsetAsync(nactive, 0, sizeof(int32_t), s));
+    k_to_f32<<<(unsigned)std::min<int64_t>(ceil_div((int64_t)c.nK * m.nnz, 256), 65535), 256, 0, s>>>(
+        (int64_t)c.nK * m.nnz, c.d_S.p, c.d_S32.p);
+    k_to_f32<<<(unsigned)std::min<int64_t>(ceil_div((int64_t)c.nK * n, 256), 65535), 256, 0, s>>>(
+        (int64_t)c.nK * n, c.d_dinv.p, c.d_dinv32.p);
+    const dim3 vb(32, kRows), vg((unsigned)(Rpad / 32), (unsigned)NB);
+    const dim3 sg((unsigned)NB, (unsigned)nchunk);
+    const dim3 fb(32, 32), fg((unsigned)(Rpad / 32));
+    const double rtol2 = c.rtol * c.rtol;
+    k_m_init<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, c.d_dinv32.p, b, c.d_r32.p, c.d_p32.p, c.d_y32.p, part_a, part_b);
+    pcg_finish_init(fg, fb, s, Rpad, R, NB, part_a, part_b, c.d_col.p, active, iters, nactive);
+    ERTGB_CUDA(cudaGetLastError());
+    c.stats.launches_response += 5;
+
+    cudaGraph_t g_it = nullptr, g_ru = nullptr;
+    cudaGraphExec_t e_it = nullptr, e_ru = nullptr;
+    auto cleanup = [&] {
+        if (e_it) cudaGraphExecDestroy(e_it);
+        if (g_it) cudaGraphDestroy(g_it);
+        if (e_ru) cudaGraphExecDestroy(e_ru);
+        if (g_ru) cudaGraphDestroy(g_ru);
+    };
+    int status = ERTGB_OK;
+    int iterations = 0;
+    try {
+        ERTGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        for (int it = 0; it < kGraphIters; it++) {
+            dispatch_ch<SpmmL>(ch, sg, s, n, m.nnz, c.nE, c.nK, Rpad, m.d_rowptr.p, m.d_colidx.p, c.d_S32.p, c.d_p32.p,
+                               c.d_q32.p, part_c);
+            pcg_finish_alpha(fg, fb, s, Rpad, NB, part_c, c.d_col.p, active, nactive);
+            k_m_update_xr<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, c.d_dinv32.p, c.d_col.p, active, c.d_y32.p, c.d_r32.p,
+                                            c.d_p32.p, c.d_q32.p, part_a, part_b);
+            k_m_finish_beta<<<fg, fb, 0, s>>>(Rpad, NB, part_a, part_b, c.d_col.p, active, iters);
+            k_m_update_p<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, c.d_dinv32.p, c.d_col.p, active, c.d_r32.p, c.d_p32.p);
+        }
+        ERTGB_CUDA(cudaStreamEndCapture(s, &g_it));
+        ERTGB_CUDA(cudaGraphInstantiate(&e_it, g_it, 0));
+        ERTGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        k_m_accum<<<vg, vb, 0, s>>>(n, Rpad, active, c.d_x.p, c.d_y32.p, nactive);
+        dispatch_ch<ResidL>(ch, sg, s, n, m.nnz, c.nE, c.nK, R, Rpad, m.d_rowptr.p, m.d_colidx.p, c.d_S.p, c.d_x.p,
+                            b, c.d_dinv32.p, active, c.d_r32.p, part_a, part_b);
+        k_m_finish_ru<<<fg, fb, 0, s>>>(Rpad, NB, rtol2, part_a, part_b, c.d_col.p, active, nactive);
+        ERTGB_CUDA(cudaStreamEndCapture(s, &g_ru));
+        ERTGB_CUDA(cudaGraphInstantiate(&e_ru, g_ru, 0));
+
+        int32_t h_active = 0;
+        ERTGB_CUDA(cudaMemcpyAsync(&h_active, nactive, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        ERTGB_CUDA(cudaStreamSynchronize(s));
+        while (h_active > 0) {
+            if (iterations >= c.max_iter) {
+                status = ERTGB_NOT_CONVERGED;
+                break;
+            }
+            for (int u = 0; u < kReliableEvery; u++) ERTGB_CUDA(cudaGraphLaunch(e_it, s));
+            iterations += kReliableEvery * kGraphIters;
+            ERTGB_CUDA(cudaGraphLaunch(e_ru, s));
+            c.stats.launches_response += 5 * kGraphIters * kReliableEvery + 3;
+            ERTGB_CUDA(cudaMemcpyAsync(&h_active, nactive, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+            ERTGB_CUDA(cudaStreamSynchronize(s));
+        }
+    } catch (...) {
+        cudaStreamEndCapture(s, &g_it);
+        cleanup();
+        throw;
+    }
+    cleanup();
+    std::vector<int32_t> it_h(Rpad);
+    std::vector<double> rn(Rpad), bn(Rpad);
+    ERTGB_CUDA(cudaMemcpyAsync(it_h.data(), iters, sizeof(int32_t) * Rpad, cudaMemcpyDeviceToHost, s));
+    ERTGB_CUDA(cudaMemcpyAsync(rn.data(), c.d_col.p + RNORM2 * Rpad, sizeof(double) * Rpad, cudaMemcpyDeviceToHost, s));
+    ERTGB_CUDA(cudaMemcpyAsync(bn.data(), c.d_col.p + BNORM2 * Rpad, sizeof(double) * Rpad, cudaMemcpyDeviceToHost, s));
+    ERTGB_CUDA(cudaStreamSynchronize(s));
+    int maxit = 0;
+    double maxres = 0.0;
+    bool finite = true;
+    for (int64_t t = 0; t < R; t++) {
+        maxit = std::max(maxit, it_h[t]);
+        if (bn[t] > 0) {
+            const double rel = std::sqrt(rn[t] / bn[t]);
+            if (!std::isfinite(rel)) finite = false;
+            else maxres = std::max(maxres, rel);
+        }
+    }
+    if (!finite) {
+        status = ERTGB_NOT_CONVERGED;
+        maxres = NAN;
+    }
+    c.stats.iterations = maxit;
+    c.stats.n_rhs = (int32_t)R;
+    c.stats.max_rel_residual = maxres;
+    return status;
+}
+
+void profile_spmm32(Context &c, int reps, double *ms, double *bytes, double *flops) {
+    MeshData &m = c.mesh;
+    const int64_t n = m.n, Rpad = c.Rpad;
+    const int NB = (int)std::min<int64_t>(ceil_div(n, kRows), kPartRows);
+    const int ch = choose_ch(Rpad);
+    const dim3 sg((unsigned)NB, (unsigned)(Rpad / (32 * ch)));
+    if (c.d_q32.n < (size_t)n * Rpad || c.d_S32.n < (size_t)c.nK * m.nnz || c.d_part.n < (size_t)NB * Rpad * 3)
+        throw Error(ERTGB_STATE, "profile needs a completed mixed-precision response");
+    cudaStream_t s = c.stream;
+    double *part_c = c.d_part.p + 2 * (size_t)NB * Rpad;
+    auto go = [&] {
+        dispatch_ch<SpmmL>(ch, sg, s, n, m.nnz, c.nE, c.nK, Rpad, m.d_rowptr.p, m.d_colidx.p, c.d_S32.p, c.d_r32.p,
+                           c.d_q32.p, part_c);
+    };
+    go();
+    ERTGB_CUDA(cudaEventRecord(c.ev[0], s));
+    for (int r = 0; r < reps; r++) go();
+    ERTGB_CUDA(cudaEventRecord(c.ev[1], s));
+    ERTGB_CUDA(cudaEventSynchronize(c.ev[1]));
+    float t = 0.f;
+    ERTGB_CUDA(cudaEventElapsedTime(&t, c.ev[0], c.ev[1]));
+    *ms = (double)t / reps;
+    *bytes = (double)m.nnz * (4.0 + 4.0 * c.nK) + (double)(n + 1) * 4.0 + 2.0 * n * Rpad * 4.0 + (double)NB * Rpad * 8.0;
+    *flops = 2.0 * (double)m.nnz * Rpad + 2.0 * (double)n * Rpad;
+}
+
+}  // namespace ertgb

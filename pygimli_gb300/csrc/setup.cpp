@@ -101,41 +101,4 @@ void build_assembly_map(MeshData &m, std::vector<int32_t> &cptr, std::vector<int
     for (int64_t r = 0; r < m.n; r++) diag[r] = find_slot(m, (int32_t)r, (int32_t)r);
 }
 
-// Parameters -> cells and the Jacobian tiles (consecutive parameters whose
-// cells fit the shared-memory staging budget of jacobian.cu).
-void build_jacobian_tiles(Context &c) {
-    MeshData &m = c.mesh;
-    const int64_t P = m.P;
-    m.pcell_ptr.assign(P + 1, 0);
-    for (int64_t i = 0; i < m.C; i++)
-        if (m.marker[i] >= 0) m.pcell_ptr[m.marker[i] + 1]++;
-    for (int64_t p = 0; p < P; p++) m.pcell_ptr[p + 1] += m.pcell_ptr[p];
-    m.pcell.assign(m.pcell_ptr[P], 0);
-    std::vector<int32_t> pos(m.pcell_ptr.begin(), m.pcell_ptr.end() - 1);
-    for (int64_t i = 0; i < m.C; i++)
-        if (m.marker[i] >= 0) m.pcell[pos[m.marker[i]]++] = (int32_t)i;
-    // staging bytes per cell: U and V for nv nodes x nK x (nE + 1) doubles
-    const size_t per_cell = (size_t)m.nv * c.nK * (c.nE + 1) * 2 * sizeof(double);
-    const size_t budget = 200 * 1024;
-    int max_cells = (int)std::max<size_t>(1, budget / std::max<size_t>(per_cell, 1));
-    if (per_cell > budget) max_cells = 1;  // staged in chunks of one cell
-    max_cells = std::min(max_cells, 32);
-    m.jtile_cells_max = max_cells;
-    m.jtile_p.clear();
-    m.jtile_p.push_back(0);
-    int64_t p = 0;
-    while (p < P) {
-        int64_t q = p, cells = 0;
-        while (q < P && q - p < 32) {
-            int64_t cq = m.pcell_ptr[q + 1] - m.pcell_ptr[q];
-            if (q > p && cells + cq > max_cells) break;
-            cells += cq;
-            q++;
-        }
-        if (q == p) q = p + 1;
-        m.jtile_p.push_back((int32_t)q);
-        p = q;
-    }
-}
-
 }  // namespace ertgb

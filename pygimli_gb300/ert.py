@@ -77,7 +77,7 @@ def surface_info(mesh):
 class ERTModelling:
     """ERT forward operator (singularity removal) on one GB300."""
 
-    def __init__(self, sr=True, verbose=False, device=0, rtol=1e-10, maxIter=20000):
+    def __init__(self, sr=True, verbose=False, device=0, rtol=1e-10, maxIter=20000, precision="fp64"):
         if not sr:
             raise NotImplementedError("only the singularity-removal operator (sr=True) is provided")
         self.verbose = verbose
@@ -94,6 +94,16 @@ class ERTModelling:
         self._elec_nodes = None
         self._last_model = None
         self.setSolverTolerance(rtol, maxIter)
+        self.setPrecision(precision)
+
+    def setPrecision(self, precision):
+        """Solver arithmetic: ``"fp64"`` or ``"mixed"`` (FP32 recurrence with
+        FP64 reliable updates; same converged accuracy)."""
+        modes = {"fp64": 0, "mixed": 1}
+        if precision not in modes:
+            raise ValueError(f"precision must be one of {sorted(modes)}")
+        self._check(self._lib.ertgb_set_precision(self._ctx, modes[precision]))
+        self.precision = precision
 
     def __del__(self):
         try:

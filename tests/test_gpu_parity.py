@@ -57,10 +57,11 @@ def rel(a, b):
     return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("name", ["ert2d_small", "ert2d_pd_wa", "ert3d_small"])
-def test_golden_parity(torch, golden_dir, name):
+def test_golden_parity(torch, golden_dir, name, precision):
     z, mesh, data = load_case(golden_dir, name)
-    fop = fop_for(mesh, data)
+    fop = fop_for(mesh, data, precision=precision)
     assert np.array_equal(fop.kValues(), z["k"]) and np.array_equal(fop.weights(), z["w"])
     rp, ci = fop.pattern()
     assert np.array_equal(rp, z["rowptr"]) and np.array_equal(ci, z["colidx"])
@@ -73,9 +74,11 @@ def test_golden_parity(torch, golden_dir, name):
     for j, ki in enumerate(z["kidx"]):
         assert rel(prim[ki], z["primary"][j]) <= TOL_MAT
     e_pot = rel(fop.subPotentials(), z["subpot"])
-    J = fop.createJacobian(z["rho"]).cpu().numpy()
+    jdt = "float64" if precision == "fp64" else "float32"
+    J = fop.createJacobian(z["rho"], dtype=jdt).cpu().numpy().astype(np.float64)
     e_J = float(np.linalg.norm(J - z["J"]) / np.linalg.norm(z["J"]))
-    print(f"{name}: rhoa {e_rhoa:.2e} potentials {e_pot:.2e} J {e_J:.2e} iters {fop.stats()['iterations']}")
+    print(f"{name} {precision}: rhoa {e_rhoa:.2e} potentials {e_pot:.2e} J({jdt}) {e_J:.2e} "
+          f"iters {fop.stats()['iterations']}")
     assert e_rhoa <= TOL_POT and e_pot <= TOL_POT and e_J <= TOL_J
 
 
@@ -92,19 +95,21 @@ def _c1_case(seed=1):
     return mesh, data, rho
 
 
-def test_2d_config_vs_oracle(torch):
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_2d_config_vs_oracle(torch, precision):
     """41 electrodes, 741 dipole-dipole data, ~3.6k nodes, 17 wavenumbers."""
     mesh, data, rho = _c1_case()
-    fop = fop_for(mesh, data)
+    fop = fop_for(mesh, data, precision=precision)
     assert len(fop.kValues()) == 17
     rhoa = fop.response(rho)
-    J = fop.createJacobian(rho).cpu().numpy()
+    jdt = "float64" if precision == "fp64" else "float32"
+    J = fop.createJacobian(rho, dtype=jdt).cpu().numpy().astype(np.float64)
     P = O.Problem(mesh, data.sensorPositions(), data.abmn(), data["k"], fop.kValues(), fop.weights())
     rhoa_o, u = P.response(rho)
     J_o = P.jacobian(u, rho)
     e_r = float(np.max(np.abs(rhoa - rhoa_o) / rhoa_o))
     e_J = float(np.linalg.norm(J - J_o) / np.linalg.norm(J_o))
-    print(f"2d config: rhoa {e_r:.2e} J {e_J:.2e} iters {fop.stats()['iterations']}")
+    print(f"2d config {precision}: rhoa {e_r:.2e} J {e_J:.2e} iters {fop.stats()['iterations']}")
     assert e_r <= TOL_POT and e_J <= TOL_J
 
 
@@ -119,17 +124,20 @@ def _small_3d(nx=5, ny=4):
     return mesh, data, rho
 
 
-def test_3d_vs_oracle(torch):
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_3d_vs_oracle(torch, precision):
     mesh, data, rho = _small_3d()
-    fop = fop_for(mesh, data)
+    fop = fop_for(mesh, data, precision=precision)
     rhoa = fop.response(rho)
-    J = fop.createJacobian(rho).cpu().numpy()
+    jdt = "float64" if precision == "fp64" else "float32"
+    J = fop.createJacobian(rho, dtype=jdt).cpu().numpy().astype(np.float64)
     P = O.Problem(mesh, data.sensorPositions(), data.abmn(), data["k"], fop.kValues(), fop.weights())
     rhoa_o, u = P.response(rho)
     J_o = P.jacobian(u, rho)
     e_r = float(np.max(np.abs(rhoa - rhoa_o) / rhoa_o))
     e_J = float(np.linalg.norm(J - J_o) / np.linalg.norm(J_o))
-    print(f"3d small ({mesh.nodeCount()} nodes): rhoa {e_r:.2e} J {e_J:.2e} iters {fop.stats()['iterations']}")
+    print(f"3d small {precision} ({mesh.nodeCount()} nodes): rhoa {e_r:.2e} J {e_J:.2e} "
+          f"iters {fop.stats()['iterations']}")
     assert e_r <= TOL_POT and e_J <= TOL_J
 
 
@@ -160,7 +168,7 @@ def test_fp32_jacobian_and_host_abi(torch, golden_dir):
     r_dev = fop.response(z["rho"])
     J64 = fop.createJacobian(z["rho"]).cpu().numpy()
     J32 = fop.createJacobian(z["rho"], dtype="float32").cpu().numpy()
-    assert np.linalg.norm(J32 - J64) <= 1e-6 * np.linalg.norm(J64)
+    assert np.linalg.norm(J32 - J64) <= TOL_J * np.linalg.norm(J64)
     L = _native.load()
     rho = np.ascontiguousarray(z["rho"])
     out = np.zeros(data.size())
@@ -236,6 +244,18 @@ def test_3d_config_properties(torch):
     u = fop.subPotentials()
     Jo = _jacobian_rows_from_potentials(mesh, data, fop.kValues(), fop.weights(), u, 2.0 * rho, rows)
     assert float(np.linalg.norm(Jr - Jo) / np.linalg.norm(Jo)) <= TOL_J
+    # FP32 Jacobian (FP64 differences) against the same rows
+    J32 = fop.createJacobian(2.0 * rho, dtype="float32")
+    J32r = J32[torch.as_tensor(rows, device=J32.device)].cpu().numpy().astype(np.float64)
+    assert float(np.linalg.norm(J32r - Jo) / np.linalg.norm(Jo)) <= TOL_J
+    del J, J32
+    # mixed-precision solve reaches the same answer
+    fop.setPrecision("mixed")
+    r3 = fop.response(2.0 * rho)
+    st3 = fop.stats()
+    assert float(np.max(np.abs(r3 - r2) / r2)) <= TOL_POT
+    fop.setPrecision("fp64")
+    print(f"3d config: mixed iters {st3['iterations']} solve {st3['ms_solve']:.1f} ms")
     # homogeneous half-space: apparent resistivity equals the resistivity
     rh = fop.response(np.full(mesh.cellCount(), 100.0))
     assert float(np.max(np.abs(rh - 100.0) / 100.0)) < 0.05
