@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["box_3d", "box_3d_probe", "line_2d"], default="box_3d")
     ap.add_argument("--rtol", type=float, default=1e-10)
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
@@ -192,7 +193,7 @@ def run_ours(args, world, rank, local):
     dev = torch.device("cuda", local)
     mesh, data, rho, cfg = workload(args.workload)
     t_setup = time.perf_counter()
-    fop = ERTModelling(device=local, rtol=args.rtol)
+    fop = ERTModelling(device=local, rtol=args.rtol, precision=args.precision)
     fop.setData(data)
     fop.setMesh(mesh)
     setup_s = time.perf_counter() - t_setup
@@ -200,14 +201,16 @@ def run_ours(args, world, rank, local):
     D, P, C = data.size(), fop.parameterCount, mesh.cellCount()
     rho_d = torch.from_numpy(rho).to(dev)
     rhoa_d = torch.empty(D, dtype=torch.float64, device=dev)
-    J_d = torch.empty((D, P), dtype=torch.float64, device=dev)
+    jdt = 0 if args.precision == "fp64" else 1
+    J_d = torch.empty((D, P), dtype=torch.float64 if jdt == 0 else torch.float32, device=dev)
+    J_scratch = J_d if jdt == 0 else None
     import ctypes
 
     def step():
         fop._response_dev(rho_d, rhoa_d)
         stream = torch.cuda.current_stream(dev).cuda_stream
         fop._check(L.ertgb_jacobian(fop._ctx, ctypes.c_void_p(rho_d.data_ptr()), C,
-                                    ctypes.c_void_p(J_d.data_ptr()), 0, ctypes.c_void_p(stream)))
+                                    ctypes.c_void_p(J_d.data_ptr()), jdt, ctypes.c_void_p(stream)))
 
     for _ in range(max(args.warmup, 0)):
         step()
@@ -241,41 +244,47 @@ def run_ours(args, world, rank, local):
     by = ctypes.c_double()
     fl = ctypes.c_double()
     prof = {}
-    for name, kid, reps in (("spmm", 0, 20), ("jacobian", 1, 2), ("assemble", 2, 10)):
-        fop._check(L.ertgb_profile_kernel(fop._ctx, kid, reps, ctypes.c_void_p(J_d.data_ptr()),
+    if J_scratch is None:
+        J_scratch = torch.empty((D, P), dtype=torch.float64, device=dev)
+    spmm_kind = ("spmm", 0) if args.precision == "fp64" else ("spmm32", 3)
+    for name, kid, reps in ((spmm_kind[0], spmm_kind[1], 20), ("jacobian", 1, 2), ("assemble", 2, 10)):
+        fop._check(L.ertgb_profile_kernel(fop._ctx, kid, reps, ctypes.c_void_p(J_scratch.data_ptr()),
                                           ctypes.byref(ms), ctypes.byref(by), ctypes.byref(fl)))
         prof[name] = (ms.value, by.value, fl.value)
-    per_step = {"spmm": prof["spmm"][0] * st["iterations"], "jacobian": prof["jacobian"][0],
+    if J_scratch is not J_d:
+        del J_scratch
+    per_step = {spmm_kind[0]: prof[spmm_kind[0]][0] * st["iterations"],
+                "jacobian": prof["jacobian"][0] * (0.5 if jdt == 1 else 1.0),
                 "assemble": prof["assemble"][0]}
     dom = max(per_step, key=per_step.get)
     peak, peak_kind = measured_peaks()
     d_ms, d_bytes, d_flops = prof[dom]
     achieved = d_bytes / (d_ms * 1e-3) / 1e9
-    traffic = ncu_traffic(f"{dom}_fp64_{args.workload}.txt")
+    traffic = ncu_traffic(f"{dom}_{args.precision}_{args.workload}.txt")
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                 "algorithmic_bytes": d_bytes, "ms_per_launch": d_ms,
-                "fp64_tflops": d_flops / (d_ms * 1e-3) / 1e12,
+                "tflops": d_flops / (d_ms * 1e-3) / 1e12,
                 "share_of_step": per_step[dom] / (total_ms / args.steps)}
 
     # end to end through the public API, host buffers
     e2e = None
     if not args.no_e2e:
-        Jh = torch.empty((D, P), dtype=torch.float64, pin_memory=True)
+        Jh = torch.empty((D, P), dtype=J_d.dtype, pin_memory=True)
         model = rho.copy()
         tt = []
         for i in range(max(1, min(args.steps, 3)) + 1):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             r = fop.response(model)
-            J = fop.createJacobian(model)
+            J = fop.createJacobian(model, dtype="float64" if jdt == 0 else "float32")
             Jh.copy_(J, non_blocking=True)
             torch.cuda.synchronize()
             if i > 0:
                 tt.append(time.perf_counter() - t0)
             del J
         e2e = {"value": float(np.mean(tt)), "unit": UNIT, "h2d_bytes_per_step": int(C * 8 + P * 8),
-               "d2h_bytes_per_step": int(D * 8 + D * P * 8), "steps": len(tt),
+               "d2h_bytes_per_step": int(D * 8 + D * P * J_d.element_size()), "steps": len(tt),
                "check_rhoa_vs_device": float(np.max(np.abs(r - rhoa_d.cpu().numpy()) / r))}
         del Jh
 
@@ -289,8 +298,12 @@ def run_ours(args, world, rank, local):
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": value * 1e3 * world, "higher_is_better": False,
-               "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-               "config": dict(cfg, parallelism=f"replicas x{world}", solver="block PCG (Jacobi), FP64",
+               "scaling": "weak", "vs_baseline": None,
+               "dtype": "f64" if args.precision == "fp64" else "f32+f64 (FP32 PCG, FP64 reliable updates)",
+               "data": "synthetic (seeded)",
+               "config": dict(cfg, parallelism=f"replicas x{world}",
+                              solver=f"block PCG (Jacobi), {args.precision}",
+                              jacobian="FP64" if jdt == 0 else "FP32 (FP64 differences)",
                               rtol=args.rtol, l2="working set > L2: PCG blocks 4 x "
                               f"{mesh.nodeCount() * 96 * 8 / 1e6:.0f} MB, J {D * P * 8 / 1e9:.1f} GB"),
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
@@ -298,7 +311,8 @@ def run_ours(args, world, rank, local):
                "breakdown_ms": {"assemble": st["ms_assemble"], "rhs": st["ms_rhs"], "solve": st["ms_solve"],
                                 "collect": st["ms_collect"], "jacobian": st["ms_jacobian"],
                                 "pcg_iterations": st["iterations"], "n_rhs": st["n_rhs"],
-                                "max_rel_residual": st["max_rel_residual"], "setup_s": setup_s}}
+                                "max_rel_residual": st["max_rel_residual"],
+                                "stalled_columns_fp64_finish": st["stalled_columns"], "setup_s": setup_s}}
         print(json.dumps(out), flush=True)
 
 

@@ -41,7 +41,9 @@ typedef enum { ERTGB_PRECOND_JACOBI = 0 } ertgb_precond;
  * recurrence (operator, preconditioner, vectors) with FP64 reliable updates
  * every 64 iterations (the FP64 solution accumulates the FP32 increments and
  * the residual restarts from the FP64 true residual); convergence is tested
- * on the FP64 true residual, so the tolerance means the same in both. */
+ * on the FP64 true residual, so the tolerance means the same in both.
+ * Columns whose true residual stops falling (systems too ill-conditioned
+ * for FP32) are finished by the FP64 solver from where they stalled. */
 typedef enum { ERTGB_PRECISION_FP64 = 0, ERTGB_PRECISION_MIXED = 1 } ertgb_precision;
 
 /* Solver statistics of the last response. */
@@ -56,6 +58,7 @@ typedef struct {
     double ms_jacobian;       /* device time of the last jacobian            */
     int64_t launches_response; /* kernels launched by the last response       */
     int64_t launches_jacobian; /* kernels launched by the last jacobian       */
+    int32_t stalled_columns;   /* mixed precision: columns finished in FP64   */
 } ertgb_stats;
 
 /* Kernels that ertgb_profile_kernel can time. */

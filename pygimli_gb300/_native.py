@@ -27,7 +27,8 @@ class Stats(ctypes.Structure):
                 ("max_rel_residual", ctypes.c_double), ("ms_assemble", ctypes.c_double),
                 ("ms_rhs", ctypes.c_double), ("ms_solve", ctypes.c_double),
                 ("ms_collect", ctypes.c_double), ("ms_jacobian", ctypes.c_double),
-                ("launches_response", ctypes.c_int64), ("launches_jacobian", ctypes.c_int64)]
+                ("launches_response", ctypes.c_int64), ("launches_jacobian", ctypes.c_int64),
+                ("stalled_columns", ctypes.c_int32)]
 
 
 # name -> (restype, argtypes)

@@ -124,6 +124,7 @@ int do_response(Context &c, const double *rho, double *rhoa, void *stream) {
     cudaStream_t s = c.stream;
     c.have_pot = false;
     c.stats.launches_response = 0;
+    c.stats.stalled_columns = 0;
     check_rho(c, rho, s);
     c.d_rho_last = rho;
     MeshData &m = c.mesh;

@@ -92,7 +92,8 @@ struct MeshData {
 struct JacTiles {
     std::vector<int32_t> tile_p;
     DBuf<int32_t> d_tile_p;
-    int max_cells = 0;
+    int max_cells = 0;    // tile width TW (cells, = parameters when one cell each)
+    int stage_cells = 0;  // cells whose potentials are staged at a time
 };
 
 struct Context {
@@ -172,7 +173,8 @@ void finish_potentials(Context &c, cudaStream_t s);
 void collect_response(Context &c, double *rhoa, cudaStream_t s);
 void check_rho(Context &c, const double *rho_cell, cudaStream_t s);
 // pcg.cu
-int pcg_solve(Context &c, cudaStream_t s);
+// mask: warm start (x kept) on the columns with mask[t] != 0; nullptr = cold start, all columns
+int pcg_solve(Context &c, cudaStream_t s, const int32_t *mask = nullptr);
 // pcg_mixed.cu
 int pcg_solve_mixed(Context &c, cudaStream_t s);
 void profile_spmm32(Context &c, int reps, double *ms, double *bytes, double *flops);

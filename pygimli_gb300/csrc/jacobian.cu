@@ -12,18 +12,18 @@
 // block); an electrode index -1 contributes a zero potential.
 //
 // Dipole tables: a scheme uses far fewer distinct current dipoles (a, b) and
-// potential dipoles (m, n) than data.  One block handles a tile of
-// consecutive parameters.  For each cell of the tile and each wavenumber it
-// stages the node potentials U[i][e] of every electrode, V = S U, and then
+// potential dipoles (m, n) than data.  One block handles a tile of up to TW
+// consecutive parameters (TW cells).  For G cells at a time it stages the
+// node potentials U[i][e] of every electrode and V = S U in FP64, then forms
 // the FP64 differences
 //   TA[ia][i] = V[a][i] - V[b][i]   for every distinct current dipole,
 //   TM[im][i] = U[m][i] - U[n][i]   for every distinct potential dipole,
-// stored with the cell index fastest (conflict-free shared-memory reads).
-// Every (datum, parameter) pair is then an nv-term dot product of two table
-// rows.  The differences are formed in FP64 (they cancel); the FP32 form
-// rounds the differences to FP32 and accumulates and stores in FP32.
-// Threads walk (datum, parameter) pairs with the parameter fastest, so a
-// warp writes contiguous runs of a J row.
+// stored with the cell index fastest.  Every (datum, parameter) pair is then
+// an nv-term dot product of two table rows per wavenumber.  The differences
+// are formed in FP64 (they cancel); the FP32 form rounds them to FP32 and
+// accumulates and stores in FP32.  Lane layout in the pair phase: lane =
+// (datum sub-row, cell) with the cell fastest, so conflict-free table reads
+// and contiguous runs of a J row per sub-row.
 #include <algorithm>
 
 #include "ertgb_internal.cuh"
@@ -32,138 +32,143 @@ namespace ertgb {
 
 namespace {
 
-template <int NV, typename CT>
-__global__ void __launch_bounds__(256)
+constexpr int kThreads = 512;
+constexpr size_t kSmemBudget = 200 * 1024;
+
+template <int NV, typename CT, int TW>
+__global__ void __launch_bounds__(kThreads)
     k_jacobian(const int32_t *__restrict__ tile_p, const int32_t *__restrict__ pcell_ptr,
                const int32_t *__restrict__ pcell, const int32_t *__restrict__ cells,
                const double *__restrict__ K, const double *__restrict__ M, const double *__restrict__ kv,
                const double *__restrict__ w, int nK, int nE, int64_t Rpad, const double *__restrict__ pot,
                int nA, const int32_t *__restrict__ dip_a, int nM, const int32_t *__restrict__ dip_m,
                const int32_t *__restrict__ data_dip, const CT *__restrict__ scale_d,
-               const CT *__restrict__ scale_p, int64_t P, int64_t D, int max_cells, CT *__restrict__ J) {
+               const CT *__restrict__ scale_p, int64_t P, int64_t D, int G, CT *__restrict__ J) {
     extern __shared__ double smem[];
     const int E1 = nE + 1;
-    const int uv_cell = nK * NV * E1;  // doubles per cell for U (same for V)
+    const int uv_cell = nK * NV * E1;  // doubles per staged cell (U; V the same)
     double *U = smem;
-    double *V = smem + (size_t)max_cells * uv_cell;
-    CT *TA = reinterpret_cast<CT *>(V + (size_t)max_cells * uv_cell);
-    CT *TM = TA + (size_t)nK * nA * NV * max_cells;
-    const int64_t p0 = tile_p[blockIdx.x], p1 = tile_p[blockIdx.x + 1];
-    const int TP = (int)(p1 - p0);
-    const int cbeg = pcell_ptr[p0], cend = pcell_ptr[p1];
-    const int ncell = cend - cbeg;
-    const int nchunks = (ncell + max_cells - 1) / max_cells;
-    const int64_t pairs = D * TP;
-    const int64_t nbatch = (pairs + blockDim.x - 1) / blockDim.x;
-    const int W = max_cells;  // row stride of the tables (cell fastest)
+    double *V = smem + (size_t)G * uv_cell;
+    CT *TA = reinterpret_cast<CT *>(V + (size_t)G * uv_cell);
+    CT *TM = TA + (size_t)nK * nA * NV * TW;
+    const int p0 = tile_p[blockIdx.x], p1 = tile_p[blockIdx.x + 1];
+    const int TP = p1 - p0;
+    const int cbeg = pcell_ptr[p0];
+    const int ncell = pcell_ptr[p1] - cbeg;
+    const int nchunks = (ncell + TW - 1) / TW;
 
-    auto stage = [&](int c0, int cn) {
-        const int total = cn * uv_cell;
-        for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-            const int lc = idx / uv_cell;
-            int rem = idx - lc * uv_cell;
-            const int ki = rem / (NV * E1);
-            rem -= ki * NV * E1;
-            const int i = rem / E1;
-            const int e = rem - i * E1;
-            const int cell = pcell[cbeg + c0 + lc];
-            const int64_t node = cells[(int64_t)cell * NV + i];
-            U[idx] = (e < nE) ? pot[node * Rpad + (int64_t)ki * nE + e] : 0.0;
-        }
-        __syncthreads();
-        for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-            const int lc = idx / uv_cell;
-            int rem = idx - lc * uv_cell;
-            const int ki = rem / (NV * E1);
-            rem -= ki * NV * E1;
-            const int i = rem / E1;
-            const int e = rem - i * E1;
-            const int cell = pcell[cbeg + c0 + lc];
-            const double k = kv[ki];
-            const double kk = k * k;
-            const double *Kc = K + (int64_t)cell * NV * NV + i * NV;
-            const double *Mc = M + (int64_t)cell * NV * NV + i * NV;
-            const double *Uc = U + (size_t)lc * uv_cell + (size_t)ki * NV * E1 + e;
-            double acc = 0.0;
+    // pair-phase lane layout
+    constexpr int SUB = 32 / TW;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int c = lane % TW, sub = lane / TW;
+    const int dstep = (kThreads / 32) * SUB;
+    const int d0 = warp * SUB + sub;
+    const bool has_p = c < TP;
+    const int p = p0 + (has_p ? c : 0);
+    const int pc0 = pcell_ptr[p] - cbeg, pc1 = pcell_ptr[p + 1] - cbeg;  // this parameter's cells in the tile
+    const CT sp = (scale_p && has_p) ? scale_p[p] : (CT)1;
+    __shared__ CT wk[64];  // wavenumber weights (nK <= 64)
+    for (int ki = threadIdx.x; ki < nK; ki += kThreads) wk[ki] = (CT)w[ki];
+    __syncthreads();
+
+    // stage cells [c0 + g0, c0 + g0 + gn) and write their table columns g0.. of the chunk
+    auto build = [&](int c0, int cn) {
+        for (int g0 = 0; g0 < cn; g0 += G) {
+            const int gn = min(G, cn - g0);
+            __syncthreads();
+            for (int q = threadIdx.x; q < gn * uv_cell; q += kThreads) {
+                const int g = q / uv_cell;
+                const int rem = q - g * uv_cell;
+                const int kin = rem / E1;  // ki * NV + i
+                const int e = rem - kin * E1;
+                const int ki = kin / NV, i = kin - ki * NV;
+                const int cell = pcell[cbeg + c0 + g0 + g];
+                const int64_t node = cells[(int64_t)cell * NV + i];
+                U[q] = (e < nE) ? pot[node * Rpad + (int64_t)ki * nE + e] : 0.0;
+            }
+            __syncthreads();
+            for (int q = threadIdx.x; q < gn * uv_cell; q += kThreads) {
+                const int g = q / uv_cell;
+                const int rem = q - g * uv_cell;
+                const int kin = rem / E1;
+                const int e = rem - kin * E1;
+                const int ki = kin / NV, i = kin - ki * NV;
+                const int cell = pcell[cbeg + c0 + g0 + g];
+                const double k = kv[ki];
+                const double kk = k * k;
+                const double *Kc = K + (int64_t)cell * NV * NV + i * NV;
+                const double *Mc = M + (int64_t)cell * NV * NV + i * NV;
+                const double *Uc = U + (size_t)g * uv_cell + (size_t)ki * NV * E1 + e;
+                double acc = 0.0;
 #pragma unroll
-            for (int j = 0; j < NV; j++) acc = fma(Mc[j] * kk + Kc[j], Uc[j * E1], acc);
-            V[idx] = acc;
-        }
-        __syncthreads();
-        // dipole tables, FP64 differences
-        const int ta = nK * nA * NV * cn;
-        for (int idx = threadIdx.x; idx < ta; idx += blockDim.x) {
-            const int lc = idx % cn;
-            int rem = idx / cn;
-            const int i = rem % NV;
-            rem /= NV;
-            const int ia = rem % nA;
-            const int ki = rem / nA;
-            int a = dip_a[2 * ia], b = dip_a[2 * ia + 1];
-            a = a < 0 ? nE : a;
-            b = b < 0 ? nE : b;
-            const double *Vc = V + (size_t)lc * uv_cell + ((size_t)ki * NV + i) * E1;
-            TA[(((size_t)ki * nA + ia) * NV + i) * W + lc] = (CT)(Vc[a] - Vc[b]);
-        }
-        const int tm = nK * nM * NV * cn;
-        for (int idx = threadIdx.x; idx < tm; idx += blockDim.x) {
-            const int lc = idx % cn;
-            int rem = idx / cn;
-            const int i = rem % NV;
-            rem /= NV;
-            const int im = rem % nM;
-            const int ki = rem / nM;
-            int m = dip_m[2 * im], n = dip_m[2 * im + 1];
-            m = m < 0 ? nE : m;
-            n = n < 0 ? nE : n;
-            const double *Uc = U + (size_t)lc * uv_cell + ((size_t)ki * NV + i) * E1;
-            TM[(((size_t)ki * nM + im) * NV + i) * W + lc] = (CT)(Uc[m] - Uc[n]);
+                for (int j = 0; j < NV; j++) acc = fma(Mc[j] * kk + Kc[j], Uc[j * E1], acc);
+                V[q] = acc;
+            }
+            __syncthreads();
+            const int rowsA = nK * nA * NV, rowsM = nK * nM * NV;
+            for (int q = threadIdx.x; q < (rowsA + rowsM) * gn; q += kThreads) {
+                const int g = q % gn;
+                int row = q / gn;
+                const bool isA = row < rowsA;
+                if (!isA) row -= rowsA;
+                const int i = row % NV;
+                const int kd = row / NV;  // ki * n{A,M} + dipole
+                const int nd = isA ? nA : nM;
+                const int ki = kd / nd, dp = kd - ki * nd;
+                const int32_t *dip = isA ? dip_a : dip_m;
+                int a = dip[2 * dp], b = dip[2 * dp + 1];
+                a = a < 0 ? nE : a;
+                b = b < 0 ? nE : b;
+                const double *src = (isA ? V : U) + (size_t)g * uv_cell + ((size_t)ki * NV + i) * E1;
+                CT *dst = isA ? TA : TM;
+                dst[(size_t)row * TW + g0 + g] = (CT)(src[a] - src[b]);
+            }
         }
         __syncthreads();
     };
 
-    auto accumulate = [&](int64_t pr, int c0, int cn, CT acc) -> CT {
-        const int pl = (int)(pr % TP);
-        const int64_t d = pr / TP;
-        const int64_t p = p0 + pl;
+    auto pair_sum = [&](int64_t d, int lo, int hi) -> CT {
         const int ia = data_dip[2 * d], im = data_dip[2 * d + 1];
-        const int lo = max(pcell_ptr[p] - cbeg, c0), hi = min(pcell_ptr[p + 1] - cbeg, c0 + cn);
-        for (int lc = lo - c0; lc < hi - c0; lc++) {
+        CT acc = 0;
+        for (int lc = lo; lc < hi; lc++) {
             for (int ki = 0; ki < nK; ki++) {
-                const CT *ta = TA + ((size_t)ki * nA + ia) * NV * W + lc;
-                const CT *tm = TM + ((size_t)ki * nM + im) * NV * W + lc;
+                const CT *ta = TA + ((size_t)ki * nA + ia) * NV * TW + lc;
+                const CT *tm = TM + ((size_t)ki * nM + im) * NV * TW + lc;
                 CT s = 0;
 #pragma unroll
-                for (int i = 0; i < NV; i++) s = fma(ta[i * W], tm[i * W], s);
-                acc = fma(s, (CT)w[ki], acc);
+                for (int i = 0; i < NV; i++) s = fma(ta[i * TW], tm[i * TW], s);
+                acc = fma(s, wk[ki], acc);
             }
         }
         return acc;
     };
 
-    auto store = [&](int64_t pr, CT acc) {
-        const int pl = (int)(pr % TP);
-        const int64_t d = pr / TP;
-        const int64_t p = p0 + pl;
-        if (scale_p) acc = (acc * scale_d[d]) * scale_p[p];
-        J[d * P + p] = acc;
-    };
-
     if (nchunks <= 1) {
-        if (ncell > 0) stage(0, ncell);
-        for (int64_t pr = threadIdx.x; pr < pairs; pr += blockDim.x) store(pr, accumulate(pr, 0, ncell, (CT)0));
+        if (ncell > 0) build(0, ncell);
+        if (has_p) {
+            for (int64_t d = d0; d < D; d += dstep) {
+                CT acc = pair_sum(d, pc0, pc1);
+                if (scale_p) acc = (acc * scale_d[d]) * sp;
+                J[d * P + p] = acc;
+            }
+        }
     } else {
+        // a parameter with more cells than a tile holds: accumulate over chunks
+        const int64_t nbatch = (D + dstep - 1) / dstep;
         for (int64_t bt = 0; bt < nbatch; bt++) {
-            const int64_t pr = bt * blockDim.x + threadIdx.x;
+            const int64_t d = bt * dstep + d0;
             CT acc = 0;
             for (int ch = 0; ch < nchunks; ch++) {
-                const int c0 = ch * max_cells;
-                const int cn = min(max_cells, ncell - c0);
-                __syncthreads();
-                stage(c0, cn);
-                if (pr < pairs) acc = accumulate(pr, c0, cn, acc);
+                const int c0 = ch * TW;
+                const int cn = min(TW, ncell - c0);
+                build(c0, cn);
+                const int lo = max(pc0, c0) - c0, hi = min(pc1, c0 + cn) - c0;
+                if (has_p && d < D && lo < hi) acc += pair_sum(d, lo, hi);
             }
-            if (pr < pairs) store(pr, acc);
+            if (has_p && d < D) {
+                if (scale_p) acc = (acc * scale_d[d]) * sp;
+                J[d * P + p] = acc;
+            }
         }
     }
 }
@@ -184,10 +189,18 @@ __global__ void k_jac_scales(int64_t D, int64_t P, const double *__restrict__ kf
     }
 }
 
-size_t jac_cell_bytes(const Context &c, int dtype) {
+// shared-memory plan: tile width TW (power of two, <= 16) and the cells G
+// staged at a time for the given table precision
+bool plan(const Context &c, int dtype, int *TW, int *G) {
     const size_t uv = 2 * (size_t)c.nK * c.mesh.nv * (c.nE + 1) * sizeof(double);
     const size_t tab = (size_t)c.nK * (c.nA + c.nM) * c.mesh.nv * (dtype == 0 ? 8 : 4);
-    return uv + tab;
+    for (int tw : {16, 8, 4}) {
+        if (tw * tab + uv > kSmemBudget) continue;
+        *TW = tw;
+        *G = (int)std::max<size_t>(1, std::min<size_t>(4, (kSmemBudget - tw * tab) / uv));
+        return true;
+    }
+    return false;
 }
 
 template <typename CT>
@@ -196,7 +209,10 @@ void launch(Context &c, const double *model, CT *J, int dtype, cudaStream_t s) {
     JacTiles &T = c.jtiles[dtype];
     const int ntiles = (int)T.tile_p.size() - 1;
     if (ntiles <= 0) return;
-    const size_t smem = jac_cell_bytes(c, dtype) * T.max_cells;
+    if (c.nK > 64) throw Error(ERTGB_BAD_INPUT, "Jacobian supports at most 64 wavenumbers");
+    const int TW = T.max_cells, G = T.stage_cells;
+    const size_t uv = (size_t)c.nK * m.nv * (c.nE + 1);
+    const size_t smem = 2 * uv * G * sizeof(double) + (size_t)c.nK * (c.nA + c.nM) * m.nv * TW * sizeof(CT);
     const CT *sd = nullptr, *sp = nullptr;
     if (model) {
         c.d_jscale.alloc((size_t)(c.D + m.P) * sizeof(CT));
@@ -209,19 +225,26 @@ void launch(Context &c, const double *model, CT *J, int dtype, cudaStream_t s) {
     }
     auto go = [&](auto kern) {
         ERTGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        kern<<<ntiles, 256, smem, s>>>(T.d_tile_p.p, m.d_pcell_ptr.p, m.d_pcell.p, m.d_cells.p, m.d_K.p, m.d_M.p,
-                                       c.d_k.p, c.d_w.p, c.nK, c.nE, c.Rpad, c.d_x.p, c.nA, c.d_dip_a.p, c.nM,
-                                       c.d_dip_m.p, c.d_data_dip.p, sd, sp, m.P, c.D, T.max_cells, J);
+        kern<<<ntiles, kThreads, smem, s>>>(T.d_tile_p.p, m.d_pcell_ptr.p, m.d_pcell.p, m.d_cells.p, m.d_K.p, m.d_M.p,
+                                            c.d_k.p, c.d_w.p, c.nK, c.nE, c.Rpad, c.d_x.p, c.nA, c.d_dip_a.p, c.nM,
+                                            c.d_dip_m.p, c.d_data_dip.p, sd, sp, m.P, c.D, G, J);
         ERTGB_CUDA(cudaGetLastError());
     };
-    if (m.nv == 3) go(k_jacobian<3, CT>);
-    else go(k_jacobian<4, CT>);
+    if (m.nv == 3) {
+        if (TW == 16) go(k_jacobian<3, CT, 16>);
+        else if (TW == 8) go(k_jacobian<3, CT, 8>);
+        else go(k_jacobian<3, CT, 4>);
+    } else {
+        if (TW == 16) go(k_jacobian<4, CT, 16>);
+        else if (TW == 8) go(k_jacobian<4, CT, 8>);
+        else go(k_jacobian<4, CT, 4>);
+    }
 }
 
 }  // namespace
 
 // Parameter -> cells and the Jacobian tiles of both table precisions
-// (consecutive parameters whose cells fit the shared-memory budget).
+// (consecutive parameters with at most TW cells per tile).
 void build_jacobian_tiles(Context &c) {
     MeshData &m = c.mesh;
     const int64_t P = m.P;
@@ -235,19 +258,22 @@ void build_jacobian_tiles(Context &c) {
         if (m.marker[i] >= 0) m.pcell[pos[m.marker[i]]++] = (int32_t)i;
     m.d_pcell_ptr.upload(m.pcell_ptr, c.stream);
     m.d_pcell.upload(m.pcell, c.stream);
-    const size_t budget = 200 * 1024;
     for (int dt = 0; dt < 2; dt++) {
         JacTiles &T = c.jtiles[dt];
-        const size_t per_cell = jac_cell_bytes(c, dt);
-        T.max_cells = per_cell > budget ? 0 : (int)std::min<size_t>(32, budget / per_cell);
         T.tile_p.assign(1, 0);
-        if (T.max_cells == 0) continue;
+        int TW = 0, G = 0;
+        if (!plan(c, dt, &TW, &G)) {
+            T.max_cells = 0;
+            continue;
+        }
+        T.max_cells = TW;
+        T.stage_cells = G;
         int64_t p = 0;
         while (p < P) {
             int64_t q = p, ncell = 0;
-            while (q < P && q - p < 32) {
+            while (q < P && q - p < TW) {
                 const int64_t cq = m.pcell_ptr[q + 1] - m.pcell_ptr[q];
-                if (q > p && ncell + cq > T.max_cells) break;
+                if (q > p && ncell + cq > TW) break;
                 ncell += cq;
                 q++;
             }
@@ -261,8 +287,8 @@ void build_jacobian_tiles(Context &c) {
 
 void jacobian(Context &c, const double *model, int n_model, void *J, int dtype, cudaStream_t s) {
     if (c.jtiles[dtype].max_cells == 0)
-        throw Error(ERTGB_BAD_INPUT, "Jacobian staging of one cell exceeds shared memory "
-                                     "(too many electrodes x wavenumbers x dipoles)");
+        throw Error(ERTGB_BAD_INPUT, "Jacobian tables of one cell exceed shared memory "
+                                     "(too many wavenumbers x distinct dipoles)");
     const double *mdl = (n_model == c.mesh.P) ? model : nullptr;
     if (dtype == 0) launch<double>(c, mdl, (double *)J, 0, s);
     else launch<float>(c, mdl, (float *)J, 1, s);

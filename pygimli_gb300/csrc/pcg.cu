@@ -32,8 +32,6 @@ constexpr int kRowsPerBlock = 8;  // warps per block in spmm, rows per block in 
 constexpr int kGraphIters = 16;
 constexpr int kPartRows = 608;  // block partial rows of every column reduction (4 x 152 SMs)
 
-// per-column scalar slots in Context::d_col
-enum Col { RHO = 0, ALPHA, BETA, BNORM2, RNORM2, PQ, NCOL };
 
 template <int CH>
 __global__ void __launch_bounds__(256) k_spmm_dot(int64_t n, int64_t nnz, int nE, int nK, int64_t Rpad,
@@ -118,21 +116,80 @@ __global__ void k_init(int64_t n, int nE, int nK, int64_t R, int64_t Rpad, const
 __global__ void k_finish_init(int64_t Rpad, int64_t R, int NB, const double *__restrict__ part_a,
                               const double *__restrict__ part_b, double *__restrict__ col,
                               int32_t *__restrict__ active, int32_t *__restrict__ iters,
-                              int32_t *__restrict__ nactive) {
+                              int32_t *__restrict__ nactive, const int32_t *__restrict__ mask) {
     __shared__ double ra[32][33], rb[32][33];
     const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
     const double rz = col_sum(part_a, NB, Rpad, t, ra);
     const double rr = col_sum(part_b, NB, Rpad, t, rb);
     if (threadIdx.y != 0) return;
     col[RHO * Rpad + t] = rz;
-    col[BNORM2 * Rpad + t] = rr;
-    col[RNORM2 * Rpad + t] = rr;
     col[ALPHA * Rpad + t] = 0.0;
     col[BETA * Rpad + t] = 0.0;
+    if (mask) {  // warm start of selected columns: keep the right-hand side norms
+        if (!mask[t]) return;
+        col[RNORM2 * Rpad + t] = rr;
+        col[RPREV * Rpad + t] = rr;
+        const int a = (rr > 0.0) ? 1 : 0;
+        active[t] = a;
+        if (a) atomicAdd(nactive, 1);
+        return;
+    }
+    col[BNORM2 * Rpad + t] = rr;
+    col[RNORM2 * Rpad + t] = rr;
+    col[RPREV * Rpad + t] = rr;
+    col[STALLS * Rpad + t] = 0.0;
     const int a = (t < R && rr > 0.0) ? 1 : 0;
     active[t] = a;
     iters[t] = 0;
     if (a) atomicAdd(nactive, 1);
+}
+
+// Columns marked 2 (diverged in the mixed solver) restart from x = 0.
+__global__ void k_zero_restart(int64_t n, int64_t Rpad, const int32_t *__restrict__ mask, double *__restrict__ x) {
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    if (mask[t] != 2) return;
+    for (int64_t row = (int64_t)blockIdx.y * kRowsPerBlock + threadIdx.y; row < n;
+         row += (int64_t)gridDim.y * kRowsPerBlock)
+        x[row * Rpad + t] = 0.0;
+}
+
+// FP64 residual in place for a warm start: r = b - A x on masked columns
+// (warp per row, lanes over columns; each element is read and written by
+// the same thread).
+template <int CH>
+__global__ void __launch_bounds__(256) k_residual64(int64_t n, int64_t nnz, int nE, int nK, int64_t Rpad,
+                                                    const int32_t *__restrict__ rowptr,
+                                                    const int32_t *__restrict__ colidx,
+                                                    const double *__restrict__ vals, const double *__restrict__ x,
+                                                    const int32_t *__restrict__ mask, double *__restrict__ rb) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t t0 = (int64_t)blockIdx.y * 32 * CH + lane;
+    int64_t kofs[CH];
+    bool on[CH];
+#pragma unroll
+    for (int j = 0; j < CH; j++) {
+        kofs[j] = min((t0 + 32 * j) / nE, (int64_t)nK - 1) * nnz;
+        on[j] = mask[t0 + 32 * j] != 0;
+    }
+    for (int64_t row = (int64_t)blockIdx.x * kRowsPerBlock + wid; row < n; row += (int64_t)gridDim.x * kRowsPerBlock) {
+        double acc[CH];
+#pragma unroll
+        for (int j = 0; j < CH; j++) acc[j] = 0.0;
+        const int32_t s1 = rowptr[row + 1];
+        for (int32_t s = rowptr[row]; s < s1; s++) {
+            const int64_t col = colidx[s];
+#pragma unroll
+            for (int j = 0; j < CH; j++)
+                if (on[j]) acc[j] = fma(vals[kofs[j] + s], x[col * Rpad + t0 + 32 * j], acc[j]);
+        }
+        // (columns restarted from zero have x = 0 here, see k_zero_restart)
+#pragma unroll
+        for (int j = 0; j < CH; j++)
+            if (on[j]) {
+                const int64_t i = row * Rpad + t0 + 32 * j;
+                rb[i] = rb[i] - acc[j];
+            }
+    }
 }
 
 __global__ void k_finish_alpha(int64_t Rpad, int NB, const double *__restrict__ part,
@@ -245,30 +302,46 @@ void launch_spmm(int ch, dim3 grid, cudaStream_t s, int64_t n, int64_t nnz, int 
 
 }  // namespace
 
-int pcg_solve(Context &c, cudaStream_t s) {
+int pcg_solve(Context &c, cudaStream_t s, const int32_t *mask) {
     MeshData &m = c.mesh;
     const int64_t n = m.n, Rpad = c.Rpad, R = c.R;
     const int NB = (int)std::min<int64_t>(ceil_div(n, kRowsPerBlock), kPartRows);
     const int ch = choose_ch(Rpad);
     const int nchunk = (int)(Rpad / (32 * ch));
     // workspaces
-    c.d_x.alloc((size_t)n * Rpad);
+    if (!mask) c.d_x.alloc((size_t)n * Rpad);
     c.d_p.alloc((size_t)n * Rpad);
     c.d_q.alloc((size_t)n * Rpad);
     c.d_part.alloc((size_t)NB * Rpad * 3);
-    c.d_col.alloc((size_t)NCOL * Rpad);
-    c.d_active.alloc((size_t)Rpad * 2 + 1);
+    if (!mask) {
+        c.d_col.alloc((size_t)NCOL * Rpad);
+        c.d_active.alloc(ColState::size(Rpad));
+    }
     double *part_a = c.d_part.p, *part_b = c.d_part.p + (size_t)NB * Rpad, *part_c = c.d_part.p + 2 * (size_t)NB * Rpad;
-    int32_t *active = c.d_active.p, *iters = c.d_active.p + Rpad, *nactive = c.d_active.p + 2 * Rpad;
-    ERTGB_CUDA(cudaMemsetAsync(c.d_x.p, 0, sizeof(double) * n * Rpad, s));
-    ERTGB_CUDA(cudaMemsetAsync(nactive, 0, sizeof(int32_t), s));
+    ColState cs(c.d_active.p, Rpad);
+    int32_t *active = cs.active, *iters = cs.iters, *nactive = cs.nactive;
     const dim3 vb(32, kRowsPerBlock), vg((unsigned)(Rpad / 32), (unsigned)NB);
     const dim3 sg((unsigned)NB, (unsigned)nchunk);
     const unsigned fg = (unsigned)(Rpad / 32);
     const dim3 fb(32, 32);
     const double rtol2 = c.rtol * c.rtol;
+    if (mask) {
+        // warm start from x on the masked columns: r = b - A x in place
+        k_zero_restart<<<vg, vb, 0, s>>>(n, Rpad, mask, c.d_x.p);
+        c.stats.launches_response += 1;
+        switch (ch) {
+            case 4: k_residual64<4><<<sg, 256, 0, s>>>(n, m.nnz, c.nE, c.nK, Rpad, m.d_rowptr.p, m.d_colidx.p, c.d_S.p, c.d_x.p, mask, c.d_r.p); break;
+            case 3: k_residual64<3><<<sg, 256, 0, s>>>(n, m.nnz, c.nE, c.nK, Rpad, m.d_rowptr.p, m.d_colidx.p, c.d_S.p, c.d_x.p, mask, c.d_r.p); break;
+            case 2: k_residual64<2><<<sg, 256, 0, s>>>(n, m.nnz, c.nE, c.nK, Rpad, m.d_rowptr.p, m.d_colidx.p, c.d_S.p, c.d_x.p, mask, c.d_r.p); break;
+            default: k_residual64<1><<<sg, 256, 0, s>>>(n, m.nnz, c.nE, c.nK, Rpad, m.d_rowptr.p, m.d_colidx.p, c.d_S.p, c.d_x.p, mask, c.d_r.p); break;
+        }
+        c.stats.launches_response += 1;
+    } else {
+        ERTGB_CUDA(cudaMemsetAsync(c.d_x.p, 0, sizeof(double) * n * Rpad, s));
+    }
+    ERTGB_CUDA(cudaMemsetAsync(nactive, 0, sizeof(int32_t), s));
     k_init<<<vg, vb, 0, s>>>(n, c.nE, c.nK, R, Rpad, c.d_dinv.p, c.d_r.p, c.d_p.p, part_a, part_b);
-    k_finish_init<<<fg, fb, 0, s>>>(Rpad, R, NB, part_a, part_b, c.d_col.p, active, iters, nactive);
+    k_finish_init<<<fg, fb, 0, s>>>(Rpad, R, NB, part_a, part_b, c.d_col.p, active, iters, nactive, mask);
     ERTGB_CUDA(cudaGetLastError());
 
     // capture a chunk of iterations
@@ -338,9 +411,10 @@ int pcg_solve(Context &c, cudaStream_t s) {
         status = ERTGB_NOT_CONVERGED;
         maxres = NAN;
     }
+    // with a mask the per-column counts continue those of the mixed solve
     c.stats.iterations = maxit;
-    c.stats.n_rhs = (int32_t)R;
     c.stats.max_rel_residual = maxres;
+    c.stats.n_rhs = (int32_t)R;
     return status;
 }
 
@@ -355,7 +429,7 @@ __global__ void k_col_total(int64_t Rpad, int NB, const double *__restrict__ par
 
 void pcg_finish_init(dim3 g, dim3 b, cudaStream_t s, int64_t Rpad, int64_t R, int NB, const double *pa, const double *pb,
                      double *col, int32_t *active, int32_t *iters, int32_t *nactive) {
-    k_finish_init<<<g, b, 0, s>>>(Rpad, R, NB, pa, pb, col, active, iters, nactive);
+    k_finish_init<<<g, b, 0, s>>>(Rpad, R, NB, pa, pb, col, active, iters, nactive, nullptr);
 }
 
 void pcg_finish_alpha(dim3 g, dim3 b, cudaStream_t s, int64_t Rpad, int NB, const double *part, double *col,

@@ -24,9 +24,8 @@ namespace {
 constexpr int kRows = 8;            // warps per block (spmm) / rows per block (vector kernels)
 constexpr int kGraphIters = 16;     // iterations per captured graph
 constexpr int kReliableEvery = 4;   // graphs between reliable updates (64 iterations)
-constexpr int kPartRows = 608;
+constexpr int kPartRows = 1216;  // 8 row blocks per SM: the FP32 kernels need more warps in flight
 
-enum Col { RHO = 0, ALPHA, BETA, BNORM2, RNORM2, PQ, NCOL };
 
 __global__ void k_to_f32(int64_t n, const double *__restrict__ a, float *__restrict__ b) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -98,6 +97,57 @@ __global__ void __launch_bounds__(256) k_spmm32_dot(int64_t n, int64_t nnz, int 
             const float *pc = p + col * Rpad + t0;
 #pragma unroll
             for (int j = 0; j < CH; j++) acc[j] = fmaf(vals[kofs[j] + s], pc[32 * j], acc[j]);
+        }
+        float *qr = q + row * Rpad + t0;
+        const float *pr = p + row * Rpad + t0;
+#pragma unroll
+        for (int j = 0; j < CH; j++) {
+            qr[32 * j] = acc[j];
+            dot[j] = fmaf(pr[32 * j], acc[j], dot[j]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < CH; j++) red[wid][lane + 32 * j] = (double)dot[j];
+    __syncthreads();
+    for (int c = threadIdx.x; c < 32 * CH; c += blockDim.x) {
+        double s = 0.0;
+#pragma unroll
+        for (int w = 0; w < kRows; w++) s += red[w][c];
+        part[(int64_t)blockIdx.x * Rpad + (int64_t)blockIdx.y * 32 * CH + c] = s;
+    }
+}
+
+// Single-matrix variant (nK = 1): the warp loads up to 32 (column, value)
+// pairs of its row at once, one per lane, and broadcasts them with
+// shuffles, leaving the coalesced gathers of p as the only dependent loads.
+template <int CH>
+__global__ void __launch_bounds__(256) k_spmm32_dot_k1(int64_t n, int64_t Rpad, const int32_t *__restrict__ rowptr,
+                                                       const int32_t *__restrict__ colidx,
+                                                       const float *__restrict__ vals, const float *__restrict__ p,
+                                                       float *__restrict__ q, double *__restrict__ part) {
+    __shared__ double red[kRows][32 * CH];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t t0 = (int64_t)blockIdx.y * 32 * CH + lane;
+    float dot[CH];
+#pragma unroll
+    for (int j = 0; j < CH; j++) dot[j] = 0.f;
+    for (int64_t row = (int64_t)blockIdx.x * kRows + wid; row < n; row += (int64_t)gridDim.x * kRows) {
+        float acc[CH];
+#pragma unroll
+        for (int j = 0; j < CH; j++) acc[j] = 0.f;
+        const int32_t s0 = rowptr[row], len = rowptr[row + 1] - s0;
+        for (int base = 0; base < len; base += 32) {
+            const int cnt = min(32, len - base);
+            const int32_t mc = lane < cnt ? colidx[s0 + base + lane] : 0;
+            const float mv = lane < cnt ? vals[s0 + base + lane] : 0.f;
+#pragma unroll 4
+            for (int e = 0; e < cnt; e++) {
+                const int64_t col = __shfl_sync(0xffffffffu, mc, e);
+                const float v = __shfl_sync(0xffffffffu, mv, e);
+                const float *pc = p + col * Rpad + t0;
+#pragma unroll
+                for (int j = 0; j < CH; j++) acc[j] = fmaf(v, pc[32 * j], acc[j]);
+            }
         }
         float *qr = q + row * Rpad + t0;
         const float *pr = p + row * Rpad + t0;
@@ -255,22 +305,50 @@ __global__ void __launch_bounds__(256) k_m_residual(int64_t n, int64_t nnz, int 
     }
 }
 
-// reliable update, part 3: FP64 convergence test, rho of the restarted residual
+// reliable update, part 3: FP64 convergence test on the true residual, rho
+// of the restarted residual, and stall detection.  A column whose best true
+// residual has not improved by 10 % over four reliable-update intervals
+// (256 iterations), or whose FP32 recurrence diverged (residual above twice
+// the right-hand side, or not finite), stops here and is finished by the
+// FP64 solver: nearly singular systems such as the smallest 2.5-D
+// wavenumbers are beyond FP32 (their FP32 matrix can lose definiteness).
+// stalled[t] = 1: warm start from the FP64 solution; 2: restart from zero.
 __global__ void k_m_finish_ru(int64_t Rpad, int NB, double rtol2, const double *__restrict__ part_a,
-                              const double *__restrict__ part_b, double *__restrict__ col,
-                              int32_t *__restrict__ active, int32_t *__restrict__ nactive) {
+                              const double *__restrict__ part_b, double *__restrict__ col, ColState cs) {
     __shared__ double ra[32][33], rb[32][33];
     const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
     const double rz = col_sum(part_a, NB, Rpad, t, ra);
     const double rr = col_sum(part_b, NB, Rpad, t, rb);
-    if (threadIdx.y != 0 || !active[t]) return;
+    if (threadIdx.y != 0 || !cs.active[t]) return;
+    const double bb = col[BNORM2 * Rpad + t];
     col[RNORM2 * Rpad + t] = rr;
     col[RHO * Rpad + t] = rz;
-    if (rr <= rtol2 * col[BNORM2 * Rpad + t] || !(rr == rr)) {
-        active[t] = 0;
-    } else {
-        atomicAdd(nactive, 1);
+    if (rr <= rtol2 * bb) {
+        cs.active[t] = 0;
+        return;
     }
+    if (!(rr <= 4.0 * bb) || !(rz == rz)) {  // diverged or not finite
+        cs.active[t] = 0;
+        cs.stalled[t] = 2;
+        atomicAdd(cs.nstalled, 1);
+        return;
+    }
+    const double best = col[RPREV * Rpad + t];
+    double stalls = col[STALLS * Rpad + t];
+    if (rr < 0.81 * best) {
+        col[RPREV * Rpad + t] = rr;
+        stalls = 0.0;
+    } else {
+        stalls += 1.0;
+    }
+    col[STALLS * Rpad + t] = stalls;
+    if (stalls >= 4.0) {
+        cs.active[t] = 0;
+        cs.stalled[t] = 1;
+        atomicAdd(cs.nstalled, 1);
+        return;
+    }
+    atomicAdd(cs.nactive, 1);
 }
 
 int choose_ch(int64_t Rpad) {
@@ -292,7 +370,8 @@ template <template <int> class F, typename... A> void dispatch_ch(int ch, A &&..
 template <int CH> struct SpmmL {
     static void go(dim3 g, cudaStream_t s, int64_t n, int64_t nnz, int nE, int nK, int64_t Rpad, const int32_t *rp,
                    const int32_t *ci, const float *v, const float *p, float *q, double *part) {
-        k_spmm32_dot<CH><<<g, 256, 0, s>>>(n, nnz, nE, nK, Rpad, rp, ci, v, p, q, part);
+        if (nK == 1) k_spmm32_dot_k1<CH><<<g, 256, 0, s>>>(n, Rpad, rp, ci, v, p, q, part);
+        else k_spmm32_dot<CH><<<g, 256, 0, s>>>(n, nnz, nE, nK, Rpad, rp, ci, v, p, q, part);
     }
 };
 
@@ -327,12 +406,13 @@ int pcg_solve_mixed(Context &c, cudaStream_t s) {
     c.d_y32.alloc((size_t)n * Rpad);
     c.d_part.alloc((size_t)NB * Rpad * 3);
     c.d_col.alloc((size_t)NCOL * Rpad);
-    c.d_active.alloc((size_t)Rpad * 2 + 1);
+    c.d_active.alloc(ColState::size(Rpad));
     double *part_a = c.d_part.p, *part_b = c.d_part.p + (size_t)NB * Rpad, *part_c = c.d_part.p + 2 * (size_t)NB * Rpad;
-    int32_t *active = c.d_active.p, *iters = c.d_active.p + Rpad, *nactive = c.d_active.p + 2 * Rpad;
+    ColState cs(c.d_active.p, Rpad);
+    int32_t *active = cs.active, *iters = cs.iters, *nactive = cs.nactive;
     const double *b = c.d_r.p;  // the right-hand sides (FP64), kept for the true residual
     ERTGB_CUDA(cudaMemsetAsync(c.d_x.p, 0, sizeof(double) * n * Rpad, s));
-    ERTGB_CUDA(cudaMemsetAsync(nactive, 0, sizeof(int32_t), s));
+    ERTGB_CUDA(cudaMemsetAsync(cs.stalled, 0, sizeof(int32_t) * (Rpad + 2), s));  // stalled flags + counters
     k_to_f32<<<(unsigned)std::min<int64_t>(ceil_div((int64_t)c.nK * m.nnz, 256), 65535), 256, 0, s>>>(
         (int64_t)c.nK * m.nnz, c.d_S.p, c.d_S32.p);
     k_to_f32<<<(unsigned)std::min<int64_t>(ceil_div((int64_t)c.nK * n, 256), 65535), 256, 0, s>>>(
@@ -373,7 +453,7 @@ int pcg_solve_mixed(Context &c, cudaStream_t s) {
         k_m_accum<<<vg, vb, 0, s>>>(n, Rpad, active, c.d_x.p, c.d_y32.p, nactive);
         dispatch_ch<ResidL>(ch, sg, s, n, m.nnz, c.nE, c.nK, R, Rpad, m.d_rowptr.p, m.d_colidx.p, c.d_S.p, c.d_x.p,
                             b, c.d_dinv32.p, active, c.d_r32.p, part_a, part_b);
-        k_m_finish_ru<<<fg, fb, 0, s>>>(Rpad, NB, rtol2, part_a, part_b, c.d_col.p, active, nactive);
+        k_m_finish_ru<<<fg, fb, 0, s>>>(Rpad, NB, rtol2, part_a, part_b, c.d_col.p, cs);
         ERTGB_CUDA(cudaStreamEndCapture(s, &g_ru));
         ERTGB_CUDA(cudaGraphInstantiate(&e_ru, g_ru, 0));
 
@@ -398,6 +478,15 @@ int pcg_solve_mixed(Context &c, cudaStream_t s) {
         throw;
     }
     cleanup();
+    int32_t h_stalled = 0;
+    ERTGB_CUDA(cudaMemcpyAsync(&h_stalled, cs.nstalled, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    ERTGB_CUDA(cudaStreamSynchronize(s));
+    c.stats.stalled_columns = h_stalled;
+    if (status == ERTGB_OK && h_stalled > 0) {
+        // FP64 PCG on the stalled columns, warm-started from their FP64 solution
+        c.stats.iterations = 0;
+        return pcg_solve(c, s, cs.stalled);
+    }
     std::vector<int32_t> it_h(Rpad);
     std::vector<double> rn(Rpad), bn(Rpad);
     ERTGB_CUDA(cudaMemcpyAsync(it_h.data(), iters, sizeof(int32_t) * Rpad, cudaMemcpyDeviceToHost, s));

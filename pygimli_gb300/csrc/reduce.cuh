@@ -6,6 +6,20 @@
 
 namespace ertgb {
 
+// Per-column scalar slots of Context::d_col (NCOL x Rpad doubles), shared by
+// the FP64 and the mixed-precision solvers.
+enum ColSlot { RHO = 0, ALPHA, BETA, BNORM2, RNORM2, PQ, RPREV, STALLS, NCOL };
+
+// Integer per-column state of Context::d_active: active flags, iteration
+// counts, stalled flags (Rpad each), then the active and stalled counters.
+struct ColState {
+    int32_t *active, *iters, *stalled, *nactive, *nstalled;
+    ColState(int32_t *base, int64_t Rpad)
+        : active(base), iters(base + Rpad), stalled(base + 2 * Rpad), nactive(base + 3 * Rpad),
+          nstalled(base + 3 * Rpad + 1) {}
+    static size_t size(int64_t Rpad) { return (size_t)Rpad * 3 + 2; }
+};
+
 // Column reductions: block (32, 32), grid Rpad/32; thread (tx, ty) sums the
 // partial rows ty, ty+32, ... of column t, then the 32 sums are added in a
 // fixed order (deterministic).  Every thread of the block must call it.

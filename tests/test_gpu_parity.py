@@ -78,7 +78,7 @@ def test_golden_parity(torch, golden_dir, name, precision):
     J = fop.createJacobian(z["rho"], dtype=jdt).cpu().numpy().astype(np.float64)
     e_J = float(np.linalg.norm(J - z["J"]) / np.linalg.norm(z["J"]))
     print(f"{name} {precision}: rhoa {e_rhoa:.2e} potentials {e_pot:.2e} J({jdt}) {e_J:.2e} "
-          f"iters {fop.stats()['iterations']}")
+          f"iters {fop.stats()['iterations']} stalled {fop.stats()['stalled_columns']}")
     assert e_rhoa <= TOL_POT and e_pot <= TOL_POT and e_J <= TOL_J
 
 
@@ -109,7 +109,8 @@ def test_2d_config_vs_oracle(torch, precision):
     J_o = P.jacobian(u, rho)
     e_r = float(np.max(np.abs(rhoa - rhoa_o) / rhoa_o))
     e_J = float(np.linalg.norm(J - J_o) / np.linalg.norm(J_o))
-    print(f"2d config {precision}: rhoa {e_r:.2e} J {e_J:.2e} iters {fop.stats()['iterations']}")
+    print(f"2d config {precision}: rhoa {e_r:.2e} J {e_J:.2e} iters {fop.stats()['iterations']} "
+          f"stalled {fop.stats()['stalled_columns']}")
     assert e_r <= TOL_POT and e_J <= TOL_J
 
 
