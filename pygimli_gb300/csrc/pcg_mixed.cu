@@ -520,8 +520,9 @@ void profile_spmm32(Context &c, int reps, double *ms, double *bytes, double *flo
     const int NB = (int)std::min<int64_t>(ceil_div(n, kRows), kPartRows);
     const int ch = choose_ch(Rpad);
     const dim3 sg((unsigned)NB, (unsigned)(Rpad / (32 * ch)));
-    if (c.d_q32.n < (size_t)n * Rpad || c.d_S32.n < (size_t)c.nK * m.nnz || c.d_part.n < (size_t)NB * Rpad * 3)
+    if (c.d_q32.n < (size_t)n * Rpad || c.d_S32.n < (size_t)c.nK * m.nnz)
         throw Error(ERTGB_STATE, "profile needs a completed mixed-precision response");
+    if (c.d_part.n < (size_t)NB * Rpad * 3) c.d_part.alloc((size_t)NB * Rpad * 3);
     cudaStream_t s = c.stream;
     double *part_c = c.d_part.p + 2 * (size_t)NB * Rpad;
     auto go = [&] {
