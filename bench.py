@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--workload", choices=["box_3d", "box_3d_probe", "line_2d"], default="box_3d")
     ap.add_argument("--rtol", type=float, default=1e-10)
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--precond", choices=["jacobi", "fsai"], default="jacobi")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
@@ -193,7 +194,7 @@ def run_ours(args, world, rank, local):
     dev = torch.device("cuda", local)
     mesh, data, rho, cfg = workload(args.workload)
     t_setup = time.perf_counter()
-    fop = ERTModelling(device=local, rtol=args.rtol, precision=args.precision)
+    fop = ERTModelling(device=local, rtol=args.rtol, precision=args.precision, precond=args.precond)
     fop.setData(data)
     fop.setMesh(mesh)
     setup_s = time.perf_counter() - t_setup
@@ -302,7 +303,7 @@ def run_ours(args, world, rank, local):
                "dtype": "f64" if args.precision == "fp64" else "f32+f64 (FP32 PCG, FP64 reliable updates)",
                "data": "synthetic (seeded)",
                "config": dict(cfg, parallelism=f"replicas x{world}",
-                              solver=f"block PCG (Jacobi), {args.precision}",
+                              solver=f"block PCG ({args.precond}), {args.precision}",
                               jacobian="FP64" if jdt == 0 else "FP32 (FP64 differences)",
                               rtol=args.rtol, l2="working set > L2: PCG blocks 4 x "
                               f"{mesh.nodeCount() * 96 * 8 / 1e6:.0f} MB, J {D * P * 8 / 1e9:.1f} GB"),

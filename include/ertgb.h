@@ -34,8 +34,10 @@ typedef enum {
     ERTGB_STATE = 5          /* call order (e.g. jacobian before response)   */
 } ertgb_status;
 
-/* Preconditioners of the block PCG. */
-typedef enum { ERTGB_PRECOND_JACOBI = 0 } ertgb_precond;
+/* Preconditioners of the block PCG.  JACOBI: diagonal.  FSAI: factorized
+ * sparse approximate inverse M^-1 = G^T G, G lower triangular on A's pattern
+ * (mixed precision only; columns that stall finish with FP64 Jacobi). */
+typedef enum { ERTGB_PRECOND_JACOBI = 0, ERTGB_PRECOND_FSAI = 1 } ertgb_precond;
 
 /* Arithmetic of the block PCG.  FP64: everything in FP64.  MIXED: FP32
  * recurrence (operator, preconditioner, vectors) with FP64 reliable updates

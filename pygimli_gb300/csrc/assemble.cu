@@ -409,6 +409,13 @@ void build_mesh_device(Context &c) {
     m.d_cptr.upload(cptr, s);
     m.d_centry.upload(centry, s);
     m.d_diag.upload(diag, s);
+    build_lower_pattern(m);
+    m.d_Lrowptr.upload(m.Lrowptr, s);
+    m.d_Lcolidx.upload(m.Lcolidx, s);
+    m.d_LtoA.upload(m.LtoA, s);
+    m.d_Urowptr.upload(m.Urowptr, s);
+    m.d_Ucolidx.upload(m.Ucolidx, s);
+    m.d_UtoL.upload(m.UtoL, s);
     m.d_K.alloc((size_t)m.C * m.nv * m.nv);
     m.d_M.alloc((size_t)m.C * m.nv * m.nv);
     k_element_matrices<<<grid1(m.C), kThreads, 0, s>>>(m.C, m.dim, m.d_xyz.p, m.d_cells.p, m.d_K.p, m.d_M.p);

@@ -136,6 +136,8 @@ int do_response(Context &c, const double *rho, double *rhoa, void *stream) {
     c.d_r.alloc((size_t)m.n * c.Rpad);
     build_rhs(c, s);
     ERTGB_CUDA(cudaEventRecord(c.ev[2], s));
+    if (c.precision != ERTGB_PRECISION_MIXED && c.precond != ERTGB_PRECOND_JACOBI)
+        throw Error(ERTGB_BAD_INPUT, "the FSAI preconditioner needs mixed precision");
     status = (c.precision == ERTGB_PRECISION_MIXED) ? pcg_solve_mixed(c, s) : pcg_solve(c, s);
     ERTGB_CUDA(cudaEventRecord(c.ev[3], s));
     finish_potentials(c, s);
@@ -382,7 +384,7 @@ int ertgb_set_solver(ertgb_ctx *ctx, double rtol, int max_iter, int precond) {
     return guard(c, [&] {
         ERTGB_REQUIRE(rtol > 0.0 && rtol < 1.0, "rtol must be in (0, 1)");
         ERTGB_REQUIRE(max_iter > 0, "max_iter must be positive");
-        ERTGB_REQUIRE(precond == ERTGB_PRECOND_JACOBI, "unknown preconditioner");
+        ERTGB_REQUIRE(precond == ERTGB_PRECOND_JACOBI || precond == ERTGB_PRECOND_FSAI, "unknown preconditioner");
         c->rtol = rtol;
         c->max_iter = max_iter;
         c->precond = precond;

@@ -75,6 +75,9 @@ struct MeshData {
     std::vector<int32_t> marker;  // C
     std::vector<int32_t> rowptr, colidx;
     std::vector<int32_t> bnd_nodes, bnd_cell;  // mixed boundaries only
+    // FSAI factor pattern: lower triangle of A and its transpose
+    std::vector<int32_t> Lrowptr, Lcolidx, LtoA, Urowptr, Ucolidx, UtoL;
+    DBuf<int32_t> d_Lrowptr, d_Lcolidx, d_LtoA, d_Urowptr, d_Ucolidx, d_UtoL;
     // device
     DBuf<double> d_xyz;
     DBuf<int32_t> d_cells, d_rowptr, d_colidx, d_diag;
@@ -148,6 +151,10 @@ struct Context {
     DBuf<double> d_x, d_r, d_p, d_q;  // n x Rpad (d_r holds the right-hand sides)
     // mixed precision: FP32 matrix, Jacobi diagonal and recurrence vectors
     DBuf<float> d_S32, d_dinv32, d_r32, d_p32, d_q32, d_y32;
+    // FSAI preconditioner M^-1 = G^T G: G (lower) and G^T values per wavenumber
+    DBuf<double> d_G;
+    DBuf<float> d_G32, d_GT32, d_t32, d_z32;
+    int32_t fsai_fallback_rows = 0;
     DBuf<double> d_part;          // reduction partials
     DBuf<double> d_col;           // per-column scalars (see pcg.cu)
     DBuf<int32_t> d_active;
@@ -199,6 +206,9 @@ void build_pattern(MeshData &m);
 void build_assembly_map(MeshData &m, std::vector<int32_t> &cptr, std::vector<int32_t> &centry,
                         std::vector<int32_t> &diag);
 void build_jacobian_tiles(Context &c);
+void build_lower_pattern(MeshData &m);
+// fsai.cu
+void fsai_setup(Context &c, cudaStream_t s);
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 

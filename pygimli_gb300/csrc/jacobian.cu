@@ -33,7 +33,7 @@ namespace ertgb {
 namespace {
 
 constexpr int kThreads = 512;
-constexpr size_t kSmemBudget = 200 * 1024;
+constexpr size_t kSmemBudget = 110 * 1024;  // two blocks per SM
 
 template <int NV, typename CT, int TW>
 __global__ void __launch_bounds__(kThreads)
@@ -146,10 +146,21 @@ __global__ void __launch_bounds__(kThreads)
     if (nchunks <= 1) {
         if (ncell > 0) build(0, ncell);
         if (has_p) {
-            for (int64_t d = d0; d < D; d += dstep) {
-                CT acc = pair_sum(d, pc0, pc1);
-                if (scale_p) acc = (acc * scale_d[d]) * sp;
-                J[d * P + p] = acc;
+            int64_t d = d0;
+            for (; d + dstep < D; d += 2 * dstep) {  // two independent rows in flight
+                CT a0 = pair_sum(d, pc0, pc1);
+                CT a1 = pair_sum(d + dstep, pc0, pc1);
+                if (scale_p) {
+                    a0 = (a0 * scale_d[d]) * sp;
+                    a1 = (a1 * scale_d[d + dstep]) * sp;
+                }
+                J[d * P + p] = a0;
+                J[(d + dstep) * P + p] = a1;
+            }
+            if (d < D) {
+                CT a0 = pair_sum(d, pc0, pc1);
+                if (scale_p) a0 = (a0 * scale_d[d]) * sp;
+                J[d * P + p] = a0;
             }
         }
     } else {

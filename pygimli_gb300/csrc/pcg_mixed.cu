@@ -117,9 +117,11 @@ __global__ void __launch_bounds__(256) k_spmm32_dot(int64_t n, int64_t nnz, int 
     }
 }
 
-// Single-matrix variant (nK = 1): the warp loads up to 32 (column, value)
-// pairs of its row at once, one per lane, and broadcasts them with
-// shuffles, leaving the coalesced gathers of p as the only dependent loads.
+// Single-matrix variant (nK = 1): every block owns a contiguous range of
+// rows (neighbour rows share their gathers of p through L1), each warp keeps
+// two rows in flight, and the (column, value) pairs of a row are loaded one
+// per lane and broadcast with shuffles, leaving the coalesced gathers of p
+// as the only dependent loads.
 template <int CH>
 __global__ void __launch_bounds__(256) k_spmm32_dot_k1(int64_t n, int64_t Rpad, const int32_t *__restrict__ rowptr,
                                                        const int32_t *__restrict__ colidx,
@@ -128,33 +130,54 @@ __global__ void __launch_bounds__(256) k_spmm32_dot_k1(int64_t n, int64_t Rpad, 
     __shared__ double red[kRows][32 * CH];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int64_t t0 = (int64_t)blockIdx.y * 32 * CH + lane;
+    const int64_t per_block = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t r_begin = (int64_t)blockIdx.x * per_block;
+    const int64_t r_end = min(n, r_begin + per_block);
     float dot[CH];
 #pragma unroll
     for (int j = 0; j < CH; j++) dot[j] = 0.f;
-    for (int64_t row = (int64_t)blockIdx.x * kRows + wid; row < n; row += (int64_t)gridDim.x * kRows) {
-        float acc[CH];
+    for (int64_t r0 = r_begin + 2 * wid; r0 < r_end; r0 += 2 * kRows) {
+        const bool two = r0 + 1 < r_end;
+        float a0[CH], a1[CH];
 #pragma unroll
-        for (int j = 0; j < CH; j++) acc[j] = 0.f;
-        const int32_t s0 = rowptr[row], len = rowptr[row + 1] - s0;
-        for (int base = 0; base < len; base += 32) {
-            const int cnt = min(32, len - base);
-            const int32_t mc = lane < cnt ? colidx[s0 + base + lane] : 0;
-            const float mv = lane < cnt ? vals[s0 + base + lane] : 0.f;
-#pragma unroll 4
-            for (int e = 0; e < cnt; e++) {
-                const int64_t col = __shfl_sync(0xffffffffu, mc, e);
-                const float v = __shfl_sync(0xffffffffu, mv, e);
-                const float *pc = p + col * Rpad + t0;
+        for (int j = 0; j < CH; j++) a0[j] = a1[j] = 0.f;
+        const int32_t s0 = rowptr[r0], s1 = rowptr[r0 + 1];
+        const int32_t s2 = two ? rowptr[r0 + 2] : s1;
+        const int len0 = s1 - s0, len1 = s2 - s1;
+        const int lmax = max(len0, len1);
+        for (int base = 0; base < lmax; base += 32) {
+            const int c0 = min(32, max(0, len0 - base)), c1 = min(32, max(0, len1 - base));
+            const int32_t mc0 = lane < c0 ? colidx[s0 + base + lane] : 0;
+            const float mv0 = lane < c0 ? vals[s0 + base + lane] : 0.f;
+            const int32_t mc1 = lane < c1 ? colidx[s1 + base + lane] : 0;
+            const float mv1 = lane < c1 ? vals[s1 + base + lane] : 0.f;
+            const int cm = max(c0, c1);
+#pragma unroll 2
+            for (int e = 0; e < cm; e++) {
+                const int64_t col0 = __shfl_sync(0xffffffffu, mc0, e);
+                const float v0 = __shfl_sync(0xffffffffu, mv0, e);
+                const int64_t col1 = __shfl_sync(0xffffffffu, mc1, e);
+                const float v1 = __shfl_sync(0xffffffffu, mv1, e);
+                const float *pc0 = p + col0 * Rpad + t0;
+                const float *pc1 = p + col1 * Rpad + t0;
+                if (e < c0) {
 #pragma unroll
-                for (int j = 0; j < CH; j++) acc[j] = fmaf(v, pc[32 * j], acc[j]);
+                    for (int j = 0; j < CH; j++) a0[j] = fmaf(v0, pc0[32 * j], a0[j]);
+                }
+                if (e < c1) {
+#pragma unroll
+                    for (int j = 0; j < CH; j++) a1[j] = fmaf(v1, pc1[32 * j], a1[j]);
+                }
             }
         }
-        float *qr = q + row * Rpad + t0;
-        const float *pr = p + row * Rpad + t0;
 #pragma unroll
         for (int j = 0; j < CH; j++) {
-            qr[32 * j] = acc[j];
-            dot[j] = fmaf(pr[32 * j], acc[j], dot[j]);
+            q[r0 * Rpad + t0 + 32 * j] = a0[j];
+            dot[j] = fmaf(p[r0 * Rpad + t0 + 32 * j], a0[j], dot[j]);
+            if (two) {
+                q[(r0 + 1) * Rpad + t0 + 32 * j] = a1[j];
+                dot[j] = fmaf(p[(r0 + 1) * Rpad + t0 + 32 * j], a1[j], dot[j]);
+            }
         }
     }
 #pragma unroll
@@ -165,6 +188,83 @@ __global__ void __launch_bounds__(256) k_spmm32_dot_k1(int64_t n, int64_t Rpad, 
 #pragma unroll
         for (int w = 0; w < kRows; w++) s += red[w][c];
         part[(int64_t)blockIdx.x * Rpad + (int64_t)blockIdx.y * 32 * CH + c] = s;
+    }
+}
+
+// Generic FP32 CSR product y = B x for the FSAI factors (nK value arrays of
+// stride nnzB; warp per row, lanes over columns); with DOT the column
+// partials of w . y are written to part.
+template <int CH, bool DOT>
+__global__ void __launch_bounds__(256) k_spmm32_gen(int64_t n, int64_t nnzB, int nE, int nK, int64_t Rpad,
+                                                    const int32_t *__restrict__ rowptr,
+                                                    const int32_t *__restrict__ colidx,
+                                                    const float *__restrict__ vals, const float *__restrict__ x,
+                                                    float *__restrict__ y, const float *__restrict__ w,
+                                                    double *__restrict__ part) {
+    __shared__ double red[kRows][32 * CH];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t t0 = (int64_t)blockIdx.y * 32 * CH + lane;
+    int64_t kofs[CH];
+#pragma unroll
+    for (int j = 0; j < CH; j++) kofs[j] = min((t0 + 32 * j) / nE, (int64_t)nK - 1) * nnzB;
+    float dot[CH];
+#pragma unroll
+    for (int j = 0; j < CH; j++) dot[j] = 0.f;
+    const int64_t per_block = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t r_begin = (int64_t)blockIdx.x * per_block, r_end = min(n, r_begin + per_block);
+    for (int64_t row = r_begin + wid; row < r_end; row += kRows) {
+        float acc[CH];
+#pragma unroll
+        for (int j = 0; j < CH; j++) acc[j] = 0.f;
+        const int32_t s1 = rowptr[row + 1];
+#pragma unroll 2
+        for (int32_t s = rowptr[row]; s < s1; s++) {
+            const int64_t col = colidx[s];
+            const float *xc = x + col * Rpad + t0;
+#pragma unroll
+            for (int j = 0; j < CH; j++) acc[j] = fmaf(vals[kofs[j] + s], xc[32 * j], acc[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < CH; j++) {
+            y[row * Rpad + t0 + 32 * j] = acc[j];
+            if (DOT) dot[j] = fmaf(w[row * Rpad + t0 + 32 * j], acc[j], dot[j]);
+        }
+    }
+    if (!DOT) return;
+#pragma unroll
+    for (int j = 0; j < CH; j++) red[wid][lane + 32 * j] = (double)dot[j];
+    __syncthreads();
+    for (int c = threadIdx.x; c < 32 * CH; c += blockDim.x) {
+        double s = 0.0;
+#pragma unroll
+        for (int w2 = 0; w2 < kRows; w2++) s += red[w2][c];
+        part[(int64_t)blockIdx.x * Rpad + (int64_t)blockIdx.y * 32 * CH + c] = s;
+    }
+}
+
+// FSAI iteration: y += alpha p, r -= alpha q (the dots follow from z = G^T G r)
+__global__ void k_m_update_yr(int64_t n, int64_t Rpad, const double *__restrict__ col,
+                              const int32_t *__restrict__ active, float *__restrict__ y, float *__restrict__ r,
+                              const float *__restrict__ p, const float *__restrict__ q) {
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    if (!active[t]) return;
+    const float alpha = (float)col[ALPHA * Rpad + t];
+    for (int64_t row = (int64_t)blockIdx.y * kRows + threadIdx.y; row < n; row += (int64_t)gridDim.y * kRows) {
+        const int64_t i = row * Rpad + t;
+        y[i] = fmaf(alpha, p[i], y[i]);
+        r[i] = fmaf(-alpha, q[i], r[i]);
+    }
+}
+
+// FSAI iteration: p = z + beta p
+__global__ void k_m_update_pz(int64_t n, int64_t Rpad, const double *__restrict__ col,
+                              const int32_t *__restrict__ active, const float *__restrict__ z, float *__restrict__ p) {
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    if (!active[t]) return;
+    const float beta = (float)col[BETA * Rpad + t];
+    for (int64_t row = (int64_t)blockIdx.y * kRows + threadIdx.y; row < n; row += (int64_t)gridDim.y * kRows) {
+        const int64_t i = row * Rpad + t;
+        p[i] = fmaf(beta, p[i], z[i]);
     }
 }
 
@@ -375,6 +475,14 @@ template <int CH> struct SpmmL {
     }
 };
 
+template <int CH> struct GenL {
+    static void go(dim3 g, cudaStream_t s, int64_t n, int64_t nnzB, int nE, int nK, int64_t Rpad, const int32_t *rp,
+                   const int32_t *ci, const float *v, const float *x, float *y, const float *w, double *part) {
+        if (w) k_spmm32_gen<CH, true><<<g, 256, 0, s>>>(n, nnzB, nE, nK, Rpad, rp, ci, v, x, y, w, part);
+        else k_spmm32_gen<CH, false><<<g, 256, 0, s>>>(n, nnzB, nE, nK, Rpad, rp, ci, v, x, y, w, part);
+    }
+};
+
 template <int CH> struct ResidL {
     static void go(dim3 g, cudaStream_t s, int64_t n, int64_t nnz, int nE, int nK, int64_t R, int64_t Rpad,
                    const int32_t *rp, const int32_t *ci, const double *v, const double *x, const double *b,
@@ -411,6 +519,20 @@ int pcg_solve_mixed(Context &c, cudaStream_t s) {
     ColState cs(c.d_active.p, Rpad);
     int32_t *active = cs.active, *iters = cs.iters, *nactive = cs.nactive;
     const double *b = c.d_r.p;  // the right-hand sides (FP64), kept for the true residual
+    const bool fsai = c.precond == ERTGB_PRECOND_FSAI;
+    const int64_t nL = (int64_t)m.Lcolidx.size();
+    if (fsai) {
+        fsai_setup(c, s);
+        c.d_t32.alloc((size_t)n * Rpad);
+        c.d_z32.alloc((size_t)n * Rpad);
+    }
+    // z = G^T (G r) with the column partials of r . z into pz
+    auto apply_fsai = [&](double *pz) {
+        dispatch_ch<GenL>(ch, dim3((unsigned)NB, (unsigned)nchunk), s, n, nL, c.nE, c.nK, Rpad, m.d_Lrowptr.p,
+                          m.d_Lcolidx.p, c.d_G32.p, c.d_r32.p, c.d_t32.p, (const float *)nullptr, (double *)nullptr);
+        dispatch_ch<GenL>(ch, dim3((unsigned)NB, (unsigned)nchunk), s, n, nL, c.nE, c.nK, Rpad, m.d_Urowptr.p,
+                          m.d_Ucolidx.p, c.d_GT32.p, c.d_t32.p, c.d_z32.p, (const float *)c.d_r32.p, pz);
+    };
     ERTGB_CUDA(cudaMemsetAsync(c.d_x.p, 0, sizeof(double) * n * Rpad, s));
     ERTGB_CUDA(cudaMemsetAsync(cs.stalled, 0, sizeof(int32_t) * (Rpad + 2), s));  // stalled flags + counters
     k_to_f32<<<(unsigned)std::min<int64_t>(ceil_div((int64_t)c.nK * m.nnz, 256), 65535), 256, 0, s>>>(
@@ -422,6 +544,11 @@ int pcg_solve_mixed(Context &c, cudaStream_t s) {
     const dim3 fb(32, 32), fg((unsigned)(Rpad / 32));
     const double rtol2 = c.rtol * c.rtol;
     k_m_init<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, c.d_dinv32.p, b, c.d_r32.p, c.d_p32.p, c.d_y32.p, part_a, part_b);
+    if (fsai) {
+        apply_fsai(part_a);
+        ERTGB_CUDA(cudaMemcpyAsync(c.d_p32.p, c.d_z32.p, sizeof(float) * n * Rpad, cudaMemcpyDeviceToDevice, s));
+        c.stats.launches_response += 2;
+    }
     pcg_finish_init(fg, fb, s, Rpad, R, NB, part_a, part_b, c.d_col.p, active, iters, nactive);
     ERTGB_CUDA(cudaGetLastError());
     c.stats.launches_response += 5;
@@ -442,10 +569,18 @@ int pcg_solve_mixed(Context &c, cudaStream_t s) {
             dispatch_ch<SpmmL>(ch, sg, s, n, m.nnz, c.nE, c.nK, Rpad, m.d_rowptr.p, m.d_colidx.p, c.d_S32.p, c.d_p32.p,
                                c.d_q32.p, part_c);
             pcg_finish_alpha(fg, fb, s, Rpad, NB, part_c, c.d_col.p, active, nactive);
-            k_m_update_xr<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, c.d_dinv32.p, c.d_col.p, active, c.d_y32.p, c.d_r32.p,
-                                            c.d_p32.p, c.d_q32.p, part_a, part_b);
-            k_m_finish_beta<<<fg, fb, 0, s>>>(Rpad, NB, part_a, part_b, c.d_col.p, active, iters);
-            k_m_update_p<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, c.d_dinv32.p, c.d_col.p, active, c.d_r32.p, c.d_p32.p);
+            if (fsai) {
+                k_m_update_yr<<<vg, vb, 0, s>>>(n, Rpad, c.d_col.p, active, c.d_y32.p, c.d_r32.p, c.d_p32.p, c.d_q32.p);
+                apply_fsai(part_a);
+                k_m_finish_beta<<<fg, fb, 0, s>>>(Rpad, NB, part_a, part_a, c.d_col.p, active, iters);
+                k_m_update_pz<<<vg, vb, 0, s>>>(n, Rpad, c.d_col.p, active, c.d_z32.p, c.d_p32.p);
+            } else {
+                k_m_update_xr<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, c.d_dinv32.p, c.d_col.p, active, c.d_y32.p,
+                                                c.d_r32.p, c.d_p32.p, c.d_q32.p, part_a, part_b);
+                k_m_finish_beta<<<fg, fb, 0, s>>>(Rpad, NB, part_a, part_b, c.d_col.p, active, iters);
+                k_m_update_p<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, c.d_dinv32.p, c.d_col.p, active, c.d_r32.p,
+                                               c.d_p32.p);
+            }
         }
         ERTGB_CUDA(cudaStreamEndCapture(s, &g_it));
         ERTGB_CUDA(cudaGraphInstantiate(&e_it, g_it, 0));
@@ -453,6 +588,7 @@ int pcg_solve_mixed(Context &c, cudaStream_t s) {
         k_m_accum<<<vg, vb, 0, s>>>(n, Rpad, active, c.d_x.p, c.d_y32.p, nactive);
         dispatch_ch<ResidL>(ch, sg, s, n, m.nnz, c.nE, c.nK, R, Rpad, m.d_rowptr.p, m.d_colidx.p, c.d_S.p, c.d_x.p,
                             b, c.d_dinv32.p, active, c.d_r32.p, part_a, part_b);
+        if (fsai) apply_fsai(part_a);
         k_m_finish_ru<<<fg, fb, 0, s>>>(Rpad, NB, rtol2, part_a, part_b, c.d_col.p, cs);
         ERTGB_CUDA(cudaStreamEndCapture(s, &g_ru));
         ERTGB_CUDA(cudaGraphInstantiate(&e_ru, g_ru, 0));
@@ -468,7 +604,7 @@ int pcg_solve_mixed(Context &c, cudaStream_t s) {
             for (int u = 0; u < kReliableEvery; u++) ERTGB_CUDA(cudaGraphLaunch(e_it, s));
             iterations += kReliableEvery * kGraphIters;
             ERTGB_CUDA(cudaGraphLaunch(e_ru, s));
-            c.stats.launches_response += 5 * kGraphIters * kReliableEvery + 3;
+            c.stats.launches_response += (fsai ? 6 : 5) * kGraphIters * kReliableEvery + (fsai ? 5 : 3);
             ERTGB_CUDA(cudaMemcpyAsync(&h_active, nactive, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
             ERTGB_CUDA(cudaStreamSynchronize(s));
         }

@@ -101,4 +101,39 @@ void build_assembly_map(MeshData &m, std::vector<int32_t> &cptr, std::vector<int
     for (int64_t r = 0; r < m.n; r++) diag[r] = find_slot(m, (int32_t)r, (int32_t)r);
 }
 
+// Lower-triangular pattern of A (the FSAI factor G) and its transpose:
+//   L: rows of A restricted to columns <= row (diagonal last), with the A slot
+//      of every entry;
+//   U: the transpose of L (row j lists the rows i >= j that have column j),
+//      with the L slot of every entry, so G^T values are a gather of G.
+void build_lower_pattern(MeshData &m) {
+    const int64_t n = m.n;
+    m.Lrowptr.assign(n + 1, 0);
+    m.Lcolidx.clear();
+    m.LtoA.clear();
+    for (int64_t r = 0; r < n; r++) {
+        for (int32_t s = m.rowptr[r]; s < m.rowptr[r + 1]; s++) {
+            if (m.colidx[s] <= r) {
+                m.Lcolidx.push_back(m.colidx[s]);
+                m.LtoA.push_back(s);
+            }
+        }
+        m.Lrowptr[r + 1] = (int32_t)m.Lcolidx.size();
+    }
+    const int64_t nL = (int64_t)m.Lcolidx.size();
+    m.Urowptr.assign(n + 1, 0);
+    for (int64_t q = 0; q < nL; q++) m.Urowptr[m.Lcolidx[q] + 1]++;
+    for (int64_t i = 0; i < n; i++) m.Urowptr[i + 1] += m.Urowptr[i];
+    m.Ucolidx.assign(nL, 0);
+    m.UtoL.assign(nL, 0);
+    std::vector<int32_t> pos(m.Urowptr.begin(), m.Urowptr.end() - 1);
+    for (int64_t r = 0; r < n; r++)
+        for (int32_t q = m.Lrowptr[r]; q < m.Lrowptr[r + 1]; q++) {
+            const int32_t cidx = m.Lcolidx[q];
+            m.Ucolidx[pos[cidx]] = (int32_t)r;
+            m.UtoL[pos[cidx]] = q;
+            pos[cidx]++;
+        }
+}
+
 }  // namespace ertgb

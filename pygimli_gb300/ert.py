@@ -77,7 +77,8 @@ def surface_info(mesh):
 class ERTModelling:
     """ERT forward operator (singularity removal) on one GB300."""
 
-    def __init__(self, sr=True, verbose=False, device=0, rtol=1e-10, maxIter=20000, precision="fp64"):
+    def __init__(self, sr=True, verbose=False, device=0, rtol=1e-10, maxIter=20000, precision="fp64",
+                 precond="jacobi"):
         if not sr:
             raise NotImplementedError("only the singularity-removal operator (sr=True) is provided")
         self.verbose = verbose
@@ -93,6 +94,7 @@ class ERTModelling:
         self._J = None
         self._elec_nodes = None
         self._last_model = None
+        self._precond = {"jacobi": 0, "fsai": 1}[precond]
         self.setSolverTolerance(rtol, maxIter)
         self.setPrecision(precision)
 
@@ -127,7 +129,14 @@ class ERTModelling:
         raise NotImplementedError("the linear solver is the built-in GPU block PCG")
 
     def setSolverTolerance(self, rtol=1e-10, maxIter=20000):
-        self._check(self._lib.ertgb_set_solver(self._ctx, float(rtol), int(maxIter), 0))
+        self._rtol, self._maxIter = float(rtol), int(maxIter)
+        self._check(self._lib.ertgb_set_solver(self._ctx, self._rtol, self._maxIter, self._precond))
+
+    def setPreconditioner(self, precond):
+        """``"jacobi"`` or ``"fsai"`` (factorized sparse approximate inverse,
+        mixed precision only)."""
+        self._precond = {"jacobi": 0, "fsai": 1}[precond]
+        self._check(self._lib.ertgb_set_solver(self._ctx, self._rtol, self._maxIter, self._precond))
 
     def setComplex(self, c):
         if c:

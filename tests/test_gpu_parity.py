@@ -33,8 +33,14 @@ def torch():
     return t
 
 
-def fop_for(mesh, data, k=None, w=None, **kw):
+FORMS = {"fp64": dict(precision="fp64"), "mixed": dict(precision="mixed"),
+         "mixed-fsai": dict(precision="mixed", precond="fsai")}
+
+
+def fop_for(mesh, data, k=None, w=None, form=None, **kw):
     from pygimli_gb300 import ERTModelling
+    if form is not None:
+        kw.update(FORMS[form])
     fop = ERTModelling(**kw)
     if k is not None:
         fop.setkValues(k)
@@ -57,11 +63,11 @@ def rel(a, b):
     return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", list(FORMS))
 @pytest.mark.parametrize("name", ["ert2d_small", "ert2d_pd_wa", "ert3d_small"])
 def test_golden_parity(torch, golden_dir, name, precision):
     z, mesh, data = load_case(golden_dir, name)
-    fop = fop_for(mesh, data, precision=precision)
+    fop = fop_for(mesh, data, form=precision)
     assert np.array_equal(fop.kValues(), z["k"]) and np.array_equal(fop.weights(), z["w"])
     rp, ci = fop.pattern()
     assert np.array_equal(rp, z["rowptr"]) and np.array_equal(ci, z["colidx"])
@@ -95,11 +101,11 @@ def _c1_case(seed=1):
     return mesh, data, rho
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", list(FORMS))
 def test_2d_config_vs_oracle(torch, precision):
     """41 electrodes, 741 dipole-dipole data, ~3.6k nodes, 17 wavenumbers."""
     mesh, data, rho = _c1_case()
-    fop = fop_for(mesh, data, precision=precision)
+    fop = fop_for(mesh, data, form=precision)
     assert len(fop.kValues()) == 17
     rhoa = fop.response(rho)
     jdt = "float64" if precision == "fp64" else "float32"
@@ -125,10 +131,10 @@ def _small_3d(nx=5, ny=4):
     return mesh, data, rho
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", list(FORMS))
 def test_3d_vs_oracle(torch, precision):
     mesh, data, rho = _small_3d()
-    fop = fop_for(mesh, data, precision=precision)
+    fop = fop_for(mesh, data, form=precision)
     rhoa = fop.response(rho)
     jdt = "float64" if precision == "fp64" else "float32"
     J = fop.createJacobian(rho, dtype=jdt).cpu().numpy().astype(np.float64)
@@ -250,13 +256,19 @@ def test_3d_config_properties(torch):
     J32r = J32[torch.as_tensor(rows, device=J32.device)].cpu().numpy().astype(np.float64)
     assert float(np.linalg.norm(J32r - Jo) / np.linalg.norm(Jo)) <= TOL_J
     del J, J32
-    # mixed-precision solve reaches the same answer
+    # mixed-precision solves (Jacobi and FSAI) reach the same answer
     fop.setPrecision("mixed")
     r3 = fop.response(2.0 * rho)
     st3 = fop.stats()
     assert float(np.max(np.abs(r3 - r2) / r2)) <= TOL_POT
+    fop.setPreconditioner("fsai")
+    r4 = fop.response(2.0 * rho)
+    st4 = fop.stats()
+    assert float(np.max(np.abs(r4 - r2) / r2)) <= TOL_POT
+    fop.setPreconditioner("jacobi")
     fop.setPrecision("fp64")
-    print(f"3d config: mixed iters {st3['iterations']} solve {st3['ms_solve']:.1f} ms")
+    print(f"3d config: mixed iters {st3['iterations']} solve {st3['ms_solve']:.1f} ms; mixed+fsai iters "
+          f"{st4['iterations']} solve {st4['ms_solve']:.1f} ms")
     # homogeneous half-space: apparent resistivity equals the resistivity
     rh = fop.response(np.full(mesh.cellCount(), 100.0))
     assert float(np.max(np.abs(rh - 100.0) / 100.0)) < 0.05
