@@ -33,7 +33,8 @@ namespace ertgb {
 namespace {
 
 constexpr int kThreads = 512;
-constexpr size_t kSmemBudget = 110 * 1024;  // two blocks per SM
+constexpr size_t kSmemBudget = 110 * 1024;       // two blocks per SM
+constexpr size_t kSmemBudgetLarge = 220 * 1024;  // one block per SM (many wavenumbers x dipoles)
 
 template <int NV, typename CT, int TW>
 __global__ void __launch_bounds__(kThreads)
@@ -205,12 +206,13 @@ __global__ void k_jac_scales(int64_t D, int64_t P, const double *__restrict__ kf
 bool plan(const Context &c, int dtype, int *TW, int *G) {
     const size_t uv = 2 * (size_t)c.nK * c.mesh.nv * (c.nE + 1) * sizeof(double);
     const size_t tab = (size_t)c.nK * (c.nA + c.nM) * c.mesh.nv * (dtype == 0 ? 8 : 4);
-    for (int tw : {16, 8, 4}) {
-        if (tw * tab + uv > kSmemBudget) continue;
-        *TW = tw;
-        *G = (int)std::max<size_t>(1, std::min<size_t>(4, (kSmemBudget - tw * tab) / uv));
-        return true;
-    }
+    for (size_t budget : {kSmemBudget, kSmemBudgetLarge})
+        for (int tw : {16, 8, 4}) {
+            if (tw * tab + uv > budget) continue;
+            *TW = tw;
+            *G = (int)std::max<size_t>(1, std::min<size_t>(4, (budget - tw * tab) / uv));
+            return true;
+        }
     return false;
 }
 
