@@ -46,8 +46,9 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["box_3d", "box_3d_probe", "line_2d"], default="box_3d")
     ap.add_argument("--rtol", type=float, default=1e-10)
-    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
-    ap.add_argument("--precond", choices=["jacobi", "fsai"], default="jacobi")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
+    ap.add_argument("--precond", choices=["jacobi", "fsai"], default="fsai")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 Jacobi comparison run")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
@@ -240,6 +241,41 @@ def run_ours(args, world, rank, local):
         total_ms = float(t.item())
     value = total_ms / 1e3 / (args.steps * world)
 
+    # the plain FP64 Jacobi PCG path (FP64 Jacobian) on the same workload, same timing
+    plain = None
+    if not args.no_plain and (args.precision, args.precond) != ("fp64", "jacobi"):
+        fop_p = ERTModelling(device=local, rtol=args.rtol, precision="fp64", precond="jacobi")
+        fop_p.setData(data)
+        fop_p.setMesh(mesh)
+        Jp = torch.empty((D, P), dtype=torch.float64, device=dev)
+
+        def step_p():
+            fop_p._response_dev(rho_d, rhoa_p)
+            stream = torch.cuda.current_stream(dev).cuda_stream
+            fop_p._check(L.ertgb_jacobian(fop_p._ctx, ctypes.c_void_p(rho_d.data_ptr()), C,
+                                          ctypes.c_void_p(Jp.data_ptr()), 0, ctypes.c_void_p(stream)))
+
+        rhoa_p = torch.empty(D, dtype=torch.float64, device=dev)
+        np_steps = max(1, min(args.steps, 3))
+        for _ in range(max(1, min(args.warmup, 2))):
+            step_p()
+        torch.cuda.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record()
+        for _ in range(np_steps):
+            step_p()
+        f1.record()
+        torch.cuda.synchronize()
+        stp = fop_p.stats()
+        t_plain = f0.elapsed_time(f1) / 1e3 / np_steps
+        rel = float(torch.max(torch.abs(rhoa_d - rhoa_p) / torch.abs(rhoa_p)).item())
+        plain = {"value": t_plain, "unit": UNIT, "steps": np_steps, "solver": "block PCG (Jacobi), FP64",
+                 "jacobian": "FP64", "pcg_iterations": stp["iterations"], "ms_solve": stp["ms_solve"],
+                 "ms_jacobian": stp["ms_jacobian"], "speedup_of_value": t_plain / (total_ms / 1e3 / args.steps),
+                 "max_rel_diff_rhoa_vs_value_form": rel}
+        del Jp, fop_p
+
     # roofline of the dominant kernel (CUDA events on the context stream)
     ms = ctypes.c_double()
     by = ctypes.c_double()
@@ -308,6 +344,7 @@ def run_ours(args, world, rank, local):
                               rtol=args.rtol, l2="working set > L2: PCG blocks 4 x "
                               f"{mesh.nodeCount() * 96 * 8 / 1e6:.0f} MB, J {D * P * 8 / 1e9:.1f} GB"),
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+               "plain_fp64_gpu_pcg": plain,
                "clocks": clk,
                "breakdown_ms": {"assemble": st["ms_assemble"], "rhs": st["ms_rhs"], "solve": st["ms_solve"],
                                 "collect": st["ms_collect"], "jacobian": st["ms_jacobian"],
