@@ -122,11 +122,13 @@ __global__ void __launch_bounds__(256) k_spmm32_dot(int64_t n, int64_t nnz, int 
 // two rows in flight, and the (column, value) pairs of a row are loaded one
 // per lane and broadcast with shuffles, leaving the coalesced gathers of p
 // as the only dependent loads.
-template <int CH>
-__global__ void __launch_bounds__(256) k_spmm32_dot_k1(int64_t n, int64_t Rpad, const int32_t *__restrict__ rowptr,
-                                                       const int32_t *__restrict__ colidx,
-                                                       const float *__restrict__ vals, const float *__restrict__ p,
-                                                       float *__restrict__ q, double *__restrict__ part) {
+// DOT: 0 = column dots p . q (the PCG operator), 1 = none, 2 = w . q.
+template <int CH, int DOT>
+__global__ void __launch_bounds__(256) k_spmm32_k1(int64_t n, int64_t Rpad, const int32_t *__restrict__ rowptr,
+                                                   const int32_t *__restrict__ colidx,
+                                                   const float *__restrict__ vals, const float *__restrict__ p,
+                                                   float *__restrict__ q, const float *__restrict__ w,
+                                                   double *__restrict__ part) {
     __shared__ double red[kRows][32 * CH];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int64_t t0 = (int64_t)blockIdx.y * 32 * CH + lane;
@@ -170,16 +172,18 @@ __global__ void __launch_bounds__(256) k_spmm32_dot_k1(int64_t n, int64_t Rpad, 
                 }
             }
         }
+        const float *dv = DOT == 2 ? w : p;
 #pragma unroll
         for (int j = 0; j < CH; j++) {
             q[r0 * Rpad + t0 + 32 * j] = a0[j];
-            dot[j] = fmaf(p[r0 * Rpad + t0 + 32 * j], a0[j], dot[j]);
+            if (DOT != 1) dot[j] = fmaf(dv[r0 * Rpad + t0 + 32 * j], a0[j], dot[j]);
             if (two) {
                 q[(r0 + 1) * Rpad + t0 + 32 * j] = a1[j];
-                dot[j] = fmaf(p[(r0 + 1) * Rpad + t0 + 32 * j], a1[j], dot[j]);
+                if (DOT != 1) dot[j] = fmaf(dv[(r0 + 1) * Rpad + t0 + 32 * j], a1[j], dot[j]);
             }
         }
     }
+    if (DOT == 1) return;
 #pragma unroll
     for (int j = 0; j < CH; j++) red[wid][lane + 32 * j] = (double)dot[j];
     __syncthreads();
@@ -470,7 +474,7 @@ template <template <int> class F, typename... A> void dispatch_ch(int ch, A &&..
 template <int CH> struct SpmmL {
     static void go(dim3 g, cudaStream_t s, int64_t n, int64_t nnz, int nE, int nK, int64_t Rpad, const int32_t *rp,
                    const int32_t *ci, const float *v, const float *p, float *q, double *part) {
-        if (nK == 1) k_spmm32_dot_k1<CH><<<g, 256, 0, s>>>(n, Rpad, rp, ci, v, p, q, part);
+        if (nK == 1) k_spmm32_k1<CH, 0><<<g, 256, 0, s>>>(n, Rpad, rp, ci, v, p, q, nullptr, part);
         else k_spmm32_dot<CH><<<g, 256, 0, s>>>(n, nnz, nE, nK, Rpad, rp, ci, v, p, q, part);
     }
 };
@@ -478,8 +482,14 @@ template <int CH> struct SpmmL {
 template <int CH> struct GenL {
     static void go(dim3 g, cudaStream_t s, int64_t n, int64_t nnzB, int nE, int nK, int64_t Rpad, const int32_t *rp,
                    const int32_t *ci, const float *v, const float *x, float *y, const float *w, double *part) {
-        if (w) k_spmm32_gen<CH, true><<<g, 256, 0, s>>>(n, nnzB, nE, nK, Rpad, rp, ci, v, x, y, w, part);
-        else k_spmm32_gen<CH, false><<<g, 256, 0, s>>>(n, nnzB, nE, nK, Rpad, rp, ci, v, x, y, w, part);
+        if (nK == 1) {
+            if (w) k_spmm32_k1<CH, 2><<<g, 256, 0, s>>>(n, Rpad, rp, ci, v, x, y, w, part);
+            else k_spmm32_k1<CH, 1><<<g, 256, 0, s>>>(n, Rpad, rp, ci, v, x, y, w, part);
+        } else if (w) {
+            k_spmm32_gen<CH, true><<<g, 256, 0, s>>>(n, nnzB, nE, nK, Rpad, rp, ci, v, x, y, w, part);
+        } else {
+            k_spmm32_gen<CH, false><<<g, 256, 0, s>>>(n, nnzB, nE, nK, Rpad, rp, ci, v, x, y, w, part);
+        }
     }
 };
 

@@ -25,9 +25,18 @@ struct ColState {
 // fixed order (deterministic).  Every thread of the block must call it.
 __device__ inline double col_sum(const double *__restrict__ part, int NB, int64_t Rpad, int64_t t,
                                  double (*red)[33]) {
-    double s = 0.0;
-    for (int b = threadIdx.y; b < NB; b += 32) s += part[(int64_t)b * Rpad + t];
-    red[threadIdx.y][threadIdx.x] = s;
+    // four independent accumulators keep several loads in flight; the
+    // grouping is fixed, so the sum is deterministic
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int b = threadIdx.y;
+    for (; b + 96 < NB; b += 128) {
+        s0 += part[(int64_t)b * Rpad + t];
+        s1 += part[(int64_t)(b + 32) * Rpad + t];
+        s2 += part[(int64_t)(b + 64) * Rpad + t];
+        s3 += part[(int64_t)(b + 96) * Rpad + t];
+    }
+    for (; b < NB; b += 32) s0 += part[(int64_t)b * Rpad + t];
+    red[threadIdx.y][threadIdx.x] = (s0 + s1) + (s2 + s3);
     __syncthreads();
     double tot = 0.0;
     if (threadIdx.y == 0)
