@@ -82,12 +82,15 @@ const char *ertgb_last_error(const ertgb_ctx *ctx);
 /* Mesh: replaces ModellingBase::setMesh (core/src/modellingbase.cpp:179-206)
  * with DCMultiElectrodeModelling::updateMeshDependency_
  * (core/src/bert/dcfemmodelling.cpp:711-773).  dim 2 (triangles, y = depth,
- * 2.5-D) or 3 (tetrahedra).  xyz: n_nodes x 3.  cell_nodes: n_cells x
- * (dim+1).  bnd_nodes: n_bnd x dim, bnd_marker -1 Neumann / -2 mixed,
+ * 2.5-D) or 3 (tetrahedra); order 1 (linear) or 2 (quadratic: Triangle6 /
+ * Tetrahedron10 in the node order of Mesh::createP2, core/src/mesh.cpp:
+ * 1284-1600).  xyz: n_nodes x 3.  cell_nodes: n_cells x (dim+1) for order 1,
+ * x 6 / 10 for order 2.  bnd_nodes: n_bnd x dim (order 1) or x 3 / 6
+ * (order 2), bnd_marker -1 Neumann / -2 mixed,
  * bnd_cell: adjacent cell of each boundary.  Builds the CSR pattern
  * (core/src/sparsematrix.h:966-1024), the per-slot assembly map and the
  * element matrices (core/src/elementmatrix.cpp:683-1122). */
-int ertgb_set_mesh(ertgb_ctx *ctx, int dim, int n_nodes, const double *xyz_host,
+int ertgb_set_mesh(ertgb_ctx *ctx, int dim, int order, int n_nodes, const double *xyz_host,
                    int n_cells, const int32_t *cell_nodes_host, const int32_t *cell_marker_host,
                    int n_bnd, const int32_t *bnd_nodes_host, const int32_t *bnd_marker_host,
                    const int32_t *bnd_cell_host);

@@ -109,13 +109,114 @@ def besselK1(x):
 
 
 # ------------------------------------------------------------- geometry --
+_TET10_EDGES = ((0, 1), (0, 2), (0, 3), (1, 2), (2, 3), (3, 1))
+_TRI6_EDGES = ((0, 1), (1, 2), (2, 0))
+
+
+def _p2_shape(dim, lam):
+    """P2 Lagrange functions at barycentric points lam (Q x dim+1): vertex
+    l(2l-1), edge 4 l_a l_b in Tetrahedron10 / Triangle6 order."""
+    edges = _TET10_EDGES if dim == 3 else _TRI6_EDGES
+    vert = lam * (2.0 * lam - 1.0)
+    edge = np.stack([4.0 * lam[:, a] * lam[:, b] for a, b in edges], axis=1)
+    return np.concatenate([vert, edge], axis=1)
+
+
+def _p2_grad(dim, lam, g):
+    """Gradients (C x Q x nv x 3) of the P2 functions; g: barycentric gradients C x (dim+1) x 3."""
+    edges = _TET10_EDGES if dim == 3 else _TRI6_EDGES
+    out = [(4.0 * lam[None, :, i, None] - 1.0) * g[:, None, i, :] for i in range(dim + 1)]
+    for a, b in edges:
+        out.append(4.0 * (lam[None, :, b, None] * g[:, None, a, :] + lam[None, :, a, None] * g[:, None, b, :]))
+    return np.stack(out, axis=2)
+
+
+def _rule_tri_deg4():
+    """6-point degree-4 triangle rule (Dunavant)."""
+    a1, b1, w1 = 0.816847572980458513080, 0.091576213509770743460, 0.109951743655321868504
+    a2, b2, w2 = 0.108103018168070227360, 0.445948490915964886320, 0.223381589678011464830
+    pts, w = [], []
+    for a, b, ww in ((a1, b1, w1), (a2, b2, w2)):
+        for q in range(3):
+            lam = [b, b, b]
+            lam[q] = a
+            pts.append(lam)
+            w.append(ww)
+    return np.array(pts), np.array(w)
+
+
+def _rule_tet_deg4():
+    """Keast's 11-point degree-4 tetrahedron rule (weights sum to 1)."""
+    sq = math.sqrt(5.0 / 14.0)
+    ca, cb = (1.0 + sq) / 4.0, (1.0 - sq) / 4.0
+    pts = [[0.25] * 4]
+    w = [-74.0 / 5625.0 * 6.0]
+    for q in range(4):
+        lam = [1.0 / 14.0] * 4
+        lam[q] = 11.0 / 14.0
+        pts.append(lam)
+        w.append(343.0 / 45000.0 * 6.0)
+    for a, b in ((0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3)):
+        lam = [cb] * 4
+        lam[a] = lam[b] = ca
+        pts.append(lam)
+        w.append(56.0 / 2250.0 * 6.0)
+    return np.array(pts), np.array(w)
+
+
+def _bary_gradients(dim, p):
+    if dim == 2:
+        x1, x2, x3 = p[:, 0, 0], p[:, 1, 0], p[:, 2, 0]
+        y1, y2, y3 = p[:, 0, 1], p[:, 1, 1], p[:, 2, 1]
+        det = (x2 - x1) * (y3 - y1) - (x3 - x1) * (y2 - y1)
+        g = np.zeros((len(p), 3, 3))
+        g[:, 1, 0] = (y3 - y1) / det
+        g[:, 1, 1] = -(x3 - x1) / det
+        g[:, 2, 0] = -(y2 - y1) / det
+        g[:, 2, 1] = (x2 - x1) / det
+        g[:, 0] = -(g[:, 1] + g[:, 2])
+        return g, np.abs(det) / 2.0
+    Jm = np.stack([p[:, 1] - p[:, 0], p[:, 2] - p[:, 0], p[:, 3] - p[:, 0]], axis=2)
+    inv = np.linalg.inv(Jm)
+    g = np.empty((len(p), 4, 3))
+    g[:, 1:, :] = inv
+    g[:, 0, :] = -inv.sum(axis=1)
+    return g, np.abs(np.linalg.det(Jm)) / 6.0
+
+
+def element_matrices_p2(dim, nodes, cells):
+    """Tetrahedron10 / Triangle6 gradient and mass matrices, integrated with
+    rules exact for their degrees (gradient products degree 2, function
+    products degree 4), as the reference does (core/src/elementmatrix.cpp:
+    780-781, 1043-1096; core/src/integration.cpp:302-440)."""
+    g, V = _bary_gradients(dim, nodes[cells[:, :dim + 1]])
+    if dim == 3:
+        a, b = (5.0 + 3.0 * math.sqrt(5.0)) / 20.0, (5.0 - math.sqrt(5.0)) / 20.0
+        lam2 = np.full((4, 4), b)
+        np.fill_diagonal(lam2, a)
+        w2 = np.full(4, 0.25)
+        lam4, w4 = _rule_tet_deg4()
+    else:
+        lam2 = np.array([[0.0, 0.5, 0.5], [0.5, 0.0, 0.5], [0.5, 0.5, 0.0]])
+        w2 = np.full(3, 1.0 / 3.0)
+        lam4, w4 = _rule_tri_deg4()
+    dN = _p2_grad(dim, lam2, g)                               # C x Q x nv x 3
+    K = V[:, None, None] * np.einsum("q,cqid,cqjd->cij", w2, dN, dN)
+    N = _p2_shape(dim, lam4)                                  # Q x nv
+    M = V[:, None, None] * np.einsum("q,qi,qj->ij", w4, N, N)[None]
+    return K, M
+
+
 def element_matrices(dim, nodes, cells):
-    """Per-cell P1 gradient matrix K (without 1/rho) and mass matrix M.
+    """Per-cell gradient matrix K (without 1/rho) and mass matrix M; P2
+    cells are handled by element_matrices_p2.  P1 below.
 
     Triangle K: closed form of elementmatrix.cpp:817-860 with J = 2*area.
     Tetrahedron K: one-point rule, V * grad(N_i) . grad(N_j).
     Mass: A/12 (1 + delta_ij) (triangle), V/20 (1 + delta_ij) (tetrahedron),
     which the reference's quadrature rules integrate exactly."""
+    if cells.shape[1] > dim + 1:
+        return element_matrices_p2(dim, nodes, cells)
     p = nodes[cells]
     C = len(cells)
     if dim == 2:
@@ -154,7 +255,18 @@ def element_matrices(dim, nodes, cells):
 
 
 def boundary_mass(dim, nodes, bnd):
-    """u2 of a boundary facet: edge L/6 (1 + delta), triangle A/12 (1 + delta)."""
+    """u2 of a boundary facet: edge L/6 (1 + delta), triangle A/12 (1 + delta);
+    Edge3 L/30 [4 -1 2; -1 4 2; 2 2 16]; Triangle6 with the degree-4 rule."""
+    if bnd.shape[1] == 3 and dim == 2:
+        L = np.linalg.norm(nodes[bnd[:, 1]] - nodes[bnd[:, 0]], axis=1)
+        m = np.array([[4.0, -1.0, 2.0], [-1.0, 4.0, 2.0], [2.0, 2.0, 16.0]])
+        return (L / 30.0)[:, None, None] * m[None]
+    if bnd.shape[1] == 6:
+        p = nodes[bnd[:, :3]]
+        A = 0.5 * np.linalg.norm(np.cross(p[:, 1] - p[:, 0], p[:, 2] - p[:, 0]), axis=1)
+        lam, w = _rule_tri_deg4()
+        N = _p2_shape(2, lam)
+        return A[:, None, None] * np.einsum("q,qi,qj->ij", w, N, N)[None]
     p = nodes[bnd]
     if dim == 2:
         L = np.linalg.norm(p[:, 1] - p[:, 0], axis=1)
@@ -164,8 +276,8 @@ def boundary_mass(dim, nodes, bnd):
 
 
 def boundary_center_normal(dim, nodes, bnd):
-    p = nodes[bnd]
-    c = p.mean(axis=1)
+    c = nodes[bnd].mean(axis=1)
+    p = nodes[bnd[:, :dim]]
     if dim == 2:
         t = p[:, 1] - p[:, 0]
         n = np.column_stack([t[:, 1], -t[:, 0], np.zeros(len(t))])

@@ -43,7 +43,9 @@ def lib():
         L.ref_create.restype = vp
         L.ref_create.argtypes = [ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int, vp, vp,
                                  ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, vp, ctypes.c_int, vp,
-                                 vp, ctypes.c_int]
+                                 vp, ctypes.c_int, ctypes.c_int]
+        L.ref_mesh_sizes.argtypes = [vp, vp, vp, vp, vp, vp]
+        L.ref_mesh_arrays.argtypes = [vp, vp, vp, vp, vp, vp, vp]
         L.ref_destroy.argtypes = [vp]
         L.ref_last_error.restype = ctypes.c_char_p
         L.ref_set_solver.argtypes = [vp, _FACTOR, _SOLVE]
@@ -81,7 +83,7 @@ def _check(rc):
 class RefModelling:
     """The reference's DCSRMultiElectrodeModelling on a given mesh/scheme."""
 
-    def __init__(self, mesh, sensors, abmn, kfac=None, threads=1, keep_matrices=False):
+    def __init__(self, mesh, sensors, abmn, kfac=None, threads=1, keep_matrices=False, p2=False):
         L = lib()
         self.mesh = mesh
         self._keep = [np.ascontiguousarray(mesh.nodes, np.float64),
@@ -99,7 +101,7 @@ class RefModelling:
         self.nE = len(sens)
         h = L.ref_create(mesh.dim(), len(nodes), _p(nodes), _p(nm), len(cells), cells.shape[1], _p(cells),
                          _p(cm), len(bnd), bnd.shape[1], _p(bnd), _p(bm), len(sens), _p(sens), len(ab),
-                         _p(ab), None if kf is None else _p(kf), 0)
+                         _p(ab), None if kf is None else _p(kf), 0, int(bool(p2)))
         if not h:
             raise RuntimeError("ref_create failed: " + L.ref_last_error().decode())
         self.h = h
@@ -132,6 +134,21 @@ class RefModelling:
         self._cb = (_FACTOR(factor), _SOLVE(solve))
         _check(L.ref_set_solver(h, self._cb[0], self._cb[1]))
         _check(L.ref_set_threads(h, int(threads)))
+
+    def mesh_arrays(self):
+        """Mesh the reference operator runs on (nodes, node markers, cells,
+        cell markers, boundaries, boundary markers)."""
+        v = [ctypes.c_int() for _ in range(5)]
+        lib().ref_mesh_sizes(self.h, *[ctypes.byref(x) for x in v])
+        n, C, nv, B, nvb = [x.value for x in v]
+        xyz = np.zeros((n, 3))
+        nm = np.zeros(n, np.int32)
+        cells = np.zeros((C, nv), np.int32)
+        cm = np.zeros(C, np.int32)
+        bnd = np.zeros((B, nvb), np.int32)
+        bm = np.zeros(B, np.int32)
+        _check(lib().ref_mesh_arrays(self.h, _p(xyz), _p(nm), _p(cells), _p(cm), _p(bnd), _p(bm)))
+        return xyz, nm, cells, cm, bnd, bm
 
     def close(self):
         if self.h:
@@ -205,8 +222,14 @@ class RefModelling:
                                   _p(rp), _p(ci), _p(va)))
         return rp, ci, va
 
+    def node_count(self):
+        """Nodes of the mesh the reference operator runs on (after createP2)."""
+        v = [ctypes.c_int() for _ in range(5)]
+        lib().ref_mesh_sizes(self.h, *[ctypes.byref(x) for x in v])
+        return v[0].value
+
     def primary(self, e, k, surface_z=0.0):
-        out = np.zeros(self.mesh.nodeCount())
+        out = np.zeros(self.node_count())
         _check(lib().ref_primary(self.h, int(e), float(k), float(surface_z), _p(out)))
         return out
 

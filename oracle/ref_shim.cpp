@@ -111,7 +111,7 @@ void *ref_create(int dim, int nNodes, const double *xyz, const int *nodeMarker,
                  int nCells, int nv, const int *cellNodes, const int *cellMarker,
                  int nBnd, int nvb, const int *bndNodes, const int *bndMarker,
                  int nSensors, const double *sensorXyz, int nData, const int *abmn,
-                 const double *kfac, int verbose) {
+                 const double *kfac, int verbose, int p2) {
     RefHandle *h = nullptr;
     int rc = guarded([&] {
         h = new RefHandle(dim);
@@ -131,6 +131,11 @@ void *ref_create(int dim, int nNodes, const double *xyz, const int *nodeMarker,
             else throwError("unsupported boundary node count");
         }
         m.createNeighborInfos();
+        if (p2) {  // quadratic elements: the reference's own refinement
+            Mesh m2 = m.createP2();
+            h->mesh = m2;
+            h->mesh.createNeighborInfos();
+        }
         for (int s = 0; s < nSensors; s++)
             h->data.createSensor(RVector3(sensorXyz[3 * s], sensorXyz[3 * s + 1], sensorXyz[3 * s + 2]), 1e-9);
         for (int d = 0; d < nData; d++)
@@ -151,6 +156,41 @@ void *ref_create(int dim, int nNodes, const double *xyz, const int *nodeMarker,
 }
 
 void ref_destroy(void *hp) { delete (RefHandle *)hp; }
+
+// Sizes and arrays of the mesh the operator runs on (after createP2).
+int ref_mesh_sizes(void *hp, int *n, int *C, int *nv, int *B, int *nvb) {
+    RefHandle *h = (RefHandle *)hp;
+    Mesh &m = h->mesh;
+    *n = (int)m.nodeCount();
+    *C = (int)m.cellCount();
+    *nv = m.cellCount() ? (int)m.cell(0).nodeCount() : 0;
+    *B = (int)m.boundaryCount();
+    *nvb = m.boundaryCount() ? (int)m.boundary(0).nodeCount() : 0;
+    return 0;
+}
+
+int ref_mesh_arrays(void *hp, double *xyz, int *nodeMarker, int *cells, int *cellMarker, int *bnd, int *bndMarker) {
+    RefHandle *h = (RefHandle *)hp;
+    return guarded([&] {
+        Mesh &m = h->mesh;
+        for (Index i = 0; i < m.nodeCount(); i++) {
+            xyz[3 * i] = m.node(i).pos()[0];
+            xyz[3 * i + 1] = m.node(i).pos()[1];
+            xyz[3 * i + 2] = m.node(i).pos()[2];
+            nodeMarker[i] = m.node(i).marker();
+        }
+        for (Index c = 0; c < m.cellCount(); c++) {
+            const Cell &cl = m.cell(c);
+            for (Index j = 0; j < cl.nodeCount(); j++) cells[c * cl.nodeCount() + j] = (int)cl.node(j).id();
+            cellMarker[c] = cl.marker();
+        }
+        for (Index b = 0; b < m.boundaryCount(); b++) {
+            const Boundary &bd = m.boundary(b);
+            for (Index j = 0; j < bd.nodeCount(); j++) bnd[b * bd.nodeCount() + j] = (int)bd.node(j).id();
+            bndMarker[b] = bd.marker();
+        }
+    });
+}
 
 int ref_set_solver(void *hp, ref_factor_fn f, ref_solve_fn s) {
     RefHandle *h = (RefHandle *)hp;

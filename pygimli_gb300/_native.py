@@ -38,7 +38,7 @@ SIGNATURES = {
     "ertgb_create": (_ci, [ctypes.POINTER(_vp), _ci]),
     "ertgb_destroy": (_ci, [_vp]),
     "ertgb_last_error": (ctypes.c_char_p, [_vp]),
-    "ertgb_set_mesh": (_ci, [_vp, _ci, _ci, _vp, _ci, _vp, _vp, _ci, _vp, _vp, _vp]),
+    "ertgb_set_mesh": (_ci, [_vp, _ci, _ci, _ci, _vp, _ci, _vp, _vp, _ci, _vp, _vp, _vp]),
     "ertgb_set_electrodes": (_ci, [_vp, _ci, _vp, _d]),
     "ertgb_set_kw": (_ci, [_vp, _ci, _vp, _vp]),
     "ertgb_set_scheme": (_ci, [_vp, _ci, _vp, _vp]),

@@ -106,12 +106,203 @@ __global__ void k_element_matrices(int64_t C, int dim, const double *__restrict_
     }
 }
 
+// ------------------------------------------------------- quadratic cells
+// Quadrature in barycentric coordinates, weights summing to 1 (multiplied by
+// the cell size).  Gradient products of P2 functions are quadratic: the
+// degree-2 rules are exact (tetrahedron: 4 points, a = (5 + 3 sqrt 5)/20,
+// b = (5 - sqrt 5)/20; triangle: the three edge midpoints).  Products of P2
+// functions are quartic: Keast's 11-point tetrahedron rule and the 6-point
+// Dunavant triangle rule are exact for degree 4.  The reference integrates
+// with the same degrees (core/src/integration.cpp:302-440, used by
+// core/src/elementmatrix.cpp:780-781 and 1043-1096), so both agree to rounding.
+__device__ inline void p2_shape(int dim, const double *l, double *N) {
+    if (dim == 3) {
+        for (int i = 0; i < 4; i++) N[i] = l[i] * (2.0 * l[i] - 1.0);
+        N[4] = 4.0 * l[0] * l[1];
+        N[5] = 4.0 * l[0] * l[2];
+        N[6] = 4.0 * l[0] * l[3];
+        N[7] = 4.0 * l[1] * l[2];
+        N[8] = 4.0 * l[2] * l[3];
+        N[9] = 4.0 * l[3] * l[1];
+    } else {
+        for (int i = 0; i < 3; i++) N[i] = l[i] * (2.0 * l[i] - 1.0);
+        N[3] = 4.0 * l[0] * l[1];
+        N[4] = 4.0 * l[1] * l[2];
+        N[5] = 4.0 * l[2] * l[0];
+    }
+}
+
+// gradients of the P2 functions at l given the barycentric gradients g[k][3]
+__device__ inline void p2_grad(int dim, const double *l, const double (*g)[3], double (*dN)[3]) {
+    const int nvx = dim + 1;
+    for (int i = 0; i < nvx; i++)
+        for (int d = 0; d < 3; d++) dN[i][d] = (4.0 * l[i] - 1.0) * g[i][d];
+    const int e3[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {2, 3}, {3, 1}};
+    const int e2[3][2] = {{0, 1}, {1, 2}, {2, 0}};
+    const int ne = dim == 3 ? 6 : 3;
+    for (int e = 0; e < ne; e++) {
+        const int a = dim == 3 ? e3[e][0] : e2[e][0], b = dim == 3 ? e3[e][1] : e2[e][1];
+        for (int d = 0; d < 3; d++) dN[nvx + e][d] = 4.0 * (l[b] * g[a][d] + l[a] * g[b][d]);
+    }
+}
+
+__global__ void k_element_matrices_p2(int64_t C, int dim, const double *__restrict__ xyz,
+                                      const int32_t *__restrict__ cells, double *__restrict__ K,
+                                      double *__restrict__ M) {
+    const int nv = dim == 3 ? 10 : 6, nvx = dim + 1;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t *cn = cells + c * nv;
+        double g[4][3] = {{0}};
+        double V;
+        if (dim == 3) {
+            double p[4][3];
+            for (int i = 0; i < 4; i++)
+                for (int d = 0; d < 3; d++) p[i][d] = xyz[3 * cn[i] + d];
+            double e1[3], e2[3], e3[3];
+            for (int d = 0; d < 3; d++) {
+                e1[d] = p[1][d] - p[0][d];
+                e2[d] = p[2][d] - p[0][d];
+                e3[d] = p[3][d] - p[0][d];
+            }
+            const double c23[3] = {e2[1] * e3[2] - e2[2] * e3[1], e2[2] * e3[0] - e2[0] * e3[2], e2[0] * e3[1] - e2[1] * e3[0]};
+            const double c31[3] = {e3[1] * e1[2] - e3[2] * e1[1], e3[2] * e1[0] - e3[0] * e1[2], e3[0] * e1[1] - e3[1] * e1[0]};
+            const double c12[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+            const double det = e1[0] * c23[0] + e1[1] * c23[1] + e1[2] * c23[2];
+            for (int d = 0; d < 3; d++) {
+                g[1][d] = c23[d] / det;
+                g[2][d] = c31[d] / det;
+                g[3][d] = c12[d] / det;
+                g[0][d] = -(g[1][d] + g[2][d] + g[3][d]);
+            }
+            V = fabs(det) / 6.0;
+        } else {
+            const double x1 = xyz[3 * cn[0]], y1 = xyz[3 * cn[0] + 1];
+            const double x2 = xyz[3 * cn[1]], y2 = xyz[3 * cn[1] + 1];
+            const double x3 = xyz[3 * cn[2]], y3 = xyz[3 * cn[2] + 1];
+            const double det = (x2 - x1) * (y3 - y1) - (x3 - x1) * (y2 - y1);
+            g[1][0] = (y3 - y1) / det;
+            g[1][1] = -(x3 - x1) / det;
+            g[2][0] = -(y2 - y1) / det;
+            g[2][1] = (x2 - x1) / det;
+            g[0][0] = -(g[1][0] + g[2][0]);
+            g[0][1] = -(g[1][1] + g[2][1]);
+            V = fabs(det) / 2.0;
+        }
+        double Kc[10][10] = {{0}}, Mc[10][10] = {{0}};
+        double l[4], N[10], dN[10][3];
+        // stiffness: degree-2 rule
+        const int nq2 = dim == 3 ? 4 : 3;
+        for (int q = 0; q < nq2; q++) {
+            if (dim == 3) {
+                const double a = 0.58541019662496845446, b = 0.13819660112501051518;
+                for (int i = 0; i < 4; i++) l[i] = (i == q) ? a : b;
+            } else {
+                l[0] = l[1] = l[2] = 0.5;
+                l[q] = 0.0;
+            }
+            p2_grad(dim, l, g, dN);
+            const double wq = 1.0 / nq2;
+            for (int i = 0; i < nv; i++)
+                for (int j = 0; j < nv; j++)
+                    Kc[i][j] += wq * (dN[i][0] * dN[j][0] + dN[i][1] * dN[j][1] + dN[i][2] * dN[j][2]);
+        }
+        // mass: degree-4 rule
+        if (dim == 3) {
+            const double sq = sqrt(5.0 / 14.0);
+            const double ca = (1.0 + sq) / 4.0, cb = (1.0 - sq) / 4.0;
+            const int pairs[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+            for (int q = 0; q < 11; q++) {
+                double wq;
+                if (q == 0) {
+                    l[0] = l[1] = l[2] = l[3] = 0.25;
+                    wq = -74.0 / 5625.0 * 6.0;
+                } else if (q < 5) {
+                    for (int i = 0; i < 4; i++) l[i] = (i == q - 1) ? 11.0 / 14.0 : 1.0 / 14.0;
+                    wq = 343.0 / 45000.0 * 6.0;
+                } else {
+                    for (int i = 0; i < 4; i++) l[i] = cb;
+                    l[pairs[q - 5][0]] = ca;
+                    l[pairs[q - 5][1]] = ca;
+                    wq = 56.0 / 2250.0 * 6.0;
+                }
+                p2_shape(3, l, N);
+                for (int i = 0; i < nv; i++)
+                    for (int j = 0; j < nv; j++) Mc[i][j] += wq * N[i] * N[j];
+            }
+        } else {
+            const double A1 = 0.816847572980458513080, B1 = 0.091576213509770743460;
+            const double A2 = 0.108103018168070227360, B2 = 0.445948490915964886320;
+            const double W1 = 0.109951743655321868504, W2 = 0.223381589678011464830;
+            for (int q = 0; q < 6; q++) {
+                const double a = q < 3 ? A1 : A2, b = q < 3 ? B1 : B2;
+                for (int i = 0; i < 3; i++) l[i] = (i == q % 3) ? a : b;
+                p2_shape(2, l, N);
+                const double wq = q < 3 ? W1 : W2;
+                for (int i = 0; i < nv; i++)
+                    for (int j = 0; j < nv; j++) Mc[i][j] += wq * N[i] * N[j];
+            }
+        }
+        double *kk = K + c * nv * nv;
+        double *mm = M + c * nv * nv;
+        for (int i = 0; i < nv; i++)
+            for (int j = 0; j < nv; j++) {
+                kk[i * nv + j] = V * Kc[i][j];
+                mm[i * nv + j] = V * Mc[i][j];
+            }
+        (void)nvx;
+    }
+}
+
 __global__ void k_boundary_geometry(int64_t B, int dim, const double *__restrict__ xyz,
                                     const int32_t *__restrict__ bnd, double *__restrict__ mass,
-                                    double *__restrict__ center, double *__restrict__ normal) {
+                                    double *__restrict__ center, double *__restrict__ normal, int nvb) {
     for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < B;
          b += (int64_t)gridDim.x * blockDim.x) {
-        if (dim == 2) {
+        if (nvb == 3 && dim == 2) {
+            // Edge3 (nodes v0, v1, midpoint): exact mass L/30 [4 -1 2; -1 4 2; 2 2 16]
+            const int32_t *bn = bnd + b * 3;
+            const double tx = xyz[3 * bn[1]] - xyz[3 * bn[0]], ty = xyz[3 * bn[1] + 1] - xyz[3 * bn[0] + 1];
+            const double L = sqrt(tx * tx + ty * ty);
+            const double m30[9] = {4, -1, 2, -1, 4, 2, 2, 2, 16};
+            for (int i = 0; i < 9; i++) mass[b * 9 + i] = L / 30.0 * m30[i];
+            for (int d = 0; d < 3; d++)
+                center[b * 3 + d] = (xyz[3 * bn[0] + d] + xyz[3 * bn[1] + d] + xyz[3 * bn[2] + d]) / 3.0;
+            normal[b * 3 + 0] = ty / L;
+            normal[b * 3 + 1] = -tx / L;
+            normal[b * 3 + 2] = 0.0;
+        } else if (nvb == 6) {
+            // Triangle6 face: 6-point degree-4 rule on the P2 functions
+            const int32_t *bn = bnd + b * 6;
+            double p[3][3];
+            for (int i = 0; i < 3; i++)
+                for (int d = 0; d < 3; d++) p[i][d] = xyz[3 * bn[i] + d];
+            const double u[3] = {p[1][0] - p[0][0], p[1][1] - p[0][1], p[1][2] - p[0][2]};
+            const double v[3] = {p[2][0] - p[0][0], p[2][1] - p[0][1], p[2][2] - p[0][2]};
+            const double n[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]};
+            const double nl = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+            const double A = 0.5 * nl;
+            const double A1 = 0.816847572980458513080, B1 = 0.091576213509770743460;
+            const double A2 = 0.108103018168070227360, B2 = 0.445948490915964886320;
+            const double W1 = 0.109951743655321868504, W2 = 0.223381589678011464830;
+            double Mf[6][6] = {{0}};
+            double l[3], N[6];
+            for (int q = 0; q < 6; q++) {
+                const double a = q < 3 ? A1 : A2, bb = q < 3 ? B1 : B2;
+                for (int i = 0; i < 3; i++) l[i] = (i == q % 3) ? a : bb;
+                p2_shape(2, l, N);
+                const double wq = q < 3 ? W1 : W2;
+                for (int i = 0; i < 6; i++)
+                    for (int j = 0; j < 6; j++) Mf[i][j] += wq * N[i] * N[j];
+            }
+            for (int i = 0; i < 6; i++)
+                for (int j = 0; j < 6; j++) mass[b * 36 + i * 6 + j] = A * Mf[i][j];
+            for (int d = 0; d < 3; d++) {
+                double sum = 0.0;
+                for (int i = 0; i < 6; i++) sum += xyz[3 * bn[i] + d];
+                center[b * 3 + d] = sum / 6.0;
+                normal[b * 3 + d] = n[d] / nl;
+            }
+        } else if (dim == 2) {
             const int32_t *bn = bnd + b * 2;
             const double x0 = xyz[3 * bn[0]], y0 = xyz[3 * bn[0] + 1], z0 = xyz[3 * bn[0] + 2];
             const double x1 = xyz[3 * bn[1]], y1 = xyz[3 * bn[1] + 1], z1 = xyz[3 * bn[1] + 2];
@@ -418,7 +609,10 @@ void build_mesh_device(Context &c) {
     m.d_UtoL.upload(m.UtoL, s);
     m.d_K.alloc((size_t)m.C * m.nv * m.nv);
     m.d_M.alloc((size_t)m.C * m.nv * m.nv);
-    k_element_matrices<<<grid1(m.C), kThreads, 0, s>>>(m.C, m.dim, m.d_xyz.p, m.d_cells.p, m.d_K.p, m.d_M.p);
+    if (m.order == 1)
+        k_element_matrices<<<grid1(m.C), kThreads, 0, s>>>(m.C, m.dim, m.d_xyz.p, m.d_cells.p, m.d_K.p, m.d_M.p);
+    else
+        k_element_matrices_p2<<<grid1(m.C, 128), 128, 0, s>>>(m.C, m.dim, m.d_xyz.p, m.d_cells.p, m.d_K.p, m.d_M.p);
     ERTGB_CUDA(cudaGetLastError());
     m.d_bnd_nodes.upload(m.bnd_nodes, s);
     m.d_bnd_cell.upload(m.bnd_cell, s);
@@ -428,7 +622,7 @@ void build_mesh_device(Context &c) {
     if (m.B) {
         k_boundary_geometry<<<grid1(m.B), kThreads, 0, s>>>(m.B, m.dim, m.d_xyz.p, m.d_bnd_nodes.p,
                                                              m.d_bnd_mass.p, m.d_bnd_center.p,
-                                                             m.d_bnd_normal.p);
+                                                             m.d_bnd_normal.p, m.nvb);
         ERTGB_CUDA(cudaGetLastError());
     }
     // host copies of large maps are not kept

@@ -211,12 +211,13 @@ const char *ertgb_last_error(const ertgb_ctx *ctx) {
     return c->last_error.c_str();
 }
 
-int ertgb_set_mesh(ertgb_ctx *ctx, int dim, int n_nodes, const double *xyz, int n_cells,
+int ertgb_set_mesh(ertgb_ctx *ctx, int dim, int order, int n_nodes, const double *xyz, int n_cells,
                    const int32_t *cell_nodes, const int32_t *cell_marker, int n_bnd, const int32_t *bnd_nodes,
                    const int32_t *bnd_marker, const int32_t *bnd_cell) {
     Context *c = reinterpret_cast<Context *>(ctx);
     return guard(c, [&] {
         ERTGB_REQUIRE(dim == 2 || dim == 3, "dim must be 2 or 3");
+        ERTGB_REQUIRE(order == 1 || order == 2, "order must be 1 (linear) or 2 (quadratic)");
         ERTGB_REQUIRE(n_nodes > 0 && n_cells > 0 && n_bnd >= 0, "empty mesh");
         ERTGB_REQUIRE(xyz && cell_nodes && cell_marker, "null mesh array");
         ERTGB_CUDA(cudaSetDevice(c->device));
@@ -224,8 +225,9 @@ int ertgb_set_mesh(ertgb_ctx *ctx, int dim, int n_nodes, const double *xyz, int 
         new (&c->mesh) MeshData();
         MeshData &m = c->mesh;
         m.dim = dim;
-        m.nv = dim + 1;
-        m.nvb = dim;
+        m.order = order;
+        m.nv = order == 1 ? dim + 1 : (dim == 2 ? 6 : 10);
+        m.nvb = order == 1 ? dim : (dim == 2 ? 3 : 6);
         m.n = n_nodes;
         m.C = n_cells;
         m.xyz.assign(xyz, xyz + (size_t)n_nodes * 3);

@@ -66,7 +66,7 @@ template <class T> struct DBuf {
 
 // Mesh-dependent structures.
 struct MeshData {
-    int dim = 0, nv = 0, nvb = 0;
+    int dim = 0, order = 1, nv = 0, nvb = 0;  // nv / nvb: nodes per cell / boundary
     int64_t n = 0, C = 0, B = 0;  // nodes, cells, mixed boundaries
     int64_t nnz = 0;
     int64_t P = 0;                // parameters = max(cell marker) + 1

@@ -25,6 +25,7 @@
 // (datum sub-row, cell) with the cell fastest, so conflict-free table reads
 // and contiguous runs of a J row per sub-row.
 #include <algorithm>
+#include <type_traits>
 
 #include "ertgb_internal.cuh"
 
@@ -207,7 +208,7 @@ bool plan(const Context &c, int dtype, int *TW, int *G) {
     const size_t uv = 2 * (size_t)c.nK * c.mesh.nv * (c.nE + 1) * sizeof(double);
     const size_t tab = (size_t)c.nK * (c.nA + c.nM) * c.mesh.nv * (dtype == 0 ? 8 : 4);
     for (size_t budget : {kSmemBudget, kSmemBudgetLarge})
-        for (int tw : {16, 8, 4}) {
+        for (int tw : {16, 8, 4, 2, 1}) {
             if (tw * tab + uv > budget) continue;
             *TW = tw;
             *G = (int)std::max<size_t>(1, std::min<size_t>(4, (budget - tw * tab) / uv));
@@ -243,14 +244,19 @@ void launch(Context &c, const double *model, CT *J, int dtype, cudaStream_t s) {
                                             c.d_dip_m.p, c.d_data_dip.p, sd, sp, m.P, c.D, G, J);
         ERTGB_CUDA(cudaGetLastError());
     };
-    if (m.nv == 3) {
-        if (TW == 16) go(k_jacobian<3, CT, 16>);
-        else if (TW == 8) go(k_jacobian<3, CT, 8>);
-        else go(k_jacobian<3, CT, 4>);
-    } else {
-        if (TW == 16) go(k_jacobian<4, CT, 16>);
-        else if (TW == 8) go(k_jacobian<4, CT, 8>);
-        else go(k_jacobian<4, CT, 4>);
+    auto by_tw = [&](auto nvc) {
+        constexpr int NV = decltype(nvc)::value;
+        if (TW == 16) go(k_jacobian<NV, CT, 16>);
+        else if (TW == 8) go(k_jacobian<NV, CT, 8>);
+        else if (TW == 4) go(k_jacobian<NV, CT, 4>);
+        else if (TW == 2) go(k_jacobian<NV, CT, 2>);
+        else go(k_jacobian<NV, CT, 1>);
+    };
+    switch (m.nv) {
+        case 3: by_tw(std::integral_constant<int, 3>()); break;
+        case 4: by_tw(std::integral_constant<int, 4>()); break;
+        case 6: by_tw(std::integral_constant<int, 6>()); break;
+        default: by_tw(std::integral_constant<int, 10>()); break;
     }
 }
 

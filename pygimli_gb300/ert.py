@@ -156,7 +156,7 @@ class ERTModelling:
             raise NotImplementedError("Neumann-only domains are not supported")
         b = np.ascontiguousarray(mesh.boundaries, np.int32)
         self._check(self._lib.ertgb_set_mesh(
-            self._ctx, mesh.dim(), mesh.nodeCount(), _ptr(mesh.nodes), mesh.cellCount(),
+            self._ctx, mesh.dim(), mesh.order, mesh.nodeCount(), _ptr(mesh.nodes), mesh.cellCount(),
             _ptr(mesh.cells), _ptr(mesh.cell_markers), len(b), _ptr(b),
             _ptr(mesh.boundary_markers), _ptr(mesh.boundary_cells)))
         self._mesh = mesh

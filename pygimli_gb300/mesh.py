@@ -34,7 +34,8 @@ MARKER_BOUND_HOMOGEN_DIRICHLET = -3
 
 
 class Mesh:
-    """Linear simplex mesh (triangles in 2-D, tetrahedra in 3-D)."""
+    """Simplex mesh: triangles (2-D) or tetrahedra (3-D), linear (P1) or
+    quadratic (P2: Triangle6 / Tetrahedron10 with edge-midpoint nodes)."""
 
     def __init__(self, dim, nodes, cells, cell_markers=None, node_markers=None,
                  boundaries=None, boundary_markers=None, boundary_cells=None):
@@ -44,23 +45,30 @@ class Mesh:
             nodes = np.column_stack([nodes, np.zeros(len(nodes))])
         self.nodes = np.ascontiguousarray(nodes)
         self.cells = np.ascontiguousarray(np.asarray(cells, dtype=np.int32))
-        nv = self.dim_ + 1
-        if self.cells.ndim != 2 or self.cells.shape[1] != nv:
-            raise ValueError(f"cells must be (C, {nv}) for a {dim}-D simplex mesh")
+        nv1 = self.dim_ + 1
+        nv2 = 6 if self.dim_ == 2 else 10
+        if self.cells.ndim != 2 or self.cells.shape[1] not in (nv1, nv2):
+            raise ValueError(f"cells must be (C, {nv1}) or (C, {nv2}) for a {dim}-D simplex mesh")
+        self.order = 1 if self.cells.shape[1] == nv1 else 2
+        nvb = self.dim_ if self.order == 1 else (3 if self.dim_ == 2 else 6)
         C = len(self.cells)
         self.cell_markers = (np.arange(C, dtype=np.int32) if cell_markers is None
                              else np.ascontiguousarray(np.asarray(cell_markers, dtype=np.int32)))
         self.node_markers = (np.zeros(len(self.nodes), np.int32) if node_markers is None
                              else np.ascontiguousarray(np.asarray(node_markers, dtype=np.int32)))
         if boundaries is None:
-            boundaries = np.zeros((0, self.dim_), np.int32)
+            boundaries = np.zeros((0, nvb), np.int32)
             boundary_markers = np.zeros(0, np.int32)
-        self.boundaries = np.ascontiguousarray(np.asarray(boundaries, dtype=np.int32).reshape(-1, self.dim_))
+        self.boundaries = np.ascontiguousarray(np.asarray(boundaries, dtype=np.int32).reshape(-1, nvb))
         self.boundary_markers = np.ascontiguousarray(np.asarray(boundary_markers, dtype=np.int32))
         if boundary_cells is None:
-            boundary_cells = find_boundary_cells(self.cells, self.boundaries, len(self.nodes))
+            boundary_cells = find_boundary_cells(self.cells[:, :nv1], self.boundaries[:, :self.dim_],
+                                                 len(self.nodes))
         self.boundary_cells = np.ascontiguousarray(np.asarray(boundary_cells, dtype=np.int32))
-        self._fix_orientation()
+        if self.order == 1:
+            self._fix_orientation()
+        else:
+            self._check_orientation()
 
     # -- reference-style accessors (core/src/mesh.h:331-351) --------------
     def dim(self):
@@ -93,9 +101,29 @@ class Mesh:
     def findNodesIdxByMarker(self, marker):
         return np.nonzero(self.node_markers == marker)[0]
 
+    def _check_orientation(self):
+        d = self._signed_sizes()
+        if np.any(d <= 0):
+            raise ValueError("P2 cells must be positively oriented (orient the P1 mesh before createP2)")
+
+    def _signed_sizes(self):
+        p = self.nodes[self.cells[:, :self.dim_ + 1]]
+        if self.dim_ == 2:
+            a = p[:, 1, :2] - p[:, 0, :2]
+            b = p[:, 2, :2] - p[:, 0, :2]
+            return a[:, 0] * b[:, 1] - a[:, 1] * b[:, 0]
+        a = p[:, 1] - p[:, 0]
+        b = p[:, 2] - p[:, 0]
+        c = p[:, 3] - p[:, 0]
+        return np.einsum("ij,ij->i", a, np.cross(b, c))
+
+    def createP2(self):
+        """Quadratic mesh, see create_p2."""
+        return create_p2(self)
+
     def cellSizes(self):
         """Cell areas (2-D) or volumes (3-D), positive."""
-        p = self.nodes[self.cells]
+        p = self.nodes[self.cells[:, :self.dim_ + 1]]
         if self.dim_ == 2:
             a = p[:, 1, :2] - p[:, 0, :2]
             b = p[:, 2, :2] - p[:, 0, :2]
@@ -106,7 +134,7 @@ class Mesh:
         return np.abs(np.einsum("ij,ij->i", a, np.cross(b, c))) / 6.0
 
     def cellCenters(self):
-        return self.nodes[self.cells].mean(axis=1)
+        return self.nodes[self.cells[:, :self.dim_ + 1]].mean(axis=1)
 
     def _fix_orientation(self):
         """Make every simplex positively oriented (the element matrices use
@@ -141,8 +169,72 @@ class Mesh:
                     z["boundaries"], z["boundary_markers"], z["boundary_cells"])
 
     def __repr__(self):
-        return (f"Mesh(dim={self.dim_}, nodes={self.nodeCount()}, cells={self.cellCount()}, "
-                f"boundaries={self.boundaryCount()})")
+        return (f"Mesh(dim={self.dim_}, order={self.order}, nodes={self.nodeCount()}, "
+                f"cells={self.cellCount()}, boundaries={self.boundaryCount()})")
+
+
+# Tetrahedron10 node order (Zienkiewicz): vertices, then edges 01 02 03 12 23 31
+_TET10_EDGES = ((0, 1), (0, 2), (0, 3), (1, 2), (2, 3), (3, 1))
+# Triangle6: vertices, then edges 01 12 20
+_TRI6_EDGES = ((0, 1), (1, 2), (2, 0))
+
+
+def _marker_mid(m0, m1):
+    """Marker of an edge-midpoint node (core/src/mesh.cpp:1293-1299)."""
+    if m0 == -99 and m1 == -99:
+        return -1
+    if m0 == -99:
+        return m1
+    if m1 == -99:
+        return m0
+    return m1 if m0 == m1 else 0
+
+
+def create_p2(mesh):
+    """Quadratic (P2) mesh with the node numbering of Mesh::createP2
+    (core/src/mesh.cpp:1284-1288, createRefined_ 1315-1600): the P1 nodes keep
+    their ids; a midpoint node is created for every edge at its first use,
+    walking the cells in order and each cell's edges in Tetrahedron10
+    (Zienkiewicz) / Triangle6 order, then the boundaries.  Cell markers become
+    the P1 cell index (createRefined_ passes the cell index as marker);
+    boundary markers are kept."""
+    if mesh.order != 1:
+        raise ValueError("mesh is already quadratic")
+    n0 = mesh.nodeCount()
+    edges = _TET10_EDGES if mesh.dim() == 3 else _TRI6_EDGES
+    cells = mesh.cells.astype(np.int64)
+    C = len(cells)
+    # candidate midpoints in creation order: cells (edge order), then boundaries
+    pairs_c = np.stack([cells[:, [a for a, _ in edges]], cells[:, [b for _, b in edges]]], axis=2)
+    pairs_c = pairs_c.reshape(-1, 2)
+    bnd = mesh.boundaries.astype(np.int64)
+    if mesh.dim() == 3:
+        bedges = ((0, 1), (1, 2), (2, 0))
+    else:
+        bedges = ((0, 1),)
+    pairs_b = np.stack([bnd[:, [a for a, _ in bedges]], bnd[:, [b for _, b in bedges]]], axis=2).reshape(-1, 2)
+    pairs = np.concatenate([pairs_c, pairs_b])
+    key = np.minimum(pairs[:, 0], pairs[:, 1]) * n0 + np.maximum(pairs[:, 0], pairs[:, 1])
+    uniq, first, inv = np.unique(key, return_index=True, return_inverse=True)
+    order = np.argsort(first, kind="stable")        # unique edges in creation order
+    rank = np.empty(len(uniq), np.int64)
+    rank[order] = np.arange(len(uniq))
+    mid_id = n0 + rank[inv]                          # node id of every candidate
+    ea = pairs[first[order], 0]
+    eb = pairs[first[order], 1]
+    mids = 0.5 * (mesh.nodes[ea] + mesh.nodes[eb])
+    nm = mesh.node_markers
+    mid_markers = np.array([_marker_mid(int(nm[a]), int(nm[b])) for a, b in zip(ea, eb)], np.int32)
+    nodes = np.concatenate([mesh.nodes, mids])
+    node_markers = np.concatenate([nm, mid_markers])
+    ne = len(edges)
+    cell_mid = mid_id[:C * ne].reshape(C, ne)
+    cells2 = np.concatenate([cells, cell_mid], axis=1).astype(np.int32)
+    nb = len(bedges)
+    bnd_mid = mid_id[C * ne:].reshape(len(bnd), nb)
+    bnd2 = np.concatenate([bnd, bnd_mid], axis=1).astype(np.int32)
+    return Mesh(mesh.dim(), nodes, cells2, np.arange(C, dtype=np.int32), node_markers, bnd2,
+                mesh.boundary_markers.copy(), mesh.boundary_cells.copy())
 
 
 def _facet_keys(facets, n_nodes):

@@ -39,14 +39,15 @@ def _resistivity(mesh, seed):
     return rho
 
 
-def case(name, mesh, data, seed, threads=1):
+def case(name, mesh, data, seed, threads=1, p2=False):
     R = RefModelling(mesh, data.sensorPositions(), data.abmn(), data["k"], threads=threads,
-                     keep_matrices=True)
+                     keep_matrices=True, p2=p2)
     k, w = R.kw()
     rho = _resistivity(mesh, seed)
     rhoa = R.response(rho)
     mats = R.matrices
-    sub = R.subpotentials().reshape(len(k), data.sensorCount(), mesh.nodeCount())
+    sub = R.subpotentials()
+    sub = sub.reshape(len(k), data.sensorCount(), -1)
     J = R.jacobian(rho)
     kidx = np.unique([0, len(k) // 2, len(k) - 1])
     prim = np.stack([np.stack([R.primary(e, k[i], 0.0) for e in range(data.sensorCount())]) for i in kidx])
@@ -54,7 +55,8 @@ def case(name, mesh, data, seed, threads=1):
     ci = np.stack([mats[i][1] for i in kidx])
     va = np.stack([mats[i][2] for i in kidx])
     rho1 = np.ones(mesh.cellCount())
-    src_center = mesh.nodes[R.electrode_nodes()].mean(axis=0)
+    xyz_r, nm_r, cells_r, cm_r, bnd_r, bm_r = R.mesh_arrays()
+    src_center = xyz_r[R.electrode_nodes()].mean(axis=0)
     S1 = np.stack([R.assemble(rho1, k[i], src_center)[2] for i in kidx])
     np.savez_compressed(
         os.path.join(OUT, name + ".npz"),
@@ -64,7 +66,9 @@ def case(name, mesh, data, seed, threads=1):
         sensors=data.sensorPositions(), abmn=data.abmn(), kfac=data["k"],
         kfac_ref=R.geometric_factors(), rho=rho, k=k, w=w, rhoa=rhoa,
         electrode_nodes=R.electrode_nodes(), kidx=kidx, rowptr=rp[0], colidx=ci[0], S=va, S1=S1,
-        primary=prim, subpot=sub, J=J)
+        primary=prim, subpot=sub, J=J, p2=int(p2), ref_nodes=xyz_r, ref_cells=cells_r,
+        ref_node_markers=nm_r, ref_cell_markers=cm_r, ref_boundaries=bnd_r[:mesh.boundaryCount()],
+        ref_boundary_markers=bm_r[:mesh.boundaryCount()])
     R.close()
     print(name, mesh, len(data), "k:", len(k), "J:", J.shape)
 
@@ -111,6 +115,19 @@ def main():
     d3 = DataContainerERT(np.column_stack([e, np.zeros(len(e))]), ab)
     d3["k"] = geometricFactors(d3, 3)
     case("ert3d_small", m3, d3, seed=13)
+    # quadratic elements (the reference's Mesh::createP2 of the same meshes)
+    m3p = create_box_mesh_3d(np.array([(x, y) for x in np.arange(3) * 4.0 for y in np.arange(2) * 4.0]),
+                             h=2.0, para_margin=(1, 1), para_depth=4.0, outer=40.0, growth=2.2, depth_growth=1.6)
+    e3p = np.array([(x, y) for x in np.arange(3) * 4.0 for y in np.arange(2) * 4.0])
+    ab3p = np.vstack([grid_line_scheme((3, 2), "pd"), np.array([[0, 1, 2, 3], [0, 2, 4, 5]], np.int32)])
+    d3p = DataContainerERT(np.column_stack([e3p, np.zeros(len(e3p))]), ab3p)
+    d3p["k"] = geometricFactors(d3p, 3)
+    case("ert3d_p2_small", m3p, d3p, seed=14, p2=True)
+    xs7 = np.arange(7.0)
+    m2p = create_para_mesh_2d(xs7, para_dx=1.0, para_depth=3.0)
+    d2p = createData(xs7, "dd")
+    d2p["k"] = geometricFactors(d2p, 2)
+    case("ert2d_p2_small", m2p, d2p, seed=15, p2=True)
 
 
 if __name__ == "__main__":

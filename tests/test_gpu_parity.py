@@ -54,6 +54,8 @@ def load_case(golden_dir, name):
     z = np.load(os.path.join(golden_dir, name + ".npz"))
     mesh = Mesh(int(z["dim"]), z["nodes"], z["cells"], z["cell_markers"], z["node_markers"],
                 z["boundaries"], z["boundary_markers"], z["boundary_cells"])
+    if int(z["p2"]):
+        mesh = mesh.createP2()
     data = DataContainerERT(z["sensors"], z["abmn"])
     data.set("k", z["kfac"])
     return z, mesh, data
@@ -64,7 +66,7 @@ def rel(a, b):
 
 
 @pytest.mark.parametrize("precision", list(FORMS))
-@pytest.mark.parametrize("name", ["ert2d_small", "ert2d_pd_wa", "ert3d_small"])
+@pytest.mark.parametrize("name", ["ert2d_small", "ert2d_pd_wa", "ert3d_small", "ert3d_p2_small", "ert2d_p2_small"])
 def test_golden_parity(torch, golden_dir, name, precision):
     z, mesh, data = load_case(golden_dir, name)
     fop = fop_for(mesh, data, form=precision)

@@ -16,14 +16,29 @@ from pygimli_gb300.ert import search_electrodes, surface_info
 from pygimli_gb300.kwave import gauss_laguerre, gauss_legendre, init_kwave_list
 from pygimli_gb300.mesh import Mesh
 
-CASES = ["ert2d_small", "ert2d_pd_wa", "ert3d_small"]
+CASES = ["ert2d_small", "ert2d_pd_wa", "ert3d_small", "ert3d_p2_small", "ert2d_p2_small"]
 
 
 def load_case(golden_dir, name):
+    """Mesh of a fixture: the stored P1 mesh, refined with create_p2 for the
+    quadratic cases (the reference ran its own Mesh::createP2)."""
     z = np.load(os.path.join(golden_dir, name + ".npz"))
     mesh = Mesh(int(z["dim"]), z["nodes"], z["cells"], z["cell_markers"], z["node_markers"],
                 z["boundaries"], z["boundary_markers"], z["boundary_cells"])
+    if int(z["p2"]):
+        mesh = mesh.createP2()
     return z, mesh
+
+
+@pytest.mark.parametrize("name", ["ert3d_p2_small", "ert2d_p2_small"])
+def test_create_p2_matches_reference(golden_dir, name):
+    z, mesh = load_case(golden_dir, name)
+    assert np.array_equal(mesh.nodes, z["ref_nodes"])
+    assert np.array_equal(mesh.cells, z["ref_cells"])
+    assert np.array_equal(mesh.node_markers, z["ref_node_markers"])
+    assert np.array_equal(mesh.cell_markers, z["ref_cell_markers"])
+    assert np.array_equal(mesh.boundaries, z["ref_boundaries"])
+    assert np.array_equal(mesh.boundary_markers, z["ref_boundary_markers"])
 
 
 def test_bessel_matches_reference(golden_dir):
