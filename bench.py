@@ -197,7 +197,7 @@ def run_ours(args, world, rank, local):
     t_setup = time.perf_counter()
     fop = ERTModelling(device=local, rtol=args.rtol, precision=args.precision, precond=args.precond)
     fop.setData(data)
-    fop.setMesh(mesh)
+    fop.setMesh(mesh, ignoreRegionManager=True)
     setup_s = time.perf_counter() - t_setup
     L = _native.load()
     D, P, C = data.size(), fop.parameterCount, mesh.cellCount()
@@ -246,7 +246,7 @@ def run_ours(args, world, rank, local):
     if not args.no_plain and (args.precision, args.precond) != ("fp64", "jacobi"):
         fop_p = ERTModelling(device=local, rtol=args.rtol, precision="fp64", precond="jacobi")
         fop_p.setData(data)
-        fop_p.setMesh(mesh)
+        fop_p.setMesh(mesh, ignoreRegionManager=True)
         Jp = torch.empty((D, P), dtype=torch.float64, device=dev)
 
         def step_p():

@@ -83,7 +83,7 @@ def _check(rc):
 class RefModelling:
     """The reference's DCSRMultiElectrodeModelling on a given mesh/scheme."""
 
-    def __init__(self, mesh, sensors, abmn, kfac=None, threads=1, keep_matrices=False, p2=False):
+    def __init__(self, mesh, sensors, abmn, kfac=None, threads=1, keep_matrices=False, p2=False, h2=False):
         L = lib()
         self.mesh = mesh
         self._keep = [np.ascontiguousarray(mesh.nodes, np.float64),
@@ -101,7 +101,7 @@ class RefModelling:
         self.nE = len(sens)
         h = L.ref_create(mesh.dim(), len(nodes), _p(nodes), _p(nm), len(cells), cells.shape[1], _p(cells),
                          _p(cm), len(bnd), bnd.shape[1], _p(bnd), _p(bm), len(sens), _p(sens), len(ab),
-                         _p(ab), None if kf is None else _p(kf), 0, int(bool(p2)))
+                         _p(ab), None if kf is None else _p(kf), 0, 2 if h2 else int(bool(p2)))
         if not h:
             raise RuntimeError("ref_create failed: " + L.ref_last_error().decode())
         self.h = h

@@ -131,8 +131,8 @@ void *ref_create(int dim, int nNodes, const double *xyz, const int *nodeMarker,
             else throwError("unsupported boundary node count");
         }
         m.createNeighborInfos();
-        if (p2) {  // quadratic elements: the reference's own refinement
-            Mesh m2 = m.createP2();
+        if (p2) {  // 1: quadratic elements, 2: uniform H2 refinement (the reference's own)
+            Mesh m2 = p2 == 2 ? m.createH2() : m.createP2();
             h->mesh = m2;
             h->mesh.createNeighborInfos();
         }

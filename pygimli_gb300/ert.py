@@ -95,6 +95,10 @@ class ERTModelling:
         self._elec_nodes = None
         self._last_model = None
         self._precond = {"jacobi": 0, "fsai": 1}[precond]
+        # forward-mesh refinement applied by setMesh(mesh) without
+        # ignoreRegionManager (MeshModelling, pygimli/frameworks/modelling.py:584-586)
+        self._refineH2 = True
+        self._refineP2 = False
         self.setSolverTolerance(rtol, maxIter)
         self.setPrecision(precision)
 
@@ -145,9 +149,28 @@ class ERTModelling:
     def complex(self):
         return False
 
-    def setMesh(self, mesh, ignoreRegionManager=True):
+    def createRefinedFwdMesh(self, mesh):
+        """Forward mesh of a parameter mesh: H2 refinement, then P2, as
+        enabled by ``_refineH2`` / ``_refineP2``
+        (pygimli/frameworks/modelling.py:682-699).  Refined cells keep their
+        parent's marker, so the model stays one value per parameter."""
+        m = mesh
+        if self._refineH2:
+            m = m.createH2()
+        if self._refineP2:
+            m = m.createP2()
+        return m
+
+    def setMesh(self, mesh, ignoreRegionManager=False):
+        """Set the mesh.  ``ignoreRegionManager=True`` solves on ``mesh``
+        itself; otherwise the forward mesh is ``createRefinedFwdMesh(mesh)``
+        and the cell markers of ``mesh`` are the parameter indices (the
+        region manager's own marker bookkeeping -- background and single
+        regions -- is not provided)."""
         if not isinstance(mesh, Mesh):
             raise TypeError("mesh must be a pygimli_gb300.mesh.Mesh")
+        if not ignoreRegionManager:
+            mesh = self.createRefinedFwdMesh(mesh)
         surf, topo = surface_info(mesh)
         if topo:
             raise NotImplementedError("meshes with topography need numerical primary potentials (not supported)")

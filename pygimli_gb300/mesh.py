@@ -65,10 +65,8 @@ class Mesh:
             boundary_cells = find_boundary_cells(self.cells[:, :nv1], self.boundaries[:, :self.dim_],
                                                  len(self.nodes))
         self.boundary_cells = np.ascontiguousarray(np.asarray(boundary_cells, dtype=np.int32))
-        if self.order == 1:
-            self._fix_orientation()
-        else:
-            self._check_orientation()
+        if np.any(self._signed_sizes() == 0):
+            raise ValueError("degenerate cell in mesh")
 
     # -- reference-style accessors (core/src/mesh.h:331-351) --------------
     def dim(self):
@@ -101,11 +99,6 @@ class Mesh:
     def findNodesIdxByMarker(self, marker):
         return np.nonzero(self.node_markers == marker)[0]
 
-    def _check_orientation(self):
-        d = self._signed_sizes()
-        if np.any(d <= 0):
-            raise ValueError("P2 cells must be positively oriented (orient the P1 mesh before createP2)")
-
     def _signed_sizes(self):
         p = self.nodes[self.cells[:, :self.dim_ + 1]]
         if self.dim_ == 2:
@@ -121,6 +114,10 @@ class Mesh:
         """Quadratic mesh, see create_p2."""
         return create_p2(self)
 
+    def createH2(self):
+        """Uniformly refined mesh, see create_h2."""
+        return create_h2(self)
+
     def cellSizes(self):
         """Cell areas (2-D) or volumes (3-D), positive."""
         p = self.nodes[self.cells[:, :self.dim_ + 1]]
@@ -135,26 +132,6 @@ class Mesh:
 
     def cellCenters(self):
         return self.nodes[self.cells[:, :self.dim_ + 1]].mean(axis=1)
-
-    def _fix_orientation(self):
-        """Make every simplex positively oriented (the element matrices use
-        absolute sizes, so this only normalises the input)."""
-        p = self.nodes[self.cells]
-        if self.dim_ == 2:
-            a = p[:, 1, :2] - p[:, 0, :2]
-            b = p[:, 2, :2] - p[:, 0, :2]
-            det = a[:, 0] * b[:, 1] - a[:, 1] * b[:, 0]
-            flip = det < 0
-            self.cells[flip, 1], self.cells[flip, 2] = self.cells[flip, 2].copy(), self.cells[flip, 1].copy()
-        else:
-            a = p[:, 1] - p[:, 0]
-            b = p[:, 2] - p[:, 0]
-            c = p[:, 3] - p[:, 0]
-            det = np.einsum("ij,ij->i", a, np.cross(b, c))
-            flip = det < 0
-            self.cells[flip, 2], self.cells[flip, 3] = self.cells[flip, 3].copy(), self.cells[flip, 2].copy()
-        if np.any(det == 0):
-            raise ValueError("degenerate cell in mesh")
 
     def save(self, path):
         np.savez_compressed(path, dim=self.dim_, nodes=self.nodes, cells=self.cells,
@@ -190,50 +167,91 @@ def _marker_mid(m0, m1):
     return m1 if m0 == m1 else 0
 
 
-def create_p2(mesh):
-    """Quadratic (P2) mesh with the node numbering of Mesh::createP2
-    (core/src/mesh.cpp:1284-1288, createRefined_ 1315-1600): the P1 nodes keep
-    their ids; a midpoint node is created for every edge at its first use,
-    walking the cells in order and each cell's edges in Tetrahedron10
-    (Zienkiewicz) / Triangle6 order, then the boundaries.  Cell markers become
-    the P1 cell index (createRefined_ passes the cell index as marker);
-    boundary markers are kept."""
-    if mesh.order != 1:
-        raise ValueError("mesh is already quadratic")
+def _edge_midpoints(mesh, pairs_c, pairs_b):
+    """Node ids of the midpoints of the edge pairs, created in order of first
+    use (Mesh::createRefinementNode_, core/src/mesh.cpp:1301-1313): new
+    nodes, their markers (markerT) and the ids of the cell / boundary pairs."""
     n0 = mesh.nodeCount()
-    edges = _TET10_EDGES if mesh.dim() == 3 else _TRI6_EDGES
-    cells = mesh.cells.astype(np.int64)
-    C = len(cells)
-    # candidate midpoints in creation order: cells (edge order), then boundaries
-    pairs_c = np.stack([cells[:, [a for a, _ in edges]], cells[:, [b for _, b in edges]]], axis=2)
-    pairs_c = pairs_c.reshape(-1, 2)
-    bnd = mesh.boundaries.astype(np.int64)
-    if mesh.dim() == 3:
-        bedges = ((0, 1), (1, 2), (2, 0))
-    else:
-        bedges = ((0, 1),)
-    pairs_b = np.stack([bnd[:, [a for a, _ in bedges]], bnd[:, [b for _, b in bedges]]], axis=2).reshape(-1, 2)
     pairs = np.concatenate([pairs_c, pairs_b])
     key = np.minimum(pairs[:, 0], pairs[:, 1]) * n0 + np.maximum(pairs[:, 0], pairs[:, 1])
     uniq, first, inv = np.unique(key, return_index=True, return_inverse=True)
-    order = np.argsort(first, kind="stable")        # unique edges in creation order
+    order = np.argsort(first, kind="stable")
     rank = np.empty(len(uniq), np.int64)
     rank[order] = np.arange(len(uniq))
-    mid_id = n0 + rank[inv]                          # node id of every candidate
+    mid_id = n0 + rank[inv]
     ea = pairs[first[order], 0]
     eb = pairs[first[order], 1]
     mids = 0.5 * (mesh.nodes[ea] + mesh.nodes[eb])
     nm = mesh.node_markers
     mid_markers = np.array([_marker_mid(int(nm[a]), int(nm[b])) for a, b in zip(ea, eb)], np.int32)
+    return mids, mid_markers, mid_id[:len(pairs_c)], mid_id[len(pairs_c):]
+
+
+# H2 children in terms of the Tetrahedron10 nodes (core/src/mesh.cpp:1399-1406)
+_TET_H2 = ((4, 6, 5, 0), (4, 5, 6, 9), (7, 9, 4, 1), (7, 4, 9, 5),
+           (8, 7, 5, 2), (8, 5, 7, 9), (6, 9, 8, 3), (6, 8, 9, 5))
+# ... and of the Triangle6 nodes (mesh.cpp:1357-1362)
+_TRI_H2 = ((0, 3, 5), (1, 4, 3), (2, 5, 4), (3, 4, 5))
+
+
+def create_h2(mesh):
+    """Uniform refinement (every cell split into 4 triangles / 8 tetrahedra)
+    with the node, cell and boundary numbering of Mesh::createH2
+    (core/src/mesh.cpp:1278-1283, createRefined_): children follow their
+    parent in cell order and inherit its marker; boundary edges / faces are
+    split into 2 / 4 with the parent's marker.  pyGIMLi uses this as the
+    forward mesh of a parameter mesh (pygimli/frameworks/modelling.py:586,
+    682-699)."""
+    if mesh.order != 1:
+        raise ValueError("H2 refinement of a quadratic mesh is not supported")
+    edges = _TET10_EDGES if mesh.dim() == 3 else _TRI6_EDGES
+    cells = mesh.cells.astype(np.int64)
+    C = len(cells)
+    pairs_c = np.stack([cells[:, [a for a, _ in edges]], cells[:, [b for _, b in edges]]], axis=2).reshape(-1, 2)
+    bnd = mesh.boundaries.astype(np.int64)
+    bedges = ((0, 1), (1, 2), (2, 0)) if mesh.dim() == 3 else ((0, 1),)
+    pairs_b = np.stack([bnd[:, [a for a, _ in bedges]], bnd[:, [b for _, b in bedges]]], axis=2).reshape(-1, 2)
+    mids, mid_markers, cm, bm = _edge_midpoints(mesh, pairs_c, pairs_b)
+    full = np.concatenate([cells, cm.reshape(C, len(edges))], axis=1)
+    children = _TET_H2 if mesh.dim() == 3 else _TRI_H2
+    cells2 = full[:, np.array(children)].reshape(-1, mesh.dim() + 1)
+    markers2 = np.repeat(mesh.cell_markers, len(children))
+    bfull = np.concatenate([bnd, bm.reshape(len(bnd), len(bedges))], axis=1)
+    if mesh.dim() == 3:
+        bnd2 = bfull[:, np.array(_TRI_H2)].reshape(-1, 3)
+        bmk = np.repeat(mesh.boundary_markers, 4)
+    else:
+        bnd2 = bfull[:, np.array(((0, 2), (2, 1)))].reshape(-1, 2)
+        bmk = np.repeat(mesh.boundary_markers, 2)
     nodes = np.concatenate([mesh.nodes, mids])
-    node_markers = np.concatenate([nm, mid_markers])
-    ne = len(edges)
-    cell_mid = mid_id[:C * ne].reshape(C, ne)
-    cells2 = np.concatenate([cells, cell_mid], axis=1).astype(np.int32)
-    nb = len(bedges)
-    bnd_mid = mid_id[C * ne:].reshape(len(bnd), nb)
-    bnd2 = np.concatenate([bnd, bnd_mid], axis=1).astype(np.int32)
-    return Mesh(mesh.dim(), nodes, cells2, np.arange(C, dtype=np.int32), node_markers, bnd2,
+    node_markers = np.concatenate([mesh.node_markers, mid_markers])
+    return Mesh(mesh.dim(), nodes, cells2.astype(np.int32), markers2, node_markers, bnd2.astype(np.int32), bmk)
+
+
+def create_p2(mesh):
+    """Quadratic (P2) mesh with the node numbering of Mesh::createP2
+    (core/src/mesh.cpp:1284-1288, createRefined_ 1315-1600): the P1 nodes keep
+    their ids; a midpoint node is created for every edge at its first use,
+    walking the cells in order and each cell's edges in Tetrahedron10
+    (Zienkiewicz) / Triangle6 order, then the boundaries.  Every cell keeps
+    its marker (createRefined_ maps the parent marker onto the new cells);
+    boundary markers are kept."""
+    if mesh.order != 1:
+        raise ValueError("mesh is already quadratic")
+    edges = _TET10_EDGES if mesh.dim() == 3 else _TRI6_EDGES
+    cells = mesh.cells.astype(np.int64)
+    C = len(cells)
+    # candidate midpoints in creation order: cells (edge order), then boundaries
+    pairs_c = np.stack([cells[:, [a for a, _ in edges]], cells[:, [b for _, b in edges]]], axis=2).reshape(-1, 2)
+    bnd = mesh.boundaries.astype(np.int64)
+    bedges = ((0, 1), (1, 2), (2, 0)) if mesh.dim() == 3 else ((0, 1),)
+    pairs_b = np.stack([bnd[:, [a for a, _ in bedges]], bnd[:, [b for _, b in bedges]]], axis=2).reshape(-1, 2)
+    mids, mid_markers, cm, bm = _edge_midpoints(mesh, pairs_c, pairs_b)
+    nodes = np.concatenate([mesh.nodes, mids])
+    node_markers = np.concatenate([mesh.node_markers, mid_markers])
+    cells2 = np.concatenate([cells, cm.reshape(C, len(edges))], axis=1).astype(np.int32)
+    bnd2 = np.concatenate([bnd, bm.reshape(len(bnd), len(bedges))], axis=1).astype(np.int32)
+    return Mesh(mesh.dim(), nodes, cells2, mesh.cell_markers.copy(), node_markers, bnd2,
                 mesh.boundary_markers.copy(), mesh.boundary_cells.copy())
 
 

@@ -4,8 +4,9 @@ into oracle/_ref/libgimli_ref.so and driven through oracle/ref_driver.py).
 
 Run from the repository root after ``make -C oracle``:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [fixture names ...]
 
+(no names: all fixtures).
 Each fixture holds the inputs (mesh arrays, sensors, ABMN, geometric
 factors, resistivity) and the reference outputs: wavenumbers/weights, the
 assembled system matrices (CSR), primary potentials, sub-potentials,
@@ -39,9 +40,15 @@ def _resistivity(mesh, seed):
     return rho
 
 
-def case(name, mesh, data, seed, threads=1, p2=False):
+def case(name, mesh, data, seed, threads=1, p2=False, h2=False):
+    """One fixture.  With p2 / h2 the reference refines the given mesh itself
+    (Mesh::createP2 / Mesh::createH2); the resistivity stays one value per
+    cell of the given mesh and reaches the refined cells through their
+    markers (the parent's cell index)."""
+    if only and name not in only:
+        return
     R = RefModelling(mesh, data.sensorPositions(), data.abmn(), data["k"], threads=threads,
-                     keep_matrices=True, p2=p2)
+                     keep_matrices=True, p2=p2, h2=h2)
     k, w = R.kw()
     rho = _resistivity(mesh, seed)
     rhoa = R.response(rho)
@@ -54,9 +61,12 @@ def case(name, mesh, data, seed, threads=1, p2=False):
     rp = np.stack([mats[i][0] for i in kidx])
     ci = np.stack([mats[i][1] for i in kidx])
     va = np.stack([mats[i][2] for i in kidx])
-    rho1 = np.ones(mesh.cellCount())
     xyz_r, nm_r, cells_r, cm_r, bnd_r, bm_r = R.mesh_arrays()
+    rho1 = np.ones(len(cells_r))
     src_center = xyz_r[R.electrode_nodes()].mean(axis=0)
+    # boundaries of the refined mesh: the reference appends the new ones
+    # after those created from the input boundaries
+    nb_r = mesh.boundaryCount() * (1 if not h2 else (4 if mesh.dim() == 3 else 2))
     S1 = np.stack([R.assemble(rho1, k[i], src_center)[2] for i in kidx])
     np.savez_compressed(
         os.path.join(OUT, name + ".npz"),
@@ -66,9 +76,9 @@ def case(name, mesh, data, seed, threads=1, p2=False):
         sensors=data.sensorPositions(), abmn=data.abmn(), kfac=data["k"],
         kfac_ref=R.geometric_factors(), rho=rho, k=k, w=w, rhoa=rhoa,
         electrode_nodes=R.electrode_nodes(), kidx=kidx, rowptr=rp[0], colidx=ci[0], S=va, S1=S1,
-        primary=prim, subpot=sub, J=J, p2=int(p2), ref_nodes=xyz_r, ref_cells=cells_r,
-        ref_node_markers=nm_r, ref_cell_markers=cm_r, ref_boundaries=bnd_r[:mesh.boundaryCount()],
-        ref_boundary_markers=bm_r[:mesh.boundaryCount()])
+        primary=prim, subpot=sub, J=J, p2=2 if h2 else int(p2), ref_nodes=xyz_r, ref_cells=cells_r,
+        ref_node_markers=nm_r, ref_cell_markers=cm_r, ref_boundaries=bnd_r[:nb_r],
+        ref_boundary_markers=bm_r[:nb_r])
     R.close()
     print(name, mesh, len(data), "k:", len(k), "J:", J.shape)
 
@@ -93,8 +103,12 @@ def bessel_table():
     print("bessel_quadrature", len(x))
 
 
+only = set(sys.argv[1:])
+
+
 def main():
-    bessel_table()
+    if not only or "bessel_quadrature" in only:
+        bessel_table()
     # 2.5-D: 11 electrodes, dipole-dipole
     xs = np.arange(11.0)
     m2 = create_para_mesh_2d(xs, para_dx=0.5, para_depth=4.0)
@@ -128,6 +142,10 @@ def main():
     d2p = createData(xs7, "dd")
     d2p["k"] = geometricFactors(d2p, 2)
     case("ert2d_p2_small", m2p, d2p, seed=15, p2=True)
+    # uniform refinement, the default forward mesh of pyGIMLi's mesh-based
+    # modelling (one parameter per parent cell)
+    case("ert2d_h2_small", m2p, d2p, seed=16, h2=True)
+    case("ert3d_h2_small", m3p, d3p, seed=17, h2=True)
 
 
 if __name__ == "__main__":

@@ -46,7 +46,7 @@ def fop_for(mesh, data, k=None, w=None, form=None, **kw):
         fop.setkValues(k)
         fop.setWeights(w)
     fop.setData(data)
-    fop.setMesh(mesh)
+    fop.setMesh(mesh, ignoreRegionManager=True)
     return fop
 
 
@@ -54,8 +54,10 @@ def load_case(golden_dir, name):
     z = np.load(os.path.join(golden_dir, name + ".npz"))
     mesh = Mesh(int(z["dim"]), z["nodes"], z["cells"], z["cell_markers"], z["node_markers"],
                 z["boundaries"], z["boundary_markers"], z["boundary_cells"])
-    if int(z["p2"]):
+    if int(z["p2"]) == 1:
         mesh = mesh.createP2()
+    elif int(z["p2"]) == 2:
+        mesh = mesh.createH2()
     data = DataContainerERT(z["sensors"], z["abmn"])
     data.set("k", z["kfac"])
     return z, mesh, data
@@ -66,7 +68,8 @@ def rel(a, b):
 
 
 @pytest.mark.parametrize("precision", list(FORMS))
-@pytest.mark.parametrize("name", ["ert2d_small", "ert2d_pd_wa", "ert3d_small", "ert3d_p2_small", "ert2d_p2_small"])
+@pytest.mark.parametrize("name", ["ert2d_small", "ert2d_pd_wa", "ert3d_small", "ert3d_p2_small", "ert2d_p2_small",
+                                  "ert2d_h2_small", "ert3d_h2_small"])
 def test_golden_parity(torch, golden_dir, name, precision):
     z, mesh, data = load_case(golden_dir, name)
     fop = fop_for(mesh, data, form=precision)
@@ -213,6 +216,28 @@ def test_error_paths(torch, golden_dir):
     fop.setSolverTolerance(1e-10, 20000)
     r = fop.response(z["rho"])
     assert np.max(np.abs(r - z["rhoa"]) / z["rhoa"]) <= TOL_POT
+
+
+@pytest.mark.parametrize("name", ["ert2d_h2_small", "ert3d_h2_small"])
+def test_forward_mesh_refinement(torch, golden_dir, name):
+    """setMesh(parameter mesh) solves on its H2 refinement (the default of
+    pyGIMLi's mesh-based modelling) with one parameter per parent cell."""
+    from pygimli_gb300 import ERTModelling
+    z = np.load(os.path.join(golden_dir, name + ".npz"))
+    para = Mesh(int(z["dim"]), z["nodes"], z["cells"], z["cell_markers"], z["node_markers"],
+                z["boundaries"], z["boundary_markers"], z["boundary_cells"])
+    data = DataContainerERT(z["sensors"], z["abmn"])
+    data.set("k", z["kfac"])
+    fop = ERTModelling(precision="mixed", precond="fsai")
+    fop.setData(data)
+    fop.setMesh(para)
+    assert fop.mesh().cellCount() == para.cellCount() * (4 if para.dim() == 2 else 8)
+    assert fop.parameterCount == para.cellCount()
+    rhoa = fop.response(z["rho"])
+    assert float(np.max(np.abs(rhoa - z["rhoa"]) / z["rhoa"])) <= TOL_POT
+    J = fop.createJacobian(z["rho"]).cpu().numpy()
+    assert J.shape == z["J"].shape
+    assert float(np.linalg.norm(J - z["J"]) / np.linalg.norm(z["J"])) <= TOL_J
 
 
 def _jacobian_rows_from_potentials(mesh, data, k, w, u, model, rows):

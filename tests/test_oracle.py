@@ -16,22 +16,26 @@ from pygimli_gb300.ert import search_electrodes, surface_info
 from pygimli_gb300.kwave import gauss_laguerre, gauss_legendre, init_kwave_list
 from pygimli_gb300.mesh import Mesh
 
-CASES = ["ert2d_small", "ert2d_pd_wa", "ert3d_small", "ert3d_p2_small", "ert2d_p2_small"]
+CASES = ["ert2d_small", "ert2d_pd_wa", "ert3d_small", "ert3d_p2_small", "ert2d_p2_small", "ert2d_h2_small",
+         "ert3d_h2_small"]
 
 
 def load_case(golden_dir, name):
-    """Mesh of a fixture: the stored P1 mesh, refined with create_p2 for the
-    quadratic cases (the reference ran its own Mesh::createP2)."""
+    """Mesh of a fixture: the stored P1 mesh, refined with create_p2 / create_h2
+    for the refined cases (the reference ran its own Mesh::createP2 /
+    Mesh::createH2)."""
     z = np.load(os.path.join(golden_dir, name + ".npz"))
     mesh = Mesh(int(z["dim"]), z["nodes"], z["cells"], z["cell_markers"], z["node_markers"],
                 z["boundaries"], z["boundary_markers"], z["boundary_cells"])
-    if int(z["p2"]):
+    if int(z["p2"]) == 1:
         mesh = mesh.createP2()
+    elif int(z["p2"]) == 2:
+        mesh = mesh.createH2()
     return z, mesh
 
 
-@pytest.mark.parametrize("name", ["ert3d_p2_small", "ert2d_p2_small"])
-def test_create_p2_matches_reference(golden_dir, name):
+@pytest.mark.parametrize("name", ["ert3d_p2_small", "ert2d_p2_small", "ert2d_h2_small", "ert3d_h2_small"])
+def test_refinement_matches_reference(golden_dir, name):
     z, mesh = load_case(golden_dir, name)
     assert np.array_equal(mesh.nodes, z["ref_nodes"])
     assert np.array_equal(mesh.cells, z["ref_cells"])
@@ -78,13 +82,14 @@ def test_oracle_matches_reference(golden_dir, name):
     # CSR pattern: bit-exact
     assert np.array_equal(P.rowptr, z["rowptr"]) and np.array_equal(P.cols, z["colidx"])
     rho = z["rho"]
+    rho_cell = O.map_model(mesh, rho)
     for j, ki in enumerate(z["kidx"]):
-        S = P.assemble(rho, ki)
-        S1 = P.assemble(np.ones_like(rho), ki)
+        S = P.assemble(rho_cell, ki)
+        S1 = P.assemble(np.ones_like(rho_cell), ki)
         assert np.max(np.abs(S - z["S"][j])) <= 1e-12 * np.max(np.abs(z["S"][j]))
         assert np.max(np.abs(S1 - z["S1"][j])) <= 1e-12 * np.max(np.abs(z["S1"][j]))
         assert np.max(np.abs(P.up[ki] - z["primary"][j])) <= 1e-13 * np.max(np.abs(z["primary"][j]))
-    rhoa, u = P.response(rho)
+    rhoa, u = P.response(rho_cell)
     assert np.max(np.abs(rhoa - z["rhoa"]) / z["rhoa"]) < 1e-10
     assert np.max(np.abs(u - z["subpot"])) <= 1e-10 * np.max(np.abs(z["subpot"]))
     J = P.jacobian(u, rho)
