@@ -36,8 +36,16 @@ typedef enum {
 
 /* Preconditioners of the block PCG.  JACOBI: diagonal.  FSAI: factorized
  * sparse approximate inverse M^-1 = G^T G, G lower triangular on A's pattern
- * (mixed precision only; columns that stall finish with FP64 Jacobi). */
-typedef enum { ERTGB_PRECOND_JACOBI = 0, ERTGB_PRECOND_FSAI = 1 } ertgb_precond;
+ * (mixed precision only; columns that stall finish with FP64 Jacobi).
+ * LEARNED: M^-1 = G^T G with G emitted by a message-passing network on the
+ * graph of A (weights: ertgb_set_precond_weights), same pattern, same
+ * application and the same FP64 Jacobi fallback as FSAI. */
+typedef enum { ERTGB_PRECOND_JACOBI = 0, ERTGB_PRECOND_FSAI = 1, ERTGB_PRECOND_LEARNED = 2 } ertgb_precond;
+
+/* Length of the learned preconditioner's FP32 parameter vector: encoders
+ * (2 x (64x4 + 64)), 4 layers of (W1 64x192, b1 64, W2 64x128, b2 64) and the
+ * decoder (wo 64, bo, wd 64, bd), in that order. */
+#define ERTGB_LP_NPARAM 83202
 
 /* Arithmetic of the block PCG.  FP64: everything in FP64.  MIXED: FP32
  * recurrence (operator, preconditioner, vectors) with FP64 reliable updates
@@ -192,6 +200,36 @@ int ertgb_csr_spmm_dot_noalloc(int64_t n, int64_t nnz, const int32_t *rowptr_dev
  * n_data x n_param doubles for ERTGB_KERNEL_JACOBIAN (else unused). */
 int ertgb_profile_kernel(ertgb_ctx *ctx, int kernel, int reps, void *J_scratch_dev, double *ms_per_launch,
                          double *bytes_per_launch, double *flops_per_launch);
+
+/* ---- learned preconditioner (no counterpart in the reference, which
+ * factors every system with CHOLMOD: core/src/bert/dcfemmodelling.cpp:2199-2210).
+ * The network runs on the system matrices of the context. */
+
+/* Network weights used by ERTGB_PRECOND_LEARNED (host, ERTGB_LP_NPARAM floats). */
+int ertgb_set_precond_weights(ertgb_ctx *ctx, const float *theta_host, int64_t n);
+
+/* Assemble the system matrices of every wavenumber for a per-cell
+ * resistivity (device) without solving: the training data of the network. */
+int ertgb_assemble(ertgb_ctx *ctx, const double *rho_cell_dev, void *stream);
+
+/* Network factor of the current matrices (device weights): G values in the
+ * row-major order of A's lower triangle, n_k x n_lower floats (G_dev may be
+ * NULL). */
+int ertgb_lp_forward(ertgb_ctx *ctx, const float *theta_dev, float *G_dev, void *stream);
+
+/* Training loss (Kaporin's condition number of G A G^T, mean over the
+ * wavenumbers; host scalar) and, if grad_dev is not NULL, its gradient in the
+ * weights (device, ERTGB_LP_NPARAM floats, overwritten). */
+int ertgb_lp_loss_grad(ertgb_ctx *ctx, const float *theta_dev, float *grad_dev, double *loss_host, void *stream);
+
+/* One Adam step on device vectors (gradient clipped to norm clip if clip > 0;
+ * step counts from 1). */
+int ertgb_lp_adam(float *theta_dev, const float *grad_dev, float *m_dev, float *v_dev, int64_t n, double lr,
+                  double beta1, double beta2, double eps, int step, double clip, void *stream);
+
+/* Network input features of the current matrices: node features n_k x n x 4,
+ * edge features n_k x nnz x 4 (device; either may be NULL). */
+int ertgb_lp_features(ertgb_ctx *ctx, float *x_dev, float *f_dev, void *stream);
 
 #ifdef __cplusplus
 }

@@ -59,7 +59,15 @@ SIGNATURES = {
     "ertgb_csr_spmm_dot_noalloc": (_ci, [_i64, _i64, _vp, _vp, _vp, _ci, _ci, _i64, _vp, _vp, _vp, _vp]),
     "ertgb_profile_kernel": (_ci, [_vp, _ci, _ci, _vp, ctypes.POINTER(_d), ctypes.POINTER(_d),
                                    ctypes.POINTER(_d)]),
+    "ertgb_set_precond_weights": (_ci, [_vp, _vp, _i64]),
+    "ertgb_assemble": (_ci, [_vp, _vp, _vp]),
+    "ertgb_lp_forward": (_ci, [_vp, _vp, _vp, _vp]),
+    "ertgb_lp_loss_grad": (_ci, [_vp, _vp, _vp, ctypes.POINTER(_d), _vp]),
+    "ertgb_lp_adam": (_ci, [_vp, _vp, _vp, _vp, _i64, _d, _d, _d, _d, _ci, _d, _vp]),
+    "ertgb_lp_features": (_ci, [_vp, _vp, _vp, _vp]),
 }
+
+LP_NPARAM = 83202
 
 _lib = None
 

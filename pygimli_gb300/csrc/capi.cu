@@ -52,6 +52,7 @@ void invalidate_derived(Context &c) {
     c.prim_ready = false;
     c.s1_ready = false;
     c.have_pot = false;
+    c.have_S = false;
 }
 
 // Join the caller's stream into the context stream and back.
@@ -136,8 +137,9 @@ int do_response(Context &c, const double *rho, double *rhoa, void *stream) {
     c.d_r.alloc((size_t)m.n * c.Rpad);
     build_rhs(c, s);
     ERTGB_CUDA(cudaEventRecord(c.ev[2], s));
+    c.have_S = true;
     if (c.precision != ERTGB_PRECISION_MIXED && c.precond != ERTGB_PRECOND_JACOBI)
-        throw Error(ERTGB_BAD_INPUT, "the FSAI preconditioner needs mixed precision");
+        throw Error(ERTGB_BAD_INPUT, "the FSAI and learned preconditioners need mixed precision");
     status = (c.precision == ERTGB_PRECISION_MIXED) ? pcg_solve_mixed(c, s) : pcg_solve(c, s);
     ERTGB_CUDA(cudaEventRecord(c.ev[3], s));
     finish_potentials(c, s);
@@ -223,6 +225,7 @@ int ertgb_set_mesh(ertgb_ctx *ctx, int dim, int order, int n_nodes, const double
         ERTGB_CUDA(cudaSetDevice(c->device));
         c->mesh.~MeshData();  // release the previous mesh's device buffers
         new (&c->mesh) MeshData();
+        c->lp.graph_ready = false;
         MeshData &m = c->mesh;
         m.dim = dim;
         m.order = order;
@@ -386,7 +389,9 @@ int ertgb_set_solver(ertgb_ctx *ctx, double rtol, int max_iter, int precond) {
     return guard(c, [&] {
         ERTGB_REQUIRE(rtol > 0.0 && rtol < 1.0, "rtol must be in (0, 1)");
         ERTGB_REQUIRE(max_iter > 0, "max_iter must be positive");
-        ERTGB_REQUIRE(precond == ERTGB_PRECOND_JACOBI || precond == ERTGB_PRECOND_FSAI, "unknown preconditioner");
+        ERTGB_REQUIRE(precond == ERTGB_PRECOND_JACOBI || precond == ERTGB_PRECOND_FSAI ||
+                          precond == ERTGB_PRECOND_LEARNED,
+                      "unknown preconditioner");
         c->rtol = rtol;
         c->max_iter = max_iter;
         c->precond = precond;
@@ -480,6 +485,7 @@ int ertgb_get_matrix(ertgb_ctx *ctx, int k_index, int which, double *vals) {
         ERTGB_REQUIRE(k_index >= 0 && k_index < c->nK && vals, "bad k index");
         const DBuf<double> &src = which == 0 ? c->d_S : c->d_S1;
         if (src.n < (size_t)c->nK * c->mesh.nnz) throw Error(ERTGB_STATE, "matrix not assembled yet");
+        ERTGB_CUDA(cudaStreamSynchronize(c->stream));
         ERTGB_CUDA(cudaMemcpy(vals, src.p + (size_t)k_index * c->mesh.nnz, sizeof(double) * c->mesh.nnz,
                               cudaMemcpyDeviceToHost));
     });
@@ -558,6 +564,85 @@ int ertgb_profile_kernel(ertgb_ctx *ctx, int kernel, int reps, void *J_scratch, 
             case ERTGB_KERNEL_SPMM32: profile_spmm32(*c, reps, ms, bytes, flops); break;
             default: throw Error(ERTGB_BAD_INPUT, "unknown kernel id");
         }
+    });
+}
+
+int ertgb_set_precond_weights(ertgb_ctx *ctx, const float *theta, int64_t n) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        ERTGB_REQUIRE(theta && n == ERTGB_LP_NPARAM, "weights must be ERTGB_LP_NPARAM floats");
+        for (int64_t i = 0; i < n; ++i) ERTGB_REQUIRE(std::isfinite(theta[i]), "non-finite weight");
+        ERTGB_CUDA(cudaSetDevice(c->device));
+        c->lp.d_theta.upload(theta, (size_t)n, c->stream);
+        ERTGB_CUDA(cudaStreamSynchronize(c->stream));
+        c->lp.have_weights = true;
+    });
+}
+
+int ertgb_assemble(ertgb_ctx *ctx, const double *rho, void *stream) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        ERTGB_REQUIRE(rho, "null resistivity");
+        StreamJoin j(*c, stream);
+        ensure_derived(*c);
+        c->have_pot = false;
+        check_rho(*c, rho, c->stream);
+        c->d_S.alloc((size_t)c->nK * c->mesh.nnz);
+        assemble_all(*c, rho, c->d_S.p, c->stream);
+        c->have_S = true;
+        j.done();
+    });
+}
+
+int ertgb_lp_forward(ertgb_ctx *ctx, const float *theta, float *G, void *stream) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        ERTGB_REQUIRE(theta, "null weights");
+        if (!c->have_S) throw Error(ERTGB_STATE, "no assembled matrices (ertgb_assemble or a response first)");
+        StreamJoin j(*c, stream);
+        lp_forward(*c, theta, c->stream);
+        if (G)
+            ERTGB_CUDA(cudaMemcpyAsync(G, c->d_G32.p, (size_t)c->lp.nL * c->nK * sizeof(float),
+                                       cudaMemcpyDeviceToDevice, c->stream));
+        j.done();
+    });
+}
+
+int ertgb_lp_loss_grad(ertgb_ctx *ctx, const float *theta, float *grad, double *loss, void *stream) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        ERTGB_REQUIRE(theta && loss, "null weights or loss");
+        if (!c->have_S) throw Error(ERTGB_STATE, "no assembled matrices (ertgb_assemble or a response first)");
+        StreamJoin j(*c, stream);
+        *loss = lp_loss_grad(*c, theta, grad, c->stream);
+        j.done();
+    });
+}
+
+int ertgb_lp_adam(float *theta, const float *grad, float *m, float *v, int64_t n, double lr, double beta1,
+                  double beta2, double eps, int step, double clip, void *stream) {
+    try {
+        ERTGB_REQUIRE(theta && grad && m && v && n > 0, "null Adam vector");
+        ERTGB_REQUIRE(step >= 1 && lr > 0.0 && beta1 >= 0.0 && beta1 < 1.0 && beta2 >= 0.0 && beta2 < 1.0,
+                      "bad Adam hyper-parameters");
+        static thread_local DBuf<float> scratch;
+        scratch.alloc(1);
+        lp_adam(theta, grad, m, v, n, lr, beta1, beta2, eps, step, clip, scratch.p, (cudaStream_t)stream);
+        return ERTGB_OK;
+    } catch (Error &e) {
+        set_free_error(e.what());
+        return e.code;
+    }
+}
+
+int ertgb_lp_features(ertgb_ctx *ctx, float *x, float *f, void *stream) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        if (!c->have_S) throw Error(ERTGB_STATE, "no assembled matrices (ertgb_assemble or a response first)");
+        StreamJoin j(*c, stream);
+        lp_features(*c, x, f, c->stream);
+        ERTGB_CUDA(cudaStreamSynchronize(c->stream));
+        j.done();
     });
 }
 

@@ -99,6 +99,26 @@ struct JacTiles {
     int stage_cells = 0;  // cells whose potentials are staged at a time
 };
 
+// Learned preconditioner (learned.cu): graph of the system matrix, network
+// weights, activations of every layer and the training buffers.  bf16
+// tensors are stored as uint16_t.
+struct LPState {
+    bool graph_ready = false;
+    int64_t n = 0, E = 0, nL = 0;
+    int T1 = 0;                           // row-aligned edge tiles per matrix
+    int nKb = 0;                          // matrices the activation buffers hold
+    bool train_alloc = false;
+    DBuf<int32_t> d_erow, d_T, d_tile_row, d_LtoU;
+    DBuf<float> d_theta;                  // inference weights (ERTGB_LP_NPARAM)
+    bool have_weights = false;
+    DBuf<float> x, f, dsq, delta;
+    DBuf<uint16_t> h, e, z, a, y;         // (layers + 1) x rows x 64 / layers x rows x 64
+    DBuf<double> gA, kpart, kq;
+    DBuf<float> dh0, dh1, de, dXj, dhrow, da, ddelta, wpart, gnorm;
+    DBuf<uint16_t> dz;
+    DBuf<int32_t> err;
+};
+
 struct Context {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -161,9 +181,11 @@ struct Context {
     DBuf<double> d_U;             // nE x nE collected electrode potentials
     DBuf<double> d_rhoa;
     bool have_pot = false;
+    bool have_S = false;          // d_S holds the matrices of the current setup
     const double *d_rho_last = nullptr;  // resistivity of the last response (caller's buffer)
     DBuf<double> d_rho_tmp, d_model_tmp;
     DBuf<char> d_J_tmp;
+    LPState lp;
     ertgb_stats stats{};
 };
 
@@ -209,6 +231,13 @@ void build_jacobian_tiles(Context &c);
 void build_lower_pattern(MeshData &m);
 // fsai.cu
 void fsai_setup(Context &c, cudaStream_t s);
+// learned.cu
+void lp_setup(Context &c, cudaStream_t s);  // network G into d_G32 / d_GT32 (the solver's factor)
+void lp_forward(Context &c, const float *theta, cudaStream_t s);
+double lp_loss_grad(Context &c, const float *theta, float *grad, cudaStream_t s);
+void lp_features(Context &c, float *x, float *f, cudaStream_t s);
+void lp_adam(float *theta, const float *grad, float *m, float *v, int64_t n, double lr, double beta1,
+             double beta2, double eps, int step, double clip, float *gnorm_scratch, cudaStream_t s);
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 

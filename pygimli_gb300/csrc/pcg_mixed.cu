@@ -529,10 +529,13 @@ int pcg_solve_mixed(Context &c, cudaStream_t s) {
     ColState cs(c.d_active.p, Rpad);
     int32_t *active = cs.active, *iters = cs.iters, *nactive = cs.nactive;
     const double *b = c.d_r.p;  // the right-hand sides (FP64), kept for the true residual
-    const bool fsai = c.precond == ERTGB_PRECOND_FSAI;
+    const bool fsai = c.precond != ERTGB_PRECOND_JACOBI;  // FSAI or learned: the same G^T G application
     const int64_t nL = (int64_t)m.Lcolidx.size();
     if (fsai) {
-        fsai_setup(c, s);
+        if (c.precond == ERTGB_PRECOND_FSAI)
+            fsai_setup(c, s);
+        else
+            lp_setup(c, s);
         c.d_t32.alloc((size_t)n * Rpad);
         c.d_z32.alloc((size_t)n * Rpad);
     }

@@ -78,7 +78,7 @@ class ERTModelling:
     """ERT forward operator (singularity removal) on one GB300."""
 
     def __init__(self, sr=True, verbose=False, device=0, rtol=1e-10, maxIter=20000, precision="fp64",
-                 precond="jacobi"):
+                 precond="jacobi", weights=None):
         if not sr:
             raise NotImplementedError("only the singularity-removal operator (sr=True) is provided")
         self.verbose = verbose
@@ -94,13 +94,14 @@ class ERTModelling:
         self._J = None
         self._elec_nodes = None
         self._last_model = None
-        self._precond = {"jacobi": 0, "fsai": 1}[precond]
+        self._precond = 0
         # forward-mesh refinement applied by setMesh(mesh) without
         # ignoreRegionManager (MeshModelling, pygimli/frameworks/modelling.py:584-586)
         self._refineH2 = True
         self._refineP2 = False
         self.setSolverTolerance(rtol, maxIter)
         self.setPrecision(precision)
+        self.setPreconditioner(precond, weights)
 
     def setPrecision(self, precision):
         """Solver arithmetic: ``"fp64"`` or ``"mixed"`` (FP32 recurrence with
@@ -136,10 +137,25 @@ class ERTModelling:
         self._rtol, self._maxIter = float(rtol), int(maxIter)
         self._check(self._lib.ertgb_set_solver(self._ctx, self._rtol, self._maxIter, self._precond))
 
-    def setPreconditioner(self, precond):
-        """``"jacobi"`` or ``"fsai"`` (factorized sparse approximate inverse,
-        mixed precision only)."""
-        self._precond = {"jacobi": 0, "fsai": 1}[precond]
+    def setPreconditioner(self, precond, weights=None):
+        """``"jacobi"``, ``"fsai"`` (factorized sparse approximate inverse) or
+        ``"learned"`` (network-emitted factor; ``weights``: a
+        LearnedPreconditioner, a weight array or an .npz path).  FSAI and
+        learned need mixed precision; stalled columns finish with FP64 Jacobi."""
+        codes = {"jacobi": 0, "fsai": 1, "learned": 2}
+        if precond not in codes:
+            raise ValueError(f"precond must be one of {sorted(codes)}")
+        if weights is not None:
+            from .learned import LearnedPreconditioner
+            if isinstance(weights, str):
+                weights = LearnedPreconditioner.load(weights)
+            w = weights.weights if isinstance(weights, LearnedPreconditioner) else np.asarray(weights)
+            w = np.ascontiguousarray(w, np.float32)
+            self._check(self._lib.ertgb_set_precond_weights(self._ctx, _ptr(w), w.size))
+            self._have_weights = True
+        if precond == "learned" and not getattr(self, "_have_weights", False):
+            raise ValueError("the learned preconditioner needs weights")
+        self._precond = codes[precond]
         self._check(self._lib.ertgb_set_solver(self._ctx, self._rtol, self._maxIter, self._precond))
 
     def setComplex(self, c):
@@ -299,6 +315,59 @@ class ERTModelling:
         stream = torch.cuda.current_stream(rho.device).cuda_stream
         self._check(self._lib.ertgb_response(self._ctx, ctypes.c_void_p(rho.data_ptr()),
                                              ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream)))
+
+    # ------------------------------------------- learned preconditioner
+    def assemble(self, model):
+        """Assemble the system matrices of every wavenumber for ``model``
+        without solving (training data of the learned preconditioner)."""
+        self._ready()
+        torch = _torch()
+        dev = torch.device("cuda", self.device)
+        if isinstance(model, torch.Tensor) and model.is_cuda:
+            rho = model.to(torch.float64).contiguous()
+        else:
+            rho = torch.from_numpy(np.ascontiguousarray(self.mapERTModel(np.asarray(model, np.float64)))).to(dev)
+        if rho.numel() != self._mesh.cellCount():
+            raise ValueError("model does not match the mesh")
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        self._check(self._lib.ertgb_assemble(self._ctx, ctypes.c_void_p(rho.data_ptr()), ctypes.c_void_p(stream)))
+        self._assembled = rho  # keep the buffer alive until the stream has used it
+
+    def lpForward(self, theta):
+        """Network factor G of the assembled matrices for device weights
+        ``theta``: (n_k, n_lower) float32 tensor, A's lower triangle row-major."""
+        torch = _torch()
+        n, nnz, _, _ = self.sizes()
+        nL = (nnz + n) // 2
+        G = torch.empty((len(self._k), nL), dtype=torch.float32, device=theta.device)
+        stream = torch.cuda.current_stream(theta.device).cuda_stream
+        self._check(self._lib.ertgb_lp_forward(self._ctx, ctypes.c_void_p(theta.data_ptr()),
+                                               ctypes.c_void_p(G.data_ptr()), ctypes.c_void_p(stream)))
+        return G
+
+    def lpLossGrad(self, theta, grad=None):
+        """Kaporin loss of the assembled matrices (float) and, into ``grad``
+        (device tensor of the weights' size), its gradient."""
+        torch = _torch()
+        loss = ctypes.c_double()
+        stream = torch.cuda.current_stream(theta.device).cuda_stream
+        self._check(self._lib.ertgb_lp_loss_grad(
+            self._ctx, ctypes.c_void_p(theta.data_ptr()), None if grad is None else ctypes.c_void_p(grad.data_ptr()),
+            ctypes.byref(loss), ctypes.c_void_p(stream)))
+        return loss.value
+
+    def lpFeatures(self):
+        """Network inputs of the assembled matrices: node (n_k, n, 4) and edge
+        (n_k, nnz, 4) features (device tensors)."""
+        torch = _torch()
+        n, nnz, _, _ = self.sizes()
+        dev = torch.device("cuda", self.device)
+        x = torch.empty((len(self._k), n, 4), dtype=torch.float32, device=dev)
+        f = torch.empty((len(self._k), nnz, 4), dtype=torch.float32, device=dev)
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        self._check(self._lib.ertgb_lp_features(self._ctx, ctypes.c_void_p(x.data_ptr()),
+                                                ctypes.c_void_p(f.data_ptr()), ctypes.c_void_p(stream)))
+        return x, f
 
     def createJacobian(self, model, dtype="float64"):
         """Jacobian d rhoa / d model from the potentials of the last response
