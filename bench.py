@@ -5,8 +5,12 @@ One step = one Gauss-Newton iteration's operator work: ``response(model)``
 (assembly, SR right-hand sides, multi-RHS PCG over all current sources,
 collect, apparent resistivities) followed by ``createJacobian(model)``
 (dense D x P Jacobian), on a seeded synthetic workload (default ``box_3d``:
-96 electrodes, 5336 data, ~486k tetrahedra, ~88k nodes, FP64 block PCG to a
-relative residual of 1e-10).
+96 electrodes, 5336 data, ~486k tetrahedra, ~88k nodes).  The headline form
+is the mixed-precision block PCG with the learned preconditioner (packaged
+weights trained for the workload) to an FP64 true relative residual of
+1e-10, with an FP32 Jacobian built from FP64 potential differences; the
+plain FP64 Jacobi block PCG (FP64 Jacobian) and the FSAI form are timed
+beside it on the same workload.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -47,8 +51,10 @@ def parse():
     ap.add_argument("--workload", choices=["box_3d", "box_3d_probe", "line_2d"], default="box_3d")
     ap.add_argument("--rtol", type=float, default=1e-10)
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
-    ap.add_argument("--precond", choices=["jacobi", "fsai"], default="fsai")
-    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 Jacobi comparison run")
+    ap.add_argument("--precond", choices=["jacobi", "fsai", "learned"], default="learned")
+    ap.add_argument("--weights", default=None, help="learned preconditioner weights (.npz); default: the "
+                    "packaged weights trained for the workload")
+    ap.add_argument("--no-plain", action="store_true", help="skip the comparison runs (plain FP64 Jacobi, FSAI)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
@@ -65,6 +71,11 @@ def workload(name):
         cfg = {"workload": f"{name}: 3-D, 96 electrodes (12x8 @4 m), {data.size()} ABMN, "
                            f"{mesh.nodeCount()} nodes, {mesh.cellCount()} tetrahedra, P1"}
     return mesh, data, rho, cfg
+
+
+def default_weights(name):
+    base = "box_3d" if name.startswith("box_3d") else name
+    return os.path.join(ROOT, "pygimli_gb300", "weights", base + ".npz")
 
 
 def dist_init(n):
@@ -195,7 +206,11 @@ def run_ours(args, world, rank, local):
     dev = torch.device("cuda", local)
     mesh, data, rho, cfg = workload(args.workload)
     t_setup = time.perf_counter()
-    fop = ERTModelling(device=local, rtol=args.rtol, precision=args.precision, precond=args.precond)
+    weights = None
+    if args.precond == "learned":
+        weights = args.weights or default_weights(args.workload)
+    fop = ERTModelling(device=local, rtol=args.rtol, precision=args.precision, precond=args.precond,
+                       weights=weights)
     fop.setData(data)
     fop.setMesh(mesh, ignoreRegionManager=True)
     setup_s = time.perf_counter() - t_setup
@@ -241,21 +256,21 @@ def run_ours(args, world, rank, local):
         total_ms = float(t.item())
     value = total_ms / 1e3 / (args.steps * world)
 
-    # the plain FP64 Jacobi PCG path (FP64 Jacobian) on the same workload, same timing
-    plain = None
-    if not args.no_plain and (args.precision, args.precond) != ("fp64", "jacobi"):
-        fop_p = ERTModelling(device=local, rtol=args.rtol, precision="fp64", precond="jacobi")
+    def time_form(precision, precond, jac_dtype, label):
+        """The same step with another solver form on the same workload (CUDA
+        events, up to 3 timed steps after 2 warm-up steps)."""
+        fop_p = ERTModelling(device=local, rtol=args.rtol, precision=precision, precond=precond)
         fop_p.setData(data)
         fop_p.setMesh(mesh, ignoreRegionManager=True)
-        Jp = torch.empty((D, P), dtype=torch.float64, device=dev)
+        Jp = torch.empty((D, P), dtype=torch.float64 if jac_dtype == 0 else torch.float32, device=dev)
+        rhoa_p = torch.empty(D, dtype=torch.float64, device=dev)
 
         def step_p():
             fop_p._response_dev(rho_d, rhoa_p)
             stream = torch.cuda.current_stream(dev).cuda_stream
             fop_p._check(L.ertgb_jacobian(fop_p._ctx, ctypes.c_void_p(rho_d.data_ptr()), C,
-                                          ctypes.c_void_p(Jp.data_ptr()), 0, ctypes.c_void_p(stream)))
+                                          ctypes.c_void_p(Jp.data_ptr()), jac_dtype, ctypes.c_void_p(stream)))
 
-        rhoa_p = torch.empty(D, dtype=torch.float64, device=dev)
         np_steps = max(1, min(args.steps, 3))
         for _ in range(max(1, min(args.warmup, 2))):
             step_p()
@@ -268,13 +283,21 @@ def run_ours(args, world, rank, local):
         f1.record()
         torch.cuda.synchronize()
         stp = fop_p.stats()
-        t_plain = f0.elapsed_time(f1) / 1e3 / np_steps
+        t_p = f0.elapsed_time(f1) / 1e3 / np_steps
         rel = float(torch.max(torch.abs(rhoa_d - rhoa_p) / torch.abs(rhoa_p)).item())
-        plain = {"value": t_plain, "unit": UNIT, "steps": np_steps, "solver": "block PCG (Jacobi), FP64",
-                 "jacobian": "FP64", "pcg_iterations": stp["iterations"], "ms_solve": stp["ms_solve"],
-                 "ms_jacobian": stp["ms_jacobian"], "speedup_of_value": t_plain / (total_ms / 1e3 / args.steps),
-                 "max_rel_diff_rhoa_vs_value_form": rel}
+        out = {"value": t_p, "unit": UNIT, "steps": np_steps, "solver": label,
+               "jacobian": "FP64" if jac_dtype == 0 else "FP32 (FP64 differences)",
+               "pcg_iterations": stp["iterations"], "ms_solve": stp["ms_solve"],
+               "ms_jacobian": stp["ms_jacobian"], "ratio_to_value": t_p / (total_ms / 1e3 / args.steps),
+               "max_rel_diff_rhoa_vs_value_form": rel}
         del Jp, fop_p
+        return out
+
+    plain = fsai_form = None
+    if not args.no_plain and (args.precision, args.precond) != ("fp64", "jacobi"):
+        plain = time_form("fp64", "jacobi", 0, "block PCG (Jacobi), FP64")
+    if not args.no_plain and args.precond == "learned":
+        fsai_form = time_form(args.precision, "fsai", jdt, f"block PCG (FSAI), {args.precision}")
 
     # roofline of the dominant kernel (CUDA events on the context stream)
     ms = ctypes.c_double()
@@ -344,7 +367,8 @@ def run_ours(args, world, rank, local):
                               rtol=args.rtol, l2="working set > L2: PCG blocks 4 x "
                               f"{mesh.nodeCount() * 96 * 8 / 1e6:.0f} MB, J {D * P * 8 / 1e9:.1f} GB"),
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-               "plain_fp64_gpu_pcg": plain,
+               "plain_fp64_gpu_pcg": plain, "fsai_form": fsai_form,
+               "learned_weights": os.path.relpath(weights, ROOT) if weights else None,
                "clocks": clk,
                "breakdown_ms": {"assemble": st["ms_assemble"], "rhs": st["ms_rhs"], "solve": st["ms_solve"],
                                 "collect": st["ms_collect"], "jacobian": st["ms_jacobian"],

@@ -117,80 +117,80 @@ __global__ void __launch_bounds__(256) k_spmm32_dot(int64_t n, int64_t nnz, int 
     }
 }
 
-// Single-matrix variant (nK = 1): every block owns a contiguous range of
-// rows (neighbour rows share their gathers of p through L1), each warp keeps
-// two rows in flight, and the (column, value) pairs of a row are loaded one
-// per lane and broadcast with shuffles, leaving the coalesced gathers of p
-// as the only dependent loads.
+// Single-matrix variant (nK = 1): an 8-lane group per matrix row, every lane
+// gathering CH float4 of the 32*CH columns of the chunk (coalesced 128-byte
+// segments per group), so a warp keeps four rows and, with the unrolled
+// nonzero loop, many gathers of p in flight.  Every block owns a contiguous
+// range of rows (neighbour rows share their gathers of p through L1).  The
+// column dots are summed per lane in FP32 and across the block's groups in
+// FP64, in a fixed order.
 // DOT: 0 = column dots p . q (the PCG operator), 1 = none, 2 = w . q.
+constexpr int kQThreads = 128;
+constexpr int kQGroups = kQThreads / 8;
+
 template <int CH, int DOT>
-__global__ void __launch_bounds__(256) k_spmm32_k1(int64_t n, int64_t Rpad, const int32_t *__restrict__ rowptr,
-                                                   const int32_t *__restrict__ colidx,
-                                                   const float *__restrict__ vals, const float *__restrict__ p,
-                                                   float *__restrict__ q, const float *__restrict__ w,
-                                                   double *__restrict__ part) {
-    __shared__ double red[kRows][32 * CH];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int64_t t0 = (int64_t)blockIdx.y * 32 * CH + lane;
+__global__ void __launch_bounds__(kQThreads, 4) k_spmm32_q(int64_t n, int64_t Rpad, const int32_t *__restrict__ rowptr,
+                                                           const int32_t *__restrict__ colidx,
+                                                           const float *__restrict__ vals, const float *__restrict__ p,
+                                                           float *__restrict__ q, const float *__restrict__ w,
+                                                           double *__restrict__ part) {
+    __shared__ float red[DOT == 1 ? 1 : kQGroups][DOT == 1 ? 1 : 32 * CH + 1];
+    const int l8 = threadIdx.x & 7, g = threadIdx.x >> 3;
+    const int64_t t0 = (int64_t)blockIdx.y * 32 * CH + l8 * 4;
     const int64_t per_block = (n + gridDim.x - 1) / gridDim.x;
     const int64_t r_begin = (int64_t)blockIdx.x * per_block;
     const int64_t r_end = min(n, r_begin + per_block);
-    float dot[CH];
+    float4 dot[CH];
 #pragma unroll
-    for (int j = 0; j < CH; j++) dot[j] = 0.f;
-    for (int64_t r0 = r_begin + 2 * wid; r0 < r_end; r0 += 2 * kRows) {
-        const bool two = r0 + 1 < r_end;
-        float a0[CH], a1[CH];
+    for (int j = 0; j < CH; j++) dot[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int64_t row = r_begin + g; row < r_end; row += kQGroups) {
+        float4 acc[CH];
 #pragma unroll
-        for (int j = 0; j < CH; j++) a0[j] = a1[j] = 0.f;
-        const int32_t s0 = rowptr[r0], s1 = rowptr[r0 + 1];
-        const int32_t s2 = two ? rowptr[r0 + 2] : s1;
-        const int len0 = s1 - s0, len1 = s2 - s1;
-        const int lmax = max(len0, len1);
-        for (int base = 0; base < lmax; base += 32) {
-            const int c0 = min(32, max(0, len0 - base)), c1 = min(32, max(0, len1 - base));
-            const int32_t mc0 = lane < c0 ? colidx[s0 + base + lane] : 0;
-            const float mv0 = lane < c0 ? vals[s0 + base + lane] : 0.f;
-            const int32_t mc1 = lane < c1 ? colidx[s1 + base + lane] : 0;
-            const float mv1 = lane < c1 ? vals[s1 + base + lane] : 0.f;
-            const int cm = max(c0, c1);
-#pragma unroll 2
-            for (int e = 0; e < cm; e++) {
-                const int64_t col0 = __shfl_sync(0xffffffffu, mc0, e);
-                const float v0 = __shfl_sync(0xffffffffu, mv0, e);
-                const int64_t col1 = __shfl_sync(0xffffffffu, mc1, e);
-                const float v1 = __shfl_sync(0xffffffffu, mv1, e);
-                const float *pc0 = p + col0 * Rpad + t0;
-                const float *pc1 = p + col1 * Rpad + t0;
-                if (e < c0) {
+        for (int j = 0; j < CH; j++) acc[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+        const int32_t s1 = rowptr[row + 1];
+#pragma unroll 4
+        for (int32_t s = rowptr[row]; s < s1; s++) {
+            const int64_t col = colidx[s];
+            const float v = vals[s];
+            const float4 *pc = reinterpret_cast<const float4 *>(p + col * Rpad + t0);
 #pragma unroll
-                    for (int j = 0; j < CH; j++) a0[j] = fmaf(v0, pc0[32 * j], a0[j]);
-                }
-                if (e < c1) {
-#pragma unroll
-                    for (int j = 0; j < CH; j++) a1[j] = fmaf(v1, pc1[32 * j], a1[j]);
-                }
+            for (int j = 0; j < CH; j++) {
+                const float4 x = __ldg(pc + 8 * j);
+                acc[j].x = fmaf(v, x.x, acc[j].x);
+                acc[j].y = fmaf(v, x.y, acc[j].y);
+                acc[j].z = fmaf(v, x.z, acc[j].z);
+                acc[j].w = fmaf(v, x.w, acc[j].w);
             }
         }
-        const float *dv = DOT == 2 ? w : p;
+        float4 *qr = reinterpret_cast<float4 *>(q + row * Rpad + t0);
 #pragma unroll
-        for (int j = 0; j < CH; j++) {
-            q[r0 * Rpad + t0 + 32 * j] = a0[j];
-            if (DOT != 1) dot[j] = fmaf(dv[r0 * Rpad + t0 + 32 * j], a0[j], dot[j]);
-            if (two) {
-                q[(r0 + 1) * Rpad + t0 + 32 * j] = a1[j];
-                if (DOT != 1) dot[j] = fmaf(dv[(r0 + 1) * Rpad + t0 + 32 * j], a1[j], dot[j]);
+        for (int j = 0; j < CH; j++) qr[8 * j] = acc[j];
+        if (DOT != 1) {
+            const float4 *dr = reinterpret_cast<const float4 *>((DOT == 2 ? w : p) + row * Rpad + t0);
+#pragma unroll
+            for (int j = 0; j < CH; j++) {
+                const float4 d = dr[8 * j];
+                dot[j].x = fmaf(d.x, acc[j].x, dot[j].x);
+                dot[j].y = fmaf(d.y, acc[j].y, dot[j].y);
+                dot[j].z = fmaf(d.z, acc[j].z, dot[j].z);
+                dot[j].w = fmaf(d.w, acc[j].w, dot[j].w);
             }
         }
     }
     if (DOT == 1) return;
 #pragma unroll
-    for (int j = 0; j < CH; j++) red[wid][lane + 32 * j] = (double)dot[j];
+    for (int j = 0; j < CH; j++) {
+        const int c = 32 * j + l8 * 4;
+        red[g][c] = dot[j].x;
+        red[g][c + 1] = dot[j].y;
+        red[g][c + 2] = dot[j].z;
+        red[g][c + 3] = dot[j].w;
+    }
     __syncthreads();
-    for (int c = threadIdx.x; c < 32 * CH; c += blockDim.x) {
+    for (int c = threadIdx.x; c < 32 * CH; c += kQThreads) {
         double s = 0.0;
 #pragma unroll
-        for (int w = 0; w < kRows; w++) s += red[w][c];
+        for (int gg = 0; gg < kQGroups; gg++) s += (double)red[gg][c];
         part[(int64_t)blockIdx.x * Rpad + (int64_t)blockIdx.y * 32 * CH + c] = s;
     }
 }
@@ -474,7 +474,7 @@ template <template <int> class F, typename... A> void dispatch_ch(int ch, A &&..
 template <int CH> struct SpmmL {
     static void go(dim3 g, cudaStream_t s, int64_t n, int64_t nnz, int nE, int nK, int64_t Rpad, const int32_t *rp,
                    const int32_t *ci, const float *v, const float *p, float *q, double *part) {
-        if (nK == 1) k_spmm32_k1<CH, 0><<<g, 256, 0, s>>>(n, Rpad, rp, ci, v, p, q, nullptr, part);
+        if (nK == 1) k_spmm32_q<CH, 0><<<g, kQThreads, 0, s>>>(n, Rpad, rp, ci, v, p, q, nullptr, part);
         else k_spmm32_dot<CH><<<g, 256, 0, s>>>(n, nnz, nE, nK, Rpad, rp, ci, v, p, q, part);
     }
 };
@@ -483,8 +483,8 @@ template <int CH> struct GenL {
     static void go(dim3 g, cudaStream_t s, int64_t n, int64_t nnzB, int nE, int nK, int64_t Rpad, const int32_t *rp,
                    const int32_t *ci, const float *v, const float *x, float *y, const float *w, double *part) {
         if (nK == 1) {
-            if (w) k_spmm32_k1<CH, 2><<<g, 256, 0, s>>>(n, Rpad, rp, ci, v, x, y, w, part);
-            else k_spmm32_k1<CH, 1><<<g, 256, 0, s>>>(n, Rpad, rp, ci, v, x, y, w, part);
+            if (w) k_spmm32_q<CH, 2><<<g, kQThreads, 0, s>>>(n, Rpad, rp, ci, v, x, y, w, part);
+            else k_spmm32_q<CH, 1><<<g, kQThreads, 0, s>>>(n, Rpad, rp, ci, v, x, y, w, part);
         } else if (w) {
             k_spmm32_gen<CH, true><<<g, 256, 0, s>>>(n, nnzB, nE, nK, Rpad, rp, ci, v, x, y, w, part);
         } else {

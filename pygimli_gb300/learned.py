@@ -88,12 +88,18 @@ class LearnedPreconditioner:
         return obj
 
     # ----------------------------------------------------------- training
-    def train(self, fop, models, steps, lr=1e-3, clip=1.0, betas=(0.9, 0.999), eps=1e-8, log_every=0):
+    def train(self, fop, models, steps, lr=1e-3, clip=1.0, betas=(0.9, 0.999), eps=1e-8, log_every=0,
+              tasks=None, lr_final=None):
         """Adam on Kaporin's number over ``models`` (per-cell or per-parameter
         resistivities of ``fop``'s mesh), cycling through them for ``steps``
         steps; every step assembles one model's matrices (all wavenumbers).
-        Returns the list of (step, loss)."""
+        ``tasks`` = [(fop, models), ...] trains over several meshes in turn
+        (then ``fop`` and ``models`` are ignored).  The learning rate decays
+        geometrically to ``lr_final`` (default: constant).  Returns the list of
+        (step, loss)."""
         torch = _torch()
+        tasks = tasks if tasks is not None else [(fop, models)]
+        fop = tasks[0][0]
         dev = torch.device("cuda", fop.device)
         theta = torch.from_numpy(self.weights.copy()).to(dev)
         grad = torch.zeros_like(theta)
@@ -102,13 +108,16 @@ class LearnedPreconditioner:
         lib = _native.load()
         hist = []
         t0 = time.time()
+        decay = 1.0 if not lr_final else (lr_final / lr) ** (1.0 / max(1, steps - 1))
         for step in range(1, steps + 1):
-            fop.assemble(models[(step - 1) % len(models)])
+            fop, models = tasks[(step - 1) % len(tasks)]
+            fop.assemble(models[((step - 1) // len(tasks)) % len(models)])
             loss = fop.lpLossGrad(theta, grad)
+            lr_s = lr * decay ** (step - 1)
             stream = torch.cuda.current_stream(dev).cuda_stream
             _native.check(None, lib.ertgb_lp_adam(ctypes.c_void_p(theta.data_ptr()), ctypes.c_void_p(grad.data_ptr()),
                                                   ctypes.c_void_p(m.data_ptr()), ctypes.c_void_p(v.data_ptr()),
-                                                  NPARAM, lr, betas[0], betas[1], eps, step, clip,
+                                                  NPARAM, lr_s, betas[0], betas[1], eps, step, clip,
                                                   ctypes.c_void_p(stream)))
             hist.append((step, loss))
             if log_every and step % log_every == 0:

@@ -74,12 +74,25 @@ def prolongate_empty_cells(mesh, vals, background=-9e99):
         vals[upd] = vsum[upd] / wsum[upd]
 
 
+def _marker_count(mesh):
+    """Number of distinct non-negative cell markers (O(cells), cached for the
+    mesh's current marker array)."""
+    mk = mesh.cell_markers
+    cached = getattr(mesh, "_marker_count_cache", None)
+    if cached is not None and cached[0] is mk:
+        return cached[1]
+    pos = mk[mk >= 0]
+    cnt = int(np.count_nonzero(np.bincount(pos))) if len(pos) else 0
+    mesh._marker_count_cache = (mk, cnt)
+    return cnt
+
+
 def map_model(mesh, model, background=-9e99):
     """Per-cell resistivity for ``model`` (per cell or per marker)."""
     model = np.asarray(model, dtype=np.float64)
     mk = mesh.cell_markers
     C = mesh.cellCount()
-    if len(model) == C and len(np.unique(mk[mk > -1])) != len(model):
+    if len(model) == C and _marker_count(mesh) != len(model):
         return model.copy()
     att = np.zeros(C)
     pos = mk >= 0

@@ -52,3 +52,35 @@ def box_3d(seed=7, nx=12, ny=8, spacing=4.0, scheme="full", **mesh_kw):
         inside = np.sum(((c - ctr) / ax) ** 2, axis=1) <= 1.0
         rho[inside] = val
     return mesh, data, rho
+
+
+def random_models(mesh, count, seed=0, n_blocks=(1, 4), contrast=(1e2, 1e5)):
+    """Training / evaluation models on ``mesh``: log-normal background
+    (mu = ln 100, sigma = 1) plus 1-4 blocky inclusions (ellipsoids in 3-D,
+    rectangles in 2-D) whose resistivity sits a factor drawn log-uniformly in
+    ``contrast`` above or below the background median."""
+    rng = np.random.default_rng(seed)
+    c = mesh.cellCenters()
+    d = mesh.dim()
+    lo = np.percentile(c[:, :d], 5, axis=0)
+    hi = np.percentile(c[:, :d], 95, axis=0)
+    # the inclusions live in the upper part of the model (the para region)
+    depth_axis = d - 1
+    span = hi - lo
+    lo_in = lo.copy()
+    lo_in[depth_axis] = hi[depth_axis] - 0.3 * span[depth_axis]
+    out = []
+    for _ in range(count):
+        rho = np.exp(rng.normal(np.log(100.0), 1.0, mesh.cellCount()))
+        for _ in range(int(rng.integers(n_blocks[0], n_blocks[1] + 1))):
+            ctr = rng.uniform(lo_in, hi)
+            ax = rng.uniform(0.03, 0.15, d) * span
+            f = 10 ** rng.uniform(np.log10(contrast[0]), np.log10(contrast[1])) ** 0.5
+            val = 100.0 * (f if rng.random() < 0.5 else 1.0 / f)
+            if d == 3:
+                inside = np.sum(((c - ctr) / ax) ** 2, axis=1) <= 1.0
+            else:
+                inside = np.all(np.abs(c[:, :2] - ctr) <= ax, axis=1)
+            rho[inside] = val
+        out.append(rho)
+    return out
