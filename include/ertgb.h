@@ -231,6 +231,36 @@ int ertgb_lp_adam(float *theta_dev, const float *grad_dev, float *m_dev, float *
  * edge features n_k x nnz x 4 (device; either may be NULL). */
 int ertgb_lp_features(ertgb_ctx *ctx, float *x_dev, float *f_dev, void *stream);
 
+/* ---- batches of independent problems (one context each) -------------- */
+
+/* Tile shape chosen by the batch autotuner, its candidates, and the work of
+ * the last batched response. */
+typedef struct {
+    int32_t rows_per_tile;    /* matrix rows per tile                         */
+    int32_t rhs_width;        /* right-hand-side columns per operator tile    */
+    int32_t n_candidates;     /* shapes timed (0 when the shape was cached)   */
+    int32_t cached;           /* 1: shape reused from an earlier identical batch */
+    int32_t cand_rows[16], cand_width[16];
+    double cand_ms[16];       /* operator time of every candidate             */
+    int64_t spmm_tiles, vector_tiles, columns;
+    int32_t iterations;       /* batched PCG iterations (all problems)        */
+    int32_t stalled_columns;  /* columns finished by their problem's FP64 PCG */
+    int64_t launches;         /* kernel launches of the batched iterations    */
+    double ms_assemble, ms_solve, ms_collect;
+} ertgb_batch_info;
+
+/* Apparent resistivities of n independent problems in one batched solve.
+ * Every context needs mesh, electrodes, wavenumbers and scheme set; rho_dev[i]
+ * is problem i's per-cell resistivity and rhoa_dev[i] its output (device).
+ * Assembly, right-hand sides and collection run per problem; the linear
+ * systems of all problems (all sources x wavenumbers) are solved together by
+ * the mixed-precision block PCG (Jacobi, FP64 reliable updates, FP64 true
+ * residual to each context's rtol; stalled columns finish in FP64), whose
+ * kernels each cover every problem in one launch.  The potentials stay in
+ * each context (ertgb_jacobian works afterwards).  info may be NULL. */
+int ertgb_batch_response(ertgb_ctx *const *ctxs, int n, const double *const *rho_dev, double *const *rhoa_dev,
+                         ertgb_batch_info *info, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

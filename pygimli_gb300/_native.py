@@ -31,6 +31,17 @@ class Stats(ctypes.Structure):
                 ("stalled_columns", ctypes.c_int32)]
 
 
+class BatchInfo(ctypes.Structure):
+    _fields_ = [("rows_per_tile", ctypes.c_int32), ("rhs_width", ctypes.c_int32),
+                ("n_candidates", ctypes.c_int32), ("cached", ctypes.c_int32),
+                ("cand_rows", ctypes.c_int32 * 16), ("cand_width", ctypes.c_int32 * 16),
+                ("cand_ms", ctypes.c_double * 16), ("spmm_tiles", ctypes.c_int64),
+                ("vector_tiles", ctypes.c_int64), ("columns", ctypes.c_int64),
+                ("iterations", ctypes.c_int32), ("stalled_columns", ctypes.c_int32),
+                ("launches", ctypes.c_int64), ("ms_assemble", ctypes.c_double),
+                ("ms_solve", ctypes.c_double), ("ms_collect", ctypes.c_double)]
+
+
 # name -> (restype, argtypes)
 _vp, _i32, _i64, _d = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_double
 _ci = ctypes.c_int
@@ -65,6 +76,7 @@ SIGNATURES = {
     "ertgb_lp_loss_grad": (_ci, [_vp, _vp, _vp, ctypes.POINTER(_d), _vp]),
     "ertgb_lp_adam": (_ci, [_vp, _vp, _vp, _vp, _i64, _d, _d, _d, _d, _ci, _d, _vp]),
     "ertgb_lp_features": (_ci, [_vp, _vp, _vp, _vp]),
+    "ertgb_batch_response": (_ci, [_vp, _ci, _vp, _vp, ctypes.POINTER(BatchInfo), _vp]),
 }
 
 LP_NPARAM = 83202

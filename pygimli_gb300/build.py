@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libertgb.so")
-SOURCES = ["setup.cpp", "assemble.cu", "pcg.cu", "pcg_mixed.cu", "fsai.cu", "jacobian.cu", "capi.cu", "noalloc.cu", "learned.cu"]
+SOURCES = ["setup.cpp", "assemble.cu", "pcg.cu", "pcg_mixed.cu", "fsai.cu", "jacobian.cu", "capi.cu", "noalloc.cu", "learned.cu", "batch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-strict-aliasing"]
 
@@ -51,7 +51,7 @@ def build(verbose=False, extra=()):
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         list(ex.map(lambda so: _compile(so[0], so[1], list(extra)), zip(SOURCES, objs)))
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), "-shared", *ARCH, "-o", tmp, *objs]
+    cmd = [nvcc(), "-shared", *ARCH, "-o", tmp, *objs, "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

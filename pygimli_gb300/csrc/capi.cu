@@ -95,7 +95,7 @@ void ensure_derived(Context &c) {
     ERTGB_CUDA(cudaSetDevice(c.device));
     if (!c.prim_ready) {
         c.R = (int64_t)c.nE * c.nK;
-        c.Rpad = ceil_div(c.R, 32) * 32;
+        c.Rpad = ceil_div(c.R, c.rhs_align) * c.rhs_align;
         compute_boundary_alpha(c);
         compute_primary(c);
         c.prim_ready = true;
@@ -644,6 +644,78 @@ int ertgb_lp_features(ertgb_ctx *ctx, float *x, float *f, void *stream) {
         ERTGB_CUDA(cudaStreamSynchronize(c->stream));
         j.done();
     });
+}
+
+int ertgb_batch_response(ertgb_ctx *const *ctxs, int n, const double *const *rho, double *const *rhoa,
+                         ertgb_batch_info *info, void *stream) {
+    try {
+        ERTGB_REQUIRE(ctxs && rho && rhoa && n > 0, "empty batch");
+        std::vector<Context *> cs((size_t)n);
+        for (int i = 0; i < n; i++) {
+            cs[i] = reinterpret_cast<Context *>(ctxs[i]);
+            ERTGB_REQUIRE(cs[i] && rho[i] && rhoa[i], "null context or buffer in the batch");
+            ERTGB_REQUIRE(cs[i]->device == cs[0]->device, "all problems of a batch must be on one device");
+            for (int j = 0; j < i; j++) ERTGB_REQUIRE(cs[j] != cs[i], "a context appears twice in the batch");
+        }
+        Context &c0 = *cs[0];
+        ERTGB_CUDA(cudaSetDevice(c0.device));
+        for (Context *c : cs) {
+            if (c->rhs_align != 128) {
+                c->rhs_align = 128;
+                invalidate_derived(*c);
+            }
+            ensure_derived(*c);
+        }
+        // derived data (primary potentials, boundary terms, unit matrices) is
+        // built on each context's stream; the batch runs on the first one
+        for (Context *c : cs) ERTGB_CUDA(cudaStreamSynchronize(c->stream));
+        StreamJoin j(c0, stream);
+        cudaStream_t s = c0.stream;
+        ertgb_batch_info local{};
+        ertgb_batch_info *inf = info ? info : &local;
+        std::memset(inf, 0, sizeof(*inf));
+        ERTGB_CUDA(cudaEventRecord(c0.ev[0], s));
+        for (int i = 0; i < n; i++) {
+            Context &c = *cs[i];
+            c.have_pot = false;
+            c.stats = ertgb_stats{};
+            check_rho(c, rho[i], s);
+            c.d_rho_last = rho[i];
+            c.d_S.alloc((size_t)c.nK * c.mesh.nnz);
+            assemble_all(c, rho[i], c.d_S.p, s);
+            compute_source_rho(c, rho[i], s);
+            c.d_r.alloc((size_t)c.mesh.n * c.Rpad);
+            build_rhs(c, s);
+            c.have_S = true;
+        }
+        ERTGB_CUDA(cudaEventRecord(c0.ev[1], s));
+        int stalled = 0;
+        const int status = batch_solve(cs, s, inf, &stalled);
+        inf->stalled_columns = stalled;
+        ERTGB_CUDA(cudaEventRecord(c0.ev[2], s));
+        for (int i = 0; i < n; i++) {
+            finish_potentials(*cs[i], s);
+            collect_response(*cs[i], rhoa[i], s);
+        }
+        ERTGB_CUDA(cudaEventRecord(c0.ev[3], s));
+        ERTGB_CUDA(cudaEventSynchronize(c0.ev[3]));
+        inf->ms_assemble = elapsed(c0, 0, 1);
+        inf->ms_solve = elapsed(c0, 1, 2);
+        inf->ms_collect = elapsed(c0, 2, 3);
+        for (Context *c : cs) c->have_pot = status == ERTGB_OK;
+        j.done();
+        if (status != ERTGB_OK) {
+            set_free_error("batched solve did not converge within max_iter");
+            return status;
+        }
+        return ERTGB_OK;
+    } catch (Error &e) {
+        set_free_error(e.what());
+        return e.code;
+    } catch (std::exception &e) {
+        set_free_error(e.what());
+        return ERTGB_BAD_INPUT;
+    }
 }
 
 }  // extern "C"

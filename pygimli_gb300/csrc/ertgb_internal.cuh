@@ -157,6 +157,7 @@ struct Context {
     int max_iter = 20000;
     int precond = ERTGB_PRECOND_JACOBI;
     int precision = ERTGB_PRECISION_FP64;
+    int rhs_align = 32;           // Rpad granularity (batches use 128)
     // derived per (mesh, electrodes, kw)
     int64_t R = 0, Rpad = 0;     // right-hand sides nK*nE, padded to 32
     bool prim_ready = false;
@@ -204,6 +205,8 @@ void check_rho(Context &c, const double *rho_cell, cudaStream_t s);
 // pcg.cu
 // mask: warm start (x kept) on the columns with mask[t] != 0; nullptr = cold start, all columns
 int pcg_solve(Context &c, cudaStream_t s, const int32_t *mask = nullptr);
+// allocate pcg_solve's workspaces ahead (no allocation inside a later solve)
+void pcg_prepare(Context &c);
 // pcg_mixed.cu
 int pcg_solve_mixed(Context &c, cudaStream_t s);
 void profile_spmm32(Context &c, int reps, double *ms, double *bytes, double *flops);
@@ -231,6 +234,8 @@ void build_jacobian_tiles(Context &c);
 void build_lower_pattern(MeshData &m);
 // fsai.cu
 void fsai_setup(Context &c, cudaStream_t s);
+// batch.cu: batched mixed-precision PCG over the contexts' assembled systems
+int batch_solve(std::vector<Context *> &cs, cudaStream_t s, ertgb_batch_info *info, int *stalled);
 // learned.cu
 void lp_setup(Context &c, cudaStream_t s);  // network G into d_G32 / d_GT32 (the solver's factor)
 void lp_forward(Context &c, const float *theta, cudaStream_t s);

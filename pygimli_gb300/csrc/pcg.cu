@@ -302,6 +302,14 @@ void launch_spmm(int ch, dim3 grid, cudaStream_t s, int64_t n, int64_t nnz, int 
 
 }  // namespace
 
+void pcg_prepare(Context &c) {
+    const int64_t n = c.mesh.n, Rpad = c.Rpad;
+    const int NB = (int)std::min<int64_t>(ceil_div(n, kRowsPerBlock), kPartRows);
+    c.d_p.alloc((size_t)n * Rpad);
+    c.d_q.alloc((size_t)n * Rpad);
+    c.d_part.alloc((size_t)NB * Rpad * 3);
+}
+
 int pcg_solve(Context &c, cudaStream_t s, const int32_t *mask) {
     MeshData &m = c.mesh;
     const int64_t n = m.n, Rpad = c.Rpad, R = c.R;

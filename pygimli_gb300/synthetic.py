@@ -84,3 +84,37 @@ def random_models(mesh, count, seed=0, n_blocks=(1, 4), contrast=(1e2, 1e5)):
             rho[inside] = val
         out.append(rho)
     return out
+
+
+def batch_2d(n_problems=64, seed=3, nodes=(2000, 60000), electrodes=(24, 72)):
+    """Independent 2.5-D problems for the batched solver: node counts drawn
+    log-uniformly in ``nodes``, 24-72 electrodes at 1 m, dipole-dipole plus
+    Wenner data, log-normal resistivity (mu = ln 100, sigma = 1) with a 10 and
+    a 1000 Ohm m rectangle.  Returns a list of (mesh, data, rho)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_problems):
+        target = float(np.exp(rng.uniform(np.log(nodes[0]), np.log(nodes[1]))))
+        ne = int(rng.integers(electrodes[0], electrodes[1] + 1))
+        xs = np.arange(float(ne))
+        depth = ne / 4.0
+        n2 = create_para_mesh_2d(xs, para_dx=0.5, para_depth=depth).nodeCount()
+        n4 = create_para_mesh_2d(xs, para_dx=0.25, para_depth=depth).nodeCount()
+        slope = (n4 - n2) / 2.0  # nodes grow affinely in 1 / para_dx
+        k = max(1, int(round(2 + (target - n2) / slope)))
+        mesh = create_para_mesh_2d(xs, para_dx=1.0 / k, para_depth=depth)
+        while k > 1 and mesh.nodeCount() > 1.1 * nodes[1]:
+            k -= 1
+            mesh = create_para_mesh_2d(xs, para_dx=1.0 / k, para_depth=depth)
+        dd = createData(xs, "dd")
+        wa = createData(xs, "wa")
+        data = DataContainerERT(dd.sensorPositions(), np.vstack([dd.abmn(), wa.abmn()]))
+        data.set("k", geometricFactors(data, 2))
+        rho = np.exp(rng.normal(np.log(100.0), 1.0, mesh.cellCount()))
+        c = mesh.cellCenters()
+        for val in (10.0, 1000.0):
+            x0 = rng.uniform(0.15, 0.85) * (ne - 1)
+            z0 = -rng.uniform(0.1, 0.6) * depth
+            rho[(np.abs(c[:, 0] - x0) < 0.08 * ne) & (np.abs(c[:, 1] - z0) < 0.1 * depth)] = val
+        out.append((mesh, data, rho))
+    return out

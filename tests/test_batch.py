@@ -1,0 +1,81 @@
+"""Batched solve of independent problems (pygimli_gb300.batch): every
+problem's apparent resistivities and Jacobian equal those of its own FP64
+solve (potentials / rhoa <= 1e-6, Jacobian <= 1e-5 relative), one small
+problem is checked against the oracle, and the autotuner's choice is one of
+its timed candidates and is cached for an identical batch."""
+import numpy as np
+import pytest
+
+from oracle import ert_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL_POT = 1e-6
+TOL_J = 1e-5
+
+
+@pytest.fixture(scope="module")
+def torch():
+    t = pytest.importorskip("torch")
+    if not t.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from pygimli_gb300 import build
+    build.build()
+    return t
+
+
+def _fop(mesh, data, **kw):
+    from pygimli_gb300 import ERTModelling
+    f = ERTModelling(**kw)
+    f.setData(data)
+    f.setMesh(mesh, ignoreRegionManager=True)
+    return f
+
+
+def test_batch_matches_single_solves(torch):
+    from pygimli_gb300 import synthetic
+    from pygimli_gb300.batch import BatchedERTModelling
+    probs = synthetic.batch_2d(6, seed=11, nodes=(1500, 9000), electrodes=(12, 30))
+    singles = [_fop(m, d) for m, d, _ in probs]
+    ref = [f.response(r) for f, (_, _, r) in zip(singles, probs)]
+    Jref = [f.createJacobian(r).cpu().numpy() for f, (_, _, r) in zip(singles, probs)]
+    batch = BatchedERTModelling([_fop(m, d, precision="mixed") for m, d, _ in probs])
+    out = batch.response([r for _, _, r in probs])
+    info = batch.info
+    print({k: v for k, v in info.items() if k != "candidates"}, info["candidates"])
+    for i, (o, r) in enumerate(zip(out, ref)):
+        e = float(np.max(np.abs(o - r) / r))
+        assert e <= TOL_POT, (i, e)
+    J = batch.createJacobian([r for _, _, r in probs])
+    for i, (a, b) in enumerate(zip(J, Jref)):
+        assert np.linalg.norm(a.cpu().numpy() - b) <= TOL_J * np.linalg.norm(b), i
+    assert (info["rows_per_tile"], info["rhs_width"]) in [(c[0], c[1]) for c in info["candidates"]]
+    assert info["spmm_tiles"] > 0 and info["columns"] % 128 == 0
+    # smallest problem against the oracle
+    i = int(np.argmin([m.nodeCount() for m, _, _ in probs]))
+    m, d, r = probs[i]
+    f = batch.fops[i]
+    P = O.Problem(m, d.sensorPositions(), d.abmn(), d["k"], f.kValues(), f.weights())
+    ro, _ = P.response(r)
+    assert float(np.max(np.abs(out[i] - ro) / ro)) <= TOL_POT
+    # an identical batch reuses the tuned shape
+    out2 = batch.response([r * 2.0 for _, _, r in probs])
+    assert batch.info["cached"]
+    for o2, o in zip(out2, out):
+        assert float(np.max(np.abs(o2 - 2.0 * o) / (2.0 * o))) <= TOL_POT
+
+
+def test_batch_errors(torch):
+    from pygimli_gb300 import synthetic
+    from pygimli_gb300.batch import BatchedERTModelling
+    (m, d, r), = synthetic.batch_2d(1, seed=2, nodes=(1500, 2500), electrodes=(12, 14))
+    f = _fop(m, d)
+    with pytest.raises(ValueError):
+        BatchedERTModelling([f, f])
+    b = BatchedERTModelling([f])
+    bad = r.copy()
+    bad[3] = -1.0
+    with pytest.raises(ValueError):
+        b.response([bad])
+    rr = b.response([r])[0]
+    assert np.all(np.isfinite(rr))
