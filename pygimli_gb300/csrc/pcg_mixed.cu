@@ -24,7 +24,7 @@ namespace {
 constexpr int kRows = 8;            // warps per block (spmm) / rows per block (vector kernels)
 constexpr int kGraphIters = 16;     // iterations per captured graph
 constexpr int kReliableEvery = 4;   // graphs between reliable updates (64 iterations)
-constexpr int kPartRows = 1216;  // 8 row blocks per SM: the FP32 kernels need more warps in flight
+constexpr int kPartRows = 304;  // 2 row blocks per SM: few partial rows keep the column finishes short
 
 
 __global__ void k_to_f32(int64_t n, const double *__restrict__ a, float *__restrict__ b) {
@@ -58,6 +58,7 @@ __global__ void k_m_init(int64_t n, int nE, int64_t R, int64_t Rpad, const float
     const float *dk = dinv + ki * n;
     float a = 0.f;
     double bb = 0.0;
+#pragma unroll 4
     for (int64_t row = (int64_t)blockIdx.y * kRows + threadIdx.y; row < n; row += (int64_t)gridDim.y * kRows) {
         const int64_t i = row * Rpad + t;
         const double bv = b[i];
@@ -125,11 +126,11 @@ __global__ void __launch_bounds__(256) k_spmm32_dot(int64_t n, int64_t nnz, int 
 // column dots are summed per lane in FP32 and across the block's groups in
 // FP64, in a fixed order.
 // DOT: 0 = column dots p . q (the PCG operator), 1 = none, 2 = w . q.
-constexpr int kQThreads = 128;
+constexpr int kQThreads = 256;
 constexpr int kQGroups = kQThreads / 8;
 
 template <int CH, int DOT>
-__global__ void __launch_bounds__(kQThreads, 4) k_spmm32_q(int64_t n, int64_t Rpad, const int32_t *__restrict__ rowptr,
+__global__ void __launch_bounds__(kQThreads, 2) k_spmm32_q(int64_t n, int64_t Rpad, const int32_t *__restrict__ rowptr,
                                                            const int32_t *__restrict__ colidx,
                                                            const float *__restrict__ vals, const float *__restrict__ p,
                                                            float *__restrict__ q, const float *__restrict__ w,
@@ -253,6 +254,7 @@ __global__ void k_m_update_yr(int64_t n, int64_t Rpad, const double *__restrict_
     const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
     if (!active[t]) return;
     const float alpha = (float)col[ALPHA * Rpad + t];
+#pragma unroll 4
     for (int64_t row = (int64_t)blockIdx.y * kRows + threadIdx.y; row < n; row += (int64_t)gridDim.y * kRows) {
         const int64_t i = row * Rpad + t;
         y[i] = fmaf(alpha, p[i], y[i]);
@@ -266,6 +268,7 @@ __global__ void k_m_update_pz(int64_t n, int64_t Rpad, const double *__restrict_
     const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
     if (!active[t]) return;
     const float beta = (float)col[BETA * Rpad + t];
+#pragma unroll 4
     for (int64_t row = (int64_t)blockIdx.y * kRows + threadIdx.y; row < n; row += (int64_t)gridDim.y * kRows) {
         const int64_t i = row * Rpad + t;
         p[i] = fmaf(beta, p[i], z[i]);
@@ -283,7 +286,8 @@ __global__ void k_m_update_xr(int64_t n, int nE, int64_t R, int64_t Rpad, const 
     const float *dk = dinv + ki * n;
     float a = 0.f, b = 0.f;
     if (act) {
-        for (int64_t row = (int64_t)blockIdx.y * kRows + threadIdx.y; row < n; row += (int64_t)gridDim.y * kRows) {
+    #pragma unroll 4
+    for (int64_t row = (int64_t)blockIdx.y * kRows + threadIdx.y; row < n; row += (int64_t)gridDim.y * kRows) {
             const int64_t i = row * Rpad + t;
             y[i] = fmaf(alpha, p[i], y[i]);
             const float rv = fmaf(-alpha, q[i], r[i]);
@@ -299,17 +303,16 @@ __global__ void k_m_update_xr(int64_t n, int nE, int64_t R, int64_t Rpad, const 
 __global__ void k_m_finish_beta(int64_t Rpad, int NB, const double *__restrict__ part_a,
                                 const double *__restrict__ part_b, double *__restrict__ col,
                                 const int32_t *__restrict__ active, int32_t *__restrict__ iters) {
-    __shared__ double ra[32][33], rb[32][33];
+    __shared__ double ra[32][33];
     const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
     const double rz = col_sum(part_a, NB, Rpad, t, ra);
-    const double rr = col_sum(part_b, NB, Rpad, t, rb);
+    (void)part_b;
     if (threadIdx.y != 0) return;
     if (!active[t]) {
         col[BETA * Rpad + t] = 0.0;
         return;
     }
     iters[t] += 1;
-    (void)rr;
     const double rho = col[RHO * Rpad + t];
     col[BETA * Rpad + t] = (rho != 0.0 && rz == rz) ? rz / rho : 0.0;
     col[RHO * Rpad + t] = rz;
@@ -323,6 +326,7 @@ __global__ void k_m_update_p(int64_t n, int nE, int64_t R, int64_t Rpad, const f
     const float beta = (float)col[BETA * Rpad + t];
     const int64_t ki = t < R ? t / nE : 0;
     const float *dk = dinv + ki * n;
+#pragma unroll 4
     for (int64_t row = (int64_t)blockIdx.y * kRows + threadIdx.y; row < n; row += (int64_t)gridDim.y * kRows) {
         const int64_t i = row * Rpad + t;
         p[i] = fmaf(beta, p[i], r[i] * dk[row]);
@@ -335,6 +339,7 @@ __global__ void k_m_accum(int64_t n, int64_t Rpad, const int32_t *__restrict__ a
     if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) *nactive = 0;
     const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
     if (!active[t]) return;
+#pragma unroll 4
     for (int64_t row = (int64_t)blockIdx.y * kRows + threadIdx.y; row < n; row += (int64_t)gridDim.y * kRows) {
         const int64_t i = row * Rpad + t;
         x[i] += (double)y[i];
@@ -553,6 +558,8 @@ int pcg_solve_mixed(Context &c, cudaStream_t s) {
     k_to_f32<<<(unsigned)std::min<int64_t>(ceil_div((int64_t)c.nK * n, 256), 65535), 256, 0, s>>>(
         (int64_t)c.nK * n, c.d_dinv.p, c.d_dinv32.p);
     const dim3 vb(32, kRows), vg((unsigned)(Rpad / 32), (unsigned)NB);
+    // vector updates without column partials (FSAI / learned form) are free to use more row blocks
+    const dim3 vgu((unsigned)(Rpad / 32), (unsigned)std::min<int64_t>(ceil_div(n, kRows), 4 * kPartRows));
     const dim3 sg((unsigned)NB, (unsigned)nchunk);
     const dim3 fb(32, 32), fg((unsigned)(Rpad / 32));
     const double rtol2 = c.rtol * c.rtol;
@@ -583,10 +590,10 @@ int pcg_solve_mixed(Context &c, cudaStream_t s) {
                                c.d_q32.p, part_c);
             pcg_finish_alpha(fg, fb, s, Rpad, NB, part_c, c.d_col.p, active, nactive);
             if (fsai) {
-                k_m_update_yr<<<vg, vb, 0, s>>>(n, Rpad, c.d_col.p, active, c.d_y32.p, c.d_r32.p, c.d_p32.p, c.d_q32.p);
+                k_m_update_yr<<<vgu, vb, 0, s>>>(n, Rpad, c.d_col.p, active, c.d_y32.p, c.d_r32.p, c.d_p32.p, c.d_q32.p);
                 apply_fsai(part_a);
                 k_m_finish_beta<<<fg, fb, 0, s>>>(Rpad, NB, part_a, part_a, c.d_col.p, active, iters);
-                k_m_update_pz<<<vg, vb, 0, s>>>(n, Rpad, c.d_col.p, active, c.d_z32.p, c.d_p32.p);
+                k_m_update_pz<<<vgu, vb, 0, s>>>(n, Rpad, c.d_col.p, active, c.d_z32.p, c.d_p32.p);
             } else {
                 k_m_update_xr<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, c.d_dinv32.p, c.d_col.p, active, c.d_y32.p,
                                                 c.d_r32.p, c.d_p32.p, c.d_q32.p, part_a, part_b);
