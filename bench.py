@@ -48,7 +48,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["box_3d", "box_3d_probe", "line_2d"], default="box_3d")
+    ap.add_argument("--workload", choices=["box_3d", "box_3d_probe", "box_3d_large", "box_3d_large_p2", "line_2d"],
+                    default="box_3d")
     ap.add_argument("--rtol", type=float, default=1e-10)
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
     ap.add_argument("--precond", choices=["jacobi", "fsai", "learned"], default="learned")
@@ -66,6 +67,11 @@ def workload(name):
         mesh, data, rho = synthetic.line_2d()
         cfg = {"workload": "line_2d: 2.5-D, 41 electrodes, 741 dipole-dipole, "
                            f"{mesh.nodeCount()} nodes, {mesh.cellCount()} triangles, 17 wavenumbers"}
+    elif name.startswith("box_3d_large"):
+        mesh, data, rho = synthetic.box_3d_large(p2=name.endswith("p2"))
+        cfg = {"workload": f"{name}: 3-D, 256 electrodes (16x16 @4 m), {data.size()} ABMN, "
+                           f"{mesh.nodeCount()} nodes, {mesh.cellCount()} tetrahedra, "
+                           f"{'P2' if name.endswith('p2') else 'P1'}"}
     else:
         mesh, data, rho = synthetic.box_3d(scheme="inline" if name == "box_3d_probe" else "full")
         cfg = {"workload": f"{name}: 3-D, 96 electrodes (12x8 @4 m), {data.size()} ABMN, "

@@ -191,17 +191,20 @@ def createData(elecs, schemeName="dd", **kwargs):
 
 
 def grid_line_scheme(electrode_grid, kind="dd", max_separation=999):
-    """Dipole-dipole / pole-dipole lines along x and along y of a rectangular
+    """Dipole-dipole / pole-dipole / Wenner lines along x and along y of a rectangular
     surface electrode grid ``electrode_grid`` (nx, ny) whose electrode index
     is ``ix * ny + iy``."""
     nx, ny = electrode_grid
     rows = []
     lines = [[ix * ny + iy for ix in range(nx)] for iy in range(ny)]
     lines += [[ix * ny + iy for iy in range(ny)] for ix in range(nx)]
-    gen = _scheme_dd if kind == "dd" else _scheme_pd
+    gens = {"dd": lambda m: _scheme_dd(m, (1,), max_separation),
+            "pd": lambda m: _scheme_pd(m, max_separation=max_separation),
+            "wa": lambda m: _scheme_wa(m, max_separation=max_separation)}
+    if kind not in gens:
+        raise ValueError(f"unknown line scheme {kind!r}")
     for line in lines:
-        loc = gen(len(line), max_separation=max_separation) if kind == "pd" else \
-            gen(len(line), (1,), max_separation)
+        loc = gens[kind](len(line))
         for (a, b, m, n) in loc:
             rows.append(tuple(line[i] if i >= 0 else -1 for i in (a, b, m, n)))
     return np.array(rows, np.int32).reshape(-1, 4)

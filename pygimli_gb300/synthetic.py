@@ -5,6 +5,10 @@ configurations (no field data is used anywhere):
              para mesh paraDX 0.25 / paraDepth 10 m (~3.6k nodes, ~6.8k
              triangles), resistivity log-uniform in [50, 200] Ohm m with a
              10 and a 1000 Ohm m rectangle.
+``box_3d_large`` 3-D, 256 electrodes on a 16 x 16 grid at 4 m, dipole-dipole +
+             pole-dipole + Wenner lines (~8k data), ~807k tetrahedra / ~145k nodes
+             (P1; ``p2=True`` refines the whole mesh with create_p2), resistivity
+             as ``box_3d``.
 ``box_3d``   3-D, 96 electrodes on a 12 x 8 grid at 4 m, 5336 dipole-dipole /
              pole-dipole / cross-line data, tetrahedral mesh of the para box
              padded to +-500 m (~88k nodes, ~486k tetrahedra), resistivity
@@ -19,6 +23,17 @@ import numpy as np
 
 from .data import DataContainerERT, createData, geometricFactors, grid_line_scheme, grid_scheme_3d
 from .mesh import create_box_mesh_3d, create_para_mesh_2d
+
+
+def box_3d_large(seed=8, p2=False):
+    nx = ny = 16
+    mesh, data, rho = box_3d(seed=seed, nx=nx, ny=ny, scheme="inline")
+    ab = np.vstack([grid_line_scheme((nx, ny), kind) for kind in ("dd", "pd", "wa")])
+    data = DataContainerERT(data.sensorPositions(), ab)
+    data.set("k", geometricFactors(data, 3))
+    if p2:
+        mesh = mesh.createP2()
+    return mesh, data, rho
 
 
 def line_2d(seed=1):
