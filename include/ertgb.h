@@ -261,6 +261,24 @@ typedef struct {
 int ertgb_batch_response(ertgb_ctx *const *ctxs, int n, const double *const *rho_dev, double *const *rhoa_dev,
                          ertgb_batch_info *info, void *stream);
 
+/* ---- Gauss-Newton model update ------------------------------------------ */
+
+/* The regularised CGLS of pyGIMLi's inversion step (solveCGLSCDWWhtrans,
+ * core/src/solver.cpp:27-212, called by RInversion::oneStep,
+ * core/src/inversion.cpp:249-372): solves for the transformed model update x
+ *   (Jt^T Wd^2 Jt + lambda (Wc C Wm)^T (Wc C Wm)) x = Jt^T Wd^2 b - lambda (Wc C Wm)^T rough
+ * with Jt = diag(td) J diag(1/tm), starting from x.  J: device D x P row-major,
+ * dtype 0 FP64 / 1 FP32 (as written by ertgb_jacobian).  C: n_constr x P CSR
+ * (FP64 values) and its transpose (P x n_constr CSR).  Every vector is a
+ * device FP64 array: dweight, b, td (D); x, wm, tm (P); wc, rough (n_constr).
+ * tol < 0: stop when ||r||^2 <= max(1e-12, 1e-8 ||r_0||^2) as the reference.
+ * iterations_out receives the CGLS iterations. */
+int ertgb_cgls(const void *J_dev, int dtype, int64_t n_data, int64_t n_model, int64_t n_constr,
+               const int32_t *c_rowptr, const int32_t *c_colidx, const double *c_vals, const int32_t *ct_rowptr,
+               const int32_t *ct_colidx, const double *ct_vals, const double *dweight, const double *b, double *x,
+               const double *wc, const double *wm, const double *tm, const double *td, double lambda,
+               const double *rough, int max_iter, double tol, int32_t *iterations_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

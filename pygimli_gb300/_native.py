@@ -77,6 +77,8 @@ SIGNATURES = {
     "ertgb_lp_adam": (_ci, [_vp, _vp, _vp, _vp, _i64, _d, _d, _d, _d, _ci, _d, _vp]),
     "ertgb_lp_features": (_ci, [_vp, _vp, _vp, _vp]),
     "ertgb_batch_response": (_ci, [_vp, _ci, _vp, _vp, ctypes.POINTER(BatchInfo), _vp]),
+    "ertgb_cgls": (_ci, [_vp, _ci, _i64, _i64, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                         _vp, _d, _vp, _ci, _d, ctypes.POINTER(_i32), _vp]),
 }
 
 LP_NPARAM = 83202

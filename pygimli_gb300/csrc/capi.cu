@@ -718,4 +718,25 @@ int ertgb_batch_response(ertgb_ctx *const *ctxs, int n, const double *const *rho
     }
 }
 
+int ertgb_cgls(const void *J, int dtype, int64_t D, int64_t P, int64_t NC, const int32_t *c_rp, const int32_t *c_ci,
+               const double *c_v, const int32_t *ct_rp, const int32_t *ct_ci, const double *ct_v, const double *dW,
+               const double *b, double *x, const double *wc, const double *wm, const double *tm, const double *td,
+               double lambda, const double *rough, int max_iter, double tol, int32_t *iters, void *stream) {
+    try {
+        ERTGB_REQUIRE(J && D > 0 && P > 0 && NC >= 0 && (dtype == 0 || dtype == 1), "bad CGLS sizes or dtype");
+        ERTGB_REQUIRE(dW && b && x && wm && tm && td && max_iter >= 0, "null CGLS vector");
+        ERTGB_REQUIRE(NC == 0 || (c_rp && c_ci && c_v && ct_rp && ct_ci && ct_v && wc && rough),
+                      "null constraint array");
+        int it = 0;
+        const int rc = cgls_solve(J, dtype, D, P, NC, c_rp, c_ci, c_v, ct_rp, ct_ci, ct_v, dW, b, x, wc, wm, tm, td,
+                                  lambda, rough, max_iter, tol, &it, (cudaStream_t)stream);
+        if (iters) *iters = it;
+        if (rc != ERTGB_OK) set_free_error("CGLS produced a non-finite residual");
+        return rc;
+    } catch (Error &e) {
+        set_free_error(e.what());
+        return e.code;
+    }
+}
+
 }  // extern "C"

@@ -236,6 +236,11 @@ void build_lower_pattern(MeshData &m);
 void fsai_setup(Context &c, cudaStream_t s);
 // batch.cu: batched mixed-precision PCG over the contexts' assembled systems
 int batch_solve(std::vector<Context *> &cs, cudaStream_t s, ertgb_batch_info *info, int *stalled);
+// cgls.cu: regularised Gauss-Newton update (all pointers device, vectors FP64)
+int cgls_solve(const void *J, int dtype, int64_t D, int64_t P, int64_t NC, const int32_t *c_rp, const int32_t *c_ci,
+               const double *c_v, const int32_t *ct_rp, const int32_t *ct_ci, const double *ct_v, const double *dW,
+               const double *b, double *x, const double *wc, const double *wm, const double *tm, const double *td,
+               double lambda, const double *rough, int max_iter, double tol, int *iters, cudaStream_t s);
 // learned.cu
 void lp_setup(Context &c, cudaStream_t s);  // network G into d_G32 / d_GT32 (the solver's factor)
 void lp_forward(Context &c, const float *theta, cudaStream_t s);
