@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the comparison runs (plain FP64 Jacobi, FSAI)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--gn", action="store_true", help="also time one full Gauss-Newton iteration per form "
+                    "(response, Jacobian, 200 CGLS iterations on the GPU, line-search responses)")
     return ap.parse_args()
 
 
@@ -200,6 +202,46 @@ def run_reference(args, world, rank):
                             "sample": desc},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
+
+
+def gn_iteration(args, mesh, data, rho, local, weights):
+    """Wall time of one Gauss-Newton iteration through the public API for the
+    headline form and the plain FP64 form: synthetic observations = response
+    of the workload model with 2 % noise, start = homogeneous median model."""
+    import torch
+    from pygimli_gb300.ert import ERTModelling
+    from pygimli_gb300.inversion import GaussNewton
+    out = {}
+    forms = {"headline": dict(precision=args.precision, precond=args.precond, weights=weights,
+                              jdt="float64" if args.precision == "fp64" else "float32"),
+             "plain_fp64": dict(precision="fp64", precond="jacobi", weights=None, jdt="float64")}
+    obs = None
+    for name, f in forms.items():
+        fop = ERTModelling(device=local, rtol=args.rtol, precision=f["precision"], precond=f["precond"],
+                           weights=f["weights"])
+        fop.setData(data)
+        fop.setMesh(mesh, ignoreRegionManager=True)
+        if obs is None:
+            obs = fop.response(rho) * (1.0 + 0.02 * np.random.default_rng(3).normal(size=data.size()))
+        gn = GaussNewton(fop, obs, np.full(data.size(), 0.02), lam=20.0, jacobian_dtype=f["jdt"])
+        model = np.full(mesh.cellCount(), float(np.median(obs)))
+        resp = fop.response(model)
+        gn.step(model, resp)  # warm-up (allocations, graph capture)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        resp = fop.response(model)
+        pcg_first = fop.stats()["iterations"]
+        _, _, info = gn.step(model, resp)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        out[name] = {"value": dt, "unit": UNIT, "pcg_iterations_first_response": pcg_first,
+                     "cgls_iterations": info["cgls_iterations"], "tau": info["tau"],
+                     "forward_responses": info["responses"] + 1, "phi_before": info["phi_before"],
+                     "phi_after": info["phi_after"]}
+        del fop, gn
+        torch.cuda.empty_cache()
+    out["ratio_plain_to_headline"] = out["plain_fp64"]["value"] / out["headline"]["value"]
+    return out
 
 
 def run_ours(args, world, rank, local):
@@ -354,6 +396,10 @@ def run_ours(args, world, rank, local):
                "check_rhoa_vs_device": float(np.max(np.abs(r - rhoa_d.cpu().numpy()) / r))}
         del Jh
 
+    gn = None
+    if args.gn and rank == 0:
+        gn = gn_iteration(args, mesh, data, rho, local, weights)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle.cpu_baseline import SampledBaseline
@@ -373,7 +419,7 @@ def run_ours(args, world, rank, local):
                               rtol=args.rtol, l2="working set > L2: PCG blocks 4 x "
                               f"{mesh.nodeCount() * 96 * 8 / 1e6:.0f} MB, J {D * P * 8 / 1e9:.1f} GB"),
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-               "plain_fp64_gpu_pcg": plain, "fsai_form": fsai_form,
+               "plain_fp64_gpu_pcg": plain, "fsai_form": fsai_form, "gn_iteration": gn,
                "learned_weights": os.path.relpath(weights, ROOT) if weights else None,
                "clocks": clk,
                "breakdown_ms": {"assemble": st["ms_assemble"], "rhs": st["ms_rhs"], "solve": st["ms_solve"],

@@ -532,6 +532,39 @@ __global__ void k_rhs(int64_t n, int64_t nnz, int nE, int64_t R, int64_t Rpad,
     }
 }
 
+// column partials of ||S1 u_p / rho_s||^2 = ||S1 up||^2 (rho_s cancels): block
+// (32, 8) over (columns, rows), partial row per blockIdx.y
+__global__ void k_pnorm_part(int64_t n, int64_t nnz, int nE, int64_t R, int64_t Rpad,
+                             const int32_t *__restrict__ rowptr, const int32_t *__restrict__ colidx,
+                             const double *__restrict__ S1, const double *__restrict__ up, double *__restrict__ part) {
+    __shared__ double red[8][32];
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    double acc = 0.0;
+    if (t < R) {
+        const double *S1k = S1 + (t / nE) * nnz;
+        for (int64_t row = (int64_t)blockIdx.y * 8 + threadIdx.y; row < n; row += (int64_t)gridDim.y * 8) {
+            double a = 0.0;
+            for (int32_t s = rowptr[row]; s < rowptr[row + 1]; s++) a += S1k[s] * up[(int64_t)colidx[s] * Rpad + t];
+            acc = fma(a, a, acc);
+        }
+    }
+    red[threadIdx.y][threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.y == 0) {
+        double s = 0.0;
+        for (int w = 0; w < 8; w++) s += red[w][threadIdx.x];
+        part[(int64_t)blockIdx.y * Rpad + t] = s;
+    }
+}
+
+__global__ void k_pnorm_sum(int64_t Rpad, int NB, const double *__restrict__ part, double *__restrict__ out) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= Rpad) return;
+    double s = 0.0;
+    for (int b = 0; b < NB; b++) s += part[(int64_t)b * Rpad + t];
+    out[t] = s;
+}
+
 __global__ void k_finish_pot(int64_t n, int nE, int64_t R, int64_t Rpad, const double *__restrict__ up,
                              const double *__restrict__ rhos, double *__restrict__ x) {
     const int64_t total = n * Rpad;
@@ -695,6 +728,19 @@ void build_rhs(Context &c, cudaStream_t s) {
                                                                   m.d_colidx.p, c.d_S.p, c.d_S1.p, c.d_up.p,
                                                                   c.d_rhos.p, c.d_r.p);
     ERTGB_CUDA(cudaGetLastError());
+}
+
+void compute_rhs_scale(Context &c, cudaStream_t s) {
+    MeshData &m = c.mesh;
+    const int NB = (int)std::min<int64_t>(ceil_div(m.n, 8), 256);
+    DBuf<double> part;
+    part.alloc((size_t)NB * c.Rpad);
+    c.d_pnorm2.alloc((size_t)c.Rpad);
+    k_pnorm_part<<<dim3((unsigned)(c.Rpad / 32), (unsigned)NB), dim3(32, 8), 0, s>>>(
+        m.n, m.nnz, c.nE, c.R, c.Rpad, m.d_rowptr.p, m.d_colidx.p, c.d_S1.p, c.d_up.p, part.p);
+    k_pnorm_sum<<<(unsigned)ceil_div(c.Rpad, 128), 128, 0, s>>>(c.Rpad, NB, part.p, c.d_pnorm2.p);
+    ERTGB_CUDA(cudaGetLastError());
+    ERTGB_CUDA(cudaStreamSynchronize(s));
 }
 
 void finish_potentials(Context &c, cudaStream_t s) {

@@ -49,7 +49,7 @@ struct BProb {
     int64_t col0, poff;  // first batch column, first partial element
     const int32_t *rowptr, *colidx;
     const float *S32, *dinv32;
-    const double *S, *b;
+    const double *S, *b, *pnorm2;
     double *x;
     float *r, *p, *q, *y;
 };
@@ -326,7 +326,7 @@ __global__ void kb_finish_init(ColView v, const double *__restrict__ pa, const d
     col[RHO * T + g] = rz;
     col[ALPHA * T + g] = 0.0;
     col[BETA * T + g] = 0.0;
-    col[BNORM2 * T + g] = rr;
+    col[BNORM2 * T + g] = pr.pnorm2 ? fmax(rr, kRhsFloor2 * pr.pnorm2[g - pr.col0]) : rr;
     col[RNORM2 * T + g] = rr;
     col[RPREV * T + g] = rr;
     col[STALLS * T + g] = 0.0;
@@ -461,6 +461,7 @@ void build_plan(std::vector<Context *> &cs, const Shape &sh, Plan &pl, cudaStrea
         b.dinv32 = c.d_dinv32.p;
         b.S = c.d_S.p;
         b.b = c.d_r.p;
+        b.pnorm2 = c.d_pnorm2.n >= (size_t)c.Rpad ? c.d_pnorm2.p : nullptr;
         b.x = c.d_x.p;
         b.r = c.d_r32.p;
         b.p = c.d_p32.p;

@@ -136,6 +136,7 @@ int do_response(Context &c, const double *rho, double *rhoa, void *stream) {
     ERTGB_CUDA(cudaEventRecord(c.ev[1], s));
     c.d_r.alloc((size_t)m.n * c.Rpad);
     build_rhs(c, s);
+    compute_rhs_scale(c, s);
     ERTGB_CUDA(cudaEventRecord(c.ev[2], s));
     c.have_S = true;
     if (c.precision != ERTGB_PRECISION_MIXED && c.precond != ERTGB_PRECOND_JACOBI)
@@ -686,6 +687,7 @@ int ertgb_batch_response(ertgb_ctx *const *ctxs, int n, const double *const *rho
             compute_source_rho(c, rho[i], s);
             c.d_r.alloc((size_t)c.mesh.n * c.Rpad);
             build_rhs(c, s);
+            compute_rhs_scale(c, s);
             c.have_S = true;
         }
         ERTGB_CUDA(cudaEventRecord(c0.ev[1], s));

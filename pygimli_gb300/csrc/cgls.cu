@@ -14,7 +14,8 @@
 // The constraint matrix C (and its transpose) is CSR FP64.  Vectors and
 // scalars are FP64; the dot products are deterministic two-stage reductions
 // whose results the host reads every iteration (two syncs per iteration,
-// small against the two passes over J).
+// small against the two passes over J).  With an FP32 Jacobian the products
+// run in FP32 (per-thread partial sums) and are summed in FP64.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -70,6 +71,81 @@ __global__ void k_jtmul(int64_t D, int64_t P, const T *__restrict__ J, const dou
     }
     if (d < d1) a0 = fma((double)J[d * P + p], y[d], a0);
     part[(int64_t)blockIdx.y * P + p] = a0 + a1;
+}
+
+// FP32 Jacobian: products in FP32 (float4 loads of J and of an FP32 copy of
+// the vector), per-thread FP32 partial sums, FP64 across threads and
+// segments.  GB300's FP64 pipe (1/55 of FP32) would otherwise bound the pass,
+// not HBM.
+__global__ void k_jmul32(int64_t D, int64_t P, const float *__restrict__ J, const float *__restrict__ x,
+                         const double *__restrict__ scale, double *__restrict__ y) {
+    __shared__ double red[kThreads];
+    const int64_t P4 = P / 4;
+    for (int64_t d = blockIdx.x; d < D; d += gridDim.x) {
+        const float *row = J + d * P;
+        float a0 = 0.f, a1 = 0.f;
+        // rows start 16-byte aligned only when P is a multiple of 4
+        if ((P & 3) == 0) {
+            const float4 *r4 = reinterpret_cast<const float4 *>(row);
+            const float4 *x4 = reinterpret_cast<const float4 *>(x);
+            int64_t p = threadIdx.x;
+            for (; p + kThreads < P4; p += 2 * kThreads) {
+                const float4 j0 = __ldg(r4 + p), j1 = __ldg(r4 + p + kThreads);
+                const float4 v0 = x4[p], v1 = x4[p + kThreads];
+                a0 = fmaf(j0.x, v0.x, fmaf(j0.y, v0.y, fmaf(j0.z, v0.z, fmaf(j0.w, v0.w, a0))));
+                a1 = fmaf(j1.x, v1.x, fmaf(j1.y, v1.y, fmaf(j1.z, v1.z, fmaf(j1.w, v1.w, a1))));
+            }
+            for (; p < P4; p += kThreads) {
+                const float4 j0 = __ldg(r4 + p);
+                const float4 v0 = x4[p];
+                a0 = fmaf(j0.x, v0.x, fmaf(j0.y, v0.y, fmaf(j0.z, v0.z, fmaf(j0.w, v0.w, a0))));
+            }
+        } else {
+            for (int64_t p = threadIdx.x; p < P; p += kThreads) a0 = fmaf(__ldg(row + p), x[p], a0);
+        }
+        red[threadIdx.x] = (double)a0 + (double)a1;
+        __syncthreads();
+        for (int w = kThreads / 2; w > 0; w >>= 1) {
+            if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) y[d] = scale ? red[0] * scale[d] : red[0];
+        __syncthreads();
+    }
+}
+
+// part[s][p] for 4 consecutive columns per thread (P a multiple of 4)
+__global__ void k_jtmul32(int64_t D, int64_t P, const float *__restrict__ J, const float *__restrict__ y,
+                          double *__restrict__ part) {
+    const int64_t q = blockIdx.x * (int64_t)kThreads + threadIdx.x;  // float4 column group
+    const int64_t seg = (D + gridDim.y - 1) / gridDim.y;
+    const int64_t d0 = blockIdx.y * seg, d1 = min(D, d0 + seg);
+    if (q * 4 >= P) return;
+    const float4 *J4 = reinterpret_cast<const float4 *>(J);
+    const int64_t P4 = P / 4;
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = make_float4(0.f, 0.f, 0.f, 0.f);
+    int64_t d = d0;
+    for (; d + 1 < d1; d += 2) {
+        const float4 j0 = __ldg(J4 + d * P4 + q), j1 = __ldg(J4 + (d + 1) * P4 + q);
+        const float y0 = y[d], y1 = y[d + 1];
+        a.x = fmaf(j0.x, y0, a.x); a.y = fmaf(j0.y, y0, a.y); a.z = fmaf(j0.z, y0, a.z); a.w = fmaf(j0.w, y0, a.w);
+        b.x = fmaf(j1.x, y1, b.x); b.y = fmaf(j1.y, y1, b.y); b.z = fmaf(j1.z, y1, b.z); b.w = fmaf(j1.w, y1, b.w);
+    }
+    if (d < d1) {
+        const float4 j0 = __ldg(J4 + d * P4 + q);
+        const float y0 = y[d];
+        a.x = fmaf(j0.x, y0, a.x); a.y = fmaf(j0.y, y0, a.y); a.z = fmaf(j0.z, y0, a.z); a.w = fmaf(j0.w, y0, a.w);
+    }
+    double *o = part + (int64_t)blockIdx.y * P + q * 4;
+    o[0] = (double)a.x + (double)b.x;
+    o[1] = (double)a.y + (double)b.y;
+    o[2] = (double)a.z + (double)b.z;
+    o[3] = (double)a.w + (double)b.w;
+}
+
+__global__ void k_to32(int64_t n, const double *__restrict__ a, float *__restrict__ b) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
 }
 
 // out[p] = (sum_s part[s][p]) / div[p] (div may be null)
@@ -207,13 +283,32 @@ int cgls_solve(const void *J, int dtype, int64_t D, int64_t P, int64_t NC, const
     const unsigned gP = cg.grid(P), gD = cg.grid(D), gC = cg.grid(std::max<int64_t>(NC, 1));
     const dim3 gT((unsigned)ceil_div(P, kThreads), kRowSeg);
     const unsigned gJ = (unsigned)std::min<int64_t>(D, 16 * cg.sms);
+    DBuf<float> x32, y32;
+    const bool fast32 = dtype == 1 && (P & 3) == 0;
+    if (fast32) {
+        x32.alloc((size_t)P);
+        y32.alloc((size_t)D);
+    }
+    const dim3 gT4((unsigned)ceil_div(P / 4, kThreads), kRowSeg);
     auto Jx = [&](const double *xin, const double *scale, double *yout) {
-        if (dtype == 0) k_jmul<double><<<gJ, kThreads, 0, s>>>(D, P, (const double *)J, xin, scale, yout);
-        else k_jmul<float><<<gJ, kThreads, 0, s>>>(D, P, (const float *)J, xin, scale, yout);
+        if (dtype == 0) {
+            k_jmul<double><<<gJ, kThreads, 0, s>>>(D, P, (const double *)J, xin, scale, yout);
+        } else if (fast32) {
+            k_to32<<<gP, kThreads, 0, s>>>(P, xin, x32.p);
+            k_jmul32<<<gJ, kThreads, 0, s>>>(D, P, (const float *)J, x32.p, scale, yout);
+        } else {
+            k_jmul<float><<<gJ, kThreads, 0, s>>>(D, P, (const float *)J, xin, scale, yout);
+        }
     };
     auto JTy = [&](const double *yin, const double *div, double *out) {
-        if (dtype == 0) k_jtmul<double><<<gT, kThreads, 0, s>>>(D, P, (const double *)J, yin, cg.seg.p);
-        else k_jtmul<float><<<gT, kThreads, 0, s>>>(D, P, (const float *)J, yin, cg.seg.p);
+        if (dtype == 0) {
+            k_jtmul<double><<<gT, kThreads, 0, s>>>(D, P, (const double *)J, yin, cg.seg.p);
+        } else if (fast32) {
+            k_to32<<<gD, kThreads, 0, s>>>(D, yin, y32.p);
+            k_jtmul32<<<gT4, kThreads, 0, s>>>(D, P, (const float *)J, y32.p, cg.seg.p);
+        } else {
+            k_jtmul<float><<<gT, kThreads, 0, s>>>(D, P, (const float *)J, yin, cg.seg.p);
+        }
         k_seg_sum<<<gP, kThreads, 0, s>>>(P, kRowSeg, cg.seg.p, div, out);
     };
     // C^T (C (wm x) wc^2) into out

@@ -168,6 +168,7 @@ struct Context {
     // per response
     DBuf<double> d_S;             // nK x nnz
     DBuf<double> d_dinv;          // nK x n  (1 / diag)
+    DBuf<double> d_pnorm2;        // Rpad: ||S1 u_p / rho_s||^2 per right-hand side (convergence reference floor)
     DBuf<double> d_rhos;          // nE source resistivity
     DBuf<double> d_x, d_r, d_p, d_q;  // n x Rpad (d_r holds the right-hand sides)
     // mixed precision: FP32 matrix, Jacobi diagonal and recurrence vectors
@@ -199,6 +200,11 @@ void assemble_all(Context &c, const double *rho_cell, double *vals_out, cudaStre
 void assemble_unit(Context &c, cudaStream_t s);
 void compute_source_rho(Context &c, const double *rho_cell, cudaStream_t s);
 void build_rhs(Context &c, cudaStream_t s);
+// ||S1 u_p / rho_s||^2 per column into d_pnorm2 (after build_rhs)
+void compute_rhs_scale(Context &c, cudaStream_t s);
+// Floor of the convergence reference: ||b||^2 is raised to kRhsFloor2 ||S1 u_p / rho_s||^2
+// where the singularity-removal right-hand side cancels (homogeneous ground around a source).
+constexpr double kRhsFloor2 = 1e-6;
 void finish_potentials(Context &c, cudaStream_t s);
 void collect_response(Context &c, double *rhoa, cudaStream_t s);
 void check_rho(Context &c, const double *rho_cell, cudaStream_t s);
@@ -207,6 +213,9 @@ void check_rho(Context &c, const double *rho_cell, cudaStream_t s);
 int pcg_solve(Context &c, cudaStream_t s, const int32_t *mask = nullptr);
 // allocate pcg_solve's workspaces ahead (no allocation inside a later solve)
 void pcg_prepare(Context &c);
+void pcg_finish_init(dim3 g, dim3 b, cudaStream_t s, int64_t Rpad, int64_t R, int NB, const double *pa,
+                     const double *pb, double *col, int32_t *active, int32_t *iters, int32_t *nactive,
+                     const double *pnorm2);
 // pcg_mixed.cu
 int pcg_solve_mixed(Context &c, cudaStream_t s);
 void profile_spmm32(Context &c, int reps, double *ms, double *bytes, double *flops);

@@ -113,10 +113,15 @@ __global__ void k_init(int64_t n, int nE, int nK, int64_t R, int64_t Rpad, const
     }
 }
 
+// BNORM2, the convergence reference, is ||b||^2 raised to kRhsFloor2
+// ||S1 u_p / rho_s||^2 (pnorm2, may be null): where the singularity-removal
+// right-hand side cancels to rounding noise the solve stops at 1e-3 rtol of
+// the primary-field scale instead of chasing the noise.
 __global__ void k_finish_init(int64_t Rpad, int64_t R, int NB, const double *__restrict__ part_a,
                               const double *__restrict__ part_b, double *__restrict__ col,
                               int32_t *__restrict__ active, int32_t *__restrict__ iters,
-                              int32_t *__restrict__ nactive, const int32_t *__restrict__ mask) {
+                              int32_t *__restrict__ nactive, const int32_t *__restrict__ mask,
+                              const double *__restrict__ pnorm2) {
     __shared__ double ra[32][33], rb[32][33];
     const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
     const double rz = col_sum(part_a, NB, Rpad, t, ra);
@@ -134,7 +139,7 @@ __global__ void k_finish_init(int64_t Rpad, int64_t R, int NB, const double *__r
         if (a) atomicAdd(nactive, 1);
         return;
     }
-    col[BNORM2 * Rpad + t] = rr;
+    col[BNORM2 * Rpad + t] = pnorm2 ? fmax(rr, kRhsFloor2 * pnorm2[t]) : rr;
     col[RNORM2 * Rpad + t] = rr;
     col[RPREV * Rpad + t] = rr;
     col[STALLS * Rpad + t] = 0.0;
@@ -349,7 +354,8 @@ int pcg_solve(Context &c, cudaStream_t s, const int32_t *mask) {
     }
     ERTGB_CUDA(cudaMemsetAsync(nactive, 0, sizeof(int32_t), s));
     k_init<<<vg, vb, 0, s>>>(n, c.nE, c.nK, R, Rpad, c.d_dinv.p, c.d_r.p, c.d_p.p, part_a, part_b);
-    k_finish_init<<<fg, fb, 0, s>>>(Rpad, R, NB, part_a, part_b, c.d_col.p, active, iters, nactive, mask);
+    k_finish_init<<<fg, fb, 0, s>>>(Rpad, R, NB, part_a, part_b, c.d_col.p, active, iters, nactive, mask,
+                                    c.d_pnorm2.n >= (size_t)Rpad ? c.d_pnorm2.p : nullptr);
     ERTGB_CUDA(cudaGetLastError());
 
     // capture a chunk of iterations
@@ -436,8 +442,8 @@ __global__ void k_col_total(int64_t Rpad, int NB, const double *__restrict__ par
 }  // namespace
 
 void pcg_finish_init(dim3 g, dim3 b, cudaStream_t s, int64_t Rpad, int64_t R, int NB, const double *pa, const double *pb,
-                     double *col, int32_t *active, int32_t *iters, int32_t *nactive) {
-    k_finish_init<<<g, b, 0, s>>>(Rpad, R, NB, pa, pb, col, active, iters, nactive, nullptr);
+                     double *col, int32_t *active, int32_t *iters, int32_t *nactive, const double *pnorm2) {
+    k_finish_init<<<g, b, 0, s>>>(Rpad, R, NB, pa, pb, col, active, iters, nactive, nullptr, pnorm2);
 }
 
 void pcg_finish_alpha(dim3 g, dim3 b, cudaStream_t s, int64_t Rpad, int NB, const double *part, double *col,

@@ -509,8 +509,6 @@ template <int CH> struct ResidL {
 }  // namespace
 
 // kernels of pcg.cu reused here
-void pcg_finish_init(dim3 g, dim3 b, cudaStream_t s, int64_t Rpad, int64_t R, int NB, const double *pa, const double *pb,
-                     double *col, int32_t *active, int32_t *iters, int32_t *nactive);
 void pcg_finish_alpha(dim3 g, dim3 b, cudaStream_t s, int64_t Rpad, int NB, const double *part, double *col,
                       const int32_t *active, int32_t *nactive);
 
@@ -569,7 +567,8 @@ int pcg_solve_mixed(Context &c, cudaStream_t s) {
         ERTGB_CUDA(cudaMemcpyAsync(c.d_p32.p, c.d_z32.p, sizeof(float) * n * Rpad, cudaMemcpyDeviceToDevice, s));
         c.stats.launches_response += 2;
     }
-    pcg_finish_init(fg, fb, s, Rpad, R, NB, part_a, part_b, c.d_col.p, active, iters, nactive);
+    pcg_finish_init(fg, fb, s, Rpad, R, NB, part_a, part_b, c.d_col.p, active, iters, nactive,
+                    c.d_pnorm2.n >= (size_t)Rpad ? c.d_pnorm2.p : nullptr);
     ERTGB_CUDA(cudaGetLastError());
     c.stats.launches_response += 5;
 

@@ -140,16 +140,16 @@ class GaussNewton:
         self.tD = TransLog
         self.tM = TransLog
         self.C = smoothness_constraints(fop.mesh(), fop.parameterCount)
+        import scipy.sparse as sp
+        rp, ci, cv, P = self.C
+        self._Cs = sp.csr_matrix((cv, ci, rp), shape=(len(rp) - 1, P))
         self.wc = np.ones(len(self.C[0]) - 1)
         self.wm = np.ones(fop.parameterCount)
         self.dweight = 1.0 / self.tD.error(self.data, self.error)
         self.stats = []
 
     def _C_mul(self, x):
-        rp, ci, cv, _ = self.C
-        out = np.zeros(len(rp) - 1)
-        np.add.at(out, np.repeat(np.arange(len(rp) - 1), np.diff(rp)), cv * x[ci])
-        return out
+        return self._Cs @ x
 
     def roughness(self, model):
         return self._C_mul(self.tM.trans(model) * self.wm) * self.wc
@@ -193,13 +193,23 @@ class GaussNewton:
 
     def _line_search(self, model, response, model_new, response_new, dm):
         """RInversion::linesearch: best of 101 step lengths on the linear
-        interpolation of the transformed response, parabolic fit below 0.03."""
+        interpolation of the transformed response, parabolic fit below 0.03.
+        With log transforms both the interpolated data and the model are
+        linear in tau in the transformed domain, so phi(tau) is a quadratic
+        whose three coefficients are computed once (same grid, same minimum)."""
         d_model = self.tM.trans(model_new) - self.tM.trans(model)
         d_data = self.tD.trans(response_new) - self.tD.trans(response)
+        dd0 = (self.tD.trans(self.data) - self.tD.trans(response)) * self.dweight
+        dd1 = d_data * self.dweight
+        r0 = self.roughness(model)
+        r1 = self._C_mul(d_model * self.wm) * self.wc
+        c0 = dd0 @ dd0 + self.lam * (r0 @ r0)
+        c1 = -2.0 * (dd0 @ dd1) + 2.0 * self.lam * (r0 @ r1)
+        c2 = dd1 @ dd1 + self.lam * (r1 @ r1)
         min_phi, min_tau = self.phi(model, response), 0.0
         for i in range(1, 101):
             tau = 0.01 * i
-            ph = self.phi(self.tM.update(model, d_model * tau), self.tD.update(response, d_data * tau))
+            ph = c0 + tau * (c1 + tau * c2)
             if ph < min_phi:
                 min_phi, min_tau = ph, tau
         extra = 0

@@ -1,6 +1,7 @@
 """Gauss-Newton step: the oracle CGLS against the normal equations (CPU),
 the GPU CGLS against the oracle on the same Jacobian (GPU, 1e-9 relative
-after 15 iterations: the random test system has condition 1.4e7, and CG
+for an FP64 Jacobian, 1e-4 for an FP32 one whose products run in FP32, after
+15 iterations: the random test system has condition 1.4e7, and CG
 amplifies a one-ulp change of J to 2e-13 by iteration 20 and to 3e-4 by
 iteration 60, so later iterates are not comparable between any two
 summation orders), and a full step that lowers the objective."""
@@ -53,7 +54,9 @@ def torch():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("dtype,tol", [("float64", 1e-9), ("float32", 1e-9)])
+# FP32 Jacobian: the GPU forms the products in FP32 (per-thread partial sums)
+# while the oracle uses FP64 arithmetic on the same FP32 values: 1e-4
+@pytest.mark.parametrize("dtype,tol", [("float64", 1e-9), ("float32", 1e-4)])
 def test_gpu_cgls_matches_oracle(torch, dtype, tol):
     from pygimli_gb300.inversion import cgls
     J, C, v = _random_problem(seed=1, D=300, P=700)
