@@ -82,7 +82,12 @@ def workload(name):
 
 
 def default_weights(name):
-    base = "box_3d" if name.startswith("box_3d") else name
+    """Packaged weights trained on the workload's kind of matrix (element order
+    and dimension): box_3d for every P1 3-D workload, box_3d_p2 for P2."""
+    if name.startswith("box_3d"):
+        base = "box_3d_p2" if name.endswith("p2") else "box_3d"
+    else:
+        base = name
     return os.path.join(ROOT, "pygimli_gb300", "weights", base + ".npz")
 
 

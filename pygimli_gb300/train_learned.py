@@ -25,6 +25,9 @@ def meshes_for(workload):
     if workload == "box_3d":
         mesh, data, _ = synthetic.box_3d(scheme="inline")
         return [(mesh, data)]
+    if workload == "box_3d_p2":
+        mesh, data, _ = synthetic.box_3d(scheme="inline")
+        return [(mesh.createP2(), data)]
     if workload == "line_2d":
         mesh, data, _ = synthetic.line_2d()
         return [(mesh, data)]
@@ -55,7 +58,7 @@ def evaluate(fop, lp, models):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="box_3d", choices=["box_3d", "line_2d"])
+    ap.add_argument("--workload", default="box_3d", choices=["box_3d", "box_3d_p2", "line_2d"])
     ap.add_argument("--models", type=int, default=48)
     ap.add_argument("--held-out", type=int, default=4)
     ap.add_argument("--steps", type=int, default=1500)
