@@ -47,7 +47,7 @@ HIDDEN = 64
 LAYERS = 4
 NFEAT = 4
 CLAMP = 1.0
-FSAI_MAX_ROW = 20
+FSAI_MAX_ROW = 24
 
 
 def param_layout():

@@ -20,7 +20,7 @@ namespace ertgb {
 
 namespace {
 
-constexpr int kMaxRow = 20;
+constexpr int kMaxRow = 24;  // covers every lower row of P1 and P2 (Tet10) patterns
 
 __device__ inline double csr_get(const int32_t *__restrict__ rowptr, const int32_t *__restrict__ colidx,
                                  const double *__restrict__ vals, int32_t r, int32_t c) {
