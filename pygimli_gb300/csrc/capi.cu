@@ -358,6 +358,7 @@ int ertgb_set_scheme(ertgb_ctx *ctx, int n_data, const int32_t *abmn, const doub
         for (int64_t i = 0; i < 4 * (int64_t)n_data; i++)
             ERTGB_REQUIRE(abmn[i] >= -1 && abmn[i] < c->nE, "electrode index out of range in scheme");
         c->D = n_data;
+        c->abmn_h.assign(abmn, abmn + (size_t)4 * n_data);
         c->d_abmn.upload(abmn, (size_t)4 * n_data, c->stream);
         c->d_kfac.upload(kfac, (size_t)n_data, c->stream);
         // distinct current and potential dipoles, in order of first use

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -90,6 +91,15 @@ struct MeshData {
     DBuf<int32_t> d_pcell_ptr, d_pcell;
 };
 
+// A contiguous range of data [d0, d1) with its own distinct current and
+// potential dipoles (indices local to the chunk), for schemes whose dipole
+// tables of one cell exceed shared memory.
+struct JacChunk {
+    int64_t d0 = 0, d1 = 0;
+    int nA = 0, nM = 0;
+    DBuf<int32_t> dip_a, dip_m, data_dip;
+};
+
 // Jacobian tiles for one table precision: parameter boundaries of each tile
 // and the cells one tile may stage.
 struct JacTiles {
@@ -97,6 +107,7 @@ struct JacTiles {
     DBuf<int32_t> d_tile_p;
     int max_cells = 0;    // tile width TW (cells, = parameters when one cell each)
     int stage_cells = 0;  // cells whose potentials are staged at a time
+    std::vector<std::unique_ptr<JacChunk>> chunks;  // empty: the whole scheme in one pass
 };
 
 // Learned preconditioner (learned.cu): graph of the system matrix, network
@@ -143,6 +154,7 @@ struct Context {
     bool have_kw = false;
     // scheme
     int64_t D = 0;
+    std::vector<int32_t> abmn_h;  // host copy of the scheme (D x 4)
     DBuf<int32_t> d_abmn;
     DBuf<double> d_kfac;
     bool have_scheme = false;

@@ -25,6 +25,7 @@
 // (datum sub-row, cell) with the cell fastest, so conflict-free table reads
 // and contiguous runs of a J row per sub-row.
 #include <algorithm>
+#include <map>
 #include <type_traits>
 
 #include "ertgb_internal.cuh"
@@ -204,9 +205,9 @@ __global__ void k_jac_scales(int64_t D, int64_t P, const double *__restrict__ kf
 
 // shared-memory plan: tile width TW (power of two, <= 16) and the cells G
 // staged at a time for the given table precision
-bool plan(const Context &c, int dtype, int *TW, int *G) {
+bool plan(const Context &c, int dtype, int *TW, int *G, int ndip = -1) {
     const size_t uv = 2 * (size_t)c.nK * c.mesh.nv * (c.nE + 1) * sizeof(double);
-    const size_t tab = (size_t)c.nK * (c.nA + c.nM) * c.mesh.nv * (dtype == 0 ? 8 : 4);
+    const size_t tab = (size_t)c.nK * (ndip < 0 ? c.nA + c.nM : ndip) * c.mesh.nv * (dtype == 0 ? 8 : 4);
     for (size_t budget : {kSmemBudget, kSmemBudgetLarge})
         for (int tw : {16, 8, 4, 2, 1}) {
             if (tw * tab + uv > budget) continue;
@@ -238,11 +239,25 @@ void launch(Context &c, const double *model, CT *J, int dtype, cudaStream_t s) {
         sp = base + c.D;
     }
     auto go = [&](auto kern) {
-        ERTGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        kern<<<ntiles, kThreads, smem, s>>>(T.d_tile_p.p, m.d_pcell_ptr.p, m.d_pcell.p, m.d_cells.p, m.d_K.p, m.d_M.p,
-                                            c.d_k.p, c.d_w.p, c.nK, c.nE, c.Rpad, c.d_x.p, c.nA, c.d_dip_a.p, c.nM,
-                                            c.d_dip_m.p, c.d_data_dip.p, sd, sp, m.P, c.D, G, J);
-        ERTGB_CUDA(cudaGetLastError());
+        if (T.chunks.empty()) {
+            ERTGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            kern<<<ntiles, kThreads, smem, s>>>(T.d_tile_p.p, m.d_pcell_ptr.p, m.d_pcell.p, m.d_cells.p, m.d_K.p,
+                                                m.d_M.p, c.d_k.p, c.d_w.p, c.nK, c.nE, c.Rpad, c.d_x.p, c.nA,
+                                                c.d_dip_a.p, c.nM, c.d_dip_m.p, c.d_data_dip.p, sd, sp, m.P, c.D, G, J);
+            ERTGB_CUDA(cudaGetLastError());
+            return;
+        }
+        // data chunks: rows [d0, d1) of J with the chunk's own dipole tables
+        for (const auto &ch : T.chunks) {
+            const size_t sm = 2 * uv * G * sizeof(double) + (size_t)c.nK * (ch->nA + ch->nM) * m.nv * TW * sizeof(CT);
+            ERTGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            kern<<<ntiles, kThreads, sm, s>>>(T.d_tile_p.p, m.d_pcell_ptr.p, m.d_pcell.p, m.d_cells.p, m.d_K.p,
+                                              m.d_M.p, c.d_k.p, c.d_w.p, c.nK, c.nE, c.Rpad, c.d_x.p, ch->nA,
+                                              ch->dip_a.p, ch->nM, ch->dip_m.p, ch->data_dip.p,
+                                              sd ? sd + ch->d0 : nullptr, sp, m.P, ch->d1 - ch->d0, G,
+                                              J + ch->d0 * m.P);
+            ERTGB_CUDA(cudaGetLastError());
+        }
     };
     auto by_tw = [&](auto nvc) {
         constexpr int NV = decltype(nvc)::value;
@@ -262,6 +277,38 @@ void launch(Context &c, const double *model, CT *J, int dtype, cudaStream_t s) {
 
 }  // namespace
 
+// Contiguous data chunks, each with at most cap distinct current + potential
+// dipoles, and their chunk-local dipole tables.
+static void build_chunks(Context &c, int cap, JacTiles &T) {
+    const std::vector<int32_t> &ab = c.abmn_h;
+    int64_t d = 0;
+    while (d < c.D) {
+        auto ch = std::make_unique<JacChunk>();
+        ch->d0 = d;
+        std::map<std::pair<int32_t, int32_t>, int32_t> amap, mmap;
+        std::vector<int32_t> dip_a, dip_m, data_dip;
+        for (; d < c.D; d++) {
+            const auto ka = std::make_pair(ab[4 * d], ab[4 * d + 1]);
+            const auto km = std::make_pair(ab[4 * d + 2], ab[4 * d + 3]);
+            const int add = (amap.count(ka) ? 0 : 1) + (mmap.count(km) ? 0 : 1);
+            if ((int)(amap.size() + mmap.size()) + add > cap && d > ch->d0) break;
+            auto ia = amap.emplace(ka, (int32_t)amap.size());
+            if (ia.second) { dip_a.push_back(ka.first); dip_a.push_back(ka.second); }
+            auto im = mmap.emplace(km, (int32_t)mmap.size());
+            if (im.second) { dip_m.push_back(km.first); dip_m.push_back(km.second); }
+            data_dip.push_back(ia.first->second);
+            data_dip.push_back(im.first->second);
+        }
+        ch->d1 = d;
+        ch->nA = (int)amap.size();
+        ch->nM = (int)mmap.size();
+        ch->dip_a.upload(dip_a, c.stream);
+        ch->dip_m.upload(dip_m, c.stream);
+        ch->data_dip.upload(data_dip, c.stream);
+        T.chunks.push_back(std::move(ch));
+    }
+}
+
 // Parameter -> cells and the Jacobian tiles of both table precisions
 // (consecutive parameters with at most TW cells per tile).
 void build_jacobian_tiles(Context &c) {
@@ -280,10 +327,21 @@ void build_jacobian_tiles(Context &c) {
     for (int dt = 0; dt < 2; dt++) {
         JacTiles &T = c.jtiles[dt];
         T.tile_p.assign(1, 0);
+        T.chunks.clear();
         int TW = 0, G = 0;
         if (!plan(c, dt, &TW, &G)) {
-            T.max_cells = 0;
-            continue;
+            // split the scheme into data chunks whose distinct dipoles fit
+            int cap = 0;
+            for (int nd = c.nA + c.nM; nd >= 2; nd = nd * 3 / 4)
+                if (plan(c, dt, &TW, &G, nd)) {
+                    cap = nd;
+                    break;
+                }
+            if (cap < 2) {
+                T.max_cells = 0;
+                continue;
+            }
+            build_chunks(c, cap, T);
         }
         T.max_cells = TW;
         T.stage_cells = G;

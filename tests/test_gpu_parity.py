@@ -303,6 +303,35 @@ def test_3d_config_properties(torch):
           f"max dev {np.max(np.abs(rh - 100.0)):.3f}")
 
 
+def test_jacobian_data_chunks(torch):
+    """A scheme whose distinct current and potential dipoles (about 9,900)
+    make one cell's FP64 dipole tables exceed shared memory: the Jacobian is
+    built in data chunks, each with its own dipole tables; rows are checked
+    against the oracle's rows recomputed from the GPU potentials."""
+    e = np.array([(x, y) for x in np.arange(10) * 2.0 for y in np.arange(10) * 2.0])
+    mesh = create_box_mesh_3d(e, h=2.0, para_margin=(1, 1), para_depth=4.0, outer=60.0, growth=2.0,
+                              depth_growth=1.6)
+    pairs = [(a, b) for a in range(100) for b in range(a + 1, 100)]
+    npair = len(pairs)
+    ab = np.array([pairs[i % npair] + pairs[(7 * i + 3) % npair] for i in range(5000)], np.int32)
+    ab = ab[(ab[:, 0] != ab[:, 2]) & (ab[:, 0] != ab[:, 3]) & (ab[:, 1] != ab[:, 2]) & (ab[:, 1] != ab[:, 3])]
+    data = DataContainerERT(np.column_stack([e, np.zeros(len(e))]), ab)
+    with np.errstate(divide="ignore"):
+        kf = geometricFactors(data, 3)
+    ok = np.isfinite(kf) & (np.abs(kf) < 1e6)  # drop symmetric configurations (no signal)
+    data = DataContainerERT(np.column_stack([e, np.zeros(len(e))]), ab[ok])
+    data.set("k", kf[ok])
+    rng = np.random.default_rng(5)
+    rho = np.exp(rng.normal(np.log(100.0), 0.7, mesh.cellCount()))
+    fop = fop_for(mesh, data)
+    fop.response(rho)
+    J = fop.createJacobian(rho)
+    rows = np.array([0, 1, 999, 2500, data.size() - 1])
+    Jr = J[torch.as_tensor(rows, device=J.device)].cpu().numpy()
+    Jo = _jacobian_rows_from_potentials(mesh, data, fop.kValues(), fop.weights(), fop.subPotentials(), rho, rows)
+    assert float(np.linalg.norm(Jr - Jo) / np.linalg.norm(Jo)) <= TOL_J
+
+
 def _spmm_case(golden_dir, torch, seed=0, ld=64):
     """Golden system matrices of three wavenumbers as one multi-matrix
     operator, 11 columns per matrix (33 used, padded to 64)."""
