@@ -67,6 +67,26 @@ def lib():
         L.ref_besselK1.argtypes = [ctypes.c_double]
         L.ref_gauss_legendre.argtypes = [ctypes.c_int, vp, vp]
         L.ref_gauss_laguerre.argtypes = [ctypes.c_int, vp, vp]
+        cs = ctypes.c_char_p
+        L.ref_mesh_create.restype = vp
+        L.ref_mesh_create.argtypes = [ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int, vp, vp,
+                                      ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int]
+        L.ref_mesh_load.restype = vp
+        L.ref_mesh_load.argtypes = [cs]
+        L.ref_mesh_dim.argtypes = [vp]
+        L.ref_mesh_save_bms.argtypes = [vp, cs]
+        L.ref_mesh_save_bms_v1.argtypes = [vp, cs]
+        L.ref_mesh_boundary_cells.argtypes = [vp, vp, vp]
+        L.ref_mesh_add_data.argtypes = [vp, cs, ctypes.c_int, vp]
+        L.ref_mesh_export_vtk.argtypes = [vp, cs, ctypes.c_int]
+        L.ref_data_load.restype = vp
+        L.ref_data_load.argtypes = [cs, ctypes.c_int, ctypes.c_int]
+        L.ref_data_free.argtypes = [vp]
+        L.ref_data_sizes.argtypes = [vp, vp, vp]
+        L.ref_data_sensors.argtypes = [vp, vp]
+        L.ref_data_tokens.argtypes = [vp, cs, ctypes.c_int]
+        L.ref_data_get.argtypes = [vp, cs, vp]
+        L.ref_data_save.argtypes = [vp, cs, cs, cs, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -240,3 +260,110 @@ def besselK0(x):
 
 def besselK1(x):
     return lib().ref_besselK1(float(x))
+
+
+def _mesh_arrays(h):
+    v = [ctypes.c_int() for _ in range(5)]
+    lib().ref_mesh_sizes(h, *[ctypes.byref(x) for x in v])
+    n, C, nv, B, nvb = [x.value for x in v]
+    xyz = np.zeros((n, 3))
+    nm = np.zeros(n, np.int32)
+    cells = np.zeros((C, nv), np.int32)
+    cm = np.zeros(C, np.int32)
+    bnd = np.zeros((B, nvb), np.int32)
+    bm = np.zeros(B, np.int32)
+    _check(lib().ref_mesh_arrays(h, _p(xyz), _p(nm), _p(cells), _p(cm), _p(bnd), _p(bm)))
+    left = np.zeros(B, np.int32)
+    right = np.zeros(B, np.int32)
+    _check(lib().ref_mesh_boundary_cells(h, _p(left), _p(right)))
+    return {"dim": lib().ref_mesh_dim(h), "nodes": xyz, "node_markers": nm, "cells": cells, "cell_markers": cm,
+            "boundaries": bnd, "boundary_markers": bm, "left": left, "right": right}
+
+
+class RefMesh:
+    """A reference ``GIMLI::Mesh`` alone: built from arrays (with
+    createNeighborInfos, optionally createP2 / createH2) or loaded from a
+    binary mesh file; saved with saveBinaryV2 or exported with exportVTK."""
+
+    def __init__(self, mesh=None, p2=False, h2=False, path=None):
+        L = lib()
+        if path is not None:
+            self.h = L.ref_mesh_load(os.fsencode(path))
+        else:
+            a = [np.ascontiguousarray(mesh.nodes, np.float64), np.ascontiguousarray(mesh.node_markers, np.int32),
+                 np.ascontiguousarray(mesh.cells, np.int32), np.ascontiguousarray(mesh.cell_markers, np.int32),
+                 np.ascontiguousarray(mesh.boundaries, np.int32),
+                 np.ascontiguousarray(mesh.boundary_markers, np.int32)]
+            self._keep = a
+            nodes, nm, cells, cm, bnd, bm = a
+            self.h = L.ref_mesh_create(mesh.dim(), len(nodes), _p(nodes), _p(nm), len(cells), cells.shape[1],
+                                       _p(cells), _p(cm), len(bnd), bnd.shape[1], _p(bnd), _p(bm),
+                                       2 if h2 else int(bool(p2)))
+        if not self.h:
+            raise RuntimeError("reference mesh failed: " + L.ref_last_error().decode())
+
+    def arrays(self):
+        return _mesh_arrays(self.h)
+
+    def add_data(self, name, values):
+        v = np.ascontiguousarray(values, np.float64)
+        _check(lib().ref_mesh_add_data(self.h, name.encode(), len(v), _p(v)))
+
+    def save_bms(self, path):
+        _check(lib().ref_mesh_save_bms(self.h, os.fsencode(path)))
+
+    def save_bms_v1(self, path):
+        _check(lib().ref_mesh_save_bms_v1(self.h, os.fsencode(path)))
+
+    def export_vtk(self, path, cells=True):
+        _check(lib().ref_mesh_export_vtk(self.h, os.fsencode(path), int(bool(cells))))
+
+    def close(self):
+        if self.h:
+            lib().ref_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # pragma: no cover
+            pass
+
+
+def data_load(path, from_one=True, remove_invalid=True):
+    """The reference's ``DataContainerERT::load``: returns (sensors (S, 3),
+    token list, {token: values})."""
+    L = lib()
+    h = L.ref_data_load(os.fsencode(path), int(bool(from_one)), int(bool(remove_invalid)))
+    if not h:
+        raise RuntimeError("reference data load failed: " + L.ref_last_error().decode())
+    try:
+        nS, nD = ctypes.c_int(), ctypes.c_int()
+        L.ref_data_sizes(h, ctypes.byref(nS), ctypes.byref(nD))
+        xyz = np.zeros((nS.value, 3))
+        _check(L.ref_data_sensors(h, _p(xyz)))
+        buf = ctypes.create_string_buffer(4096)
+        assert L.ref_data_tokens(h, buf, 4096) == 0
+        tokens = buf.value.decode().split()
+        fields = {}
+        for t in tokens:
+            v = np.zeros(nD.value)
+            _check(L.ref_data_get(h, t.encode(), _p(v)))
+            fields[t] = v
+        return xyz, tokens, fields
+    finally:
+        L.ref_data_free(h)
+
+
+def data_resave(path_in, path_out, fmt_data="all", fmt_sensor="x y z", no_filter=False, from_one=True):
+    """Load ``path_in`` with the reference and write it back with its
+    ``DataContainer::save``."""
+    L = lib()
+    h = L.ref_data_load(os.fsencode(path_in), int(bool(from_one)), 1)
+    if not h:
+        raise RuntimeError("reference data load failed: " + L.ref_last_error().decode())
+    try:
+        _check(L.ref_data_save(h, os.fsencode(path_out), fmt_data.encode(), fmt_sensor.encode(),
+                               int(bool(no_filter))))
+    finally:
+        L.ref_data_free(h)

@@ -11,6 +11,9 @@
 //   data container         core/src/bert/bertDataContainer.h:62 addFourPointData
 //   forward operator       core/src/bert/dcfemmodelling.h:344 DCSRMultiElectrodeModelling
 //   response / Jacobian    core/src/bert/dcfemmodelling.cpp:1085-1197, 1446-1476
+//   mesh / data I/O        core/src/mesh_io.cpp:391-662 (binary mesh v3),
+//                          mesh_io.cpp:674-992 exportVTK,
+//                          core/src/datacontainer.cpp:209-470 load, 518-615 save
 //   solver injection       core/src/bert/dcfemmodelling.h:266 setSolver,
 //                          core/src/solverWrapper.h:26-56 SolverWrapper
 // The reference's default direct solver (CHOLMOD/UMFPACK) is not available,
@@ -351,6 +354,141 @@ int ref_gauss_laguerre(int n, double *x, double *w) {
         GaussLaguerre(n, xv, wv);
         for (int i = 0; i < n; i++) { x[i] = xv[i]; w[i] = wv[i]; }
     });
+}
+
+// ---- mesh and data I/O (core/src/mesh_io.cpp, core/src/datacontainer.cpp) ----
+
+// A handle holding only a mesh, built like ref_create's (no data, no operator).
+void *ref_mesh_create(int dim, int nNodes, const double *xyz, const int *nodeMarker,
+                      int nCells, int nv, const int *cellNodes, const int *cellMarker,
+                      int nBnd, int nvb, const int *bndNodes, const int *bndMarker, int p2) {
+    RefHandle *h = nullptr;
+    int rc = guarded([&] {
+        h = new RefHandle(dim);
+        Mesh &m = h->mesh;
+        for (int i = 0; i < nNodes; i++)
+            m.createNode(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], nodeMarker[i]);
+        for (int c = 0; c < nCells; c++) {
+            const int *cn = cellNodes + (size_t)c * nv;
+            if (nv == 3) m.createTriangle(m.node(cn[0]), m.node(cn[1]), m.node(cn[2]), cellMarker[c]);
+            else if (nv == 4) m.createTetrahedron(m.node(cn[0]), m.node(cn[1]), m.node(cn[2]), m.node(cn[3]), cellMarker[c]);
+            else throwError("unsupported cell node count");
+        }
+        for (int b = 0; b < nBnd; b++) {
+            const int *bn = bndNodes + (size_t)b * nvb;
+            if (nvb == 2) m.createEdge(m.node(bn[0]), m.node(bn[1]), bndMarker[b]);
+            else if (nvb == 3) m.createTriangleFace(m.node(bn[0]), m.node(bn[1]), m.node(bn[2]), bndMarker[b]);
+            else throwError("unsupported boundary node count");
+        }
+        m.createNeighborInfos();
+        if (p2) {
+            Mesh m2 = p2 == 2 ? m.createH2() : m.createP2();
+            h->mesh = m2;
+            h->mesh.createNeighborInfos();
+        }
+    });
+    if (rc) { delete h; return nullptr; }
+    return h;
+}
+
+// Mesh::load (binary format v2/v3 for a .bms name), without createNeighborInfos.
+void *ref_mesh_load(const char *path) {
+    RefHandle *h = nullptr;
+    int rc = guarded([&] {
+        h = new RefHandle(3);
+        h->mesh.load(path, false);
+    });
+    if (rc) { delete h; return nullptr; }
+    return h;
+}
+
+int ref_mesh_dim(void *hp) { return (int)((RefHandle *)hp)->mesh.dim(); }
+
+int ref_mesh_save_bms(void *hp, const char *path) {
+    RefHandle *h = (RefHandle *)hp;
+    return guarded([&] { h->mesh.saveBinaryV2(path); });
+}
+
+// The first binary format (Mesh::saveBinary, read by Mesh::load as fallback).
+int ref_mesh_save_bms_v1(void *hp, const char *path) {
+    RefHandle *h = (RefHandle *)hp;
+    return guarded([&] { h->mesh.saveBinary(path); });
+}
+
+int ref_mesh_boundary_cells(void *hp, int *left, int *right) {
+    RefHandle *h = (RefHandle *)hp;
+    return guarded([&] {
+        Mesh &m = h->mesh;
+        for (Index b = 0; b < m.boundaryCount(); b++) {
+            Boundary &bd = m.boundary(b);
+            left[b] = bd.leftCell() ? (int)bd.leftCell()->id() : -1;
+            right[b] = bd.rightCell() ? (int)bd.rightCell()->id() : -1;
+        }
+    });
+}
+
+int ref_mesh_add_data(void *hp, const char *name, int n, const double *vals) {
+    RefHandle *h = (RefHandle *)hp;
+    return guarded([&] {
+        RVector v(n);
+        for (int i = 0; i < n; i++) v[i] = vals[i];
+        h->mesh.addData(name, v);
+    });
+}
+
+int ref_mesh_export_vtk(void *hp, const char *path, int writeCells) {
+    RefHandle *h = (RefHandle *)hp;
+    return guarded([&] { h->mesh.exportVTK(path, writeCells != 0); });
+}
+
+// DataContainerERT::load (unified data format).
+void *ref_data_load(const char *path, int fromOne, int removeInvalid) {
+    DataContainerERT *d = nullptr;
+    int rc = guarded([&] {
+        d = new DataContainerERT();
+        d->load(path, fromOne != 0, removeInvalid != 0);
+    });
+    if (rc) { delete d; return nullptr; }
+    return d;
+}
+
+void ref_data_free(void *dp) { delete (DataContainerERT *)dp; }
+
+int ref_data_sizes(void *dp, int *nSensors, int *nData) {
+    DataContainerERT *d = (DataContainerERT *)dp;
+    *nSensors = (int)d->sensorCount();
+    *nData = (int)d->size();
+    return 0;
+}
+
+int ref_data_sensors(void *dp, double *xyz) {
+    DataContainerERT *d = (DataContainerERT *)dp;
+    return guarded([&] {
+        for (Index i = 0; i < d->sensorCount(); i++)
+            for (int j = 0; j < 3; j++) xyz[3 * i + j] = d->sensorPosition(i)[j];
+    });
+}
+
+// Space-separated token list (DataContainer::tokenList(false)).
+int ref_data_tokens(void *dp, char *buf, int len) {
+    DataContainerERT *d = (DataContainerERT *)dp;
+    std::string t = d->tokenList(false);
+    if ((int)t.size() + 1 > len) return (int)t.size() + 1;
+    std::memcpy(buf, t.c_str(), t.size() + 1);
+    return 0;
+}
+
+int ref_data_get(void *dp, const char *token, double *out) {
+    DataContainerERT *d = (DataContainerERT *)dp;
+    return guarded([&] {
+        const RVector &v = d->get(token);
+        for (Index i = 0; i < v.size(); i++) out[i] = v[i];
+    });
+}
+
+int ref_data_save(void *dp, const char *path, const char *fmtData, const char *fmtSensor, int noFilter) {
+    DataContainerERT *d = (DataContainerERT *)dp;
+    return guarded([&] { d->save(path, fmtData, fmtSensor, noFilter != 0, false); });
 }
 
 }  // extern "C"

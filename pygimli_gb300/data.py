@@ -18,16 +18,31 @@ u_AN + u_BN), 2-D sensor positions (x, y) are moved to (x, 0, y) first).
 """
 from __future__ import annotations
 
+import os
+
 import numpy as np
+
+# fields every ERT container has (core/src/bert/bertDataContainer.cpp:45-61)
+_DEFAULT_TOKENS = ("a", "b", "m", "n", "err", "i", "ip", "iperr", "k", "r", "rhoa", "u", "valid")
 
 
 class DataContainerERT:
     """Sensors + four-point configurations + data fields."""
 
-    def __init__(self, sensors=None, abmn=None):
+    def __init__(self, sensors=None, abmn=None, removeInvalid=True, sensorIndicesFromOne=None):
+        """``DataContainerERT(sensors, abmn)``, or like the reference's file
+        constructor ``DataContainerERT(fileName, sensorIndicesFromOne=True,
+        removeInvalid=True)``."""
         self._sensors = np.zeros((0, 3))
         self._abmn = np.zeros((0, 4), np.int32)
         self._fields = {}
+        self._topo = np.zeros((0, 3))
+        self._index_from_one = True  # sensor indices on file count from one
+        if isinstance(sensors, (str, os.PathLike)):
+            if sensorIndicesFromOne is None:
+                sensorIndicesFromOne = True if abmn is None else bool(abmn)
+            self.load(sensors, sensorIndicesFromOne, removeInvalid)
+            return
         if sensors is not None:
             self.setSensorPositions(sensors)
         if abmn is not None:
@@ -67,7 +82,7 @@ class DataContainerERT:
     def addFourPointData(self, a, b, m, n):
         self._abmn = np.vstack([self._abmn, np.array([[a, b, m, n]], np.int32)])
         for k, v in self._fields.items():
-            self._fields[k] = np.append(v, 0.0)
+            self._fields[k] = np.append(v, 1.0 if k == "valid" else 0.0)
         return len(self._abmn) - 1
 
     def size(self):
@@ -84,7 +99,9 @@ class DataContainerERT:
             return self._abmn[:, "abmn".index(token)].astype(np.float64)
         if token in self._fields:
             return self._fields[token].copy()
-        if token in ("k", "rhoa", "u", "i", "r", "err", "ip"):
+        if token == "valid":
+            return np.ones(self.size())
+        if token in _DEFAULT_TOKENS:
             return np.zeros(self.size())
         raise KeyError(token)
 
@@ -107,7 +124,84 @@ class DataContainerERT:
             self._fields[token] = v.copy()
 
     def exists(self, token):
-        return token in self._fields
+        return token in self._fields or token in _DEFAULT_TOKENS
+
+    def haveData(self, token):
+        """True when ``token`` holds a value above 1e-12 in magnitude."""
+        return self.size() > 0 and self.exists(token) and float(np.max(np.abs(self[token]))) >= 1e-12
+
+    def tokenList(self):
+        """Sensor index tokens, then the data fields, each group sorted."""
+        from .fileio import token_list
+        return token_list(self._field_map())
+
+    def markValid(self, idx, valid=True):
+        v = self["valid"]
+        v[np.asarray(idx)] = 1.0 if valid else 0.0
+        self._fields["valid"] = v
+
+    def markInvalid(self, idx):
+        self.markValid(idx, False)
+
+    def removeInvalid(self):
+        """Drop every datum whose 'valid' flag is not 1."""
+        keep = np.nonzero(self["valid"] == 1)[0]
+        self._abmn = self._abmn[keep].copy()
+        self._fields = {k: v[keep].copy() for k, v in self._fields.items()}
+
+    def checkDataValidity(self, remove=True):
+        """Validity rules of the reference's loader (non-finite values,
+        sensor indices out of range, rhoa or |r| below 1e-12, coinciding
+        electrodes); ``remove`` drops what they mark."""
+        from .fileio import check_validity
+        self._set_field_map(check_validity(self._field_map(), self.sensorCount(), remove=remove))
+
+    def removeUnusedSensors(self):
+        from .fileio import _remove_unused_sensors
+        sensors, f = _remove_unused_sensors(self._sensors, self._field_map())
+        self._sensors = np.ascontiguousarray(sensors)
+        self._set_field_map(f)
+
+    def additionalPoints(self):
+        """Additional (topography) points read from a file."""
+        return self._topo.copy()
+
+    # -- unified data format -------------------------------------------------
+    def _field_map(self):
+        f = {t: self._abmn[:, j].astype(np.float64) for j, t in enumerate("abmn")}
+        for t in _DEFAULT_TOKENS[4:]:
+            f[t] = self[t]
+        for k, v in self._fields.items():
+            f[k] = v.copy()
+        return f
+
+    def _set_field_map(self, f):
+        n = len(f["valid"])
+        self._abmn = np.column_stack([f[t] for t in "abmn"]).astype(np.int32).reshape(n, 4)
+        self._fields = {k: np.asarray(v, np.float64).copy() for k, v in f.items() if k not in "abmn"}
+
+    def load(self, fileName, sensorIndicesFromOne=True, removeInvalid=True):
+        """Read a unified data file (the reference's DataContainer::load,
+        core/src/datacontainer.cpp:209-470): sensors with an optional
+        '# x y z' format line, data columns named by the '#' line after the
+        data count (aliases such as c1 c2 p1 p2, rho_a, u/mV, err/% are
+        translated and scaled), sensor indices counted from one on file,
+        duplicated sensors merged, invalid data dropped."""
+        from .fileio import read_unified
+        u = read_unified(fileName, sensorIndicesFromOne, removeInvalid)
+        self._sensors = np.ascontiguousarray(u.sensors)
+        self._set_field_map(u.fields)
+        self._topo = u.topo
+        self._index_from_one = bool(sensorIndicesFromOne)
+        return 1
+
+    def save(self, fileName, formatData="all", formatSensor="x y z", noFilter=False, verbose=False):
+        """Write a unified data file (DataContainer::save,
+        core/src/datacontainer.cpp:518-615); ``formatData`` names the
+        columns ("all": every field and datum, else only valid data)."""
+        from .fileio import write_unified
+        return write_unified(fileName, self._sensors, self._field_map(), formatData, formatSensor, noFilter,
+                             self._index_from_one)
 
     def allNonZero(self, token):
         return token in self._fields and bool(np.all(self._fields[token] != 0))
@@ -115,6 +209,8 @@ class DataContainerERT:
     def copy(self):
         d = DataContainerERT(self._sensors, self._abmn)
         d._fields = {k: v.copy() for k, v in self._fields.items()}
+        d._topo = self._topo.copy()
+        d._index_from_one = self._index_from_one
         return d
 
     def __repr__(self):

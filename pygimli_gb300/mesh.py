@@ -25,6 +25,8 @@ around the main diagonal).
 """
 from __future__ import annotations
 
+import os
+
 import numpy as np
 
 MARKER_NODE_ELECTRODE = -99
@@ -65,6 +67,12 @@ class Mesh:
             boundary_cells = find_boundary_cells(self.cells[:, :nv1], self.boundaries[:, :self.dim_],
                                                  len(self.nodes))
         self.boundary_cells = np.ascontiguousarray(np.asarray(boundary_cells, dtype=np.int32))
+        # left / right cell of each boundary as the binary mesh format stores
+        # them (-1: none or not known); boundary_cells is the adjacent cell
+        self.boundary_left_cells = self.boundary_cells.copy()
+        self.boundary_right_cells = np.full(len(self.boundaries), -1, np.int32)
+        self.geometry = False
+        self._data = {}
         if np.any(self._signed_sizes() == 0):
             raise ValueError("degenerate cell in mesh")
 
@@ -133,17 +141,94 @@ class Mesh:
     def cellCenters(self):
         return self.nodes[self.cells[:, :self.dim_ + 1]].mean(axis=1)
 
+    # -- data map (core/src/mesh.h:603-640) ----------------------------------
+    def addData(self, name, values):
+        self._data[str(name)] = np.asarray(values, np.float64).copy()
+
+    def data(self, name):
+        return self._data[name].copy()
+
+    def haveData(self, name):
+        return name in self._data
+
+    def dataMap(self):
+        return {k: v.copy() for k, v in self._data.items()}
+
+    def __setitem__(self, name, values):
+        self.addData(name, values)
+
+    def __getitem__(self, name):
+        return self.data(name)
+
+    # -- files ------------------------------------------------------------------
     def save(self, path):
-        np.savez_compressed(path, dim=self.dim_, nodes=self.nodes, cells=self.cells,
-                            cell_markers=self.cell_markers, node_markers=self.node_markers,
-                            boundaries=self.boundaries, boundary_markers=self.boundary_markers,
-                            boundary_cells=self.boundary_cells)
+        """Binary mesh file (the reference's Mesh::save, format v3, '.bms'
+        appended when missing), or a numpy archive for a '.npz' name.
+        Returns the file name written."""
+        path = os.fspath(path)
+        if path.endswith(".npz"):
+            np.savez_compressed(path, dim=self.dim_, nodes=self.nodes, cells=self.cells,
+                                cell_markers=self.cell_markers, node_markers=self.node_markers,
+                                boundaries=self.boundaries, boundary_markers=self.boundary_markers,
+                                boundary_cells=self.boundary_cells)
+            return path
+        from .fileio import write_bms
+        return write_bms(path, self.dim_, self.nodes, self.node_markers, self.cells, self.cell_markers,
+                         self.boundaries, self.boundary_markers, self.boundary_left_cells, self.boundary_right_cells,
+                         self._data, self.geometry)
+
+    def saveBinaryV2(self, path):
+        """Binary mesh file, format v3 (Mesh::saveBinaryV2)."""
+        return self.save(os.fspath(path) if os.fspath(path).endswith(".bms") else os.fspath(path) + ".bms")
+
+    def saveBinary(self, path):
+        """The first binary mesh format (Mesh::saveBinary); no data map."""
+        from .fileio import write_bms_v1
+        return write_bms_v1(os.fspath(path), self.dim_, self.nodes, self.node_markers, self.cells, self.cell_markers,
+                            self.boundaries, self.boundary_markers, self.boundary_left_cells,
+                            self.boundary_right_cells, self.geometry)
 
     @staticmethod
     def load(path):
-        z = np.load(path)
-        return Mesh(int(z["dim"]), z["nodes"], z["cells"], z["cell_markers"], z["node_markers"],
-                    z["boundaries"], z["boundary_markers"], z["boundary_cells"])
+        """Mesh from a binary mesh file (Mesh::loadBinaryV2, versions 2 and
+        3, else the first format of Mesh::loadBinary) or a numpy archive
+        written by ``save``."""
+        path = os.fspath(path)
+        if path.endswith(".npz"):
+            z = np.load(path)
+            return Mesh(int(z["dim"]), z["nodes"], z["cells"], z["cell_markers"], z["node_markers"],
+                        z["boundaries"], z["boundary_markers"], z["boundary_cells"])
+        from .fileio import read_bms
+        r = read_bms(path)
+        if isinstance(r["cells"], list) or isinstance(r["boundaries"], list):
+            raise ValueError("mixed cell or boundary types: only simplex meshes are supported")
+        bnd = r["boundaries"]
+        if len(bnd) == 0:
+            nv = r["cells"].shape[1] if len(r["cells"]) else r["dim"] + 1
+            nvb = r["dim"] if nv == r["dim"] + 1 else (3 if r["dim"] == 2 else 6)
+            bnd = np.zeros((0, nvb), np.int32)
+        # adjacent cell: left, else right, else searched (the reference's
+        # mixed-boundary assembly, core/src/bert/dcfemmodelling.cpp:258-260)
+        adj = np.where(r["left"] >= 0, r["left"], r["right"]).astype(np.int32)
+        if np.any(adj < 0):
+            nv1 = r["dim"] + 1
+            found = find_boundary_cells(np.asarray(r["cells"])[:, :nv1], bnd[:, :r["dim"]], len(r["nodes"]))
+            adj = np.where(adj >= 0, adj, found).astype(np.int32)
+        m = Mesh(r["dim"], r["nodes"], r["cells"], r["cell_markers"], r["node_markers"], bnd,
+                 r["boundary_markers"], adj)
+        m.boundary_left_cells = np.ascontiguousarray(r["left"], np.int32)
+        m.boundary_right_cells = np.ascontiguousarray(r["right"], np.int32)
+        m.geometry = r["geometry"]
+        m._data = r["data"]
+        return m
+
+    def exportVTK(self, fbody, writeCells=True):
+        """Legacy ASCII VTK file (Mesh::exportVTK): nodes, cells with types,
+        the data map entries of cell (node) length as cell (point) scalars
+        plus the cell markers as 'Marker'.  Returns the file name."""
+        from .fileio import write_vtk
+        return write_vtk(os.fspath(fbody), self.dim_, self.nodes, self.cells, self.cell_markers, self.boundaries,
+                         self.boundary_markers, self._data, writeCells)
 
     def __repr__(self):
         return (f"Mesh(dim={self.dim_}, order={self.order}, nodes={self.nodeCount()}, "

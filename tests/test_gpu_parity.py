@@ -371,3 +371,32 @@ def test_csr_spmm_dot_entry(torch, golden_dir):
     assert rel(dots.cpu().numpy(), d_ref) <= TOL_MAT
     rc, _, _ = _call_spmm(L.ertgb_csr_spmm_dot, n, nnz, t, 48, torch)
     assert rc == _native.BAD_INPUT and b"multiple of 32" in L.ertgb_last_error(None)
+
+
+@pytest.mark.parametrize("name", ["mesh2d", "mesh3d_p2"])
+def test_files_to_response(torch, name, tmp_path):
+    """Mesh from the reference's binary mesh file (every facet a boundary,
+    outer facets with only a right cell) and data through the unified data
+    format: the GPU response and Jacobian equal the oracle's on that mesh."""
+    io = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "io", "expected")
+    mesh = Mesh.load(os.path.join(io, name + ".bms"))
+    if mesh.dim() == 2:
+        d0 = createData(np.arange(4.0), "dd")
+        d0.set("k", geometricFactors(d0, 2))
+    else:
+        d0 = DataContainerERT(np.array([[0.0, 0.0, 0.0], [2.0, 0.0, 0.0]]),
+                              np.array([[0, -1, 1, -1], [1, -1, 0, -1]]))
+        d0.set("k", geometricFactors(d0, 3))
+    f = tmp_path / "scheme.dat"
+    d0.save(str(f), "a b m n k")
+    data = DataContainerERT(str(f))
+    assert np.array_equal(data.abmn(), d0.abmn())
+    rho = 20.0 + (np.arange(mesh.cellCount()) % 5) * 15.0
+    fop = fop_for(mesh, data)
+    rhoa = fop.response(rho)
+    J = fop.createJacobian(rho).cpu().numpy()
+    P = O.Problem(mesh, data.sensorPositions(), data.abmn(), data["k"], fop.kValues(), fop.weights())
+    rhoa_o, u = P.response(rho)
+    J_o = P.jacobian(u, rho)
+    assert rel(rhoa, rhoa_o) <= TOL_POT
+    assert np.linalg.norm(J - J_o) / np.linalg.norm(J_o) <= TOL_J
