@@ -248,30 +248,34 @@ __global__ void __launch_bounds__(256) k_spmm32_gen(int64_t n, int64_t nnzB, int
 }
 
 // FSAI iteration: y += alpha p, r -= alpha q (the dots follow from z = G^T G r)
-__global__ void k_m_update_yr(int64_t n, int64_t Rpad, const double *__restrict__ col,
-                              const int32_t *__restrict__ active, float *__restrict__ y, float *__restrict__ r,
-                              const float *__restrict__ p, const float *__restrict__ q) {
+// FSAI / learned iteration, first half: r -= alpha q
+__global__ void k_m_update_r(int64_t n, int64_t Rpad, const double *__restrict__ col,
+                             const int32_t *__restrict__ active, float *__restrict__ r, const float *__restrict__ q) {
     const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
     if (!active[t]) return;
     const float alpha = (float)col[ALPHA * Rpad + t];
 #pragma unroll 4
     for (int64_t row = (int64_t)blockIdx.y * kRows + threadIdx.y; row < n; row += (int64_t)gridDim.y * kRows) {
         const int64_t i = row * Rpad + t;
-        y[i] = fmaf(alpha, p[i], y[i]);
         r[i] = fmaf(-alpha, q[i], r[i]);
     }
 }
 
-// FSAI iteration: p = z + beta p
-__global__ void k_m_update_pz(int64_t n, int64_t Rpad, const double *__restrict__ col,
-                              const int32_t *__restrict__ active, const float *__restrict__ z, float *__restrict__ p) {
+// second half, after beta: y += alpha p with the p of this iteration, then
+// p = z + beta p (one pass over p for both)
+__global__ void k_m_update_pzy(int64_t n, int64_t Rpad, const double *__restrict__ col,
+                               const int32_t *__restrict__ active, const float *__restrict__ z, float *__restrict__ p,
+                               float *__restrict__ y) {
     const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
     if (!active[t]) return;
+    const float alpha = (float)col[ALPHA * Rpad + t];
     const float beta = (float)col[BETA * Rpad + t];
 #pragma unroll 4
     for (int64_t row = (int64_t)blockIdx.y * kRows + threadIdx.y; row < n; row += (int64_t)gridDim.y * kRows) {
         const int64_t i = row * Rpad + t;
-        p[i] = fmaf(beta, p[i], z[i]);
+        const float pv = p[i];
+        y[i] = fmaf(alpha, pv, y[i]);
+        p[i] = fmaf(beta, pv, z[i]);
     }
 }
 
@@ -589,10 +593,10 @@ int pcg_solve_mixed(Context &c, cudaStream_t s) {
                                c.d_q32.p, part_c);
             pcg_finish_alpha(fg, fb, s, Rpad, NB, part_c, c.d_col.p, active, nactive);
             if (fsai) {
-                k_m_update_yr<<<vgu, vb, 0, s>>>(n, Rpad, c.d_col.p, active, c.d_y32.p, c.d_r32.p, c.d_p32.p, c.d_q32.p);
+                k_m_update_r<<<vgu, vb, 0, s>>>(n, Rpad, c.d_col.p, active, c.d_r32.p, c.d_q32.p);
                 apply_fsai(part_a);
                 k_m_finish_beta<<<fg, fb, 0, s>>>(Rpad, NB, part_a, part_a, c.d_col.p, active, iters);
-                k_m_update_pz<<<vgu, vb, 0, s>>>(n, Rpad, c.d_col.p, active, c.d_z32.p, c.d_p32.p);
+                k_m_update_pzy<<<vgu, vb, 0, s>>>(n, Rpad, c.d_col.p, active, c.d_z32.p, c.d_p32.p, c.d_y32.p);
             } else {
                 k_m_update_xr<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, c.d_dinv32.p, c.d_col.p, active, c.d_y32.p,
                                                 c.d_r32.p, c.d_p32.p, c.d_q32.p, part_a, part_b);

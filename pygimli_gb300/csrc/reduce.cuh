@@ -21,12 +21,14 @@ struct ColState {
 };
 
 // Column reductions: block (32, 32), grid Rpad/32; thread (tx, ty) sums the
-// partial rows ty, ty+32, ... of column t, then the 32 sums are added in a
-// fixed order (deterministic).  Every thread of the block must call it.
+// partial rows ty, ty+32, ... of column t, then warp w adds the 32 sums of
+// the block's column w by a shuffle tree (five dependent FP64 additions
+// instead of 32: FP64 latency dominates these small kernels) in a fixed order
+// (deterministic).  The total is returned to the threads with ty == 0; every
+// thread of the block must call it.  red[w][32] holds column w's total.
 __device__ inline double col_sum(const double *__restrict__ part, int NB, int64_t Rpad, int64_t t,
                                  double (*red)[33]) {
-    // four independent accumulators keep several loads in flight; the
-    // grouping is fixed, so the sum is deterministic
+    // four independent accumulators keep several loads in flight
     double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
     int b = threadIdx.y;
     for (; b + 96 < NB; b += 128) {
@@ -38,10 +40,12 @@ __device__ inline double col_sum(const double *__restrict__ part, int NB, int64_
     for (; b < NB; b += 32) s0 += part[(int64_t)b * Rpad + t];
     red[threadIdx.y][threadIdx.x] = (s0 + s1) + (s2 + s3);
     __syncthreads();
-    double tot = 0.0;
-    if (threadIdx.y == 0)
-        for (int w = 0; w < 32; w++) tot += red[w][threadIdx.x];
-    return tot;
+    double v = red[threadIdx.x][threadIdx.y];  // warp ty: the 32 sums of column ty
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) red[threadIdx.y][32] = v;
+    __syncthreads();
+    return threadIdx.y == 0 ? red[threadIdx.x][32] : 0.0;
 }
 
 }  // namespace ertgb
