@@ -405,6 +405,22 @@ def run_ours(args, world, rank, local):
     if args.gn and rank == 0:
         gn = gn_iteration(args, mesh, data, rho, local, weights)
 
+    refine_rec = None
+    if rank == 0 and not args.no_plain:
+        # the forward-mesh refinement pyGIMLi applies to a parameter mesh
+        # (H2): device (ertgb_refine, incl. transfers) vs the host restatement
+        from pygimli_gb300 import refine as _refine
+        _refine.createH2(mesh, local)
+        t0 = time.perf_counter()
+        mh = _refine.createH2(mesh, local)
+        t_dev = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        mesh.createH2()
+        t_host = time.perf_counter() - t0
+        refine_rec = {"what": "H2 of the workload mesh", "cells_in": mesh.cellCount(), "cells_out": mh.cellCount(),
+                      "nodes_out": mh.nodeCount(), "device_s": t_dev, "host_numpy_s": t_host}
+        del mh
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle.cpu_baseline import SampledBaseline
@@ -425,6 +441,7 @@ def run_ours(args, world, rank, local):
                               f"{mesh.nodeCount() * 96 * 8 / 1e6:.0f} MB, J {D * P * 8 / 1e9:.1f} GB"),
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
                "plain_fp64_gpu_pcg": plain, "fsai_form": fsai_form, "gn_iteration": gn,
+               "refine_h2": refine_rec,
                "learned_weights": os.path.relpath(weights, ROOT) if weights else None,
                "clocks": clk,
                "breakdown_ms": {"assemble": st["ms_assemble"], "rhs": st["ms_rhs"], "solve": st["ms_solve"],

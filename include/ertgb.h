@@ -279,6 +279,34 @@ int ertgb_cgls(const void *J_dev, int dtype, int64_t n_data, int64_t n_model, in
                const double *wc, const double *wm, const double *tm, const double *td, double lambda,
                const double *rough, int max_iter, double tol, int32_t *iterations_out, void *stream);
 
+/* Uniform refinement of a linear simplex mesh on device ``device``.  mode 1:
+ * the quadratic mesh of Mesh::createP2 (Triangle6 / Tetrahedron10, one
+ * midpoint node per edge); mode 2: Mesh::createH2 (every triangle into 4,
+ * every tetrahedron into 8, boundaries into 2 / 4).  Node, cell and boundary
+ * numbering and markers are the reference's createRefined_
+ * (core/src/mesh.cpp:1278-1600), which pyGIMLi applies to every parameter
+ * mesh handed to the forward operator (pygimli/frameworks/modelling.py:
+ * 682-699, MeshModelling.createRefinedFwdMesh).  Inputs in host memory as
+ * for ertgb_set_mesh with order 1; bnd_cell (the adjacent cell of each
+ * boundary) may be NULL.  H2 boundaries get the child of their parent's
+ * adjacent cell that holds them (-1 without one).  The refined mesh stays on
+ * the device until ertgb_refined_get copies it out; errors:
+ * ertgb_last_error(NULL). */
+typedef struct ertgb_refined ertgb_refined;
+int ertgb_refine(int device, int dim, int mode, int64_t n_nodes, const double *xyz_host,
+                 const int32_t *node_marker_host, int64_t n_cells, const int32_t *cell_nodes_host,
+                 const int32_t *cell_marker_host, int64_t n_bnd, const int32_t *bnd_nodes_host,
+                 const int32_t *bnd_marker_host, const int32_t *bnd_cell_host, ertgb_refined **out);
+/* Nodes, cells, nodes per cell, boundaries and nodes per boundary of a refined mesh. */
+int ertgb_refined_sizes(const ertgb_refined *r, int64_t *n_nodes, int64_t *n_cells, int64_t *nv, int64_t *n_bnd,
+                        int64_t *nvb);
+/* Copy a refined mesh into host arrays sized by ertgb_refined_sizes (xyz:
+ * n_nodes x 3); a NULL array is skipped. */
+int ertgb_refined_get(const ertgb_refined *r, double *xyz_host, int32_t *node_marker_host, int32_t *cell_nodes_host,
+                      int32_t *cell_marker_host, int32_t *bnd_nodes_host, int32_t *bnd_marker_host,
+                      int32_t *bnd_cell_host);
+int ertgb_refined_free(ertgb_refined *r);
+
 #ifdef __cplusplus
 }
 #endif

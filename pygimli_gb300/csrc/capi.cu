@@ -742,4 +742,36 @@ int ertgb_cgls(const void *J, int dtype, int64_t D, int64_t P, int64_t NC, const
     }
 }
 
+int ertgb_refine(int device, int dim, int mode, int64_t n_nodes, const double *xyz, const int32_t *nmark,
+                 int64_t n_cells, const int32_t *cells, const int32_t *cmark, int64_t n_bnd, const int32_t *bnd,
+                 const int32_t *bmark, const int32_t *bcell, ertgb_refined **out) {
+    return guard_free([&] {
+        ERTGB_REQUIRE(out, "null output handle");
+        *out = nullptr;
+        *out = reinterpret_cast<ertgb_refined *>(
+            refine_mesh(device, dim, mode, n_nodes, xyz, nmark, n_cells, cells, cmark, n_bnd, bnd, bmark, bcell));
+    });
+}
+
+int ertgb_refined_sizes(const ertgb_refined *r, int64_t *n_nodes, int64_t *n_cells, int64_t *nv, int64_t *n_bnd,
+                        int64_t *nvb) {
+    return guard_free([&] {
+        ERTGB_REQUIRE(r && n_nodes && n_cells && nv && n_bnd && nvb, "null argument");
+        refined_sizes(reinterpret_cast<const Refined *>(r), n_nodes, n_cells, nv, n_bnd, nvb);
+    });
+}
+
+int ertgb_refined_get(const ertgb_refined *r, double *xyz, int32_t *nmark, int32_t *cells, int32_t *cmark,
+                      int32_t *bnd, int32_t *bmark, int32_t *bcell) {
+    return guard_free([&] {
+        ERTGB_REQUIRE(r, "null refined mesh");
+        refined_get(reinterpret_cast<const Refined *>(r), xyz, nmark, cells, cmark, bnd, bmark, bcell);
+    });
+}
+
+int ertgb_refined_free(ertgb_refined *r) {
+    refined_free(reinterpret_cast<Refined *>(r));
+    return ERTGB_OK;
+}
+
 }  // extern "C"

@@ -240,6 +240,16 @@ void spmm_dot_launch(int64_t n, int64_t nnz, const int32_t *rowptr, const int32_
                      cudaStream_t s);
 // Message returned by ertgb_last_error(NULL) for the context-free entry points.
 void set_free_error(const std::string &msg);
+
+// device mesh refinement (refine.cu)
+struct Refined;
+Refined *refine_mesh(int device, int dim, int mode, int64_t n0, const double *xyz, const int32_t *nmark, int64_t C,
+                     const int32_t *cells, const int32_t *cmark, int64_t B, const int32_t *bnd, const int32_t *bmark,
+                     const int32_t *bcell);
+void refined_sizes(const Refined *r, int64_t *n, int64_t *C, int64_t *nv, int64_t *B, int64_t *nvb);
+void refined_get(const Refined *r, double *xyz, int32_t *nmark, int32_t *cells, int32_t *cmark, int32_t *bnd,
+                 int32_t *bmark, int32_t *bcell);
+void refined_free(Refined *r);
 // Checks shared by the context-free operator entry points; throws Error.
 void check_spmm_args(int64_t n, int64_t nnz, const void *rowptr, const void *colidx, const void *vals, int n_k,
                      int n_per_k, int64_t ld, const void *X, const void *Y, const void *dots);

@@ -168,13 +168,15 @@ class ERTModelling:
     def createRefinedFwdMesh(self, mesh):
         """Forward mesh of a parameter mesh: H2 refinement, then P2, as
         enabled by ``_refineH2`` / ``_refineP2``
-        (pygimli/frameworks/modelling.py:682-699).  Refined cells keep their
-        parent's marker, so the model stays one value per parameter."""
+        (pygimli/frameworks/modelling.py:682-699), computed on this
+        operator's GPU (``refine.py``).  Refined cells keep their parent's
+        marker, so the model stays one value per parameter."""
+        from . import refine
         m = mesh
         if self._refineH2:
-            m = m.createH2()
+            m = refine.createH2(m, self.device)
         if self._refineP2:
-            m = m.createP2()
+            m = refine.createP2(m, self.device)
         return m
 
     def setMesh(self, mesh, ignoreRegionManager=False):

@@ -40,7 +40,9 @@ class Mesh:
     quadratic (P2: Triangle6 / Tetrahedron10 with edge-midpoint nodes)."""
 
     def __init__(self, dim, nodes, cells, cell_markers=None, node_markers=None,
-                 boundaries=None, boundary_markers=None, boundary_cells=None):
+                 boundaries=None, boundary_markers=None, boundary_cells=None, check=True):
+        """``check=False`` skips the degenerate-cell test (for refinements of
+        a checked mesh, whose children are never degenerate)."""
         self.dim_ = int(dim)
         nodes = np.asarray(nodes, dtype=np.float64)
         if nodes.shape[1] == 2:
@@ -73,7 +75,7 @@ class Mesh:
         self.boundary_right_cells = np.full(len(self.boundaries), -1, np.int32)
         self.geometry = False
         self._data = {}
-        if np.any(self._signed_sizes() == 0):
+        if check and np.any(self._signed_sizes() == 0):
             raise ValueError("degenerate cell in mesh")
 
     # -- reference-style accessors (core/src/mesh.h:331-351) --------------
@@ -310,7 +312,8 @@ def create_h2(mesh):
         bmk = np.repeat(mesh.boundary_markers, 2)
     nodes = np.concatenate([mesh.nodes, mids])
     node_markers = np.concatenate([mesh.node_markers, mid_markers])
-    return Mesh(mesh.dim(), nodes, cells2.astype(np.int32), markers2, node_markers, bnd2.astype(np.int32), bmk)
+    return Mesh(mesh.dim(), nodes, cells2.astype(np.int32), markers2, node_markers, bnd2.astype(np.int32), bmk,
+                check=False)
 
 
 def create_p2(mesh):
@@ -337,7 +340,7 @@ def create_p2(mesh):
     cells2 = np.concatenate([cells, cm.reshape(C, len(edges))], axis=1).astype(np.int32)
     bnd2 = np.concatenate([bnd, bm.reshape(len(bnd), len(bedges))], axis=1).astype(np.int32)
     return Mesh(mesh.dim(), nodes, cells2, mesh.cell_markers.copy(), node_markers, bnd2,
-                mesh.boundary_markers.copy(), mesh.boundary_cells.copy())
+                mesh.boundary_markers.copy(), mesh.boundary_cells.copy(), check=False)
 
 
 def _facet_keys(facets, n_nodes):
