@@ -79,6 +79,7 @@ def lib():
         L.ref_mesh_boundary_cells.argtypes = [vp, vp, vp]
         L.ref_mesh_add_data.argtypes = [vp, cs, ctypes.c_int, vp]
         L.ref_mesh_export_vtk.argtypes = [vp, cs, ctypes.c_int]
+        L.ref_regions.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, vp, ctypes.c_int, vp, vp, vp, vp, vp]
         L.ref_data_load.restype = vp
         L.ref_data_load.argtypes = [cs, ctypes.c_int, ctypes.c_int]
         L.ref_data_free.argtypes = [vp]
@@ -304,6 +305,21 @@ class RefMesh:
 
     def arrays(self):
         return _mesh_arrays(self.h)
+
+    def regions(self, default_background=True, background=(), single=(), fix=None):
+        """The reference's RegionManager on this mesh: (renumbered cell
+        markers, parameter count, para-domain cell count)."""
+        fix = fix or {}
+        bg = np.ascontiguousarray(list(background) or [0], np.int32)
+        sg = np.ascontiguousarray(list(single) or [0], np.int32)
+        fm = np.ascontiguousarray(list(fix) or [0], np.int32)
+        fv = np.ascontiguousarray(list(fix.values()) or [0.0], np.float64)
+        C = len(self.arrays()["cells"])
+        out = np.zeros(C, np.int32)
+        npar, ncell = ctypes.c_int(), ctypes.c_int()
+        _check(lib().ref_regions(self.h, int(default_background), len(background), _p(bg), len(single), _p(sg),
+                                 len(fix), _p(fm), _p(fv), _p(out), ctypes.byref(npar), ctypes.byref(ncell)))
+        return out, npar.value, ncell.value
 
     def add_data(self, name, values):
         v = np.ascontiguousarray(values, np.float64)

@@ -25,6 +25,7 @@
 #include <node.h>
 #include <meshentities.h>
 #include <sparsematrix.h>
+#include <regionManager.h>
 #include <solverWrapper.h>
 #include <bert/dcfemmodelling.h>
 #include <bert/bertDataContainer.h>
@@ -439,6 +440,31 @@ int ref_mesh_add_data(void *hp, const char *name, int n, const double *vals) {
 int ref_mesh_export_vtk(void *hp, const char *path, int writeCells) {
     RefHandle *h = (RefHandle *)hp;
     return guarded([&] { h->mesh.exportVTK(path, writeCells != 0); });
+}
+
+// RegionManager (core/src/regionManager.cpp) on the handle's mesh: regions
+// from the cell markers; with default_background the lowest of several
+// regions becomes background (pyGIMLi's setDefaultBackground); then the
+// given regions are set background, single or fixed, in that order.  Out:
+// the renumbered cell markers of the manager's mesh copy, the parameter count
+// and the cell count of its para domain.
+int ref_regions(void *hp, int default_background, int n_bg, const int *bg, int n_single, const int *single,
+                int n_fix, const int *fix_marker, const double *fix_value, int *cell_markers, int *n_param,
+                int *n_para_cells) {
+    RefHandle *h = (RefHandle *)hp;
+    return guarded([&] {
+        RegionManager rm(false);
+        rm.setMesh(h->mesh);
+        IVector ids(rm.regionIdxs());
+        if (default_background && ids.size() > 1) rm.region(min(ids))->setBackground(true);
+        for (int i = 0; i < n_bg; i++) rm.region(bg[i])->setBackground(true);
+        for (int i = 0; i < n_single; i++) rm.region(single[i])->setSingle(true);
+        for (int i = 0; i < n_fix; i++) rm.region(fix_marker[i])->setFixValue(fix_value[i]);
+        const Mesh &m = rm.mesh();
+        for (Index c = 0; c < m.cellCount(); c++) cell_markers[c] = m.cell(c).marker();
+        *n_param = (int)rm.parameterCount();
+        *n_para_cells = (int)rm.paraDomain().cellCount();
+    });
 }
 
 // DataContainerERT::load (unified data format).

@@ -99,6 +99,8 @@ class ERTModelling:
         # ignoreRegionManager (MeshModelling, pygimli/frameworks/modelling.py:584-586)
         self._refineH2 = True
         self._refineP2 = False
+        self._rm = None           # region manager of the parameter mesh (setMesh without ignoreRegionManager)
+        self._fwd_parent = None   # forward-mesh cell -> parameter-mesh cell
         self.setSolverTolerance(rtol, maxIter)
         self.setPrecision(precision)
         self.setPreconditioner(precond, weights)
@@ -180,15 +182,55 @@ class ERTModelling:
         return m
 
     def setMesh(self, mesh, ignoreRegionManager=False):
-        """Set the mesh.  ``ignoreRegionManager=True`` solves on ``mesh``
-        itself; otherwise the forward mesh is ``createRefinedFwdMesh(mesh)``
-        and the cell markers of ``mesh`` are the parameter indices (the
-        region manager's own marker bookkeeping -- background and single
-        regions -- is not provided)."""
+        """Set the mesh (MeshModelling.setMesh, pygimli/frameworks/
+        modelling.py:730-757).  ``ignoreRegionManager=True`` solves on
+        ``mesh`` itself with its cell markers as parameter indices.
+        Otherwise the region manager takes the cell markers as regions (the
+        lowest of several becomes background, regions.py), renumbers them
+        into parameter indices, and the forward mesh is
+        ``createRefinedFwdMesh`` of the renumbered mesh."""
         if not isinstance(mesh, Mesh):
             raise TypeError("mesh must be a pygimli_gb300.mesh.Mesh")
-        if not ignoreRegionManager:
-            mesh = self.createRefinedFwdMesh(mesh)
+        if ignoreRegionManager:
+            self._rm = None
+            self._fwd_parent = None
+            self._set_fwd_mesh(mesh)
+            return
+        from .regions import RegionManager
+        rm = RegionManager()
+        rm.setMesh(mesh)
+        rm.setDefaultBackground()
+        self._rm = rm
+        para = Mesh(mesh.dim(), mesh.nodes, mesh.cells, rm.paraMarkers(), mesh.node_markers, mesh.boundaries,
+                    mesh.boundary_markers, mesh.boundary_cells, check=False)
+        fwd = self.createRefinedFwdMesh(para)
+        ratio = fwd.cellCount() // para.cellCount()
+        self._fwd_parent = np.arange(fwd.cellCount(), dtype=np.int64) // ratio
+        self._set_fwd_mesh(fwd)
+
+    def regionManager(self):
+        return self._rm
+
+    def setRegionProperties(self, regionNr, background=None, single=None, fix=None, **kwargs):
+        """Background / single / fixed-value flags of a region ("*": all),
+        as MeshModelling.setRegionProperties (pygimli/frameworks/
+        modelling.py:330-390); the parameters are renumbered.  Start
+        models, bounds and constraint settings belong to the inversion and
+        are not kept."""
+        if self._rm is None:
+            raise RuntimeError("no region manager: setMesh(mesh) without ignoreRegionManager first")
+        self._rm.setRegionProperties(regionNr, background=background, single=single, fix=fix)
+        fwd = self._mesh
+        fwd.setCellMarkers(self._rm.paraMarkers()[self._fwd_parent])
+        self._set_fwd_mesh(fwd)
+
+    @property
+    def paraDomain(self):
+        """Mesh of the parameter cells (the region manager's para domain);
+        without a region manager the forward mesh."""
+        return self._rm.paraDomain() if self._rm is not None else self._mesh
+
+    def _set_fwd_mesh(self, mesh):
         surf, topo = surface_info(mesh)
         if topo:
             raise NotImplementedError("meshes with topography need numerical primary potentials (not supported)")
@@ -268,6 +310,8 @@ class ERTModelling:
 
     @property
     def parameterCount(self):
+        if self._rm is not None:
+            return self._rm.parameterCount()
         return int(self._mesh.cell_markers.max()) + 1
 
     def calcGeometricFactor(self, data=None):
@@ -277,7 +321,8 @@ class ERTModelling:
         return geometricFactors(data, self._mesh.dim())
 
     def mapERTModel(self, model, background=-9e99):
-        return map_model(self._mesh, model, background)
+        fixed = self._rm.fixedValues() if self._rm is not None else None
+        return map_model(self._mesh, model, background, fixed)
 
     # ---------------------------------------------------------- forward
     def _ready(self):

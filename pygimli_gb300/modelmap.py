@@ -1,7 +1,7 @@
 """Model -> per-cell resistivity mapping.
 
-Restates ModellingBase::createMappedModel (core/src/modellingbase.cpp:401-497,
-without fixed-value regions, which need the region manager) and
+Restates ModellingBase::createMappedModel (core/src/modellingbase.cpp:401-497)
+and
 Mesh::prolongateEmptyCellsValues (core/src/mesh.cpp:2247-2316):
   * a model with one value per cell whose marker count differs is used as is;
   * otherwise cell c gets model[marker(c)];
@@ -14,6 +14,7 @@ from __future__ import annotations
 import numpy as np
 
 TOLERANCE = 1e-12
+MARKER_FIXEDVALUE_REGION = -1000000  # core/src/gimli.h:241
 
 
 def _neighbours(mesh):
@@ -87,8 +88,10 @@ def _marker_count(mesh):
     return cnt
 
 
-def map_model(mesh, model, background=-9e99):
-    """Per-cell resistivity for ``model`` (per cell or per marker)."""
+def map_model(mesh, model, background=-9e99, fixed=None):
+    """Per-cell resistivity for ``model`` (per cell or per marker); cells of
+    fixed-value regions (marker MARKER_FIXEDVALUE_REGION - region) get
+    ``fixed[region]`` after the prolongation (modellingbase.cpp:465-494)."""
     model = np.asarray(model, dtype=np.float64)
     mk = mesh.cell_markers
     C = mesh.cellCount()
@@ -103,4 +106,10 @@ def map_model(mesh, model, background=-9e99):
         raise ValueError("too many empty cells")
     if background != 0.0:
         prolongate_empty_cells(mesh, att, background)
+    fx = mk <= MARKER_FIXEDVALUE_REGION
+    if fx.any():
+        if not fixed:
+            raise ValueError("fixed-value region cells but no fixed values")
+        regions = -(mk[fx].astype(np.int64) - MARKER_FIXEDVALUE_REGION)
+        att[fx] = np.array([fixed[int(r)] for r in regions])
     return att

@@ -1,0 +1,159 @@
+"""Region bookkeeping of a parameter mesh: the part of the reference's
+``RegionManager`` that decides which cell carries which model parameter.
+
+Restates core/src/regionManager.cpp: ``setMesh`` (617-689: one region per
+distinct cell marker, ascending; more than 50 regions are all single),
+``recountParaMarker_`` (760-766) with ``Region::countParameter`` (173-201:
+a background region's cells get marker -1, or MARKER_FIXEDVALUE_REGION -
+marker with a fixed value; a single region is one parameter; any other
+region has one parameter per cell, in cell order), ``createParaDomain_``
+(734-750: the cells of the regions that are not background), and pyGIMLi's
+``MeshModelling.setDefaultBackground`` (pygimli/frameworks/modelling.py:
+757-767: with several regions the lowest marker becomes background).
+Constraint and transformation settings of regions belong to the inversion
+framework and are not kept here.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .mesh import Mesh
+
+MARKER_FIXEDVALUE_REGION = -1000000  # core/src/gimli.h:241
+TOLERANCE = 1e-12
+
+
+class Region:
+    """One region: its marker, its cells (ascending ids) and its flags."""
+
+    def __init__(self, marker, cells, single=False):
+        self.marker = int(marker)
+        self.cells = np.asarray(cells, np.int64)
+        self._background = False
+        self._single = bool(single)
+        self._fix = 0.0
+        self.startParameter = 0
+        self._count = 0
+
+    def isBackground(self):
+        return self._background
+
+    def isSingle(self):
+        return self._single
+
+    def fixValue(self):
+        return self._fix
+
+    def parameterCount(self):
+        return self._count
+
+    def setBackground(self, b=True):
+        self._background = bool(b)
+
+    def setSingle(self, b=True):
+        self._single = bool(b)
+
+    def setFixValue(self, v):
+        """A fixed region is background: its cells take the value, no parameter."""
+        self._fix = float(v)
+        self._background = True
+
+
+class RegionManager:
+    """Regions of a parameter mesh and the resulting parameter markers."""
+
+    def __init__(self):
+        self._regions = {}
+        self._mesh = None
+        self._markers = None
+
+    def setMesh(self, mesh):
+        self._mesh = mesh
+        mk = np.asarray(mesh.cell_markers, np.int64)
+        self._markers = mk.copy()  # the mesh copy's cell markers, renumbered by recount()
+        uniq = np.unique(mk)
+        single_only = len(uniq) > 50
+        order = np.argsort(mk, kind="stable")
+        bounds = np.searchsorted(mk[order], uniq)
+        ends = np.append(bounds[1:], len(mk))
+        self._regions = {int(m): Region(m, order[b:e], single_only) for m, b, e in zip(uniq, bounds, ends)}
+        self.recount()
+
+    def regionIdxs(self):
+        return sorted(self._regions)
+
+    def regionCount(self):
+        return len(self._regions)
+
+    def region(self, marker):
+        if int(marker) not in self._regions:
+            raise KeyError(f"no region with marker {marker}")
+        return self._regions[int(marker)]
+
+    def setRegionProperties(self, marker, background=None, single=None, fix=None):
+        markers = self.regionIdxs() if marker == "*" else [marker]
+        for m in markers:
+            r = self.region(m)
+            if background is not None:
+                r.setBackground(background)
+            if single is not None:
+                r.setSingle(single)
+            if fix is not None:
+                r.setFixValue(fix)
+        self.recount()
+
+    def setDefaultBackground(self):
+        """With several regions, the lowest marker is background."""
+        ids = self.regionIdxs()
+        if len(ids) > 1:
+            self.setRegionProperties(ids[0], background=True)
+
+    def recount(self):
+        start = 0
+        for m in self.regionIdxs():
+            r = self._regions[m]
+            r.startParameter = start
+            c = r.cells
+            if r.isBackground():
+                if abs(r.fixValue()) > TOLERANCE:
+                    sel = c[self._markers[c] >= -1]
+                    self._markers[sel] = MARKER_FIXEDVALUE_REGION - m
+                else:
+                    self._markers[c] = -1
+                r._count = 0
+            elif r.isSingle():
+                self._markers[c] = start
+                r._count = 1
+            else:
+                self._markers[c] = start + np.arange(len(c))
+                r._count = len(c)
+            start += r._count
+
+    def parameterCount(self):
+        return int(sum(r.parameterCount() for r in self._regions.values()))
+
+    def paraMarkers(self):
+        """Cell markers of the parameter mesh: parameter index, -1 for
+        background cells, MARKER_FIXEDVALUE_REGION - region for fixed ones."""
+        return self._markers.astype(np.int32)
+
+    def fixedValues(self):
+        """{region marker: fixed value} of the fixed regions."""
+        return {m: r.fixValue() for m, r in self._regions.items()
+                if r.isBackground() and abs(r.fixValue()) > TOLERANCE}
+
+    def paraDomain(self):
+        """Mesh of the cells of non-background regions (Mesh::createMeshByCells,
+        core/src/mesh.cpp:2008-2046: ascending cell ids, nodes renumbered in
+        order of first use), with the parameter indices as cell markers;
+        boundaries are not copied."""
+        mesh = self._mesh
+        keep = np.sort(np.concatenate([r.cells for r in self._regions.values() if not r.isBackground()]
+                                      or [np.zeros(0, np.int64)]))
+        cells = mesh.cells[keep, :mesh.dim() + 1]
+        used, first = np.unique(cells.ravel(), return_index=True)
+        order = used[np.argsort(first, kind="stable")]
+        remap = np.full(mesh.nodeCount(), -1, np.int64)
+        remap[order] = np.arange(len(order))
+        return Mesh(mesh.dim(), mesh.nodes[order], remap[cells].astype(np.int32), self._markers[keep].astype(np.int32),
+                    mesh.node_markers[order], check=False)

@@ -231,6 +231,9 @@ def test_forward_mesh_refinement(torch, golden_dir, name):
     fop = ERTModelling(precision="mixed", precond="fsai")
     fop.setData(data)
     fop.setMesh(para)
+    # one region per cell marker: the lowest became background; make every
+    # cell a parameter again, as the fixture's reference run has it
+    fop.setRegionProperties(int(para.cell_markers.min()), background=False)
     assert fop.mesh().cellCount() == para.cellCount() * (4 if para.dim() == 2 else 8)
     assert fop.parameterCount == para.cellCount()
     rhoa = fop.response(z["rho"])
@@ -398,5 +401,42 @@ def test_files_to_response(torch, name, tmp_path):
     P = O.Problem(mesh, data.sensorPositions(), data.abmn(), data["k"], fop.kValues(), fop.weights())
     rhoa_o, u = P.response(rho)
     J_o = P.jacobian(u, rho)
+    assert rel(rhoa, rhoa_o) <= TOL_POT
+    assert np.linalg.norm(J - J_o) / np.linalg.norm(J_o) <= TOL_J
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_region_manager_forward(torch, dim):
+    """setMesh(mesh) with region markers (1 outside, 2 parameter box, 3 and 4
+    blocks): region 1 becomes background (filled from its neighbours),
+    region 3 is fixed, region 4 single; response and Jacobian over the
+    renumbered parameters equal the oracle's on the same forward mesh."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from make_regions_golden import region_mesh
+    from pygimli_gb300 import ERTModelling
+    m = region_mesh(dim)
+    if dim == 2:
+        data = createData(np.arange(9.0), "dd")
+    else:
+        e = np.array([(x, y, 0.0) for x in (0.0, 2.0, 4.0) for y in (0.0, 2.0)])
+        data = DataContainerERT(e, np.array([[0, 1, 2, 3], [0, 2, 4, 5], [1, 3, 0, 5], [2, 4, 1, 3]]))
+    data.set("k", geometricFactors(data, dim))
+    fop = ERTModelling()
+    fop.setData(data)
+    fop.setMesh(m)
+    fop.setRegionProperties(3, fix=50.0)
+    fop.setRegionProperties(4, single=True)
+    P = fop.parameterCount
+    assert P == fop.regionManager().parameterCount()
+    model = np.linspace(20.0, 200.0, P)
+    rhoa = fop.response(model)
+    J = fop.createJacobian(model).cpu().numpy()
+    fwd = fop.mesh()
+    att = fop.mapERTModel(model)
+    Po = O.Problem(fwd, data.sensorPositions(), data.abmn(), data["k"], fop.kValues(), fop.weights())
+    rhoa_o, u = Po.response(att)
+    J_o = Po.jacobian(u, model, n_params=P)
+    assert J.shape == (data.size(), P)
     assert rel(rhoa, rhoa_o) <= TOL_POT
     assert np.linalg.norm(J - J_o) / np.linalg.norm(J_o) <= TOL_J
