@@ -560,6 +560,73 @@ class Problem:
             J = J / ((np.asarray(model) ** 2)[None, :] / self.kfac[:, None])
         return J
 
+    # ------------------------------------------------ complex resistivity --
+    # With complex resistivities the reference's SR operator falls back to
+    # the total-potential formulation of DCMultiElectrodeModelling
+    # (calculateK_, core/src/bert/dcfemmodelling.cpp:1756-1929): complex
+    # symmetric matrices sum (1/rho*) (K + k^2 M) + mixed term alpha / rho*,
+    # a unit point source at the current electrode's node, no singularity
+    # removal, no rounding and no reciprocity in the response.
+    def assemble_complex(self, rho_c, kidx):
+        """Complex system matrix values (CSR order) for wavenumber kidx
+        (dcfemmodelling.cpp:163-215, 217-300 with complex attributes)."""
+        kk = self.k[kidx]
+        vals = np.zeros(len(self.cols), complex)
+        Se = self.M * (kk * kk) + self.K if kk > 0.0 else self.K
+        rho_c = np.asarray(rho_c, complex)
+        valid = np.abs(rho_c) > TOLERANCE
+        sigma = np.where(valid, 1.0 / np.where(valid, rho_c, 1.0), 0.0)
+        np.add.at(vals, self.cell_slot.ravel(), (Se * sigma[:, None, None]).ravel())
+        if len(self.mixed):
+            bc = self.bnd_mass * (self.alpha[kidx] / rho_c[self.bnd_cell])[:, None, None]
+            np.add.at(vals, self.bnd_slot.ravel(), bc.ravel())
+        return vals
+
+    def solve_complex(self, rho_c):
+        """Total potentials u[kIdx, e, node] for a unit source at each
+        electrode node (ElectrodeShapeNode::assembleRHS, electrode.cpp:133-141)."""
+        nK = len(self.k)
+        u = np.zeros((nK, self.nE, self.n), complex)
+        for ki in range(nK):
+            S = sp.csr_matrix((self.assemble_complex(rho_c, ki), self.cols, self.rowptr), shape=(self.n, self.n))
+            lu = spla.splu(S.tocsc(), permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=0.0)
+            for e in range(self.nE):
+                rhs = np.zeros(self.n, complex)
+                rhs[self.enodes[e]] = 1.0
+                u[ki, e] = lu.solve(rhs)
+        return u
+
+    def response_complex(self, rho_c):
+        """Complex apparent resistivities k * u_ABMN (dcfemmodelling.cpp:
+        1103-1119, DataMap::data, datamap.cpp:159-232) and the potentials."""
+        rho_c = np.asarray(rho_c, complex)
+        if np.min(np.abs(rho_c)) < TOLERANCE:
+            raise ValueError("complex response for abs model with negative or zero resistivity is not defined")
+        u = self.solve_complex(rho_c)
+        return self.data_u(self.collect(u)) * self.kfac, u
+
+    def jacobian_complex(self, u, model_c, n_params=None):
+        """Complex J[d, p] (createSensitivityCol with complex potentials,
+        J /= model^2 / k without conjugation, dcfemmodelling.cpp:1410-1431)."""
+        mk = self.mesh.cell_markers
+        P = int(mk.max()) + 1 if n_params is None else n_params
+        J = np.zeros((len(self.abmn), P), complex)
+        cells = self.mesh.cells
+        sel = np.nonzero(mk >= 0)[0]
+        ab = self.abmn
+        for ki, kk in enumerate(self.k):
+            S = self.M[sel] * (kk * kk) + self.K[sel]
+            Uc = np.transpose(u[ki][:, cells[sel]], (1, 2, 0))
+            Uc = np.concatenate([Uc, np.zeros(Uc.shape[:2] + (1,), complex)], axis=2)
+            V = np.einsum("cij,cje->cie", S, Uc)
+            a, b, m, n = ab[:, 0], ab[:, 1], ab[:, 2], ab[:, 3]
+            contrib = np.einsum("cid,cid->dc", V[:, :, a] - V[:, :, b], Uc[:, :, m] - Uc[:, :, n]) * self.w[ki]
+            np.add.at(J.T, mk[sel], contrib.T)
+        model_c = np.asarray(model_c, complex)
+        if len(model_c) == P:
+            J = J / ((model_c ** 2)[None, :] / self.kfac[:, None])
+        return J
+
 
 def map_model(mesh, model, background=-9e99):
     """createMappedModel (modellingbase.cpp:401-497) without fixed regions:

@@ -28,6 +28,10 @@ _FACTOR = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_vo
                            ctypes.c_void_p, ctypes.c_void_p)
 _SOLVE = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p)
 
+_CFACTOR = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                            ctypes.c_void_p, ctypes.c_void_p)
+_CSOLVE = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p)
+
 _lib = None
 
 
@@ -50,6 +54,9 @@ def lib():
         L.ref_last_error.restype = ctypes.c_char_p
         L.ref_set_solver.argtypes = [vp, _FACTOR, _SOLVE]
         L.ref_set_threads.argtypes = [vp, ctypes.c_int]
+        L.ref_set_complex_solver.argtypes = [vp, _CFACTOR, _CSOLVE]
+        L.ref_response_complex.argtypes = [vp, vp, ctypes.c_int, vp]
+        L.ref_jacobian_complex.argtypes = [vp, vp, ctypes.c_int, vp, vp, vp, vp]
         L.ref_set_kw.argtypes = [vp, ctypes.c_int, vp, vp]
         L.ref_kw_count.argtypes = [vp]
         L.ref_get_kw.argtypes = [vp, vp, vp]
@@ -152,8 +159,35 @@ class RefModelling:
             except Exception:  # pragma: no cover
                 return 1
 
-        self._cb = (_FACTOR(factor), _SOLVE(solve))
+        self._clu = None
+
+        def cfactor(n, nnz, rowptr, colidx, vals):
+            try:
+                rp = np.ctypeslib.as_array(ctypes.cast(rowptr, ctypes.POINTER(ctypes.c_int)), (n + 1,)).copy()
+                ci = np.ctypeslib.as_array(ctypes.cast(colidx, ctypes.POINTER(ctypes.c_int)), (nnz,)).copy()
+                va = np.ctypeslib.as_array(ctypes.cast(vals, ctypes.POINTER(ctypes.c_double)), (2 * nnz,))
+                A = sp.csr_matrix((va[0::2] + 1j * va[1::2], ci, rp), shape=(n, n))
+                if self.keep_matrices:
+                    self.matrices.append((rp, ci, va[0::2] + 1j * va[1::2]))
+                self._clu = spla.splu(A.tocsc(), permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=0.0)
+                return 0
+            except Exception:  # pragma: no cover - reported through the C layer
+                return 1
+
+        def csolve(n, rhs, x):
+            try:
+                b = np.ctypeslib.as_array(ctypes.cast(rhs, ctypes.POINTER(ctypes.c_double)), (2 * n,))
+                out = np.ctypeslib.as_array(ctypes.cast(x, ctypes.POINTER(ctypes.c_double)), (2 * n,))
+                sol = self._clu.solve(b[0::2] + 1j * b[1::2])
+                out[0::2] = sol.real
+                out[1::2] = sol.imag
+                return 0
+            except Exception:  # pragma: no cover
+                return 1
+
+        self._cb = (_FACTOR(factor), _SOLVE(solve), _CFACTOR(cfactor), _CSOLVE(csolve))
         _check(L.ref_set_solver(h, self._cb[0], self._cb[1]))
+        _check(L.ref_set_complex_solver(h, self._cb[2], self._cb[3]))
         _check(L.ref_set_threads(h, int(threads)))
 
     def mesh_arrays(self):
@@ -218,6 +252,23 @@ class RefModelling:
         out = np.zeros((r.value, c.value))
         _check(lib().ref_subpotentials(self.h, _p(out)))
         return out
+
+    def response_complex(self, model_re, model_im):
+        """Complex resistivity: [Re, Im] of the apparent resistivities for the
+        model (Re, Im) (setComplex(true) + response)."""
+        m = np.ascontiguousarray(np.concatenate([model_re, model_im]), np.float64)
+        out = np.zeros(2 * self.nData)
+        _check(lib().ref_response_complex(self.h, _p(m), len(m), _p(out)))
+        return out[:self.nData] + 1j * out[self.nData:]
+
+    def jacobian_complex(self, model_re, model_im):
+        m = np.ascontiguousarray(np.concatenate([model_re, model_im]), np.float64)
+        r, c = ctypes.c_int(), ctypes.c_int()
+        _check(lib().ref_jacobian_complex(self.h, _p(m), len(m), None, None, ctypes.byref(r), ctypes.byref(c)))
+        Jr = np.zeros((r.value, c.value))
+        Ji = np.zeros((r.value, c.value))
+        _check(lib().ref_jacobian_complex(self.h, _p(m), len(m), _p(Jr), _p(Ji), ctypes.byref(r), ctypes.byref(c)))
+        return Jr + 1j * Ji
 
     def jacobian(self, model):
         m = np.ascontiguousarray(model, np.float64)

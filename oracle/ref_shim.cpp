@@ -51,6 +51,9 @@ typedef int (*ref_factor_fn)(int n, int nnz, const int *rowptr,
                              const int *colidx, const double *vals);
 // solve(n, rhs, x): x = A^{-1} rhs for the last factored matrix.
 typedef int (*ref_solve_fn)(int n, const double *rhs, double *x);
+// complex variants (values, right-hand side and solution interleaved re, im)
+typedef int (*ref_cfactor_fn)(int n, int nnz, const int *rowptr, const int *colidx, const double *vals);
+typedef int (*ref_csolve_fn)(int n, const double *rhs, double *x);
 }
 
 namespace {
@@ -73,16 +76,45 @@ public:
         int rc = s_(n_, &rhs[0], &sol[0]);
         if (rc != 0) throwError("oracle solve callback failed");
     }
+    void setComplex(ref_cfactor_fn f, ref_csolve_fn s) { cf_ = f; cs_ = s; }
+    void setMatrix(const CSparseMatrix &S) override {
+        if (!cf_) throwError("no complex solver callback");
+        const std::vector<int> &cp = S.vecColPtr();
+        const std::vector<int> &ri = S.vecRowIdx();
+        const CVector &v = S.vecVals();
+        n_ = (int)S.rows();
+        int rc = cf_(n_, (int)ri.size(), cp.data(), ri.data(), reinterpret_cast<const double *>(&v[0]));
+        if (rc != 0) throwError("oracle complex factor callback failed");
+    }
+    void solve(const CVector &rhs, CVector &sol) override {
+        if ((int)sol.size() != n_) sol.resize(n_);
+        int rc = cs_(n_, reinterpret_cast<const double *>(&rhs[0]), reinterpret_cast<double *>(&sol[0]));
+        if (rc != 0) throwError("oracle complex solve callback failed");
+    }
 private:
     ref_factor_fn f_;
     ref_solve_fn s_;
+    ref_cfactor_fn cf_ = nullptr;
+    ref_csolve_fn cs_ = nullptr;
     int n_ = 0;
+};
+
+// The reference operator plus one helper: drop the caller-owned real
+// sub-potential matrix so that the complex path allocates its own.
+struct ShimFop : DCSRMultiElectrodeModelling {
+    explicit ShimFop(bool verbose) : DCSRMultiElectrodeModelling(verbose) {}
+    void detachSubpotentials() {
+        if (!subpotOwner_) {
+            subSolutions_ = nullptr;
+            subpotOwner_ = true;
+        }
+    }
 };
 
 struct RefHandle {
     Mesh mesh;
     DataContainerERT data;
-    DCSRMultiElectrodeModelling *fop = nullptr;
+    ShimFop *fop = nullptr;
     CallbackSolver *solver = nullptr;
     RMatrix subpots;          // collected sub-potentials (nE*nK x nNodes)
     RefHandle(int dim) : mesh(dim) {}
@@ -149,7 +181,7 @@ void *ref_create(int dim, int nNodes, const double *xyz, const int *nodeMarker,
             for (int d = 0; d < nData; d++) k[d] = kfac[d];
             h->data.set("k", k);
         }
-        h->fop = new DCSRMultiElectrodeModelling(verbose != 0);
+        h->fop = new ShimFop(verbose != 0);
         h->fop->setData(h->data);
         h->fop->setMesh(h->mesh, true);
         h->fop->collectSubPotentials(h->subpots);
@@ -202,6 +234,55 @@ int ref_set_solver(void *hp, ref_factor_fn f, ref_solve_fn s) {
         delete h->solver;
         h->solver = new CallbackSolver(f, s);
         h->fop->setSolver(h->solver);
+    });
+}
+
+// Complex solve callbacks (the complex-resistivity path factors complex
+// symmetric matrices, core/src/bert/dcfemmodelling.cpp:1756-1929).
+int ref_set_complex_solver(void *hp, ref_cfactor_fn f, ref_csolve_fn s) {
+    RefHandle *h = (RefHandle *)hp;
+    return guarded([&] {
+        if (!h->solver) throwError("set the real solver first");
+        h->solver->setComplex(f, s);
+    });
+}
+
+// Complex resistivity: setComplex(true) and response([re, im]) -> [re, im]
+// of the apparent resistivities (dcfemmodelling.cpp:1103-1119).
+int ref_response_complex(void *hp, const double *model, int nModel2, double *out) {
+    RefHandle *h = (RefHandle *)hp;
+    return guarded([&] {
+        h->fop->detachSubpotentials();
+        h->fop->setComplex(true);
+        RVector m(nModel2);
+        for (int i = 0; i < nModel2; i++) m[i] = model[i];
+        RVector r(h->fop->response(m));
+        for (Index i = 0; i < r.size(); i++) out[i] = r[i];
+    });
+}
+
+// createJacobian([re, im]) in complex mode, J (rows x cols complex) as
+// separate real and imaginary parts.
+int ref_jacobian_complex(void *hp, const double *model, int nModel2, double *J_re, double *J_im, int *rows,
+                         int *cols) {
+    RefHandle *h = (RefHandle *)hp;
+    return guarded([&] {
+        h->fop->detachSubpotentials();
+        h->fop->setComplex(true);
+        RVector m(nModel2);
+        for (int i = 0; i < nModel2; i++) m[i] = model[i];
+        h->fop->createJacobian(m);
+        CMatrix *Jm = dynamic_cast<CMatrix *>(h->fop->jacobian());
+        if (!Jm) throwError("no complex Jacobian");
+        *rows = (int)Jm->rows();
+        *cols = (int)Jm->cols();
+        if (J_re) {
+            for (Index i = 0; i < Jm->rows(); i++)
+                for (Index j = 0; j < Jm->cols(); j++) {
+                    J_re[i * Jm->cols() + j] = (*Jm)[i][j].real();
+                    J_im[i * Jm->cols() + j] = (*Jm)[i][j].imag();
+                }
+        }
     });
 }
 

@@ -83,6 +83,31 @@ def case(name, mesh, data, seed, threads=1, p2=False, h2=False):
     print(name, mesh, len(data), "k:", len(k), "J:", J.shape)
 
 
+def case_complex(name, mesh, data, seed):
+    """Complex resistivity (setComplex(true): the reference's total-potential
+    path with complex symmetric matrices): per-cell complex resistivity of
+    amplitude 50-200 Ohm m and phase -5 to -30 mrad (one value per cell
+    marker), complex apparent resistivities and the complex Jacobian."""
+    if only and name not in only:
+        return
+    R = RefModelling(mesh, data.sensorPositions(), data.abmn(), data["k"])
+    k, w = R.kw()
+    rng = np.random.default_rng(seed)
+    C = mesh.cellCount()
+    rho_c = np.exp(rng.uniform(np.log(50.0), np.log(200.0), C)) * np.exp(-1j * rng.uniform(0.005, 0.03, C))
+    rhoa = R.response_complex(rho_c.real, rho_c.imag)
+    J = R.jacobian_complex(rho_c.real, rho_c.imag)
+    np.savez_compressed(
+        os.path.join(OUT, name + ".npz"),
+        dim=mesh.dim(), nodes=mesh.nodes, cells=mesh.cells, cell_markers=mesh.cell_markers,
+        node_markers=mesh.node_markers, boundaries=mesh.boundaries,
+        boundary_markers=mesh.boundary_markers, boundary_cells=mesh.boundary_cells,
+        sensors=data.sensorPositions(), abmn=data.abmn(), kfac=data["k"], k=k, w=w,
+        rho=rho_c, rhoa=rhoa, J=J, p2=0)
+    R.close()
+    print(name, mesh, len(data), "k:", len(k), "J:", J.shape)
+
+
 def bessel_table():
     x = np.concatenate([np.geomspace(1e-6, 2.0, 60), np.linspace(2.0, 40.0, 60), [2.0, 3.75, 50.0]])
     k0 = np.array([besselK0(v) for v in x])
@@ -146,6 +171,9 @@ def main():
     # modelling (one parameter per parent cell)
     case("ert2d_h2_small", m2p, d2p, seed=16, h2=True)
     case("ert3d_h2_small", m3p, d3p, seed=17, h2=True)
+    # complex resistivity (induced polarisation)
+    case_complex("ert2d_complex_small", m2p, d2p, seed=18)
+    case_complex("ert3d_complex_small", m3p, d3p, seed=19)
 
 
 if __name__ == "__main__":

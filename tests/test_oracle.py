@@ -110,3 +110,17 @@ def test_oracle_model_mapping_prolongation(golden_dir):
     assert np.all(a > 0) and np.allclose(a, b, rtol=1e-14, atol=0)
     c = map_model(mesh, model, background=42.0)
     assert np.all(c[mk == -1] == 42.0)
+
+
+@pytest.mark.parametrize("name", ["ert2d_complex_small", "ert3d_complex_small"])
+def test_complex_oracle_matches_reference(golden_dir, name):
+    """Complex resistivity: the oracle's total-potential restatement equals
+    the reference's own complex path (setComplex(true)) to rounding."""
+    z = np.load(os.path.join(golden_dir, name + ".npz"))
+    mesh = Mesh(int(z["dim"]), z["nodes"], z["cells"], z["cell_markers"], z["node_markers"],
+                z["boundaries"], z["boundary_markers"], z["boundary_cells"])
+    P = O.Problem(mesh, z["sensors"], z["abmn"], z["kfac"], z["k"], z["w"])
+    r, u = P.response_complex(z["rho"])
+    assert np.max(np.abs(r - z["rhoa"]) / np.abs(z["rhoa"])) < 1e-12
+    J = P.jacobian_complex(u, z["rho"])
+    assert np.linalg.norm(J - z["J"]) / np.linalg.norm(z["J"]) < 1e-12
