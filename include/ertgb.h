@@ -279,6 +279,26 @@ int ertgb_cgls(const void *J_dev, int dtype, int64_t n_data, int64_t n_model, in
                const double *wc, const double *wm, const double *tm, const double *td, double lambda,
                const double *rough, int max_iter, double tol, int32_t *iterations_out, void *stream);
 
+/* Complex resistivity (induced polarisation): the response of
+ * DCMultiElectrodeModelling with setComplex(true) (core/src/bert/
+ * dcfemmodelling.cpp:573-583, 1103-1119), which with complex resistivities
+ * uses the total-potential formulation (calculateK_, :1756-1929: complex
+ * symmetric matrices, unit point sources, no singularity removal) — solved
+ * here by a block COCG with Jacobi preconditioning in FP64 to the context's
+ * tolerance.  rho_re / rho_im: per-cell complex resistivity (device, n_cells
+ * each); rhoa_re / rhoa_im: complex apparent resistivities k * u (device,
+ * n_data each; the reference returns them as [re, im]). */
+int ertgb_response_complex(ertgb_ctx *ctx, const double *rho_re_dev, const double *rho_im_dev, double *rhoa_re_dev,
+                           double *rhoa_im_dev, void *stream);
+/* Complex Jacobian of the last complex response (createJacobian in complex
+ * mode, dcfemmodelling.cpp:1410-1431, 1446-1458): J_dev receives n_data x
+ * n_param complex values, interleaved (re, im), row-major; with a model of
+ * one complex value per parameter (n_model = n_param) J is divided by
+ * model^2 / k as the reference does (no conjugation); other n_model: the
+ * unscaled sensitivities. */
+int ertgb_jacobian_complex(ertgb_ctx *ctx, const double *model_re_dev, const double *model_im_dev, int n_model,
+                           double *J_dev, void *stream);
+
 /* Uniform refinement of a linear simplex mesh on device ``device``.  mode 1:
  * the quadratic mesh of Mesh::createP2 (Triangle6 / Tetrahedron10, one
  * midpoint node per edge); mode 2: Mesh::createH2 (every triangle into 4,

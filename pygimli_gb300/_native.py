@@ -79,6 +79,8 @@ SIGNATURES = {
     "ertgb_batch_response": (_ci, [_vp, _ci, _vp, _vp, ctypes.POINTER(BatchInfo), _vp]),
     "ertgb_cgls": (_ci, [_vp, _ci, _i64, _i64, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                          _vp, _d, _vp, _ci, _d, ctypes.POINTER(_i32), _vp]),
+    "ertgb_response_complex": (_ci, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "ertgb_jacobian_complex": (_ci, [_vp, _vp, _vp, _ci, _vp, _vp]),
     "ertgb_refine": (_ci, [_ci, _ci, _ci, _i64, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
     "ertgb_refined_sizes": (_ci, [_vp] + [ctypes.POINTER(_i64)] * 5),
     "ertgb_refined_get": (_ci, [_vp] * 8),

@@ -742,6 +742,31 @@ int ertgb_cgls(const void *J, int dtype, int64_t D, int64_t P, int64_t NC, const
     }
 }
 
+int ertgb_response_complex(ertgb_ctx *ctx, const double *rho_re, const double *rho_im, double *out_re,
+                           double *out_im, void *stream) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        ERTGB_REQUIRE(rho_re && rho_im && out_re && out_im, "null buffer");
+        StreamJoin j(*c, stream);
+        ensure_derived(*c);
+        const int st = complex_response(*c, rho_re, rho_im, out_re, out_im, c->stream);
+        j.done();
+        if (st == ERTGB_NOT_CONVERGED) throw Error(ERTGB_NOT_CONVERGED, "complex COCG did not converge");
+    });
+}
+
+int ertgb_jacobian_complex(ertgb_ctx *ctx, const double *m_re, const double *m_im, int n_model, double *J,
+                           void *stream) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        ERTGB_REQUIRE(J, "null buffer");
+        StreamJoin j(*c, stream);
+        ensure_derived(*c);
+        complex_jacobian(*c, m_re, m_im, n_model, J, c->stream);
+        j.done();
+    });
+}
+
 int ertgb_refine(int device, int dim, int mode, int64_t n_nodes, const double *xyz, const int32_t *nmark,
                  int64_t n_cells, const int32_t *cells, const int32_t *cmark, int64_t n_bnd, const int32_t *bnd,
                  const int32_t *bmark, const int32_t *bcell, ertgb_refined **out) {

@@ -130,6 +130,20 @@ struct LPState {
     DBuf<int32_t> err;
 };
 
+// Complex resistivity (complex.cu): complex system matrices and the block
+// COCG state, all n x Rpad arrays of (re, im) pairs.
+struct ComplexState {
+    DBuf<double2> sigma;            // C: 1 / rho*
+    DBuf<double2> S, dinv;          // nK x nnz, nK x n
+    DBuf<double2> x, r, z, p, q;    // n x Rpad
+    DBuf<double> part;              // partial sums (5 x NB x Rpad)
+    DBuf<double> col;               // per-column scalars
+    DBuf<int32_t> active;           // Rpad flags, Rpad iterations, counter
+    DBuf<double2> U;                // nE x nE electrode potentials
+    bool have_pot = false;
+    int32_t iterations = 0;
+};
+
 struct Context {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -200,6 +214,7 @@ struct Context {
     DBuf<double> d_rho_tmp, d_model_tmp;
     DBuf<char> d_J_tmp;
     LPState lp;
+    ComplexState cx;
     ertgb_stats stats{};
 };
 
@@ -240,6 +255,12 @@ void spmm_dot_launch(int64_t n, int64_t nnz, const int32_t *rowptr, const int32_
                      cudaStream_t s);
 // Message returned by ertgb_last_error(NULL) for the context-free entry points.
 void set_free_error(const std::string &msg);
+
+// complex resistivity (complex.cu): response [Re, Im] per datum and the
+// complex Jacobian (interleaved re, im; D x n_model)
+int complex_response(Context &c, const double *rho_re, const double *rho_im, double *out_re, double *out_im,
+                     cudaStream_t s);
+void complex_jacobian(Context &c, const double *m_re, const double *m_im, int n_model, double *J, cudaStream_t s);
 
 // device mesh refinement (refine.cu)
 struct Refined;

@@ -99,6 +99,7 @@ class ERTModelling:
         # ignoreRegionManager (MeshModelling, pygimli/frameworks/modelling.py:584-586)
         self._refineH2 = True
         self._refineP2 = False
+        self._complex = False     # complex resistivity (setComplex)
         self._rm = None           # region manager of the parameter mesh (setMesh without ignoreRegionManager)
         self._fwd_parent = None   # forward-mesh cell -> parameter-mesh cell
         self.setSolverTolerance(rtol, maxIter)
@@ -310,9 +311,83 @@ class ERTModelling:
 
     @property
     def parameterCount(self):
+        """Model parameters (twice the real count with complex resistivity,
+        real parts first, as pygimli/physics/ert/ertModelling.py:146-149)."""
+        return self._real_parameter_count() * (2 if self._complex else 1)
+
+    def _real_parameter_count(self):
         if self._rm is not None:
             return self._rm.parameterCount()
         return int(self._mesh.cell_markers.max()) + 1
+
+    # ------------------------------------------------- complex resistivity
+    def setComplex(self, c=True):
+        """Complex resistivity (induced polarisation): models and responses
+        are [Re..., Im...] vectors and createJacobian returns the complex
+        Jacobian (DCMultiElectrodeModelling::setComplex,
+        core/src/bert/dcfemmodelling.cpp:573-583).  The reference then solves
+        the total-potential problem (no singularity removal); so does this
+        operator (ertgb_response_complex)."""
+        self._complex = bool(c)
+        self._J = None
+
+    def complex(self):
+        return self._complex
+
+    def _complex_cells(self, model):
+        """Per-cell (Re, Im) of a complex model [Re..., Im...]: one value per
+        cell as given, else mapped like the reference's mapERTModel(CVector)
+        (dcfemmodelling.cpp:1199-1210): the real part with prolongation of
+        empty cells, the imaginary part as its own mapped model."""
+        m = np.asarray(model)
+        if np.iscomplexobj(m):
+            re, im = m.real.astype(np.float64), m.imag.astype(np.float64)
+        else:
+            m = m.astype(np.float64)
+            if len(m) % 2:
+                raise ValueError("a complex model needs [Re..., Im...] (even length)")
+            re, im = m[:len(m) // 2], m[len(m) // 2:]
+        if len(re) == self._mesh.cellCount():
+            return np.ascontiguousarray(re), np.ascontiguousarray(im)
+        return (np.ascontiguousarray(self.mapERTModel(re)), np.ascontiguousarray(self.mapERTModel(im)))
+
+    def _response_complex(self, model):
+        torch = _torch()
+        dev = torch.device("cuda", self.device)
+        re, im = self._complex_cells(model)
+        if np.min(np.hypot(re, im)) < TOLERANCE:
+            raise ValueError("complex response for abs model with negative or zero resistivity is not defined")
+        re_d = torch.from_numpy(re).to(dev)
+        im_d = torch.from_numpy(im).to(dev)
+        D = self._data.size()
+        out = torch.empty((2, D), dtype=torch.float64, device=dev)
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        self._check(self._lib.ertgb_response_complex(self._ctx, ctypes.c_void_p(re_d.data_ptr()),
+                                                     ctypes.c_void_p(im_d.data_ptr()),
+                                                     ctypes.c_void_p(out[0].data_ptr()),
+                                                     ctypes.c_void_p(out[1].data_ptr()), ctypes.c_void_p(stream)))
+        self._last_model = np.asarray(model)
+        return out.reshape(-1).cpu().numpy()
+
+    def _jacobian_complex(self, model):
+        torch = _torch()
+        dev = torch.device("cuda", self.device)
+        P = self._real_parameter_count()
+        m = np.asarray(model)
+        if np.iscomplexobj(m):
+            mr, mi = m.real.astype(np.float64), m.imag.astype(np.float64)
+        else:
+            m = m.astype(np.float64)
+            mr, mi = m[:len(m) // 2], m[len(m) // 2:]
+        mr_d = torch.from_numpy(np.ascontiguousarray(mr)).to(dev)
+        mi_d = torch.from_numpy(np.ascontiguousarray(mi)).to(dev)
+        J = torch.empty((self._data.size(), P), dtype=torch.complex128, device=dev)
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        self._check(self._lib.ertgb_jacobian_complex(self._ctx, ctypes.c_void_p(mr_d.data_ptr()),
+                                                     ctypes.c_void_p(mi_d.data_ptr()), int(len(mr)),
+                                                     ctypes.c_void_p(J.data_ptr()), ctypes.c_void_p(stream)))
+        self._J = J
+        return J
 
     def calcGeometricFactor(self, data=None):
         """Analytic geometric factors (flat surface, calcGeometricFactor,
@@ -334,8 +409,12 @@ class ERTModelling:
 
     def response(self, model):
         """Apparent resistivities for ``model`` (numpy in -> numpy out, or a
-        CUDA tensor of per-cell resistivities -> CUDA tensor)."""
+        CUDA tensor of per-cell resistivities -> CUDA tensor).  With
+        setComplex(True): [Re..., Im...] of the complex apparent
+        resistivities for a model [Re..., Im...] (or a complex array)."""
         self._ready()
+        if self._complex:
+            return self._response_complex(model)
         torch = _torch()
         if isinstance(model, torch.Tensor) and model.is_cuda:
             rho = model.to(torch.float64).contiguous()
@@ -423,6 +502,8 @@ class ERTModelling:
         torch = _torch()
         if self._mesh is None:
             raise RuntimeError("no mesh")
+        if self._complex:
+            return self._jacobian_complex(model)
         P = self.parameterCount
         D = self._data.size()
         tdt = torch.float64 if dtype in ("float64", torch.float64) else torch.float32

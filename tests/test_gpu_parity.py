@@ -440,3 +440,29 @@ def test_region_manager_forward(torch, dim):
     assert J.shape == (data.size(), P)
     assert rel(rhoa, rhoa_o) <= TOL_POT
     assert np.linalg.norm(J - J_o) / np.linalg.norm(J_o) <= TOL_J
+
+
+@pytest.mark.parametrize("name", ["ert2d_complex_small", "ert3d_complex_small"])
+def test_complex_resistivity_golden(torch, golden_dir, name):
+    """setComplex(True): complex apparent resistivities and the complex
+    Jacobian equal the reference's own complex path (total potential,
+    complex symmetric systems) on its fixtures; the GPU solves with block
+    COCG to rtol 1e-10 where the reference factors."""
+    z = np.load(os.path.join(golden_dir, name + ".npz"))
+    mesh = Mesh(int(z["dim"]), z["nodes"], z["cells"], z["cell_markers"], z["node_markers"],
+                z["boundaries"], z["boundary_markers"], z["boundary_cells"])
+    data = DataContainerERT(z["sensors"], z["abmn"])
+    data.set("k", z["kfac"])
+    fop = fop_for(mesh, data, z["k"], z["w"])
+    fop.setComplex(True)
+    assert fop.parameterCount == 2 * mesh.cellCount()
+    rho = z["rho"]
+    out = fop.response(np.concatenate([rho.real, rho.imag]))
+    D = data.size()
+    rhoa = out[:D] + 1j * out[D:]
+    e_r = float(np.max(np.abs(rhoa - z["rhoa"]) / np.abs(z["rhoa"])))
+    J = fop.createJacobian(rho).cpu().numpy()
+    e_j = float(np.linalg.norm(J - z["J"]) / np.linalg.norm(z["J"]))
+    print(f"{name}: rhoa {e_r:.2e} J {e_j:.2e} COCG iterations {fop.stats()['iterations']}")
+    assert J.shape == z["J"].shape
+    assert e_r <= 1e-7 and e_j <= 1e-6
