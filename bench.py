@@ -346,7 +346,46 @@ def run_ours(args, world, rank, local):
         del Jp, fop_p
         return out
 
-    plain = fsai_form = None
+    def time_complex():
+        """Complex resistivity (IP) on the same workload: the reference's
+        total-potential complex formulation, block COCG (FP64) + complex
+        Jacobian; phases of -10 mrad on the workload's amplitudes."""
+        fop_c = ERTModelling(device=local, rtol=args.rtol)
+        fop_c.setData(data)
+        fop_c.setMesh(mesh, ignoreRegionManager=True)
+        fop_c.setComplex(True)
+        zr = torch.from_numpy(rho * np.cos(-0.01)).to(dev)
+        zi = torch.from_numpy(rho * np.sin(-0.01)).to(dev)
+        out_c = torch.empty((2, D), dtype=torch.float64, device=dev)
+        Jc = torch.empty((D, P), dtype=torch.complex128, device=dev)
+
+        def step_c():
+            stream = torch.cuda.current_stream(dev).cuda_stream
+            fop_c._check(L.ertgb_response_complex(fop_c._ctx, ctypes.c_void_p(zr.data_ptr()),
+                                                  ctypes.c_void_p(zi.data_ptr()), ctypes.c_void_p(out_c[0].data_ptr()),
+                                                  ctypes.c_void_p(out_c[1].data_ptr()), ctypes.c_void_p(stream)))
+            fop_c._check(L.ertgb_jacobian_complex(fop_c._ctx, ctypes.c_void_p(zr.data_ptr()),
+                                                  ctypes.c_void_p(zi.data_ptr()), C, ctypes.c_void_p(Jc.data_ptr()),
+                                                  ctypes.c_void_p(stream)))
+
+        step_c()
+        torch.cuda.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record()
+        step_c()
+        f1.record()
+        torch.cuda.synchronize()
+        stc = fop_c.stats()
+        res = {"value": f0.elapsed_time(f1) / 1e3, "unit": UNIT, "steps": 1,
+               "solver": "block COCG (Jacobi), FP64 complex, total potential",
+               "cocg_iterations": stc["iterations"], "jacobian": "complex FP64"}
+        del Jc, fop_c
+        return res
+
+    plain = fsai_form = cx_form = None
+    if not args.no_plain:
+        cx_form = time_complex()
     if not args.no_plain and (args.precision, args.precond) != ("fp64", "jacobi"):
         plain = time_form("fp64", "jacobi", 0, "block PCG (Jacobi), FP64")
     if not args.no_plain and args.precond == "learned":
@@ -441,7 +480,7 @@ def run_ours(args, world, rank, local):
                               f"{mesh.nodeCount() * 96 * 8 / 1e6:.0f} MB, J {D * P * 8 / 1e9:.1f} GB"),
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
                "plain_fp64_gpu_pcg": plain, "fsai_form": fsai_form, "gn_iteration": gn,
-               "refine_h2": refine_rec,
+               "refine_h2": refine_rec, "complex_form": cx_form,
                "learned_weights": os.path.relpath(weights, ROOT) if weights else None,
                "clocks": clk,
                "breakdown_ms": {"assemble": st["ms_assemble"], "rhs": st["ms_rhs"], "solve": st["ms_solve"],
