@@ -303,15 +303,46 @@ __global__ void k_m_update_xr(int64_t n, int nE, int64_t R, int64_t Rpad, const 
     block_partials2((double)a, (double)b, part_a, part_b, Rpad, t);
 }
 
+// Column sums of the NB block partials by one warp per column (eight
+// columns per block, so the FP64 additions spread over many SMs instead of
+// the Rpad / 32 SMs of col_sum): lanes take rows lane, lane + 32, ... in two
+// chains, then a shuffle tree; lane 0's total is returned to every lane.
+constexpr int kFinWarps = 8;
+
+__device__ __forceinline__ double warp_col_sum(const double *__restrict__ part, int NB, int64_t Rpad, int64_t t) {
+    const int lane = threadIdx.x & 31;
+    double s0 = 0.0, s1 = 0.0;
+    int b = lane;
+    for (; b + 32 < NB; b += 64) {
+        s0 += part[(int64_t)b * Rpad + t];
+        s1 += part[(int64_t)(b + 32) * Rpad + t];
+    }
+    if (b < NB) s0 += part[(int64_t)b * Rpad + t];
+    double v = s0 + s1;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return __shfl_sync(0xffffffffu, v, 0);
+}
+
+// alpha = rho / (p . q) per active column
+__global__ void k_m_finish_alpha_w(int64_t Rpad, int NB, const double *__restrict__ part, double *__restrict__ col,
+                                   const int32_t *__restrict__ active, int32_t *__restrict__ nactive) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *nactive = 0;
+    const int64_t t = (int64_t)blockIdx.x * kFinWarps + (threadIdx.x >> 5);
+    if (t >= Rpad) return;  // whole warps
+    const double pq = warp_col_sum(part, NB, Rpad, t);
+    if ((threadIdx.x & 31) != 0 || !active[t]) return;
+    col[PQ * Rpad + t] = pq;
+    col[ALPHA * Rpad + t] = (pq != 0.0) ? col[RHO * Rpad + t] / pq : 0.0;
+}
+
 // recursive beta; convergence is left to the reliable updates
-__global__ void k_m_finish_beta(int64_t Rpad, int NB, const double *__restrict__ part_a,
-                                const double *__restrict__ part_b, double *__restrict__ col,
-                                const int32_t *__restrict__ active, int32_t *__restrict__ iters) {
-    __shared__ double ra[32][33];
-    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
-    const double rz = col_sum(part_a, NB, Rpad, t, ra);
-    (void)part_b;
-    if (threadIdx.y != 0) return;
+__global__ void k_m_finish_beta_w(int64_t Rpad, int NB, const double *__restrict__ part_a, double *__restrict__ col,
+                                  const int32_t *__restrict__ active, int32_t *__restrict__ iters) {
+    const int64_t t = (int64_t)blockIdx.x * kFinWarps + (threadIdx.x >> 5);
+    if (t >= Rpad) return;
+    const double rz = warp_col_sum(part_a, NB, Rpad, t);
+    if ((threadIdx.x & 31) != 0) return;
     if (!active[t]) {
         col[BETA * Rpad + t] = 0.0;
         return;
@@ -512,10 +543,6 @@ template <int CH> struct ResidL {
 
 }  // namespace
 
-// kernels of pcg.cu reused here
-void pcg_finish_alpha(dim3 g, dim3 b, cudaStream_t s, int64_t Rpad, int NB, const double *part, double *col,
-                      const int32_t *active, int32_t *nactive);
-
 int pcg_solve_mixed(Context &c, cudaStream_t s) {
     MeshData &m = c.mesh;
     const int64_t n = m.n, Rpad = c.Rpad, R = c.R;
@@ -564,6 +591,7 @@ int pcg_solve_mixed(Context &c, cudaStream_t s) {
     const dim3 vgu((unsigned)(Rpad / 32), (unsigned)std::min<int64_t>(ceil_div(n, kRows), 4 * kPartRows));
     const dim3 sg((unsigned)NB, (unsigned)nchunk);
     const dim3 fb(32, 32), fg((unsigned)(Rpad / 32));
+    const unsigned fwg = (unsigned)ceil_div(Rpad, kFinWarps);
     const double rtol2 = c.rtol * c.rtol;
     k_m_init<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, c.d_dinv32.p, b, c.d_r32.p, c.d_p32.p, c.d_y32.p, part_a, part_b);
     if (fsai) {
@@ -591,16 +619,16 @@ int pcg_solve_mixed(Context &c, cudaStream_t s) {
         for (int it = 0; it < kGraphIters; it++) {
             dispatch_ch<SpmmL>(ch, sg, s, n, m.nnz, c.nE, c.nK, Rpad, m.d_rowptr.p, m.d_colidx.p, c.d_S32.p, c.d_p32.p,
                                c.d_q32.p, part_c);
-            pcg_finish_alpha(fg, fb, s, Rpad, NB, part_c, c.d_col.p, active, nactive);
+            k_m_finish_alpha_w<<<fwg, 32 * kFinWarps, 0, s>>>(Rpad, NB, part_c, c.d_col.p, active, nactive);
             if (fsai) {
                 k_m_update_r<<<vgu, vb, 0, s>>>(n, Rpad, c.d_col.p, active, c.d_r32.p, c.d_q32.p);
                 apply_fsai(part_a);
-                k_m_finish_beta<<<fg, fb, 0, s>>>(Rpad, NB, part_a, part_a, c.d_col.p, active, iters);
+                k_m_finish_beta_w<<<fwg, 32 * kFinWarps, 0, s>>>(Rpad, NB, part_a, c.d_col.p, active, iters);
                 k_m_update_pzy<<<vgu, vb, 0, s>>>(n, Rpad, c.d_col.p, active, c.d_z32.p, c.d_p32.p, c.d_y32.p);
             } else {
                 k_m_update_xr<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, c.d_dinv32.p, c.d_col.p, active, c.d_y32.p,
                                                 c.d_r32.p, c.d_p32.p, c.d_q32.p, part_a, part_b);
-                k_m_finish_beta<<<fg, fb, 0, s>>>(Rpad, NB, part_a, part_b, c.d_col.p, active, iters);
+                k_m_finish_beta_w<<<fwg, 32 * kFinWarps, 0, s>>>(Rpad, NB, part_a, c.d_col.p, active, iters);
                 k_m_update_p<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, c.d_dinv32.p, c.d_col.p, active, c.d_r32.p,
                                                c.d_p32.p);
             }
