@@ -346,11 +346,11 @@ def run_ours(args, world, rank, local):
         del Jp, fop_p
         return out
 
-    def time_complex():
+    def time_complex(precision):
         """Complex resistivity (IP) on the same workload: the reference's
-        total-potential complex formulation, block COCG (FP64) + complex
-        Jacobian; phases of -10 mrad on the workload's amplitudes."""
-        fop_c = ERTModelling(device=local, rtol=args.rtol)
+        total-potential complex formulation, block COCG + complex Jacobian;
+        phases of -10 mrad on the workload's amplitudes."""
+        fop_c = ERTModelling(device=local, rtol=args.rtol, precision=precision)
         fop_c.setData(data)
         fop_c.setMesh(mesh, ignoreRegionManager=True)
         fop_c.setComplex(True)
@@ -378,14 +378,15 @@ def run_ours(args, world, rank, local):
         torch.cuda.synchronize()
         stc = fop_c.stats()
         res = {"value": f0.elapsed_time(f1) / 1e3, "unit": UNIT, "steps": 1,
-               "solver": "block COCG (Jacobi), FP64 complex, total potential",
-               "cocg_iterations": stc["iterations"], "jacobian": "complex FP64"}
+               "solver": f"block COCG (Jacobi), {precision} complex, total potential",
+               "cocg_iterations": stc["iterations"],
+               "columns_finished_fp64": stc["stalled_columns"], "jacobian": "complex FP64"}
         del Jc, fop_c
         return res
 
     plain = fsai_form = cx_form = None
     if not args.no_plain:
-        cx_form = time_complex()
+        cx_form = {"mixed": time_complex("mixed"), "fp64": time_complex("fp64")}
     if not args.no_plain and (args.precision, args.precond) != ("fp64", "jacobi"):
         plain = time_form("fp64", "jacobi", 0, "block PCG (Jacobi), FP64")
     if not args.no_plain and args.precond == "learned":

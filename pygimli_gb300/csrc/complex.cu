@@ -25,6 +25,7 @@
 #include "reduce.cuh"
 
 #include <algorithm>
+#include <functional>
 
 namespace ertgb {
 namespace {
@@ -35,7 +36,8 @@ constexpr int kPartC = 608;      // block partial rows of the column reductions
 constexpr int kGraphItersC = 16; // iterations per CUDA graph launch
 
 // per-column scalars (x Rpad)
-enum CCol { C_RHO_RE = 0, C_RHO_IM, C_ALPHA_RE, C_ALPHA_IM, C_BETA_RE, C_BETA_IM, C_BB, C_RR, C_NCOL };
+enum CCol { C_RHO_RE = 0, C_RHO_IM, C_ALPHA_RE, C_ALPHA_IM, C_BETA_RE, C_BETA_IM, C_BB, C_RR, C_BEST, C_STALLS,
+            C_NCOL };
 
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
     return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
@@ -137,14 +139,16 @@ __device__ __forceinline__ void block_partials3(double a, double b, double c, do
     }
 }
 
-// z = D^-1 r; with SETP also p = z.  Partials of r^T z (complex) and r^H r.
+// z = D^-1 r; with SETP also p = z (on the columns selected by ``sel``,
+// all when null) else on the active columns.  Partials of r^T z (complex)
+// and r^H r.
 template <bool SETP>
 __global__ void k_precond_c(int64_t n, int nE, int64_t R, int64_t Rpad, const double2 *__restrict__ dinv,
-                            const int32_t *__restrict__ active, const double2 *__restrict__ r,
+                            const int32_t *__restrict__ sel, const double2 *__restrict__ r,
                             double2 *__restrict__ z, double2 *__restrict__ p, double *__restrict__ p_re,
                             double *__restrict__ p_im, double *__restrict__ p_rr) {
     const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
-    const bool act = t < R && (SETP || active[t]);
+    const bool act = t < R && (SETP ? (!sel || sel[t]) : sel[t] != 0);
     const double2 *dk = dinv + (t < R ? t / nE : 0) * n;
     double a = 0.0, b = 0.0, c = 0.0;
     if (act) {
@@ -216,23 +220,32 @@ __global__ void k_update_p_c(int64_t n, int64_t Rpad, const double *__restrict__
 }
 
 // initial column scalars: rho = r^T z, bb = rr = ||b||^2; active where b != 0
+// initial column scalars: rho = r^T z, rr = ||r||^2, bb = ||b||^2 = 1 (unit
+// sources); active where the residual is nonzero (with mask: and mask[t],
+// a warm start of the selected columns keeping their iteration counts)
 __global__ void k_finish_init_c(int64_t Rpad, int64_t R, int NB, const double *__restrict__ p_re,
                                 const double *__restrict__ p_im, const double *__restrict__ p_rr,
                                 double *__restrict__ col, int32_t *__restrict__ active, int32_t *__restrict__ iters,
-                                int32_t *__restrict__ nactive) {
+                                int32_t *__restrict__ nactive, const int32_t *__restrict__ mask) {
     __shared__ double ra[32][33], rb[32][33], rc[32][33];
     const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
     const double re = col_sum(p_re, NB, Rpad, t, ra);
     const double im = col_sum(p_im, NB, Rpad, t, rb);
     const double rr = col_sum(p_rr, NB, Rpad, t, rc);
     if (threadIdx.y != 0) return;
+    if (mask && !mask[t]) {
+        active[t] = 0;
+        return;
+    }
     col[C_RHO_RE * Rpad + t] = re;
     col[C_RHO_IM * Rpad + t] = im;
-    col[C_BB * Rpad + t] = rr;
+    col[C_BB * Rpad + t] = t < R ? 1.0 : 0.0;
     col[C_RR * Rpad + t] = rr;
+    col[C_BEST * Rpad + t] = rr;
+    col[C_STALLS * Rpad + t] = 0.0;
     const int a = (t < R && rr > 0.0) ? 1 : 0;
     active[t] = a;
-    iters[t] = 0;
+    if (!mask) iters[t] = 0;
     if (a) atomicAdd(nactive, 1);
 }
 
@@ -373,6 +386,362 @@ __global__ void k_jacobian_c(int64_t D, int64_t P, int nE, int nK, int64_t Rpad,
 
 }  // namespace
 
+namespace {
+
+// ---- mixed precision: FP32 complex recurrence, FP64 reliable updates -------
+
+__device__ __forceinline__ float2 fmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 fadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 fsub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+
+__global__ void k_to_f32_c(int64_t n, const double2 *__restrict__ a, float2 *__restrict__ b) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = make_float2((float)a[i].x, (float)a[i].y);
+}
+
+// r = b - A x in FP64 (b: unit sources) on the columns t < R with mask[t]
+// (all when mask is null).  F32: also r32 = r, z32 = D^-1 r32 and partials
+// of r^T z (FP32 values) and ||r||^2 (FP64); else r64 = r.
+template <bool F32>
+__global__ void k_resid_c(int64_t n, int64_t nnz, int nE, int64_t R, int64_t Rpad, const int32_t *__restrict__ rowptr,
+                          const int32_t *__restrict__ colidx, const double2 *__restrict__ vals,
+                          const int32_t *__restrict__ enode, const int32_t *__restrict__ mask,
+                          const double2 *__restrict__ x, double2 *__restrict__ r64, const float2 *__restrict__ dinv32,
+                          float2 *__restrict__ r32, float2 *__restrict__ z32, double *__restrict__ p_re,
+                          double *__restrict__ p_im, double *__restrict__ p_rr) {
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    const bool act = t < R && (!mask || mask[t]);
+    const int64_t ki = t < R ? t / nE : 0;
+    const double2 *vk = vals + ki * nnz;
+    const float2 *dk = F32 ? dinv32 + ki * n : nullptr;
+    const int32_t src = t < R ? enode[t % nE] : -1;
+    double a = 0.0, b = 0.0, c = 0.0;
+    if (act) {
+        for (int64_t row = (int64_t)blockIdx.y * kRowsC + threadIdx.y; row < n; row += (int64_t)gridDim.y * kRowsC) {
+            double2 acc = make_double2(row == src ? 1.0 : 0.0, 0.0);
+            const int32_t s1 = rowptr[row + 1];
+            for (int32_t s = rowptr[row]; s < s1; s++) acc = csub(acc, cmul(vk[s], x[(int64_t)colidx[s] * Rpad + t]));
+            const int64_t i = row * Rpad + t;
+            c += acc.x * acc.x + acc.y * acc.y;
+            if (F32) {
+                const float2 rv = make_float2((float)acc.x, (float)acc.y);
+                const float2 zv = fmul(dk[row], rv);
+                r32[i] = rv;
+                z32[i] = zv;
+                const float2 rz = fmul(rv, zv);
+                a += rz.x;
+                b += rz.y;
+            } else {
+                r64[i] = acc;
+            }
+        }
+    }
+    block_partials3(a, b, c, p_re, p_im, p_rr, Rpad, t);
+}
+
+// q = A p in FP32, partials of p^T q
+__global__ void k_spmm_c32(int64_t n, int64_t nnz, int nE, int64_t R, int64_t Rpad, const int32_t *__restrict__ rowptr,
+                           const int32_t *__restrict__ colidx, const float2 *__restrict__ vals,
+                           const int32_t *__restrict__ active, const float2 *__restrict__ p, float2 *__restrict__ q,
+                           double *__restrict__ p_re, double *__restrict__ p_im) {
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    const bool act = t < R && active[t];
+    const float2 *vk = vals + (t < R ? t / nE : 0) * nnz;
+    float a = 0.f, b = 0.f;
+    if (act) {
+        for (int64_t row = (int64_t)blockIdx.y * kRowsC + threadIdx.y; row < n; row += (int64_t)gridDim.y * kRowsC) {
+            float2 acc = make_float2(0.f, 0.f);
+            const int32_t s1 = rowptr[row + 1];
+            for (int32_t s = rowptr[row]; s < s1; s++) acc = fadd(acc, fmul(vk[s], p[(int64_t)colidx[s] * Rpad + t]));
+            const int64_t i = row * Rpad + t;
+            q[i] = acc;
+            const float2 pq = fmul(p[i], acc);
+            a += pq.x;
+            b += pq.y;
+        }
+    }
+    block_partials3(a, b, 0.0, p_re, p_im, nullptr, Rpad, t);
+}
+
+// y += alpha p, r -= alpha q, z = D^-1 r; partials of r^T z and ||r||^2
+__global__ void k_update_yrz_c32(int64_t n, int nE, int64_t R, int64_t Rpad, const double *__restrict__ col,
+                                 const int32_t *__restrict__ active, const float2 *__restrict__ dinv32,
+                                 float2 *__restrict__ y, float2 *__restrict__ r, float2 *__restrict__ z,
+                                 const float2 *__restrict__ p, const float2 *__restrict__ q, double *__restrict__ p_re,
+                                 double *__restrict__ p_im, double *__restrict__ p_rr) {
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    const bool act = t < R && active[t];
+    const float2 al = make_float2((float)col[C_ALPHA_RE * Rpad + t], (float)col[C_ALPHA_IM * Rpad + t]);
+    const float2 *dk = dinv32 + (t < R ? t / nE : 0) * n;
+    float a = 0.f, b = 0.f, c = 0.f;
+    if (act) {
+        for (int64_t row = (int64_t)blockIdx.y * kRowsC + threadIdx.y; row < n; row += (int64_t)gridDim.y * kRowsC) {
+            const int64_t i = row * Rpad + t;
+            y[i] = fadd(y[i], fmul(al, p[i]));
+            const float2 rv = fsub(r[i], fmul(al, q[i]));
+            r[i] = rv;
+            const float2 zv = fmul(dk[row], rv);
+            z[i] = zv;
+            const float2 rz = fmul(rv, zv);
+            a += rz.x;
+            b += rz.y;
+            c += rv.x * rv.x + rv.y * rv.y;
+        }
+    }
+    block_partials3(a, b, c, p_re, p_im, p_rr, Rpad, t);
+}
+
+__global__ void k_update_p_c32(int64_t n, int64_t Rpad, const double *__restrict__ col,
+                               const int32_t *__restrict__ active, const float2 *__restrict__ z,
+                               float2 *__restrict__ p) {
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    if (!active[t]) return;
+    const float2 be = make_float2((float)col[C_BETA_RE * Rpad + t], (float)col[C_BETA_IM * Rpad + t]);
+    for (int64_t row = (int64_t)blockIdx.y * kRowsC + threadIdx.y; row < n; row += (int64_t)gridDim.y * kRowsC) {
+        const int64_t i = row * Rpad + t;
+        p[i] = fadd(z[i], fmul(be, p[i]));
+    }
+}
+
+// recursive beta (mixed): convergence is left to the reliable updates
+__global__ void k_finish_beta_mc(int64_t Rpad, int NB, const double *__restrict__ p_re,
+                                 const double *__restrict__ p_im, double *__restrict__ col,
+                                 const int32_t *__restrict__ active, int32_t *__restrict__ iters) {
+    __shared__ double ra[32][33], rb[32][33];
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    const double2 rz = make_double2(col_sum(p_re, NB, Rpad, t, ra), col_sum(p_im, NB, Rpad, t, rb));
+    if (threadIdx.y != 0 || !active[t]) return;
+    iters[t] += 1;
+    const double2 rho = make_double2(col[C_RHO_RE * Rpad + t], col[C_RHO_IM * Rpad + t]);
+    double2 be = make_double2(0.0, 0.0);
+    if (hypot(rho.x, rho.y) > 0.0) be = cdiv(rz, rho);
+    if (!isfinite(be.x) || !isfinite(be.y)) be = make_double2(0.0, 0.0);
+    col[C_BETA_RE * Rpad + t] = be.x;
+    col[C_BETA_IM * Rpad + t] = be.y;
+    col[C_RHO_RE * Rpad + t] = rz.x;
+    col[C_RHO_IM * Rpad + t] = rz.y;
+}
+
+// reliable update, part 1: x += y, y = 0 on active columns; counter reset
+__global__ void k_accum_c(int64_t n, int64_t Rpad, const int32_t *__restrict__ active, double2 *__restrict__ x,
+                          float2 *__restrict__ y, int32_t *__restrict__ nactive) {
+    if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) *nactive = 0;
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    if (!active[t]) return;
+    for (int64_t row = (int64_t)blockIdx.y * kRowsC + threadIdx.y; row < n; row += (int64_t)gridDim.y * kRowsC) {
+        const int64_t i = row * Rpad + t;
+        const float2 v = y[i];
+        x[i] = make_double2(x[i].x + (double)v.x, x[i].y + (double)v.y);
+        y[i] = make_float2(0.f, 0.f);
+    }
+}
+
+// reliable update, part 3: convergence on the FP64 true residual, rho of the
+// restarted residual, stall detection as in the real mixed solver: no 10 %
+// improvement of the best residual over four intervals, or divergence
+// (above 4 ||b||^2, or not finite), hands the column to the FP64 solver
+// (stalled 1: warm start from its x; 2: from zero).
+__global__ void k_finish_ru_c(int64_t Rpad, int NB, double rtol2, const double *__restrict__ p_re,
+                              const double *__restrict__ p_im, const double *__restrict__ p_rr,
+                              double *__restrict__ col, int32_t *__restrict__ active, int32_t *__restrict__ stalled,
+                              int32_t *__restrict__ nactive, int32_t *__restrict__ nstalled) {
+    __shared__ double ra[32][33], rb[32][33], rc[32][33];
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    const double2 rz = make_double2(col_sum(p_re, NB, Rpad, t, ra), col_sum(p_im, NB, Rpad, t, rb));
+    const double rr = col_sum(p_rr, NB, Rpad, t, rc);
+    if (threadIdx.y != 0 || !active[t]) return;
+    const double bb = col[C_BB * Rpad + t];
+    col[C_RR * Rpad + t] = rr;
+    col[C_RHO_RE * Rpad + t] = rz.x;
+    col[C_RHO_IM * Rpad + t] = rz.y;
+    if (rr <= rtol2 * bb) {
+        active[t] = 0;
+        return;
+    }
+    if (!(rr <= 4.0 * bb) || !isfinite(rz.x) || !isfinite(rz.y)) {
+        active[t] = 0;
+        stalled[t] = 2;
+        atomicAdd(nstalled, 1);
+        return;
+    }
+    double stalls = col[C_STALLS * Rpad + t];
+    if (rr < 0.81 * col[C_BEST * Rpad + t]) {
+        col[C_BEST * Rpad + t] = rr;
+        stalls = 0.0;
+    } else {
+        stalls += 1.0;
+    }
+    col[C_STALLS * Rpad + t] = stalls;
+    if (stalls >= 4.0) {
+        active[t] = 0;
+        stalled[t] = 1;
+        atomicAdd(nstalled, 1);
+        return;
+    }
+    atomicAdd(nactive, 1);
+}
+
+// stalled columns restarting from zero: x = 0 there
+__global__ void k_zero_restart_c(int64_t n, int64_t Rpad, const int32_t *__restrict__ stalled,
+                                 double2 *__restrict__ x) {
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    if (stalled[t] != 2) return;
+    for (int64_t row = (int64_t)blockIdx.y * kRowsC + threadIdx.y; row < n; row += (int64_t)gridDim.y * kRowsC)
+        x[row * Rpad + t] = make_double2(0.0, 0.0);
+}
+
+}  // namespace
+
+namespace {
+
+struct CxLaunch {
+    int64_t n, nnz, R, Rpad;
+    int NB;
+    dim3 vb, vg, fb, fg;
+};
+
+void run_graph_loop(Context &c, cudaStream_t s, const std::function<void()> &body, int32_t *nactive, int launches,
+                    const std::function<void()> &after, int *status) {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    try {
+        ERTGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        body();
+        ERTGB_CUDA(cudaStreamEndCapture(s, &g));
+        ERTGB_CUDA(cudaGraphInstantiate(&ge, g, 0));
+        int32_t h_active = 0;
+        ERTGB_CUDA(cudaMemcpyAsync(&h_active, nactive, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        ERTGB_CUDA(cudaStreamSynchronize(s));
+        int done = 0;
+        while (h_active > 0) {
+            if (done >= c.max_iter) {
+                *status = ERTGB_NOT_CONVERGED;
+                break;
+            }
+            for (int u = 0; u < launches; u++) ERTGB_CUDA(cudaGraphLaunch(ge, s));
+            done += launches * kGraphItersC;
+            if (after) after();
+            ERTGB_CUDA(cudaMemcpyAsync(&h_active, nactive, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+            ERTGB_CUDA(cudaStreamSynchronize(s));
+        }
+    } catch (...) {
+        cudaGraph_t dummy = nullptr;
+        cudaStreamEndCapture(s, &dummy);
+        if (dummy) cudaGraphDestroy(dummy);
+        if (ge) cudaGraphExecDestroy(ge);
+        if (g) cudaGraphDestroy(g);
+        throw;
+    }
+    if (ge) cudaGraphExecDestroy(ge);
+    if (g) cudaGraphDestroy(g);
+}
+
+// FP64 block COCG; mask: warm start of the columns with mask[t] != 0 from x
+int cocg_fp64(Context &c, const CxLaunch &L, cudaStream_t s, const int32_t *mask) {
+    MeshData &m = c.mesh;
+    ComplexState &x = c.cx;
+    const int64_t n = L.n, nnz = L.nnz, R = L.R, Rpad = L.Rpad;
+    const int NB = L.NB;
+    double *pa = x.part.p, *pb = pa + (size_t)NB * Rpad, *pc = pb + (size_t)NB * Rpad;
+    double *pd = pc + (size_t)NB * Rpad, *pe = pd + (size_t)NB * Rpad;
+    int32_t *active = x.active.p, *iters = active + Rpad, *nactive = active + 2 * Rpad;
+    if (!mask) ERTGB_CUDA(cudaMemsetAsync(x.x.p, 0, sizeof(double2) * n * Rpad, s));
+    ERTGB_CUDA(cudaMemsetAsync(nactive, 0, sizeof(int32_t), s));
+    k_resid_c<false><<<L.vg, L.vb, 0, s>>>(n, nnz, c.nE, R, Rpad, m.d_rowptr.p, m.d_colidx.p, x.S.p, c.d_enode.p, mask,
+                                           x.x.p, x.r.p, nullptr, nullptr, nullptr, pa, pb, pc);
+    k_precond_c<true><<<L.vg, L.vb, 0, s>>>(n, c.nE, R, Rpad, x.dinv.p, mask, x.r.p, x.z.p, x.p.p, pa, pb, pc);
+    k_finish_init_c<<<L.fg, L.fb, 0, s>>>(Rpad, R, NB, pa, pb, pc, x.col.p, active, iters, nactive, mask);
+    ERTGB_CUDA(cudaGetLastError());
+    const double rtol2 = c.rtol * c.rtol;
+    int status = ERTGB_OK;
+    run_graph_loop(c, s, [&] {
+        for (int it = 0; it < kGraphItersC; it++) {
+            k_spmm_c<<<L.vg, L.vb, 0, s>>>(n, nnz, c.nE, R, Rpad, m.d_rowptr.p, m.d_colidx.p, x.S.p, active, x.p.p,
+                                           x.q.p, pd, pe);
+            k_finish_alpha_c<<<L.fg, L.fb, 0, s>>>(Rpad, NB, pd, pe, x.col.p, active, nactive);
+            k_update_xr_c<<<L.vg, L.vb, 0, s>>>(n, Rpad, x.col.p, active, x.x.p, x.r.p, x.p.p, x.q.p);
+            k_precond_c<false><<<L.vg, L.vb, 0, s>>>(n, c.nE, R, Rpad, x.dinv.p, active, x.r.p, x.z.p, nullptr, pa,
+                                                     pb, pc);
+            k_finish_beta_c<<<L.fg, L.fb, 0, s>>>(Rpad, NB, rtol2, pa, pb, pc, x.col.p, active, iters, nactive);
+            k_update_p_c<<<L.vg, L.vb, 0, s>>>(n, Rpad, x.col.p, active, x.z.p, x.p.p);
+        }
+    }, nactive, 4, nullptr, &status);
+    return status;
+}
+
+// mixed block COCG: FP32 recurrence (matrix, vectors), FP64 solution, FP64
+// true residual every 4 x 16 iterations; returns the number of stalled columns
+int cocg_mixed(Context &c, const CxLaunch &L, cudaStream_t s, int *status) {
+    MeshData &m = c.mesh;
+    ComplexState &x = c.cx;
+    const int64_t n = L.n, nnz = L.nnz, R = L.R, Rpad = L.Rpad;
+    const int NB = L.NB;
+    double *pa = x.part.p, *pb = pa + (size_t)NB * Rpad, *pc = pb + (size_t)NB * Rpad;
+    double *pd = pc + (size_t)NB * Rpad, *pe = pd + (size_t)NB * Rpad;
+    int32_t *active = x.active.p, *iters = active + Rpad, *nactive = active + 2 * Rpad;
+    int32_t *stalled = x.stalled.p, *nstalled = stalled + Rpad;
+    x.S32.alloc((size_t)c.nK * nnz);
+    x.dinv32.alloc((size_t)c.nK * n);
+    for (DBuf<float2> *v : {&x.r32, &x.z32, &x.p32, &x.q32, &x.y32}) v->alloc((size_t)n * Rpad);
+    k_to_f32_c<<<grid1c(c.nK * nnz), 256, 0, s>>>(c.nK * nnz, x.S.p, x.S32.p);
+    k_to_f32_c<<<grid1c(c.nK * n), 256, 0, s>>>(c.nK * n, x.dinv.p, x.dinv32.p);
+    ERTGB_CUDA(cudaMemsetAsync(x.x.p, 0, sizeof(double2) * n * Rpad, s));
+    ERTGB_CUDA(cudaMemsetAsync(x.y32.p, 0, sizeof(float2) * n * Rpad, s));
+    ERTGB_CUDA(cudaMemsetAsync(stalled, 0, sizeof(int32_t) * (Rpad + 1), s));
+    ERTGB_CUDA(cudaMemsetAsync(nactive, 0, sizeof(int32_t), s));
+    k_resid_c<true><<<L.vg, L.vb, 0, s>>>(n, nnz, c.nE, R, Rpad, m.d_rowptr.p, m.d_colidx.p, x.S.p, c.d_enode.p,
+                                          nullptr, x.x.p, nullptr, x.dinv32.p, x.r32.p, x.z32.p, pa, pb, pc);
+    ERTGB_CUDA(cudaMemcpyAsync(x.p32.p, x.z32.p, sizeof(float2) * n * Rpad, cudaMemcpyDeviceToDevice, s));
+    k_finish_init_c<<<L.fg, L.fb, 0, s>>>(Rpad, R, NB, pa, pb, pc, x.col.p, active, iters, nactive, nullptr);
+    ERTGB_CUDA(cudaGetLastError());
+    const double rtol2 = c.rtol * c.rtol;
+    // the reliable update as a second graph
+    cudaGraph_t gru = nullptr;
+    cudaGraphExec_t eru = nullptr;
+    ERTGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    k_accum_c<<<L.vg, L.vb, 0, s>>>(n, Rpad, active, x.x.p, x.y32.p, nactive);
+    k_resid_c<true><<<L.vg, L.vb, 0, s>>>(n, nnz, c.nE, R, Rpad, m.d_rowptr.p, m.d_colidx.p, x.S.p, c.d_enode.p, active,
+                                          x.x.p, nullptr, x.dinv32.p, x.r32.p, x.z32.p, pa, pb, pc);
+    k_finish_ru_c<<<L.fg, L.fb, 0, s>>>(Rpad, NB, rtol2, pa, pb, pc, x.col.p, active, stalled, nactive, nstalled);
+    ERTGB_CUDA(cudaStreamEndCapture(s, &gru));
+    ERTGB_CUDA(cudaGraphInstantiate(&eru, gru, 0));
+    try {
+        run_graph_loop(c, s, [&] {
+            for (int it = 0; it < kGraphItersC; it++) {
+                k_spmm_c32<<<L.vg, L.vb, 0, s>>>(n, nnz, c.nE, R, Rpad, m.d_rowptr.p, m.d_colidx.p, x.S32.p, active,
+                                                 x.p32.p, x.q32.p, pd, pe);
+                k_finish_alpha_c<<<L.fg, L.fb, 0, s>>>(Rpad, NB, pd, pe, x.col.p, active, nactive);
+                k_update_yrz_c32<<<L.vg, L.vb, 0, s>>>(n, c.nE, R, Rpad, x.col.p, active, x.dinv32.p, x.y32.p,
+                                                       x.r32.p, x.z32.p, x.p32.p, x.q32.p, pa, pb, pc);
+                k_finish_beta_mc<<<L.fg, L.fb, 0, s>>>(Rpad, NB, pa, pb, x.col.p, active, iters);
+                k_update_p_c32<<<L.vg, L.vb, 0, s>>>(n, Rpad, x.col.p, active, x.z32.p, x.p32.p);
+            }
+        }, nactive, 4, [&] { ERTGB_CUDA(cudaGraphLaunch(eru, s)); }, status);
+    } catch (...) {
+        cudaGraphExecDestroy(eru);
+        cudaGraphDestroy(gru);
+        throw;
+    }
+    cudaGraphExecDestroy(eru);
+    cudaGraphDestroy(gru);
+    if (*status == ERTGB_NOT_CONVERGED) {  // the increments since the last reliable update
+        k_accum_c<<<L.vg, L.vb, 0, s>>>(n, Rpad, active, x.x.p, x.y32.p, nactive);
+        ERTGB_CUDA(cudaGetLastError());
+    }
+    int32_t h_stalled = 0;
+    ERTGB_CUDA(cudaMemcpyAsync(&h_stalled, nstalled, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    ERTGB_CUDA(cudaStreamSynchronize(s));
+    if (h_stalled) {
+        k_zero_restart_c<<<L.vg, L.vb, 0, s>>>(n, Rpad, stalled, x.x.p);
+        ERTGB_CUDA(cudaGetLastError());
+    }
+    return h_stalled;
+}
+
+}  // namespace
+
 int complex_response(Context &c, const double *rho_re, const double *rho_im, double *out_re, double *out_im,
                      cudaStream_t s) {
     MeshData &m = c.mesh;
@@ -401,67 +770,32 @@ int complex_response(Context &c, const double *rho_re, const double *rho_im, dou
     ERTGB_CUDA(cudaGetLastError());
     k_dinv_c<<<grid1c(n * c.nK), 256, 0, s>>>(n, c.nK, nnz, m.d_diag.p, x.S.p, x.dinv.p);
     ERTGB_CUDA(cudaGetLastError());
-    // block COCG
-    const int NB = (int)std::min<int64_t>(ceil_div(n, kRowsC), kPartC);
+    CxLaunch L;
+    L.n = n;
+    L.nnz = nnz;
+    L.R = R;
+    L.Rpad = Rpad;
+    L.NB = (int)std::min<int64_t>(ceil_div(n, kRowsC), kPartC);
+    L.vb = dim3(32, kRowsC);
+    L.vg = dim3((unsigned)(Rpad / 32), (unsigned)L.NB);
+    L.fb = dim3(32, 32);
+    L.fg = dim3((unsigned)(Rpad / 32));
     for (DBuf<double2> *v : {&x.x, &x.r, &x.z, &x.p, &x.q}) v->alloc((size_t)n * Rpad);
-    x.part.alloc((size_t)5 * NB * Rpad);
+    x.part.alloc((size_t)5 * L.NB * Rpad);
     x.col.alloc((size_t)C_NCOL * Rpad);
     x.active.alloc((size_t)2 * Rpad + 1);
-    double *pa = x.part.p, *pb = pa + (size_t)NB * Rpad, *pc = pb + (size_t)NB * Rpad;
-    double *pd = pc + (size_t)NB * Rpad, *pe = pd + (size_t)NB * Rpad;
-    int32_t *active = x.active.p, *iters = active + Rpad, *nactive = active + 2 * Rpad;
-    ERTGB_CUDA(cudaMemsetAsync(x.x.p, 0, sizeof(double2) * n * Rpad, s));
-    ERTGB_CUDA(cudaMemsetAsync(x.r.p, 0, sizeof(double2) * n * Rpad, s));
+    x.stalled.alloc((size_t)Rpad + 1);
     ERTGB_CUDA(cudaMemsetAsync(x.col.p, 0, sizeof(double) * C_NCOL * Rpad, s));
-    ERTGB_CUDA(cudaMemsetAsync(nactive, 0, sizeof(int32_t), s));
-    k_sources_c<<<(unsigned)ceil_div(R, 256), 256, 0, s>>>(c.nE, R, Rpad, c.d_enode.p, x.r.p);
-    const dim3 vb(32, kRowsC), vg((unsigned)(Rpad / 32), (unsigned)NB), fb(32, 32), fg((unsigned)(Rpad / 32));
-    k_precond_c<true><<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, x.dinv.p, active, x.r.p, x.z.p, x.p.p, pa, pb, pc);
-    k_finish_init_c<<<fg, fb, 0, s>>>(Rpad, R, NB, pa, pb, pc, x.col.p, active, iters, nactive);
-    ERTGB_CUDA(cudaGetLastError());
-    const double rtol2 = c.rtol * c.rtol;
-    cudaGraph_t g = nullptr;
-    cudaGraphExec_t ge = nullptr;
     int status = ERTGB_OK;
-    try {
-        ERTGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        for (int it = 0; it < kGraphItersC; it++) {
-            k_spmm_c<<<vg, vb, 0, s>>>(n, nnz, c.nE, R, Rpad, m.d_rowptr.p, m.d_colidx.p, x.S.p, active, x.p.p, x.q.p,
-                                       pd, pe);
-            k_finish_alpha_c<<<fg, fb, 0, s>>>(Rpad, NB, pd, pe, x.col.p, active, nactive);
-            k_update_xr_c<<<vg, vb, 0, s>>>(n, Rpad, x.col.p, active, x.x.p, x.r.p, x.p.p, x.q.p);
-            k_precond_c<false><<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, x.dinv.p, active, x.r.p, x.z.p, nullptr, pa, pb,
-                                                 pc);
-            k_finish_beta_c<<<fg, fb, 0, s>>>(Rpad, NB, rtol2, pa, pb, pc, x.col.p, active, iters, nactive);
-            k_update_p_c<<<vg, vb, 0, s>>>(n, Rpad, x.col.p, active, x.z.p, x.p.p);
-        }
-        ERTGB_CUDA(cudaStreamEndCapture(s, &g));
-        ERTGB_CUDA(cudaGraphInstantiate(&ge, g, 0));
-        int32_t h_active = 0;
-        ERTGB_CUDA(cudaMemcpyAsync(&h_active, nactive, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-        ERTGB_CUDA(cudaStreamSynchronize(s));
-        int done = 0;
-        while (h_active > 0) {
-            if (done >= c.max_iter) {
-                status = ERTGB_NOT_CONVERGED;
-                break;
-            }
-            for (int u = 0; u < 4; u++) ERTGB_CUDA(cudaGraphLaunch(ge, s));
-            done += 4 * kGraphItersC;
-            ERTGB_CUDA(cudaMemcpyAsync(&h_active, nactive, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-            ERTGB_CUDA(cudaStreamSynchronize(s));
-        }
-    } catch (...) {
-        cudaGraph_t dummy = nullptr;
-        cudaStreamEndCapture(s, &dummy);
-        if (dummy) cudaGraphDestroy(dummy);
-        if (ge) cudaGraphExecDestroy(ge);
-        if (g) cudaGraphDestroy(g);
-        throw;
+    x.stalled_columns = 0;
+    if (c.precision == ERTGB_PRECISION_MIXED) {
+        x.stalled_columns = cocg_mixed(c, L, s, &status);
+        if (status == ERTGB_OK && x.stalled_columns > 0) status = cocg_fp64(c, L, s, x.stalled.p);
+    } else {
+        status = cocg_fp64(c, L, s, nullptr);
     }
-    if (ge) cudaGraphExecDestroy(ge);
-    if (g) cudaGraphDestroy(g);
     // iterations and the final relative residuals
+    int32_t *iters = x.active.p + Rpad;
     std::vector<int32_t> it_h((size_t)Rpad);
     std::vector<double> rr((size_t)Rpad), bb((size_t)Rpad);
     ERTGB_CUDA(cudaMemcpyAsync(it_h.data(), iters, sizeof(int32_t) * Rpad, cudaMemcpyDeviceToHost, s));
@@ -483,6 +817,7 @@ int complex_response(Context &c, const double *rho_re, const double *rho_im, dou
     c.stats.iterations = maxit;
     c.stats.n_rhs = (int32_t)R;
     c.stats.max_rel_residual = maxres;
+    c.stats.stalled_columns = x.stalled_columns;
     // collect and response
     x.U.alloc((size_t)c.nE * c.nE);
     k_collect_c<<<(unsigned)ceil_div((int64_t)c.nE * c.nE, 256), 256, 0, s>>>(c.nE, c.nK, Rpad, c.d_enode.p,

@@ -140,8 +140,12 @@ struct ComplexState {
     DBuf<double> col;               // per-column scalars
     DBuf<int32_t> active;           // Rpad flags, Rpad iterations, counter
     DBuf<double2> U;                // nE x nE electrode potentials
+    // mixed precision: FP32 matrices, Jacobi diagonal and recurrence vectors
+    DBuf<float2> S32, dinv32, r32, z32, p32, q32, y32;
+    DBuf<int32_t> stalled;          // Rpad flags + counter
     bool have_pot = false;
     int32_t iterations = 0;
+    int32_t stalled_columns = 0;
 };
 
 struct Context {

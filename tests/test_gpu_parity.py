@@ -442,8 +442,9 @@ def test_region_manager_forward(torch, dim):
     assert np.linalg.norm(J - J_o) / np.linalg.norm(J_o) <= TOL_J
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("name", ["ert2d_complex_small", "ert3d_complex_small"])
-def test_complex_resistivity_golden(torch, golden_dir, name):
+def test_complex_resistivity_golden(torch, golden_dir, name, precision):
     """setComplex(True): complex apparent resistivities and the complex
     Jacobian equal the reference's own complex path (total potential,
     complex symmetric systems) on its fixtures; the GPU solves with block
@@ -453,7 +454,7 @@ def test_complex_resistivity_golden(torch, golden_dir, name):
                 z["boundaries"], z["boundary_markers"], z["boundary_cells"])
     data = DataContainerERT(z["sensors"], z["abmn"])
     data.set("k", z["kfac"])
-    fop = fop_for(mesh, data, z["k"], z["w"])
+    fop = fop_for(mesh, data, z["k"], z["w"], form=precision)
     fop.setComplex(True)
     assert fop.parameterCount == 2 * mesh.cellCount()
     rho = z["rho"]
@@ -463,6 +464,8 @@ def test_complex_resistivity_golden(torch, golden_dir, name):
     e_r = float(np.max(np.abs(rhoa - z["rhoa"]) / np.abs(z["rhoa"])))
     J = fop.createJacobian(rho).cpu().numpy()
     e_j = float(np.linalg.norm(J - z["J"]) / np.linalg.norm(z["J"]))
-    print(f"{name}: rhoa {e_r:.2e} J {e_j:.2e} COCG iterations {fop.stats()['iterations']}")
+    st = fop.stats()
+    print(f"{name} {precision}: rhoa {e_r:.2e} J {e_j:.2e} COCG iterations {st['iterations']}, "
+          f"columns finished in FP64 {st['stalled_columns']}")
     assert J.shape == z["J"].shape
     assert e_r <= 1e-7 and e_j <= 1e-6
