@@ -161,13 +161,6 @@ class ERTModelling:
         self._precond = codes[precond]
         self._check(self._lib.ertgb_set_solver(self._ctx, self._rtol, self._maxIter, self._precond))
 
-    def setComplex(self, c):
-        if c:
-            raise NotImplementedError("complex resistivity is not supported")
-
-    def complex(self):
-        return False
-
     def createRefinedFwdMesh(self, mesh):
         """Forward mesh of a parameter mesh: H2 refinement, then P2, as
         enabled by ``_refineH2`` / ``_refineP2``
@@ -333,6 +326,21 @@ class ERTModelling:
 
     def complex(self):
         return self._complex
+
+    def createStartModel(self, dataVals):
+        """Start model: the median of the data values for every parameter
+        (Modelling.createStartModel, pygimli/frameworks/modelling.py:231-244);
+        complex: medians of the real and imaginary parts, the imaginary part
+        flipped to positive (ertModelling.py:168-186, which then also flips
+        it back around response and Jacobian; that convention is left to the
+        caller here)."""
+        v = np.asarray(dataVals)
+        if not self._complex:
+            return np.full(self.parameterCount, float(np.median(v)))
+        z = v if np.iscomplexobj(v) else v[:len(v) // 2] + 1j * v[len(v) // 2:]
+        P = self._real_parameter_count()
+        re, im = np.median(z.real), np.median(z.imag)
+        return np.concatenate([np.full(P, re), np.full(P, abs(im) if im < 0 else im)])
 
     def _complex_cells(self, model):
         """Per-cell (Re, Im) of a complex model [Re..., Im...]: one value per
