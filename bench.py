@@ -177,6 +177,18 @@ def ncu_traffic(kernel_file):
     return None
 
 
+def max_over_ranks(ms, world, device=None):
+    """The slowest rank's time (the job ends when the last replica does):
+    all-reduce MAX over the process group (NCCL on GPUs, gloo on CPU)."""
+    if world <= 1:
+        return float(ms)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
@@ -302,11 +314,7 @@ def run_ours(args, world, rank, local):
     total_ms = e0.elapsed_time(e1)
     st = fop.stats()
     launches = int(st["launches_response"] + st["launches_jacobian"]) * args.steps
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, world, dev)
     value = total_ms / 1e3 / (args.steps * world)
 
     def time_form(precision, precond, jac_dtype, label):
