@@ -197,14 +197,14 @@ __global__ void __launch_bounds__(256) k_residual64(int64_t n, int64_t nnz, int 
     }
 }
 
-__global__ void k_finish_alpha(int64_t Rpad, int NB, const double *__restrict__ part,
-                               double *__restrict__ col, const int32_t *__restrict__ active,
-                               int32_t *__restrict__ nactive) {
-    __shared__ double red[32][33];
-    if (blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) *nactive = 0;
-    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
-    const double pq = col_sum(part, NB, Rpad, t, red);
-    if (threadIdx.y != 0 || !active[t]) return;
+// alpha = rho / (p . q) per active column, one warp per column (warp_col_sum)
+__global__ void k_finish_alpha_w(int64_t Rpad, int NB, const double *__restrict__ part, double *__restrict__ col,
+                                 const int32_t *__restrict__ active, int32_t *__restrict__ nactive) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *nactive = 0;
+    const int64_t t = (int64_t)blockIdx.x * kFinWarps + (threadIdx.x >> 5);
+    if (t >= Rpad) return;  // whole warps
+    const double pq = warp_col_sum(part, NB, Rpad, t);
+    if ((threadIdx.x & 31) != 0 || !active[t]) return;
     col[PQ * Rpad + t] = pq;
     col[ALPHA * Rpad + t] = (pq != 0.0) ? col[RHO * Rpad + t] / pq : 0.0;
 }
@@ -246,15 +246,16 @@ __global__ void k_update_xr(int64_t n, int nE, int64_t R, int64_t Rpad, const do
     }
 }
 
-__global__ void k_finish_beta(int64_t Rpad, int NB, double rtol2, const double *__restrict__ part_a,
-                              const double *__restrict__ part_b, double *__restrict__ col,
-                              int32_t *__restrict__ active, int32_t *__restrict__ iters,
-                              int32_t *__restrict__ nactive) {
-    __shared__ double ra[32][33], rb[32][33];
-    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
-    const double rz = col_sum(part_a, NB, Rpad, t, ra);
-    const double rr = col_sum(part_b, NB, Rpad, t, rb);
-    if (threadIdx.y != 0) return;
+// beta, ||r||^2 and the convergence test per column, one warp per column
+__global__ void k_finish_beta_w(int64_t Rpad, int NB, double rtol2, const double *__restrict__ part_a,
+                                const double *__restrict__ part_b, double *__restrict__ col,
+                                int32_t *__restrict__ active, int32_t *__restrict__ iters,
+                                int32_t *__restrict__ nactive) {
+    const int64_t t = (int64_t)blockIdx.x * kFinWarps + (threadIdx.x >> 5);
+    if (t >= Rpad) return;
+    const double rz = warp_col_sum(part_a, NB, Rpad, t);
+    const double rr = warp_col_sum(part_b, NB, Rpad, t);
+    if ((threadIdx.x & 31) != 0) return;
     if (!active[t]) {
         col[BETA * Rpad + t] = 0.0;
         return;
@@ -337,6 +338,7 @@ int pcg_solve(Context &c, cudaStream_t s, const int32_t *mask) {
     const dim3 sg((unsigned)NB, (unsigned)nchunk);
     const unsigned fg = (unsigned)(Rpad / 32);
     const dim3 fb(32, 32);
+    const unsigned fwg = (unsigned)ceil_div(Rpad, kFinWarps);
     const double rtol2 = c.rtol * c.rtol;
     if (mask) {
         // warm start from x on the masked columns: r = b - A x in place
@@ -365,10 +367,11 @@ int pcg_solve(Context &c, cudaStream_t s, const int32_t *mask) {
     for (int it = 0; it < kGraphIters; it++) {
         launch_spmm(ch, sg, s, n, m.nnz, c.nE, c.nK, Rpad, m.d_rowptr.p, m.d_colidx.p, c.d_S.p, c.d_p.p, c.d_q.p,
                     part_c);
-        k_finish_alpha<<<fg, fb, 0, s>>>(Rpad, NB, part_c, c.d_col.p, active, nactive);
+        k_finish_alpha_w<<<fwg, 32 * kFinWarps, 0, s>>>(Rpad, NB, part_c, c.d_col.p, active, nactive);
         k_update_xr<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, c.d_dinv.p, c.d_col.p, active, c.d_x.p, c.d_r.p,
                                       c.d_p.p, c.d_q.p, part_a, part_b);
-        k_finish_beta<<<fg, fb, 0, s>>>(Rpad, NB, rtol2, part_a, part_b, c.d_col.p, active, iters, nactive);
+        k_finish_beta_w<<<fwg, 32 * kFinWarps, 0, s>>>(Rpad, NB, rtol2, part_a, part_b, c.d_col.p, active, iters,
+                                                       nactive);
         k_update_p<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, c.d_dinv.p, c.d_col.p, active, c.d_r.p, c.d_p.p);
     }
     cudaError_t cap = cudaStreamEndCapture(s, &graph);
@@ -444,11 +447,6 @@ __global__ void k_col_total(int64_t Rpad, int NB, const double *__restrict__ par
 void pcg_finish_init(dim3 g, dim3 b, cudaStream_t s, int64_t Rpad, int64_t R, int NB, const double *pa, const double *pb,
                      double *col, int32_t *active, int32_t *iters, int32_t *nactive, const double *pnorm2) {
     k_finish_init<<<g, b, 0, s>>>(Rpad, R, NB, pa, pb, col, active, iters, nactive, nullptr, pnorm2);
-}
-
-void pcg_finish_alpha(dim3 g, dim3 b, cudaStream_t s, int64_t Rpad, int NB, const double *part, double *col,
-                      const int32_t *active, int32_t *nactive) {
-    k_finish_alpha<<<g, b, 0, s>>>(Rpad, NB, part, col, active, nactive);
 }
 
 int spmm_partial_rows(int64_t n, int cap) { return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, kRowsPerBlock), cap)); }

@@ -303,27 +303,6 @@ __global__ void k_m_update_xr(int64_t n, int nE, int64_t R, int64_t Rpad, const 
     block_partials2((double)a, (double)b, part_a, part_b, Rpad, t);
 }
 
-// Column sums of the NB block partials by one warp per column (eight
-// columns per block, so the FP64 additions spread over many SMs instead of
-// the Rpad / 32 SMs of col_sum): lanes take rows lane, lane + 32, ... in two
-// chains, then a shuffle tree; lane 0's total is returned to every lane.
-constexpr int kFinWarps = 8;
-
-__device__ __forceinline__ double warp_col_sum(const double *__restrict__ part, int NB, int64_t Rpad, int64_t t) {
-    const int lane = threadIdx.x & 31;
-    double s0 = 0.0, s1 = 0.0;
-    int b = lane;
-    for (; b + 32 < NB; b += 64) {
-        s0 += part[(int64_t)b * Rpad + t];
-        s1 += part[(int64_t)(b + 32) * Rpad + t];
-    }
-    if (b < NB) s0 += part[(int64_t)b * Rpad + t];
-    double v = s0 + s1;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return __shfl_sync(0xffffffffu, v, 0);
-}
-
 // alpha = rho / (p . q) per active column
 __global__ void k_m_finish_alpha_w(int64_t Rpad, int NB, const double *__restrict__ part, double *__restrict__ col,
                                    const int32_t *__restrict__ active, int32_t *__restrict__ nactive) {

@@ -48,4 +48,25 @@ __device__ inline double col_sum(const double *__restrict__ part, int NB, int64_
     return threadIdx.y == 0 ? red[threadIdx.x][32] : 0.0;
 }
 
+// Column sums of the NB block partials by one warp per column (eight
+// columns per block, so the FP64 additions spread over many SMs instead of
+// the Rpad / 32 SMs of col_sum): lanes take rows lane, lane + 32, ... in two
+// chains, then a shuffle tree; lane 0's total is returned to every lane.
+constexpr int kFinWarps = 8;  // columns (warps) per block of the warp-per-column finishes
+
+__device__ __forceinline__ double warp_col_sum(const double *__restrict__ part, int NB, int64_t Rpad, int64_t t) {
+    const int lane = threadIdx.x & 31;
+    double s0 = 0.0, s1 = 0.0;
+    int b = lane;
+    for (; b + 32 < NB; b += 64) {
+        s0 += part[(int64_t)b * Rpad + t];
+        s1 += part[(int64_t)(b + 32) * Rpad + t];
+    }
+    if (b < NB) s0 += part[(int64_t)b * Rpad + t];
+    double v = s0 + s1;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return __shfl_sync(0xffffffffu, v, 0);
+}
+
 }  // namespace ertgb
