@@ -49,6 +49,7 @@ template <class F> int guard(Context *c, F &&f) {
 }
 
 void invalidate_derived(Context &c) {
+    c.fp64_k.clear();
     c.prim_ready = false;
     c.s1_ready = false;
     c.have_pot = false;

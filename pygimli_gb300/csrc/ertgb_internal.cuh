@@ -207,6 +207,10 @@ struct Context {
     DBuf<double> d_G;
     DBuf<float> d_G32, d_GT32, d_t32, d_z32;
     int32_t fsai_fallback_rows = 0;
+    // mixed precision: wavenumbers whose columns stalled in FP32 in the last
+    // response start in FP64 next time (cleared with the mesh / k / w)
+    std::vector<uint8_t> fp64_k;
+    DBuf<int32_t> d_pre;
     DBuf<double> d_part;          // reduction partials
     DBuf<double> d_col;           // per-column scalars (see pcg.cu)
     DBuf<int32_t> d_active;

@@ -39,10 +39,15 @@ __global__ void __launch_bounds__(256) k_spmm_dot(int64_t n, int64_t nnz, int nE
                                                   const int32_t *__restrict__ colidx,
                                                   const double *__restrict__ vals,
                                                   const double *__restrict__ p, double *__restrict__ q,
-                                                  double *__restrict__ part) {
+                                                  double *__restrict__ part, const int32_t *__restrict__ active) {
     __shared__ double red[kRowsPerBlock][32 * CH];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int64_t t0 = (int64_t)blockIdx.y * 32 * CH + lane;
+    if (active) {  // a chunk of columns none of which is active has nothing to do (q, partials unused)
+        int any = 0;
+        for (int c = threadIdx.x; c < 32 * CH; c += blockDim.x) any |= active[(int64_t)blockIdx.y * 32 * CH + c];
+        if (!__syncthreads_or(any)) return;
+    }
     int64_t kofs[CH];  // value-array offset of each column's wavenumber (padding -> last)
 #pragma unroll
     for (int j = 0; j < CH; j++) kofs[j] = min((t0 + 32 * j) / nE, (int64_t)nK - 1) * nnz;
@@ -295,14 +300,15 @@ int choose_ch(int64_t Rpad) {
     return 1;
 }
 
+// active: skip column chunks without an active column (nullptr: all)
 void launch_spmm(int ch, dim3 grid, cudaStream_t s, int64_t n, int64_t nnz, int nE, int nK, int64_t Rpad,
                  const int32_t *rowptr, const int32_t *colidx, const double *vals, const double *p, double *q,
-                 double *part) {
+                 double *part, const int32_t *active = nullptr) {
     switch (ch) {
-        case 4: k_spmm_dot<4><<<grid, 256, 0, s>>>(n, nnz, nE, nK, Rpad, rowptr, colidx, vals, p, q, part); break;
-        case 3: k_spmm_dot<3><<<grid, 256, 0, s>>>(n, nnz, nE, nK, Rpad, rowptr, colidx, vals, p, q, part); break;
-        case 2: k_spmm_dot<2><<<grid, 256, 0, s>>>(n, nnz, nE, nK, Rpad, rowptr, colidx, vals, p, q, part); break;
-        default: k_spmm_dot<1><<<grid, 256, 0, s>>>(n, nnz, nE, nK, Rpad, rowptr, colidx, vals, p, q, part); break;
+        case 4: k_spmm_dot<4><<<grid, 256, 0, s>>>(n, nnz, nE, nK, Rpad, rowptr, colidx, vals, p, q, part, active); break;
+        case 3: k_spmm_dot<3><<<grid, 256, 0, s>>>(n, nnz, nE, nK, Rpad, rowptr, colidx, vals, p, q, part, active); break;
+        case 2: k_spmm_dot<2><<<grid, 256, 0, s>>>(n, nnz, nE, nK, Rpad, rowptr, colidx, vals, p, q, part, active); break;
+        default: k_spmm_dot<1><<<grid, 256, 0, s>>>(n, nnz, nE, nK, Rpad, rowptr, colidx, vals, p, q, part, active); break;
     }
 }
 
@@ -366,7 +372,7 @@ int pcg_solve(Context &c, cudaStream_t s, const int32_t *mask) {
     ERTGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     for (int it = 0; it < kGraphIters; it++) {
         launch_spmm(ch, sg, s, n, m.nnz, c.nE, c.nK, Rpad, m.d_rowptr.p, m.d_colidx.p, c.d_S.p, c.d_p.p, c.d_q.p,
-                    part_c);
+                    part_c, active);
         k_finish_alpha_w<<<fwg, 32 * kFinWarps, 0, s>>>(Rpad, NB, part_c, c.d_col.p, active, nactive);
         k_update_xr<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, c.d_dinv.p, c.d_col.p, active, c.d_x.p, c.d_r.p,
                                       c.d_p.p, c.d_q.p, part_a, part_b);

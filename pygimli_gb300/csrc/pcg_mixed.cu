@@ -474,6 +474,17 @@ __global__ void k_m_finish_ru(int64_t Rpad, int NB, double rtol2, const double *
     atomicAdd(cs.nactive, 1);
 }
 
+// columns of wavenumbers that stalled in FP32 in the previous response go
+// straight to the FP64 solver (stalled = 2: from zero)
+__global__ void k_m_pre_fp64(int64_t Rpad, const int32_t *__restrict__ pre, ColState cs) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= Rpad || !pre[t] || !cs.active[t]) return;
+    cs.active[t] = 0;
+    cs.stalled[t] = 2;
+    atomicSub(cs.nactive, 1);
+    atomicAdd(cs.nstalled, 1);
+}
+
 int choose_ch(int64_t Rpad) {
     const int64_t w = Rpad / 32;
     for (int ch : {4, 3, 2})
@@ -582,6 +593,21 @@ int pcg_solve_mixed(Context &c, cudaStream_t s) {
                     c.d_pnorm2.n >= (size_t)Rpad ? c.d_pnorm2.p : nullptr);
     ERTGB_CUDA(cudaGetLastError());
     c.stats.launches_response += 5;
+    if ((int)c.fp64_k.size() == c.nK) {
+        std::vector<int32_t> pre((size_t)Rpad, 0);
+        int32_t n_pre = 0;
+        for (int64_t t = 0; t < R; t++)
+            if (c.fp64_k[(size_t)(t / c.nE)]) {
+                pre[(size_t)t] = 1;
+                n_pre++;
+            }
+        if (n_pre) {
+            c.d_pre.upload(pre, s);
+            k_m_pre_fp64<<<(unsigned)ceil_div(Rpad, 256), 256, 0, s>>>(Rpad, c.d_pre.p, cs);
+            ERTGB_CUDA(cudaGetLastError());
+            c.stats.launches_response += 1;
+        }
+    }
 
     cudaGraph_t g_it = nullptr, g_ru = nullptr;
     cudaGraphExec_t e_it = nullptr, e_ru = nullptr;
@@ -648,6 +674,17 @@ int pcg_solve_mixed(Context &c, cudaStream_t s) {
     ERTGB_CUDA(cudaMemcpyAsync(&h_stalled, cs.nstalled, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     ERTGB_CUDA(cudaStreamSynchronize(s));
     c.stats.stalled_columns = h_stalled;
+    if (status == ERTGB_OK) {  // wavenumbers with at least half of their columns stalled start in FP64 next time
+        std::vector<int32_t> st((size_t)Rpad);
+        ERTGB_CUDA(cudaMemcpyAsync(st.data(), cs.stalled, sizeof(int32_t) * Rpad, cudaMemcpyDeviceToHost, s));
+        ERTGB_CUDA(cudaStreamSynchronize(s));
+        c.fp64_k.assign((size_t)c.nK, 0);
+        for (int k = 0; k < c.nK; k++) {
+            int cnt = 0;
+            for (int e = 0; e < c.nE; e++) cnt += st[(size_t)k * c.nE + e] != 0;
+            c.fp64_k[(size_t)k] = 2 * cnt >= c.nE ? 1 : 0;
+        }
+    }
     if (status == ERTGB_OK && h_stalled > 0) {
         // FP64 PCG on the stalled columns, warm-started from their FP64 solution
         c.stats.iterations = 0;
