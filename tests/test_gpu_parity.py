@@ -469,3 +469,31 @@ def test_complex_resistivity_golden(torch, golden_dir, name, precision):
           f"columns finished in FP64 {st['stalled_columns']}")
     assert J.shape == z["J"].shape
     assert e_r <= 1e-7 and e_j <= 1e-6
+
+
+def test_complex_sign_and_mirror_symmetry(torch):
+    """The reference's complex simulate test (pygimli/testing/
+    test_ERTManager_simulate.py) on this operator: layered complex
+    resistivity (99.595 + 8.987j above -5 m, 59.595 + 8.987j below), five
+    electrodes; a configuration and its copy with the sign of k reversed give
+    the same complex apparent resistivity, its mirror image the same up to
+    the mesh's asymmetry, and phases and amplitudes are positive."""
+    from pygimli_gb300 import ERTModelling
+    xs = np.arange(-2.0, 3.0)
+    mesh = create_para_mesh_2d(xs, para_dx=0.25, para_depth=8.0)
+    data = DataContainerERT(np.column_stack([xs, np.zeros(5), np.zeros(5)]),
+                            np.array([[0, 1, 3, 2], [0, 1, 2, 3], [3, 2, 1, 0]]))
+    data.set("k", geometricFactors(data, 2))
+    assert data["k"][0] == -data["k"][1]
+    depth = mesh.cellCenters()[:, 1]
+    rho = np.where(depth > -5.0, 99.595 + 8.987j, 59.595 + 8.987j)
+    for precision in ("fp64", "mixed"):
+        fop = ERTModelling(precision=precision)
+        fop.setData(data)
+        fop.setMesh(mesh, ignoreRegionManager=True)
+        fop.setComplex(True)
+        out = fop.response(rho)
+        z = out[:3] + 1j * out[3:]
+        assert abs(z[1] - z[0]) / abs(z[0]) < 1e-9, z
+        assert abs(z[2] - z[0]) / abs(z[0]) < 2e-2, z
+        assert np.all(np.abs(z) > 0) and np.all(np.angle(z) > 0), z
