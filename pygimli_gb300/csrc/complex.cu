@@ -465,6 +465,114 @@ __global__ void k_spmm_c32(int64_t n, int64_t nnz, int nE, int64_t R, int64_t Rp
     block_partials3(a, b, 0.0, p_re, p_im, nullptr, Rpad, t);
 }
 
+// q = A p for one wavenumber (3-D): an 8-lane group per row, every lane a
+// float4 = two complex columns per chunk, CH chunks of 16 columns (Rpad =
+// 16 CH), rows of a block contiguous; column dots p^T q per lane, summed over
+// the block's groups in FP64 in a fixed order.
+constexpr int kCqThreads = 256;
+constexpr int kCqGroups = kCqThreads / 8;
+
+template <int CH>
+__global__ void __launch_bounds__(kCqThreads, 2) k_spmm_c32q(int64_t n, int64_t Rpad, const int32_t *__restrict__ rowptr,
+                                                              const int32_t *__restrict__ colidx,
+                                                              const float2 *__restrict__ vals,
+                                                              const float2 *__restrict__ p, float2 *__restrict__ q,
+                                                              double *__restrict__ p_re, double *__restrict__ p_im) {
+    __shared__ float red[kCqGroups][32 * CH + 1];
+    const int l8 = threadIdx.x & 7, g = threadIdx.x >> 3;
+    const int64_t per_block = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t r_begin = (int64_t)blockIdx.x * per_block;
+    const int64_t r_end = min(n, r_begin + per_block);
+    float4 dot[CH];
+#pragma unroll
+    for (int j = 0; j < CH; j++) dot[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int64_t row = r_begin + g; row < r_end; row += kCqGroups) {
+        float4 acc[CH];
+#pragma unroll
+        for (int j = 0; j < CH; j++) acc[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+        const int32_t s1 = rowptr[row + 1];
+#pragma unroll 2
+        for (int32_t s = rowptr[row]; s < s1; s++) {
+            const int64_t col = colidx[s];
+            const float2 v = vals[s];
+            const float4 *pc = reinterpret_cast<const float4 *>(p + col * Rpad) + l8;
+#pragma unroll
+            for (int j = 0; j < CH; j++) {
+                const float4 x = __ldg(pc + 8 * j);
+                acc[j].x = fmaf(v.x, x.x, fmaf(-v.y, x.y, acc[j].x));
+                acc[j].y = fmaf(v.x, x.y, fmaf(v.y, x.x, acc[j].y));
+                acc[j].z = fmaf(v.x, x.z, fmaf(-v.y, x.w, acc[j].z));
+                acc[j].w = fmaf(v.x, x.w, fmaf(v.y, x.z, acc[j].w));
+            }
+        }
+        float4 *qr = reinterpret_cast<float4 *>(q + row * Rpad) + l8;
+        const float4 *pr = reinterpret_cast<const float4 *>(p + row * Rpad) + l8;
+#pragma unroll
+        for (int j = 0; j < CH; j++) {
+            qr[8 * j] = acc[j];
+            const float4 d = pr[8 * j];
+            dot[j].x += d.x * acc[j].x - d.y * acc[j].y;
+            dot[j].y += d.x * acc[j].y + d.y * acc[j].x;
+            dot[j].z += d.z * acc[j].z - d.w * acc[j].w;
+            dot[j].w += d.z * acc[j].w + d.w * acc[j].z;
+        }
+    }
+    // lane l8, chunk j holds columns 16 j + 2 l8 and + 1 as (re, im, re, im)
+#pragma unroll
+    for (int j = 0; j < CH; j++) {
+        const int c = 4 * (8 * j + l8);
+        red[g][c] = dot[j].x;
+        red[g][c + 1] = dot[j].y;
+        red[g][c + 2] = dot[j].z;
+        red[g][c + 3] = dot[j].w;
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < 32 * CH; c += kCqThreads) {
+        double sum = 0.0;
+#pragma unroll 8
+        for (int gg = 0; gg < kCqGroups; gg++) sum += (double)red[gg][c];
+        const int64_t t = c >> 1;  // column
+        if (c & 1) p_im[(int64_t)blockIdx.x * Rpad + t] = sum;
+        else p_re[(int64_t)blockIdx.x * Rpad + t] = sum;
+    }
+}
+
+// alpha = rho / (p^T q), one warp per column (warp_col_sum)
+__global__ void k_finish_alpha_cw(int64_t Rpad, int NB, const double *__restrict__ p_re,
+                                  const double *__restrict__ p_im, double *__restrict__ col,
+                                  const int32_t *__restrict__ active, int32_t *__restrict__ nactive) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *nactive = 0;
+    const int64_t t = (int64_t)blockIdx.x * kFinWarps + (threadIdx.x >> 5);
+    if (t >= Rpad) return;
+    const double2 pq = make_double2(warp_col_sum(p_re, NB, Rpad, t), warp_col_sum(p_im, NB, Rpad, t));
+    if ((threadIdx.x & 31) != 0 || !active[t]) return;
+    const double2 rho = make_double2(col[C_RHO_RE * Rpad + t], col[C_RHO_IM * Rpad + t]);
+    double2 al = make_double2(0.0, 0.0);
+    if (hypot(pq.x, pq.y) > 0.0) al = cdiv(rho, pq);
+    if (!isfinite(al.x) || !isfinite(al.y)) al = make_double2(0.0, 0.0);
+    col[C_ALPHA_RE * Rpad + t] = al.x;
+    col[C_ALPHA_IM * Rpad + t] = al.y;
+}
+
+// recursive beta (mixed), one warp per column
+__global__ void k_finish_beta_mcw(int64_t Rpad, int NB, const double *__restrict__ p_re,
+                                  const double *__restrict__ p_im, double *__restrict__ col,
+                                  const int32_t *__restrict__ active, int32_t *__restrict__ iters) {
+    const int64_t t = (int64_t)blockIdx.x * kFinWarps + (threadIdx.x >> 5);
+    if (t >= Rpad) return;
+    const double2 rz = make_double2(warp_col_sum(p_re, NB, Rpad, t), warp_col_sum(p_im, NB, Rpad, t));
+    if ((threadIdx.x & 31) != 0 || !active[t]) return;
+    iters[t] += 1;
+    const double2 rho = make_double2(col[C_RHO_RE * Rpad + t], col[C_RHO_IM * Rpad + t]);
+    double2 be = make_double2(0.0, 0.0);
+    if (hypot(rho.x, rho.y) > 0.0) be = cdiv(rz, rho);
+    if (!isfinite(be.x) || !isfinite(be.y)) be = make_double2(0.0, 0.0);
+    col[C_BETA_RE * Rpad + t] = be.x;
+    col[C_BETA_IM * Rpad + t] = be.y;
+    col[C_RHO_RE * Rpad + t] = rz.x;
+    col[C_RHO_IM * Rpad + t] = rz.y;
+}
+
 // y += alpha p, r -= alpha q, z = D^-1 r; partials of r^T z and ||r||^2
 __global__ void k_update_yrz_c32(int64_t n, int nE, int64_t R, int64_t Rpad, const double *__restrict__ col,
                                  const int32_t *__restrict__ active, const float2 *__restrict__ dinv32,
@@ -503,25 +611,6 @@ __global__ void k_update_p_c32(int64_t n, int64_t Rpad, const double *__restrict
         const int64_t i = row * Rpad + t;
         p[i] = fadd(z[i], fmul(be, p[i]));
     }
-}
-
-// recursive beta (mixed): convergence is left to the reliable updates
-__global__ void k_finish_beta_mc(int64_t Rpad, int NB, const double *__restrict__ p_re,
-                                 const double *__restrict__ p_im, double *__restrict__ col,
-                                 const int32_t *__restrict__ active, int32_t *__restrict__ iters) {
-    __shared__ double ra[32][33], rb[32][33];
-    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
-    const double2 rz = make_double2(col_sum(p_re, NB, Rpad, t, ra), col_sum(p_im, NB, Rpad, t, rb));
-    if (threadIdx.y != 0 || !active[t]) return;
-    iters[t] += 1;
-    const double2 rho = make_double2(col[C_RHO_RE * Rpad + t], col[C_RHO_IM * Rpad + t]);
-    double2 be = make_double2(0.0, 0.0);
-    if (hypot(rho.x, rho.y) > 0.0) be = cdiv(rz, rho);
-    if (!isfinite(be.x) || !isfinite(be.y)) be = make_double2(0.0, 0.0);
-    col[C_BETA_RE * Rpad + t] = be.x;
-    col[C_BETA_IM * Rpad + t] = be.y;
-    col[C_RHO_RE * Rpad + t] = rz.x;
-    col[C_RHO_IM * Rpad + t] = rz.y;
 }
 
 // reliable update, part 1: x += y, y = 0 on active columns; counter reset
@@ -707,15 +796,33 @@ int cocg_mixed(Context &c, const CxLaunch &L, cudaStream_t s, int *status) {
     k_finish_ru_c<<<L.fg, L.fb, 0, s>>>(Rpad, NB, rtol2, pa, pb, pc, x.col.p, active, stalled, nactive, nstalled);
     ERTGB_CUDA(cudaStreamEndCapture(s, &gru));
     ERTGB_CUDA(cudaGraphInstantiate(&eru, gru, 0));
+    // one wavenumber and Rpad = 16 CH: the 8-lane-group operator (partials of NBq block rows)
+    const int chq = c.nK == 1 ? (int)(Rpad / 16) : 0;
+    const bool fastq = chq == 2 || chq == 4 || chq == 6 || chq == 8;
+    const int NBq = fastq ? (int)std::min<int64_t>(ceil_div(n, kCqGroups), 304) : NB;
+    const unsigned fwg = (unsigned)ceil_div(Rpad, kFinWarps);
+    auto spmm = [&] {
+        switch (fastq ? chq : 0) {
+            case 2: k_spmm_c32q<2><<<NBq, kCqThreads, 0, s>>>(n, Rpad, m.d_rowptr.p, m.d_colidx.p, x.S32.p, x.p32.p,
+                                                             x.q32.p, pd, pe); break;
+            case 4: k_spmm_c32q<4><<<NBq, kCqThreads, 0, s>>>(n, Rpad, m.d_rowptr.p, m.d_colidx.p, x.S32.p, x.p32.p,
+                                                             x.q32.p, pd, pe); break;
+            case 6: k_spmm_c32q<6><<<NBq, kCqThreads, 0, s>>>(n, Rpad, m.d_rowptr.p, m.d_colidx.p, x.S32.p, x.p32.p,
+                                                             x.q32.p, pd, pe); break;
+            case 8: k_spmm_c32q<8><<<NBq, kCqThreads, 0, s>>>(n, Rpad, m.d_rowptr.p, m.d_colidx.p, x.S32.p, x.p32.p,
+                                                             x.q32.p, pd, pe); break;
+            default: k_spmm_c32<<<L.vg, L.vb, 0, s>>>(n, nnz, c.nE, R, Rpad, m.d_rowptr.p, m.d_colidx.p, x.S32.p,
+                                                      active, x.p32.p, x.q32.p, pd, pe);
+        }
+    };
     try {
         run_graph_loop(c, s, [&] {
             for (int it = 0; it < kGraphItersC; it++) {
-                k_spmm_c32<<<L.vg, L.vb, 0, s>>>(n, nnz, c.nE, R, Rpad, m.d_rowptr.p, m.d_colidx.p, x.S32.p, active,
-                                                 x.p32.p, x.q32.p, pd, pe);
-                k_finish_alpha_c<<<L.fg, L.fb, 0, s>>>(Rpad, NB, pd, pe, x.col.p, active, nactive);
+                spmm();
+                k_finish_alpha_cw<<<fwg, 32 * kFinWarps, 0, s>>>(Rpad, NBq, pd, pe, x.col.p, active, nactive);
                 k_update_yrz_c32<<<L.vg, L.vb, 0, s>>>(n, c.nE, R, Rpad, x.col.p, active, x.dinv32.p, x.y32.p,
                                                        x.r32.p, x.z32.p, x.p32.p, x.q32.p, pa, pb, pc);
-                k_finish_beta_mc<<<L.fg, L.fb, 0, s>>>(Rpad, NB, pa, pb, x.col.p, active, iters);
+                k_finish_beta_mcw<<<fwg, 32 * kFinWarps, 0, s>>>(Rpad, NB, pa, pb, x.col.p, active, iters);
                 k_update_p_c32<<<L.vg, L.vb, 0, s>>>(n, Rpad, x.col.p, active, x.z32.p, x.p32.p);
             }
         }, nactive, 4, [&] { ERTGB_CUDA(cudaGraphLaunch(eru, s)); }, status);
