@@ -621,3 +621,75 @@ def write_vtk(path, dim, nodes, cells, cell_markers, boundaries, boundary_marker
     with open(fname, "w") as f:
         f.write("\n".join(out) + "\n")
     return fname
+
+
+def read_vtk(path):
+    """Mesh::importVTK for a legacy ASCII unstructured grid (mesh_io.cpp:
+    importVTK, readVTKPoints_, readVTKCells_, readVTKScalars_): the
+    dimension from the 'd-2__' / 'd-3__' comment line or the coordinates (no
+    z: 2-D; no y but z: 2-D with y and z swapped), POINTS, CELLS (node order as
+    written), every SCALARS array into the data map and 'Marker' as the cell
+    markers.  CELL_TYPES, boundaries and node markers are not in the file's
+    reach of the reference either (markers 0)."""
+    fname = path[:path.rfind(".vtk")] + ".vtk" if ".vtk" in path else path + ".vtk"
+    with open(fname) as f:
+        lines = f.read().split("\n")
+    comment = lines[1] if len(lines) > 1 else ""
+    dim = 2 if "d-2__" in comment else (3 if "d-3__" in comment else 0)
+    i = 2
+    while i < len(lines) and lines[i].split()[:1] not in (["ASCII"], ["BINARY"]):
+        i += 1
+    if i < len(lines) and lines[i].split()[:1] == ["BINARY"]:
+        raise ValueError("binary VTK files are not supported")
+    i += 1
+    if i >= len(lines) or not lines[i].split() or lines[i].split()[-1] != "UNSTRUCTURED_GRID":
+        raise ValueError("only unstructured grids are supported")
+    toks = " ".join(lines[i + 1:]).split()
+    pos = 0
+    nodes = np.zeros((0, 3))
+    cells = []
+    data = {}
+    while pos < len(toks):
+        t = toks[pos]
+        if t == "POINTS":
+            nv = int(toks[pos + 1])
+            pos += 3
+            nodes = np.array([float(v) for v in toks[pos:pos + 3 * nv]]).reshape(nv, 3)
+            pos += 3 * nv
+            y0 = not np.any(np.abs(nodes[:, 1]) > 1e-12)
+            z0 = not np.any(np.abs(nodes[:, 2]) > 1e-12)
+            if y0 and not z0:
+                dim = 2
+                nodes[:, 1], nodes[:, 2] = nodes[:, 2].copy(), 0.0
+            elif z0:
+                dim = 2
+        elif t == "CELLS":
+            nc = int(toks[pos + 1])
+            pos += 3
+            for _ in range(nc):
+                k = int(toks[pos])
+                cells.append([int(v) for v in toks[pos + 1:pos + 1 + k]])
+                pos += 1 + k
+        elif t == "SCALARS":
+            name = toks[pos + 1]
+            pos += 4 if pos + 3 < len(toks) and toks[pos + 3] == "1" else 3
+            if toks[pos] == "LOOKUP_TABLE":
+                pos += 2
+            vals = []
+            while pos < len(toks) and toks[pos] not in ("SCALARS", "CELL_DATA", "POINT_DATA", "VECTORS",
+                                                           "FIELD", "CELLS", "POINTS", "CELL_TYPES"):
+                vals.append(float(toks[pos]))
+                pos += 1
+            data[name] = np.array(vals)
+        else:
+            pos += 1
+    if dim == 0:
+        dim = 3
+    nv = {len(c) for c in cells}
+    if len(nv) > 1:
+        raise ValueError("mixed cell types: only simplex meshes are supported")
+    C = len(cells)
+    cell_arr = np.array(cells, np.int32).reshape(C, nv.pop() if nv else dim + 1)
+    mk = data.get("Marker")
+    markers = mk.astype(np.int32) if mk is not None and len(mk) == C else np.zeros(C, np.int32)
+    return {"dim": dim, "nodes": nodes, "cells": cell_arr, "cell_markers": markers, "data": data}

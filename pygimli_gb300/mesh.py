@@ -196,6 +196,8 @@ class Mesh:
         3, else the first format of Mesh::loadBinary) or a numpy archive
         written by ``save``."""
         path = os.fspath(path)
+        if path.endswith(".vtk"):
+            return Mesh.importVTK(path)
         if path.endswith(".npz"):
             z = np.load(path)
             return Mesh(int(z["dim"]), z["nodes"], z["cells"], z["cell_markers"], z["node_markers"],
@@ -221,6 +223,17 @@ class Mesh:
         m.boundary_left_cells = np.ascontiguousarray(r["left"], np.int32)
         m.boundary_right_cells = np.ascontiguousarray(r["right"], np.int32)
         m.geometry = r["geometry"]
+        m._data = r["data"]
+        return m
+
+    @staticmethod
+    def importVTK(path):
+        """Mesh from a legacy ASCII VTK unstructured grid (Mesh::importVTK):
+        nodes, cells, the SCALARS arrays as data and 'Marker' as cell
+        markers; no boundaries and no node markers (as the reference)."""
+        from .fileio import read_vtk
+        r = read_vtk(os.fspath(path))
+        m = Mesh(r["dim"], r["nodes"], r["cells"], r["cell_markers"], check=False)
         m._data = r["data"]
         return m
 

@@ -183,3 +183,19 @@ def test_bms_first_format(name, tmp_path):
     out = v1.saveBinary(str(tmp_path / name))
     with open(out, "rb") as a, open(src, "rb") as b:
         assert a.read() == b.read()
+
+
+@pytest.mark.parametrize("name", MESHES)
+def test_vtk_import(name):
+    """Mesh::importVTK of the reference's VTK files: the nodes, cells (a
+    Tetrahedron10 in the file's node order, as the reference reads it back),
+    cell markers and data arrays of the mesh it exported; no boundaries."""
+    m = Mesh.load(os.path.join(EXP, name + ".bms"))
+    v = Mesh.load(os.path.join(EXP, name + ".vtk"))
+    assert v.dim() == m.dim() and v.boundaryCount() == 0
+    assert np.array_equal(v.nodes, m.nodes)
+    cells = m.cells[:, [0, 1, 2, 3, 4, 7, 5, 6, 9, 8]] if m.cells.shape[1] == 10 else m.cells
+    assert np.array_equal(v.cells, cells)
+    assert np.array_equal(v.cell_markers, m.cell_markers)
+    assert np.allclose(v["res"], m["res"], rtol=1e-13, atol=0)
+    assert np.allclose(v["pot_u"], m["pot u"], rtol=1e-13, atol=1e-300)
