@@ -193,7 +193,7 @@ def test_vtk_import(name):
     m = Mesh.load(os.path.join(EXP, name + ".bms"))
     v = Mesh.load(os.path.join(EXP, name + ".vtk"))
     assert v.dim() == m.dim() and v.boundaryCount() == 0
-    assert np.array_equal(v.nodes, m.nodes)
+    assert np.allclose(v.nodes, m.nodes, rtol=1e-13, atol=1e-13)  # the file holds 14 significant digits
     cells = m.cells[:, [0, 1, 2, 3, 4, 7, 5, 6, 9, 8]] if m.cells.shape[1] == 10 else m.cells
     assert np.array_equal(v.cells, cells)
     assert np.array_equal(v.cell_markers, m.cell_markers)
