@@ -162,6 +162,12 @@ class DataContainerERT:
         self._sensors = np.ascontiguousarray(sensors)
         self._set_field_map(f)
 
+    def estimateError(self, *args, **kwargs):
+        """Set 'err' from estimateError (geometric factors first if missing)."""
+        if not self.haveData("k"):
+            self.set("k", geometricFactors(self, 3 if np.ptp(self._sensors[:, 1]) > 0 else 2))
+        self.set("err", estimateError(self, *args, **kwargs))
+
     def additionalPoints(self):
         """Additional (topography) points read from a file."""
         return self._topo.copy()
@@ -346,6 +352,33 @@ def _u_half(p, s):
     rm = np.linalg.norm(p - sm, axis=-1)
     with np.errstate(divide="ignore"):
         return (1.0 / r + 1.0 / rm) / (4.0 * np.pi)
+
+
+def estimateError(data, relativeError=0.03, absoluteUError=None, absoluteError=0, absoluteCurrent=0.1):
+    """Relative data error from a relative and an absolute part
+    (pygimli/physics/ert/ert.py:482-540): relativeError + |absoluteError /
+    rhoa|, or with ``absoluteUError`` (V) relativeError + |absoluteUError /
+    u| where u comes from 'u', else r * i, else rhoa / k * i (i: 'i' or
+    absoluteCurrent).  A relativeError of 0.5 or more is taken as percent."""
+    if relativeError >= 0.5:
+        relativeError /= 100.0
+    if absoluteUError is None:
+        if not data.allNonZero("rhoa"):
+            raise ValueError("We need apparent resistivity values (rhoa) in the data to estimate a data error.")
+        return relativeError + np.abs(absoluteError / data["rhoa"])
+    i = data["i"] if data.haveData("i") else absoluteCurrent
+    if data.haveData("u"):
+        u = data["u"]
+    elif data.haveData("r"):
+        u = data["r"] * i
+    elif data.haveData("rhoa"):
+        if not data.haveData("k"):
+            raise ValueError("We need (rhoa) and (k) in the data to estimate data error.")
+        u = data["rhoa"] / data["k"] * i
+    else:
+        raise ValueError("We need apparent resistivity values (rhoa) or impedances (r) in the data to estimate "
+                         "data error.")
+    return np.abs(absoluteUError / u) + relativeError
 
 
 def geometricFactors(data, dim=3):

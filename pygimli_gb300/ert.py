@@ -582,14 +582,106 @@ class ERTModelling:
         return None if self._elec_nodes is None else self._elec_nodes.copy()
 
 
-def simulate(mesh, scheme, res, sr=True, **kwargs):
-    """Noise-free apparent resistivities of ``res`` (per cell) for ``scheme``,
-    like pg.physics.ert.simulate without noise (pygimli/physics/ert/ert.py:12-285)."""
-    fop = ERTModelling(sr=sr, **kwargs)
+def _cell_values(mesh, res):
+    """The forms of ``res`` simulate accepts: a number (real or complex), one
+    value per cell, a map [[marker, value], ...] (pyGIMLi's parseArgToArray)
+    or N x cellCount rows.  Returns (array, is_rows)."""
+    C = mesh.cellCount()
+    if np.isscalar(res):
+        return np.full(C, res, dtype=complex if np.iscomplexobj(res) else float), False
+    first = res[0]
+    if hasattr(first, "__iter__") and len(first) == 2 and len(res) != C:
+        markers = mesh.cell_markers
+        table = {int(m): v for m, v in res}
+        missing = sorted(set(np.unique(markers).tolist()) - set(table))
+        if missing:
+            raise ValueError(f"Mesh contains markers without assigned resistivities {missing}. Please fix given rhomap.")
+        vals = np.array([table[int(m)] for m in markers])
+        return vals, False
+    arr = np.asarray(res)
+    if arr.ndim == 2:
+        return arr, True
+    if len(arr) != C:
+        raise IndexError("Simulate called with wrong resistivity array.")
+    return arr, False
+
+
+def simulate(mesh, scheme, res, **kwargs):
+    """Simulate an ERT measurement (pg.physics.ert.simulate,
+    pygimli/physics/ert/ert.py:12-285): apparent resistivities of ``res`` for
+    ``scheme`` on ``mesh``, with apparent phases ('phia') for complex
+    resistivity; ``noiseLevel`` > 0 adds Gaussian noise with the errors of
+    ``estimateError`` (``noiseAbs`` V at 1 A; ``seed`` fixes it, numpy's
+    generator: the draws differ from pyGIMLi's); ``returnArray`` returns
+    rhoa (and phia) instead of the container.  Keywords of ERTModelling
+    (device, precision, precond, ...) are passed on.  Not provided:
+    calcOnly, returnFields, contact impedances (CEM)."""
+    from .data import estimateError
+    for k in ("calcOnly", "returnFields", "contactImpedances"):
+        if kwargs.get(k):
+            raise NotImplementedError(f"simulate({k}=...) is not provided")
+        kwargs.pop(k, None)
+    kwargs.pop("verbose", None)
+    return_array = kwargs.pop("returnArray", False)
+    noise_level = float(kwargs.pop("noiseLevel", 0.0))
+    noise_abs = kwargs.pop("noiseAbs", 1e-4)
+    seed = kwargs.pop("seed", None)
+    phi_err = kwargs.pop("phiErr", None)
+    current = kwargs.pop("current", 1.0)
+    return_fop = kwargs.pop("returnFOP", False)
+    fop = ERTModelling(**kwargs)
     data = scheme.copy()
-    if not data.exists("k") or np.min(np.abs(data["k"])) < TOLERANCE:
+    vals, rows = _cell_values(mesh, res)
+    cplx = np.iscomplexobj(vals)
+    fop.setComplex(cplx)
+    if not data.allNonZero("k"):
         data.set("k", geometricFactors(data, mesh.dim()))
     fop.setData(data)
     fop.setMesh(mesh, ignoreRegionManager=True)
-    data.set("rhoa", fop.response(res))
-    return data
+    D = data.size()
+    for t in ("u", "i", "r"):
+        data.set(t, np.zeros(D))
+
+    def one(v):
+        out = fop.response(v)
+        if cplx:
+            z = out[:D] + 1j * out[D:]
+            return np.abs(z), np.angle(z)
+        return np.asarray(out), None
+
+    if rows:
+        both = [one(v) for v in vals]
+        rhoa = np.array([b[0] for b in both])
+        phia = np.array([b[1] for b in both]) if cplx else None
+        data.set("rhoa", rhoa[0])
+        if cplx:
+            data.set("phia", phia[0])
+    else:
+        rhoa, phia = one(vals)
+        data.set("rhoa", rhoa)
+        if cplx:
+            data.set("phia", phia)
+    if noise_level > 0 and not rows:
+        rng = np.random.default_rng(seed)
+        if not data.allNonZero("err"):
+            data.set("err", estimateError(data, relativeError=noise_level, absoluteUError=noise_abs,
+                                          absoluteCurrent=1))
+        rhoa = rhoa * (1.0 + rng.standard_normal(D) * data["err"])
+        data.set("rhoa", rhoa)
+        if phia is not None:
+            if data.allNonZero("iperr"):
+                ip_err = data["iperr"]
+            else:
+                level = noise_level / 100.0 if noise_level > 0.5 else noise_level
+                ip_err = np.full(D, phi_err / 1000.0) if phi_err is not None else np.abs(phia) * level
+            phia = phia + rng.standard_normal(D) * ip_err
+            data.set("iperr", ip_err)
+            data.set("phia", phia)
+    if data.allNonZero("k"):
+        data.set("r", data["rhoa"] / data["k"])
+        data.set("i", np.full(D, float(current)))
+        data.set("u", data["r"] * data["i"])
+    if return_array:
+        return (rhoa, phia) if phia is not None else rhoa
+    data.set("valid", np.ones(D))
+    return (data, fop) if return_fop else data

@@ -497,3 +497,34 @@ def test_complex_sign_and_mirror_symmetry(torch):
         assert abs(z[1] - z[0]) / abs(z[0]) < 1e-9, z
         assert abs(z[2] - z[0]) / abs(z[0]) < 2e-2, z
         assert np.all(np.abs(z) > 0) and np.all(np.angle(z) > 0), z
+
+
+def test_simulate_forms(torch):
+    """simulate() as pg.physics.ert.simulate: a resistivity map by marker, a
+    per-cell array and N rows agree; rhoa scales with the model; complex maps
+    give positive phases; seeded noise is reproducible and uses
+    estimateError's errors; u = rhoa / k at 1 A."""
+    from pygimli_gb300 import simulate
+    from pygimli_gb300.data import estimateError
+    xs = np.arange(8.0)
+    mesh = create_para_mesh_2d(xs, para_dx=0.5, para_depth=4.0)
+    mk = np.where(mesh.cellCenters()[:, 1] > -1.5, 1, 2).astype(np.int32)
+    mesh.setCellMarkers(mk)
+    scheme = createData(xs, "dd")
+    d = simulate(mesh, scheme, [[1, 100.0], [2, 10.0]])
+    assert np.all(d["rhoa"] > 0) and d.allNonZero("k")
+    assert np.allclose(d["u"], d["rhoa"] / d["k"]) and np.all(d["i"] == 1.0)
+    rho = np.where(mk == 1, 100.0, 10.0)
+    a = simulate(mesh, scheme, rho, returnArray=True)
+    rows = simulate(mesh, scheme, np.vstack([rho, 2.0 * rho]), returnArray=True)
+    assert np.allclose(a, d["rhoa"], rtol=1e-12) and rows.shape == (2, scheme.size())
+    assert np.allclose(rows[1], 2.0 * rows[0], rtol=1e-8)
+    c = simulate(mesh, scheme, [[1, 100.0 + 1.0j], [2, 10.0 + 0.5j]])
+    assert np.all(c["rhoa"] > 0) and np.all(c["phia"] > 0)
+    n1 = simulate(mesh, scheme, rho, noiseLevel=0.03, seed=5)
+    n2 = simulate(mesh, scheme, rho, noiseLevel=0.03, seed=5)
+    assert np.array_equal(n1["rhoa"], n2["rhoa"]) and not np.allclose(n1["rhoa"], a)
+    ref = d.copy()
+    for t in ("u", "i", "r"):
+        ref.set(t, np.zeros(ref.size()))
+    assert np.allclose(n1["err"], estimateError(ref, relativeError=0.03, absoluteUError=1e-4, absoluteCurrent=1))

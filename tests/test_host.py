@@ -88,3 +88,18 @@ def test_library_fails_loudly_without_device(built_lib):
     rc = L.ertgb_create(ctypes.byref(ctx), 0)
     assert rc == _native.CUDA_ERROR
     assert b"cuda" in L.ertgb_last_error(None).lower()
+
+
+def test_estimate_error_forms():
+    """estimateError (pygimli/physics/ert/ert.py:482-540) on hand values."""
+    import numpy as np
+    from pygimli_gb300.data import DataContainerERT, estimateError
+    d = DataContainerERT(np.array([[0.0, 0, 0], [1, 0, 0], [2, 0, 0], [3, 0, 0]]), np.array([[0, 1, 2, 3]] * 2))
+    d.set("rhoa", np.array([100.0, 50.0]))
+    d.set("k", np.array([10.0, 20.0]))
+    assert np.allclose(estimateError(d, 0.03, absoluteError=1.0), [0.04, 0.05])
+    assert np.allclose(estimateError(d, 3.0), [0.03, 0.03])                    # percent
+    u = np.array([100.0 / 10.0, 50.0 / 20.0]) * 0.1
+    assert np.allclose(estimateError(d, 0.02, absoluteUError=1e-3), 1e-3 / u + 0.02)
+    d.set("u", np.array([2.0, 4.0]))
+    assert np.allclose(estimateError(d, 0.02, absoluteUError=1e-2), [0.025, 0.0225])
