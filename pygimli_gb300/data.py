@@ -68,15 +68,34 @@ class DataContainerERT:
         return len(self._sensors)
 
     def createSensor(self, pos, tolerance=1e-3):
+        """Index of the sensor at ``pos``: the last one closer than
+        ``tolerance``, else a new one (DataContainer::createSensor,
+        core/src/datacontainer.cpp:170-184)."""
         p = np.zeros(3)
         p[:len(pos)] = pos
         if len(self._sensors):
-            d = np.linalg.norm(self._sensors - p, axis=1)
-            i = int(np.argmin(d))
-            if d[i] < tolerance:
-                return i
+            hit = np.nonzero(np.linalg.norm(self._sensors - p, axis=1) < tolerance)[0]
+            if len(hit):
+                return int(hit[-1])
         self._sensors = np.vstack([self._sensors, p])
         return len(self._sensors) - 1
+
+    def setSensorPosition(self, i, pos):
+        p = np.zeros(3)
+        p[:len(pos)] = pos
+        self._sensors[int(i)] = p
+
+    def translate(self, vec):
+        """Move every sensor by ``vec`` (DataContainer::translate)."""
+        v = np.zeros(3)
+        v[:len(vec)] = vec
+        self._sensors = self._sensors + v
+
+    def scale(self, vec):
+        """Scale every sensor position componentwise (DataContainer::scale)."""
+        v = np.ones(3)
+        v[:len(vec)] = vec
+        self._sensors = self._sensors * v
 
     # -- data -------------------------------------------------------------
     def addFourPointData(self, a, b, m, n):
@@ -142,6 +161,47 @@ class DataContainerERT:
 
     def markInvalid(self, idx):
         self.markValid(idx, False)
+
+    def remove(self, idx):
+        """Drop the data ``idx`` (indices or a boolean mask), as
+        DataContainer::remove (markValid(idx, false) + removeInvalid)."""
+        idx = np.asarray(idx)
+        if idx.dtype == bool:
+            idx = np.nonzero(idx)[0]
+        self.markInvalid(idx)
+        self.removeInvalid()
+
+    def resize(self, n):
+        """n data: new rows get sensor index -1 and field value 0, 'valid' 0
+        (DataContainer::resize, datacontainer.cpp:742-754)."""
+        n = int(n)
+        old = self.size()
+        if n <= old:
+            self._abmn = self._abmn[:n].copy()
+            self._fields = {k: v[:n].copy() for k, v in self._fields.items()}
+            return
+        self._abmn = np.vstack([self._abmn, np.full((n - old, 4), -1, np.int32)])
+        self._fields = {k: np.concatenate([v, np.zeros(n - old)]) for k, v in self._fields.items()}
+
+    def add(self, other, snap=1e-3):
+        """Append ``other``'s data: its sensors merged into this container's
+        (createSensor with tolerance ``snap``), its sensor indices mapped onto
+        them, the fields of this container filled from ``other``
+        (DataContainer::add, core/src/datacontainer.cpp:139-168)."""
+        start = self.size()
+        perm = np.array([self.createSensor(p, snap) for p in other.sensorPositions()], np.int64)
+        ab = other.abmn().astype(np.int64)
+        ok = (ab > -1) & (ab < len(perm))
+        mapped = np.where(ok, perm[np.where(ok, ab, 0)], -1).astype(np.int32)
+        mine = self._field_map()
+        theirs = other._field_map()
+        self._abmn = np.vstack([self._abmn, mapped]).reshape(-1, 4)
+        n = self.size()
+        for k, v in mine.items():
+            if k in "abmn":
+                continue
+            add = theirs[k] if k in theirs else np.zeros(n - start)
+            self._fields[k] = np.concatenate([v, add])
 
     def removeInvalid(self):
         """Drop every datum whose 'valid' flag is not 1."""

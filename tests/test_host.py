@@ -103,3 +103,27 @@ def test_estimate_error_forms():
     assert np.allclose(estimateError(d, 0.02, absoluteUError=1e-3), 1e-3 / u + 0.02)
     d.set("u", np.array([2.0, 4.0]))
     assert np.allclose(estimateError(d, 0.02, absoluteUError=1e-2), [0.025, 0.0225])
+
+
+def test_data_container_editing():
+    """remove / resize / add / translate / scale of DataContainerERT
+    (core/src/datacontainer.cpp:139-168, 742-767, 930-940)."""
+    import numpy as np
+    from pygimli_gb300.data import createData
+    d = createData(np.arange(6.0), "dd")
+    n = d.size()
+    d.set("rhoa", np.arange(n, dtype=float) + 1.0)
+    d.remove(d["rhoa"] > n - 2)
+    assert d.size() == n - 2 and d["rhoa"].max() == n - 2
+    e = createData(np.arange(2.0, 8.0), "dd")         # shares sensors x = 2..5
+    e.set("rhoa", np.full(e.size(), 7.0))
+    m = d.size()
+    d.add(e)
+    assert d.sensorCount() == 8 and d.size() == m + e.size()
+    assert np.allclose(d.sensorPositions()[d.abmn()[m:, 0], 0], e.sensorPositions()[e.abmn()[:, 0], 0])
+    assert np.all(d["rhoa"][m:] == 7.0)
+    d.resize(d.size() + 2)
+    assert np.all(d.abmn()[-2:] == -1) and np.all(d["rhoa"][-2:] == 0.0)
+    d.translate([1.0, 0.0])
+    d.scale([2.0, 1.0, 1.0])
+    assert np.isclose(d.sensorPosition(0)[0], 2.0)
