@@ -144,9 +144,10 @@ class RegionManager:
 
     def paraDomain(self):
         """Mesh of the cells of non-background regions (Mesh::createMeshByCells,
-        core/src/mesh.cpp:2008-2046: ascending cell ids, nodes renumbered in
-        order of first use), with the parameter indices as cell markers;
-        boundaries are not copied."""
+        core/src/mesh.cpp:2008-2088: ascending cell ids, nodes renumbered in
+        order of first use, the boundaries with a nonzero marker that lie on a
+        kept cell, the cell data of the kept cells), with the parameter
+        indices as cell markers."""
         mesh = self._mesh
         keep = np.sort(np.concatenate([r.cells for r in self._regions.values() if not r.isBackground()]
                                       or [np.zeros(0, np.int64)]))
@@ -155,5 +156,16 @@ class RegionManager:
         order = used[np.argsort(first, kind="stable")]
         remap = np.full(mesh.nodeCount(), -1, np.int64)
         remap[order] = np.arange(len(order))
-        return Mesh(mesh.dim(), mesh.nodes[order], remap[cells].astype(np.int32), self._markers[keep].astype(np.int32),
-                    mesh.node_markers[order], check=False)
+        from .mesh import find_boundary_cells
+        new_cells = remap[cells].astype(np.int32)
+        b = mesh.boundaries[:, :mesh.dim()].astype(np.int64)
+        sel = np.nonzero((mesh.boundary_markers != 0) & np.all(remap[b] >= 0, axis=1))[0]
+        nb = remap[b[sel]].astype(np.int32)
+        owner = find_boundary_cells(new_cells, nb, len(order))
+        keep_b = owner >= 0
+        pd = Mesh(mesh.dim(), mesh.nodes[order], new_cells, self._markers[keep].astype(np.int32),
+                  mesh.node_markers[order], nb[keep_b], mesh.boundary_markers[sel][keep_b], owner[keep_b],
+                  check=False)
+        C = mesh.cellCount()
+        pd._data = {k: v[keep].copy() for k, v in getattr(mesh, "_data", {}).items() if len(v) == C}
+        return pd

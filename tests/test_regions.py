@@ -80,3 +80,20 @@ def test_mapping_with_background_and_fixed_region():
     pd = rm.paraDomain()
     assert pd.cellCount() == int((mk >= 0).sum())
     assert np.array_equal(np.unique(pd.cell_markers), np.arange(rm.parameterCount()))
+
+
+def test_para_domain_boundaries_and_data():
+    """The para domain keeps the marked boundaries that lie on kept cells
+    and the cell data of the kept cells (createMeshByCells)."""
+    m = region_mesh(2)
+    m["res"] = np.arange(m.cellCount(), dtype=float)
+    rm = RegionManager()
+    rm.setMesh(m)
+    rm.setDefaultBackground()
+    pd = rm.paraDomain()
+    keep = np.nonzero(m.cell_markers != 1)[0]
+    assert np.array_equal(pd["res"], keep.astype(float))
+    assert pd.boundaryCount() > 0 and np.all(pd.boundary_markers != 0) and np.all(pd.boundary_cells >= 0)
+    # every kept boundary is a face of its cell
+    for bnd, c in zip(pd.boundaries, pd.boundary_cells):
+        assert set(bnd.tolist()) <= set(pd.cells[c].tolist())
