@@ -337,22 +337,26 @@ __global__ void kb_finish_init(ColView v, const double *__restrict__ pa, const d
     if (a) atomicAdd(nactive, 1);
 }
 
-__global__ void kb_finish_alpha(ColView v, const double *__restrict__ part, double *__restrict__ col,
-                                const int32_t *__restrict__ active) {
-    __shared__ double red[32][33];
-    const int64_t g = (int64_t)blockIdx.x * 32 + threadIdx.x;
-    const double pq = bcol_sum(v, part, g, red);
-    if (threadIdx.y != 0 || !active[g]) return;
+// the per-iteration finishes one warp per column (warp_col_sum over the
+// column's problem's partial rows)
+__global__ void kb_finish_alpha_w(ColView v, const double *__restrict__ part, double *__restrict__ col,
+                                  const int32_t *__restrict__ active) {
+    const int64_t g = (int64_t)blockIdx.x * kFinWarps + (threadIdx.x >> 5);
+    if (g >= v.T) return;
+    const BProb &pr = v.P[v.cprob[g]];
+    const double pq = warp_col_sum(part + pr.poff, pr.NB, pr.Rpad, g - pr.col0);
+    if ((threadIdx.x & 31) != 0 || !active[g]) return;
     col[PQ * v.T + g] = pq;
     col[ALPHA * v.T + g] = (pq != 0.0) ? col[RHO * v.T + g] / pq : 0.0;
 }
 
-__global__ void kb_finish_beta(ColView v, const double *__restrict__ pa, double *__restrict__ col,
-                               const int32_t *__restrict__ active, int32_t *__restrict__ iters) {
-    __shared__ double red[32][33];
-    const int64_t g = (int64_t)blockIdx.x * 32 + threadIdx.x;
-    const double rz = bcol_sum(v, pa, g, red);
-    if (threadIdx.y != 0) return;
+__global__ void kb_finish_beta_w(ColView v, const double *__restrict__ pa, double *__restrict__ col,
+                                 const int32_t *__restrict__ active, int32_t *__restrict__ iters) {
+    const int64_t g = (int64_t)blockIdx.x * kFinWarps + (threadIdx.x >> 5);
+    if (g >= v.T) return;
+    const BProb &pr = v.P[v.cprob[g]];
+    const double rz = warp_col_sum(pa + pr.poff, pr.NB, pr.Rpad, g - pr.col0);
+    if ((threadIdx.x & 31) != 0) return;
     if (!active[g]) {
         col[BETA * v.T + g] = 0.0;
         return;
@@ -624,6 +628,7 @@ int batch_solve(std::vector<Context *> &cs, cudaStream_t s, ertgb_batch_info *tu
     const int nv = (int)pl.vtiles.size();
     const int gv = grid_for(nv, 16, cs[0]->device), gs = grid_for((int)pl.stiles.size(), 8, cs[0]->device);
     const dim3 vb(32, kVecRows), fb(32, 32), fg((unsigned)(T / 32));
+    const unsigned fwg = (unsigned)ceil_div(T, kFinWarps);
     const Tile *vt = pl.d_vtiles.p;
     const BProb *pp = pl.d_probs.p;
     const int RB = sh.RB;
@@ -652,9 +657,9 @@ int batch_solve(std::vector<Context *> &cs, cudaStream_t s, ertgb_batch_info *tu
         ERTGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         for (int it = 0; it < kGraphIters; it++) {
             launch_spmm(pl, sh.W, gs, s, part_c.p);
-            kb_finish_alpha<<<fg, fb, 0, s>>>(cv, part_c.p, col.p, active);
+            kb_finish_alpha_w<<<fwg, 32 * kFinWarps, 0, s>>>(cv, part_c.p, col.p, active);
             kb_update_xr<<<gv, vb, 0, s>>>(nv, vt, pp, RB, T, col.p, active, part_a.p, part_b.p);
-            kb_finish_beta<<<fg, fb, 0, s>>>(cv, part_a.p, col.p, active, iters);
+            kb_finish_beta_w<<<fwg, 32 * kFinWarps, 0, s>>>(cv, part_a.p, col.p, active, iters);
             kb_update_p<<<gv, vb, 0, s>>>(nv, vt, pp, RB, T, col.p, active);
         }
         ERTGB_CUDA(cudaStreamEndCapture(s, &g_it));
