@@ -116,6 +116,13 @@ class Clocks:
                                       stdout=self.f, stderr=subprocess.DEVNULL)
         except (FileNotFoundError, OSError):
             self.p = None
+        # let nvidia-smi finish its start-up (first sample written) before the
+        # timed region begins, so that its initialisation does not overlap it
+        t_end = time.perf_counter() + 3.0
+        while self.p is not None and self.p.poll() is None and time.perf_counter() < t_end:
+            if os.path.getsize(self.f.name) > 0:
+                break
+            time.sleep(0.02)
 
     def stop(self):
         if self.p is None:
@@ -302,16 +309,18 @@ def run_ours(args, world, rank, local):
         dist.barrier()
     clocks = Clocks(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0])
                     if os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].isdigit() else local)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
+    # one event between consecutive steps: recording adds no synchronisation,
+    # and the per-step durations show whether a single step is an outlier
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     torch.cuda.synchronize()
-    e0.record()
-    for _ in range(args.steps):
+    ev[0].record()
+    for i in range(args.steps):
         step()
-    e1.record()
+        ev[i + 1].record()
     torch.cuda.synchronize()
     clk = clocks.stop()
-    total_ms = e0.elapsed_time(e1)
+    total_ms = ev[0].elapsed_time(ev[-1])
+    step_ms = [round(ev[i].elapsed_time(ev[i + 1]), 2) for i in range(args.steps)]
     st = fop.stats()
     launches = int(st["launches_response"] + st["launches_jacobian"]) * args.steps
     total_ms = max_over_ranks(total_ms, world, dev)
@@ -491,7 +500,7 @@ def run_ours(args, world, rank, local):
                "plain_fp64_gpu_pcg": plain, "fsai_form": fsai_form, "gn_iteration": gn,
                "refine_h2": refine_rec, "complex_form": cx_form,
                "learned_weights": os.path.relpath(weights, ROOT) if weights else None,
-               "clocks": clk,
+               "clocks": clk, "step_ms": step_ms,
                "breakdown_ms": {"assemble": st["ms_assemble"], "rhs": st["ms_rhs"], "solve": st["ms_solve"],
                                 "collect": st["ms_collect"], "jacobian": st["ms_jacobian"],
                                 "pcg_iterations": st["iterations"], "n_rhs": st["n_rhs"],
