@@ -113,6 +113,40 @@ int ertgb_set_mesh(ertgb_ctx *ctx, int dim, int order, int n_nodes, const double
 int ertgb_set_electrodes(ertgb_ctx *ctx, int n_elec, const int32_t *elec_node_host,
                          double surface_z);
 
+/* Formulation of the forward operator.  SINGULARITY_REMOVAL (default):
+ * DCSRMultiElectrodeModelling, pyGIMLi ERTModelling(sr=True)
+ * (core/src/bert/dcfemmodelling.cpp:2152-2296).  TOTAL_POTENTIAL:
+ * DCMultiElectrodeModelling, ERTModelling(sr=False) (ertModelling.py:102-106):
+ * total potentials of unit point currents (calculateK_,
+ * dcfemmodelling.cpp:1756-1929), no primary field; the only formulation that
+ * takes a matrix extension (complete electrode model, bypass resistors).
+ * With TOTAL_POTENTIAL an electrode node may be -1 (an electrode given by
+ * its extension row only).  Setting the formulation drops an extension. */
+typedef enum {
+    ERTGB_FORMULATION_SINGULARITY_REMOVAL = 0,
+    ERTGB_FORMULATION_TOTAL_POTENTIAL = 1
+} ertgb_formulation;
+int ertgb_set_formulation(ertgb_ctx *ctx, int formulation);
+
+/* Constant extension of the total-potential system matrix: the complete
+ * electrode model (assembleCompleteElectrodeModel_, dcfemmodelling.cpp:
+ * 315-414, called at :1786-1831) and bypass resistors
+ * (assembleStiffnessMatrixDCFEMByPass_, :601-709).  n_ext rows / columns
+ * follow the mesh nodes (one per electrode, then per passive body).  The
+ * n_entries (row, col, value) entries are added, in the order given, to the
+ * assembled matrix of every wavenumber after the domain and boundary terms
+ * (rows / columns < n_nodes + n_ext).  src_row[e] (n_elec values): the row
+ * of electrode e's unit current and of its potential (its node without CEM,
+ * n_nodes + e with CEM: electrode.cpp:133-150, 341-355).  src_center: the
+ * mean electrode position of the mixed boundary condition (sourceCenterPos_,
+ * :1026-1030; may be NULL).  collect_last_k != 0: the electrode potentials
+ * are those of the last wavenumber, unweighted, as the reference's
+ * potentialsCEM_ (overwritten per wavenumber, :1829, 1912; collected at
+ * :1642-1644).  Call after ertgb_set_electrodes; needs TOTAL_POTENTIAL. */
+int ertgb_set_extension(ertgb_ctx *ctx, int n_ext, int64_t n_entries, const int32_t *rows_host,
+                        const int32_t *cols_host, const double *vals_host, const int32_t *src_row_host,
+                        const double *src_center_host, int collect_last_k);
+
 /* Wavenumbers and weights: DCMultiElectrodeModelling::setkValues/setWeights
  * (core/src/bert/dcfemmodelling.h:239-243). */
 int ertgb_set_kw(ertgb_ctx *ctx, int n_k, const double *k_host, const double *w_host);
@@ -150,7 +184,9 @@ int ertgb_jacobian(ertgb_ctx *ctx, const double *model_dev, int n_model, void *J
 int ertgb_jacobian_host(ertgb_ctx *ctx, const double *model_host, int n_model, void *J_host,
                         int dtype);
 
-/* Sizes after set_mesh/set_electrodes/set_kw/set_scheme. */
+/* Sizes after set_mesh/set_electrodes/set_kw/set_scheme.  n_nodes: rows of
+ * the system matrix (mesh nodes plus the rows of ertgb_set_extension); the
+ * potentials of ertgb_get_potentials have that many entries per column. */
 int ertgb_sizes(const ertgb_ctx *ctx, int64_t *n_nodes, int64_t *nnz, int64_t *n_param,
                 int64_t *n_rhs);
 

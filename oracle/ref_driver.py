@@ -48,6 +48,8 @@ def lib():
         L.ref_create.argtypes = [ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int, vp, vp,
                                  ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, vp, ctypes.c_int, vp,
                                  vp, ctypes.c_int, ctypes.c_int]
+        L.ref_create_ex.restype = vp
+        L.ref_create_ex.argtypes = L.ref_create.argtypes + [ctypes.c_int, ctypes.c_int, vp]
         L.ref_mesh_sizes.argtypes = [vp, vp, vp, vp, vp, vp]
         L.ref_mesh_arrays.argtypes = [vp, vp, vp, vp, vp, vp, vp]
         L.ref_destroy.argtypes = [vp]
@@ -109,9 +111,12 @@ def _check(rc):
 
 
 class RefModelling:
-    """The reference's DCSRMultiElectrodeModelling on a given mesh/scheme."""
+    """The reference's DCSRMultiElectrodeModelling (sr=True) or
+    DCMultiElectrodeModelling (sr=False: total potential, complete electrode
+    model, bypass electrodes) on a given mesh/scheme."""
 
-    def __init__(self, mesh, sensors, abmn, kfac=None, threads=1, keep_matrices=False, p2=False, h2=False):
+    def __init__(self, mesh, sensors, abmn, kfac=None, threads=1, keep_matrices=False, p2=False, h2=False,
+                 sr=True, contact_impedance=None):
         L = lib()
         self.mesh = mesh
         self._keep = [np.ascontiguousarray(mesh.nodes, np.float64),
@@ -127,9 +132,12 @@ class RefModelling:
         nodes, nm, cells, cm, bnd, bm, sens, ab = self._keep[:8]
         self.nData = len(ab)
         self.nE = len(sens)
-        h = L.ref_create(mesh.dim(), len(nodes), _p(nodes), _p(nm), len(cells), cells.shape[1], _p(cells),
-                         _p(cm), len(bnd), bnd.shape[1], _p(bnd), _p(bm), len(sens), _p(sens), len(ab),
-                         _p(ab), None if kf is None else _p(kf), 0, 2 if h2 else int(bool(p2)))
+        z = None if contact_impedance is None else np.ascontiguousarray(contact_impedance, np.float64)
+        self._keep.append(z)
+        h = L.ref_create_ex(mesh.dim(), len(nodes), _p(nodes), _p(nm), len(cells), cells.shape[1], _p(cells),
+                            _p(cm), len(bnd), bnd.shape[1], _p(bnd), _p(bm), len(sens), _p(sens), len(ab),
+                            _p(ab), None if kf is None else _p(kf), 0, 2 if h2 else int(bool(p2)), int(bool(sr)),
+                            0 if z is None else len(z), None if z is None else _p(z))
         if not h:
             raise RuntimeError("ref_create failed: " + L.ref_last_error().decode())
         self.h = h

@@ -9,7 +9,9 @@
 //                          createTetrahedron/createEdge/createTriangleFace),
 //                          mesh.h:457 createNeighborInfos
 //   data container         core/src/bert/bertDataContainer.h:62 addFourPointData
-//   forward operator       core/src/bert/dcfemmodelling.h:344 DCSRMultiElectrodeModelling
+//   forward operator       core/src/bert/dcfemmodelling.h:344 DCSRMultiElectrodeModelling,
+//                          dcfemmodelling.h:105 DCMultiElectrodeModelling (total potential,
+//                          complete electrode model, bypass electrodes)
 //   response / Jacobian    core/src/bert/dcfemmodelling.cpp:1085-1197, 1446-1476
 //   mesh / data I/O        core/src/mesh_io.cpp:391-662 (binary mesh v3),
 //                          mesh_io.cpp:674-992 exportVTK,
@@ -99,22 +101,26 @@ private:
     int n_ = 0;
 };
 
-// The reference operator plus one helper: drop the caller-owned real
-// sub-potential matrix so that the complex path allocates its own.
-struct ShimFop : DCSRMultiElectrodeModelling {
-    explicit ShimFop(bool verbose) : DCSRMultiElectrodeModelling(verbose) {}
+// The reference operator (singularity removal: DCSRMultiElectrodeModelling;
+// total potential: DCMultiElectrodeModelling) plus one helper: drop the
+// caller-owned real sub-potential matrix so that the complex path allocates
+// its own.
+template <class Base> struct ShimFop : Base {
+    explicit ShimFop(bool verbose) : Base(verbose) {}
     void detachSubpotentials() {
-        if (!subpotOwner_) {
-            subSolutions_ = nullptr;
-            subpotOwner_ = true;
+        if (!this->subpotOwner_) {
+            this->subSolutions_ = nullptr;
+            this->subpotOwner_ = true;
         }
     }
+    static void detach(DCMultiElectrodeModelling *f) { static_cast<ShimFop *>(f)->detachSubpotentials(); }
 };
 
 struct RefHandle {
     Mesh mesh;
     DataContainerERT data;
-    ShimFop *fop = nullptr;
+    DCMultiElectrodeModelling *fop = nullptr;
+    void (*detach)(DCMultiElectrodeModelling *) = nullptr;
     CallbackSolver *solver = nullptr;
     RMatrix subpots;          // collected sub-potentials (nE*nK x nNodes)
     RefHandle(int dim) : mesh(dim) {}
@@ -140,14 +146,18 @@ extern "C" {
 
 const char *ref_last_error() { return g_last_error.c_str(); }
 
-// Build mesh + data container + SR forward operator.
+// Build mesh + data container + forward operator: sr = 1 the singularity-
+// removal operator (DCSRMultiElectrodeModelling), sr = 0 the total-potential
+// operator (DCMultiElectrodeModelling, which alone builds the complete
+// electrode model and bypass resistors, dcfemmodelling.cpp:1786-1833).
 // cellNodes: nCells*nv (nv=3 triangle, 4 tetrahedron), bndNodes: nBnd*nvb.
 // abmn: nData*4 with -1 for an electrode at infinity.  kfac may be NULL.
-void *ref_create(int dim, int nNodes, const double *xyz, const int *nodeMarker,
-                 int nCells, int nv, const int *cellNodes, const int *cellMarker,
-                 int nBnd, int nvb, const int *bndNodes, const int *bndMarker,
-                 int nSensors, const double *sensorXyz, int nData, const int *abmn,
-                 const double *kfac, int verbose, int p2) {
+// contactZ (nZ values, may be NULL): setContactImpedances (dcfemmodelling.cpp:786-788).
+void *ref_create_ex(int dim, int nNodes, const double *xyz, const int *nodeMarker,
+                    int nCells, int nv, const int *cellNodes, const int *cellMarker,
+                    int nBnd, int nvb, const int *bndNodes, const int *bndMarker,
+                    int nSensors, const double *sensorXyz, int nData, const int *abmn,
+                    const double *kfac, int verbose, int p2, int sr, int nZ, const double *contactZ) {
     RefHandle *h = nullptr;
     int rc = guarded([&] {
         h = new RefHandle(dim);
@@ -181,7 +191,18 @@ void *ref_create(int dim, int nNodes, const double *xyz, const int *nodeMarker,
             for (int d = 0; d < nData; d++) k[d] = kfac[d];
             h->data.set("k", k);
         }
-        h->fop = new ShimFop(verbose != 0);
+        if (sr) {
+            h->fop = new ShimFop<DCSRMultiElectrodeModelling>(verbose != 0);
+            h->detach = &ShimFop<DCSRMultiElectrodeModelling>::detach;
+        } else {
+            h->fop = new ShimFop<DCMultiElectrodeModelling>(verbose != 0);
+            h->detach = &ShimFop<DCMultiElectrodeModelling>::detach;
+        }
+        if (contactZ && nZ > 0) {
+            RVector z(nZ);
+            for (int i = 0; i < nZ; i++) z[i] = contactZ[i];
+            h->fop->setContactImpedances(z);
+        }
         h->fop->setData(h->data);
         h->fop->setMesh(h->mesh, true);
         h->fop->collectSubPotentials(h->subpots);
@@ -189,6 +210,16 @@ void *ref_create(int dim, int nNodes, const double *xyz, const int *nodeMarker,
     });
     if (rc) { delete h; return nullptr; }
     return h;
+}
+
+// The singularity-removal operator (the original entry point).
+void *ref_create(int dim, int nNodes, const double *xyz, const int *nodeMarker,
+                 int nCells, int nv, const int *cellNodes, const int *cellMarker,
+                 int nBnd, int nvb, const int *bndNodes, const int *bndMarker,
+                 int nSensors, const double *sensorXyz, int nData, const int *abmn,
+                 const double *kfac, int verbose, int p2) {
+    return ref_create_ex(dim, nNodes, xyz, nodeMarker, nCells, nv, cellNodes, cellMarker, nBnd, nvb, bndNodes,
+                         bndMarker, nSensors, sensorXyz, nData, abmn, kfac, verbose, p2, 1, 0, nullptr);
 }
 
 void ref_destroy(void *hp) { delete (RefHandle *)hp; }
@@ -252,7 +283,7 @@ int ref_set_complex_solver(void *hp, ref_cfactor_fn f, ref_csolve_fn s) {
 int ref_response_complex(void *hp, const double *model, int nModel2, double *out) {
     RefHandle *h = (RefHandle *)hp;
     return guarded([&] {
-        h->fop->detachSubpotentials();
+        h->detach(h->fop);
         h->fop->setComplex(true);
         RVector m(nModel2);
         for (int i = 0; i < nModel2; i++) m[i] = model[i];
@@ -267,7 +298,7 @@ int ref_jacobian_complex(void *hp, const double *model, int nModel2, double *J_r
                          int *cols) {
     RefHandle *h = (RefHandle *)hp;
     return guarded([&] {
-        h->fop->detachSubpotentials();
+        h->detach(h->fop);
         h->fop->setComplex(true);
         RVector m(nModel2);
         for (int i = 0; i < nModel2; i++) m[i] = model[i];

@@ -55,6 +55,8 @@ SIGNATURES = {
     "ertgb_set_scheme": (_ci, [_vp, _ci, _vp, _vp]),
     "ertgb_set_solver": (_ci, [_vp, _d, _ci, _ci]),
     "ertgb_set_precision": (_ci, [_vp, _ci]),
+    "ertgb_set_formulation": (_ci, [_vp, _ci]),
+    "ertgb_set_extension": (_ci, [_vp, _ci, ctypes.c_int64, _vp, _vp, _vp, _vp, _vp, _ci]),
     "ertgb_response": (_ci, [_vp, _vp, _vp, _vp]),
     "ertgb_response_host": (_ci, [_vp, _vp, _vp]),
     "ertgb_jacobian": (_ci, [_vp, _vp, _ci, _vp, _ci, _vp]),

@@ -441,6 +441,7 @@ __global__ void k_assemble(int64_t nnz, const int32_t *__restrict__ cptr, const 
                            const double *__restrict__ bmass, const double *__restrict__ alpha,
                            const int32_t *__restrict__ bcell, const double *__restrict__ rho,
                            const double *__restrict__ kv, int nv2, int nvb2, int64_t C, int64_t B,
+                           const int32_t *__restrict__ xptr, const double *__restrict__ xval,
                            double *__restrict__ vals) {
     const int ki = blockIdx.y;
     const double k = kv[ki];
@@ -465,6 +466,10 @@ __global__ void k_assemble(int64_t nnz, const int32_t *__restrict__ cptr, const 
                 const double r = rho ? rho[bcell[b]] : 1.0;
                 acc += (alpha[(int64_t)ki * B + b] / r) * bmass[eb];
             }
+        }
+        if (xptr) {  // constant extension (CEM, bypass), in the order given
+            const int32_t x1 = xptr[s + 1];
+            for (int32_t q = xptr[s]; q < x1; q++) acc += xval[q];
         }
         vals[(int64_t)ki * nnz + s] = acc;
     }
@@ -580,18 +585,36 @@ __global__ void k_finish_pot(int64_t n, int nE, int64_t R, int64_t Rpad, const d
 
 // U[e][f] = sum_k w_k u_k[e](node of electrode f), summed like the
 // reference's k loop (first term a product, then accumulate).
+// last_k: the last wavenumber's potential, unweighted (the complete
+// electrode model's collect, core/src/bert/dcfemmodelling.cpp:1829, 1912).
 __global__ void k_collect(int nE, int nK, int64_t Rpad, const int32_t *__restrict__ enode,
                           const double *__restrict__ w, const double *__restrict__ x,
-                          double *__restrict__ U) {
+                          double *__restrict__ U, int last_k) {
     const int64_t total = (int64_t)nE * nE;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
          t += (int64_t)gridDim.x * blockDim.x) {
         const int e = (int)(t / nE), f = (int)(t % nE);
         const double *row = x + (int64_t)enode[f] * Rpad;
+        if (last_k) {
+            U[t] = row[(int64_t)(nK - 1) * nE + e];
+            continue;
+        }
         double acc = row[e] * w[0];
         for (int ki = 1; ki < nK; ki++) acc += row[(int64_t)ki * nE + e] * w[ki];
         U[t] = acc;
     }
+}
+
+// Total potential: column t = k * nE + e carries a unit current on the
+// source row of electrode e (ElectrodeShapeNode / ElectrodeShapeDomain::
+// assembleRHS, core/src/bert/electrode.cpp:133-150, 341-355); b is zeroed
+// before.
+__global__ void k_rhs_total(int nE, int64_t R, int64_t Rpad, const int32_t *__restrict__ src_row,
+                            double *__restrict__ b) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= R) return;
+    const int e = (int)(t % nE);
+    b[(int64_t)src_row[e] * Rpad + t] = 1.0;
 }
 
 __device__ inline double abmn_u(const double *U, int nE, int a, int b, int m, int n) {
@@ -633,6 +656,18 @@ void build_mesh_device(Context &c) {
     m.d_cptr.upload(cptr, s);
     m.d_centry.upload(centry, s);
     m.d_diag.upload(diag, s);
+    {
+        std::vector<int32_t> xptr;
+        std::vector<double> xval;
+        build_extension_map(m, xptr, xval);
+        if (xval.empty()) {
+            m.d_ext_ptr.release();
+            m.d_ext_val.release();
+        } else {
+            m.d_ext_ptr.upload(xptr, s);
+            m.d_ext_val.upload(xval, s);
+        }
+    }
     build_lower_pattern(m);
     m.d_Lrowptr.upload(m.Lrowptr, s);
     m.d_Lcolidx.upload(m.Lcolidx, s);
@@ -688,7 +723,7 @@ void assemble_all(Context &c, const double *rho_cell, double *vals, cudaStream_t
     dim3 grid(grid1(m.nnz, kThreads, 1 << 16), c.nK);
     k_assemble<<<grid, kThreads, 0, s>>>(m.nnz, m.d_cptr.p, m.d_centry.p, m.d_K.p, m.d_M.p, m.d_bnd_mass.p,
                                          c.d_alpha.p, m.d_bnd_cell.p, rho_cell, c.d_k.p, m.nv * m.nv,
-                                         m.nvb * m.nvb, m.C, m.B, vals);
+                                         m.nvb * m.nvb, m.C, m.B, m.d_ext_ptr.p, m.d_ext_val.p, vals);
     ERTGB_CUDA(cudaGetLastError());
     if (rho_cell) {
         c.d_dinv.alloc((size_t)m.n * c.nK);
@@ -730,6 +765,14 @@ void build_rhs(Context &c, cudaStream_t s) {
     ERTGB_CUDA(cudaGetLastError());
 }
 
+void build_rhs_total(Context &c, cudaStream_t s) {
+    MeshData &m = c.mesh;
+    ERTGB_CUDA(cudaMemsetAsync(c.d_r.p, 0, sizeof(double) * (size_t)m.n * c.Rpad, s));
+    k_rhs_total<<<(unsigned)ceil_div(c.R, kThreads), kThreads, 0, s>>>(c.nE, c.R, c.Rpad, c.d_src_row.p, c.d_r.p);
+    ERTGB_CUDA(cudaGetLastError());
+    c.d_pnorm2.release();  // no primary field: the reference norm is ||b||
+}
+
 void compute_rhs_scale(Context &c, cudaStream_t s) {
     MeshData &m = c.mesh;
     const int NB = (int)std::min<int64_t>(ceil_div(m.n, 8), 256);
@@ -752,8 +795,10 @@ void finish_potentials(Context &c, cudaStream_t s) {
 
 void collect_response(Context &c, double *rhoa, cudaStream_t s) {
     c.d_U.alloc((size_t)c.nE * c.nE);
-    k_collect<<<grid1((int64_t)c.nE * c.nE), kThreads, 0, s>>>(c.nE, c.nK, c.Rpad, c.d_enode.p, c.d_w.p, c.d_x.p,
-                                                               c.d_U.p);
+    const bool total = c.formulation == ERTGB_FORMULATION_TOTAL_POTENTIAL;
+    k_collect<<<grid1((int64_t)c.nE * c.nE), kThreads, 0, s>>>(c.nE, c.nK, c.Rpad,
+                                                               total ? c.d_src_row.p : c.d_enode.p, c.d_w.p,
+                                                               c.d_x.p, c.d_U.p, total && c.collect_last_k ? 1 : 0);
     ERTGB_CUDA(cudaGetLastError());
     k_response<<<grid1(c.D), kThreads, 0, s>>>(c.D, c.nE, c.d_abmn.p, c.d_kfac.p, c.d_U.p, rhoa);
     ERTGB_CUDA(cudaGetLastError());
@@ -767,7 +812,7 @@ void profile_assemble(Context &c, int reps, double *ms, double *bytes, double *f
     auto go = [&] {
         k_assemble<<<grid, kThreads, 0, s>>>(m.nnz, m.d_cptr.p, m.d_centry.p, m.d_K.p, m.d_M.p, m.d_bnd_mass.p,
                                              c.d_alpha.p, m.d_bnd_cell.p, c.d_rho_last, c.d_k.p, m.nv * m.nv,
-                                             m.nvb * m.nvb, m.C, m.B, c.d_S.p);
+                                             m.nvb * m.nvb, m.C, m.B, m.d_ext_ptr.p, m.d_ext_val.p, c.d_S.p);
     };
     go();
     ERTGB_CUDA(cudaEventRecord(c.ev[0], s));

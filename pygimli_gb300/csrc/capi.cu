@@ -94,11 +94,22 @@ void ensure_derived(Context &c) {
     if (!c.have_kw) throw Error(ERTGB_STATE, "no wavenumbers set");
     if (!c.have_scheme) throw Error(ERTGB_STATE, "no measurement scheme set");
     ERTGB_CUDA(cudaSetDevice(c.device));
+    const bool total = c.formulation == ERTGB_FORMULATION_TOTAL_POTENTIAL;
+    if (total) {
+        if ((int)c.src_row.size() != c.nE) throw Error(ERTGB_STATE, "electrode source rows do not match the electrodes");
+        for (int32_t r : c.src_row)
+            if (r < 0 || r >= c.mesh.n)
+                throw Error(ERTGB_STATE, "an electrode has no source row (set the matrix extension after the electrodes)");
+    } else {
+        for (int32_t v : c.enode)
+            if (v < 0) throw Error(ERTGB_STATE, "singularity removal needs a node for every electrode");
+    }
     if (!c.prim_ready) {
         c.R = (int64_t)c.nE * c.nK;
         c.Rpad = ceil_div(c.R, c.rhs_align) * c.rhs_align;
         compute_boundary_alpha(c);
-        compute_primary(c);
+        if (total) c.d_up.release();  // no primary field
+        else compute_primary(c);
         c.prim_ready = true;
         c.s1_ready = false;
         c.jac_ready = false;
@@ -108,7 +119,8 @@ void ensure_derived(Context &c) {
         c.jac_ready = true;
     }
     if (!c.s1_ready) {
-        assemble_unit(c, c.stream);
+        if (total) c.d_S1.release();  // the unit-resistivity matrix only serves singularity removal
+        else assemble_unit(c, c.stream);
         c.s1_ready = true;
     }
 }
@@ -131,20 +143,27 @@ int do_response(Context &c, const double *rho, double *rhoa, void *stream) {
     c.d_rho_last = rho;
     MeshData &m = c.mesh;
     ERTGB_CUDA(cudaEventRecord(c.ev[0], s));
-    c.d_S.alloc((size_t)c.nK * m.nnz);
-    assemble_all(c, rho, c.d_S.p, s);
-    compute_source_rho(c, rho, s);
-    ERTGB_CUDA(cudaEventRecord(c.ev[1], s));
-    c.d_r.alloc((size_t)m.n * c.Rpad);
-    build_rhs(c, s);
-    compute_rhs_scale(c, s);
-    ERTGB_CUDA(cudaEventRecord(c.ev[2], s));
-    c.have_S = true;
+    const bool total = c.formulation == ERTGB_FORMULATION_TOTAL_POTENTIAL;
     if (c.precision != ERTGB_PRECISION_MIXED && c.precond != ERTGB_PRECOND_JACOBI)
         throw Error(ERTGB_BAD_INPUT, "the FSAI and learned preconditioners need mixed precision");
+    if (c.precond == ERTGB_PRECOND_LEARNED && !m.ext_rows.empty())
+        throw Error(ERTGB_BAD_INPUT, "the learned preconditioner does not cover a matrix extension (CEM, bypass)");
+    c.d_S.alloc((size_t)c.nK * m.nnz);
+    assemble_all(c, rho, c.d_S.p, s);
+    if (!total) compute_source_rho(c, rho, s);
+    ERTGB_CUDA(cudaEventRecord(c.ev[1], s));
+    c.d_r.alloc((size_t)m.n * c.Rpad);
+    if (total) {
+        build_rhs_total(c, s);
+    } else {
+        build_rhs(c, s);
+        compute_rhs_scale(c, s);
+    }
+    ERTGB_CUDA(cudaEventRecord(c.ev[2], s));
+    c.have_S = true;
     status = (c.precision == ERTGB_PRECISION_MIXED) ? pcg_solve_mixed(c, s) : pcg_solve(c, s);
     ERTGB_CUDA(cudaEventRecord(c.ev[3], s));
-    finish_potentials(c, s);
+    if (!total) finish_potentials(c, s);
     collect_response(c, rhoa, s);
     ERTGB_CUDA(cudaEventRecord(c.ev[4], s));
     ERTGB_CUDA(cudaEventSynchronize(c.ev[4]));
@@ -153,12 +172,27 @@ int do_response(Context &c, const double *rho, double *rhoa, void *stream) {
     c.stats.ms_solve = elapsed(c, 2, 3);
     c.stats.ms_collect = elapsed(c, 3, 4);
     // check_rho, assemble, dinv, source_rho, rhs, finish_pot, collect, response
-    c.stats.launches_response += 8;
+    // (total potential: check_rho, assemble, dinv, rhs, collect, response)
+    c.stats.launches_response += total ? 6 : 8;
     c.have_pot = true;
     j.done();
     return status;
 }
 
+// Replace the matrix extension (rows / cols / vals after the nodes) and
+// rebuild the pattern and the device structures that derive from it.
+void set_mesh_extension(Context &c, int64_t n_ext, std::vector<int32_t> rows, std::vector<int32_t> cols,
+                        std::vector<double> vals) {
+    MeshData &m = c.mesh;
+    m.n_ext = n_ext;
+    m.n = m.nn + n_ext;
+    m.ext_rows.swap(rows);
+    m.ext_cols.swap(cols);
+    m.ext_vals.swap(vals);
+    build_pattern(m);
+    build_mesh_device(c);
+    c.lp.graph_ready = false;
+}
 void do_jacobian(Context &c, const double *model, int n_model, void *J, int dtype, void *stream) {
     if (!c.have_pot) throw Error(ERTGB_STATE, "createJacobian needs the potentials of a response first");
     if (dtype != 0 && dtype != 1) throw Error(ERTGB_BAD_INPUT, "dtype must be 0 (FP64) or 1 (FP32)");
@@ -234,6 +268,7 @@ int ertgb_set_mesh(ertgb_ctx *ctx, int dim, int order, int n_nodes, const double
         m.nv = order == 1 ? dim + 1 : (dim == 2 ? 6 : 10);
         m.nvb = order == 1 ? dim : (dim == 2 ? 3 : 6);
         m.n = n_nodes;
+        m.nn = n_nodes;
         m.C = n_cells;
         m.xyz.assign(xyz, xyz + (size_t)n_nodes * 3);
         m.cells.assign(cell_nodes, cell_nodes + (size_t)n_cells * m.nv);
@@ -265,6 +300,8 @@ int ertgb_set_mesh(ertgb_ctx *ctx, int dim, int order, int n_nodes, const double
         build_mesh_device(*c);
         c->have_mesh = true;
         c->have_elec = false;
+        c->src_row.clear();
+        c->collect_last_k = false;
         invalidate_derived(*c);
     });
 }
@@ -277,25 +314,28 @@ int ertgb_set_electrodes(ertgb_ctx *ctx, int n_elec, const int32_t *elec_node, d
         MeshData &m = c->mesh;
         c->nE = n_elec;
         c->enode.assign(elec_node, elec_node + n_elec);
+        const bool total = c->formulation == ERTGB_FORMULATION_TOTAL_POTENTIAL;
         std::set<int32_t> uniq;
         for (int32_t v : c->enode) {
-            ERTGB_REQUIRE(v >= 0 && v < m.n, "electrode node index out of range");
+            if (v == -1 && total) continue;  // an electrode given by its extension row
+            ERTGB_REQUIRE(v >= 0 && v < m.nn, "electrode node index out of range");
             ERTGB_REQUIRE(uniq.insert(v).second, "two electrodes on the same node");
         }
         c->surface_z = surface_z;
-        // source centre = mean electrode position
+        // source centre = mean electrode position (an extension may replace it)
         double sc[3] = {0, 0, 0};
-        std::vector<double> epos((size_t)n_elec * 3);
+        std::vector<double> epos((size_t)n_elec * 3, 0.0);
         for (int e = 0; e < n_elec; e++)
             for (int d = 0; d < 3; d++) {
-                epos[3 * e + d] = m.xyz[3 * (size_t)c->enode[e] + d];
+                if (c->enode[e] >= 0) epos[3 * e + d] = m.xyz[3 * (size_t)c->enode[e] + d];
                 sc[d] += epos[3 * e + d];
             }
         for (int d = 0; d < 3; d++) c->src_center[d] = sc[d] / (double)n_elec;
         // incident cells and smallest neighbour distance per electrode node
         std::vector<std::vector<int32_t>> inc(n_elec);
-        std::vector<int> slot(m.n, -1);
-        for (int e = 0; e < n_elec; e++) slot[c->enode[e]] = e;
+        std::vector<int> slot(m.nn, -1);
+        for (int e = 0; e < n_elec; e++)
+            if (c->enode[e] >= 0) slot[c->enode[e]] = e;
         for (int64_t cc = 0; cc < m.C; cc++)
             for (int i = 0; i < m.nv; i++) {
                 const int e = slot[m.cells[cc * m.nv + i]];
@@ -305,6 +345,11 @@ int ertgb_set_electrodes(ertgb_ctx *ctx, int n_elec, const int32_t *elec_node, d
         c->ecell.clear();
         c->emin_r.assign(n_elec, DBL_MAX);
         for (int e = 0; e < n_elec; e++) {
+            if (c->enode[e] < 0) {
+                c->emin_r[e] = 0.0;
+                c->ecell_ptr[e + 1] = (int32_t)c->ecell.size();
+                continue;
+            }
             ERTGB_REQUIRE(!inc[e].empty(), "electrode node belongs to no cell");
             const int32_t nd = c->enode[e];
             for (int32_t cc : inc[e]) {
@@ -328,8 +373,62 @@ int ertgb_set_electrodes(ertgb_ctx *ctx, int n_elec, const int32_t *elec_node, d
         c->d_emin_r.upload(c->emin_r, s);
         c->d_ecell_ptr.upload(c->ecell_ptr, s);
         c->d_ecell.upload(c->ecell, s);
+        // total potential: the current enters on the electrode node unless an
+        // extension gives other rows
+        c->src_row = c->enode;
+        c->collect_last_k = false;
+        c->d_src_row.upload(c->src_row, s);
         ERTGB_CUDA(cudaStreamSynchronize(s));
         c->have_elec = true;
+        invalidate_derived(*c);
+    });
+}
+
+int ertgb_set_formulation(ertgb_ctx *ctx, int formulation) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        ERTGB_REQUIRE(formulation == ERTGB_FORMULATION_SINGULARITY_REMOVAL ||
+                          formulation == ERTGB_FORMULATION_TOTAL_POTENTIAL,
+                      "formulation must be 0 (singularity removal) or 1 (total potential)");
+        ERTGB_CUDA(cudaSetDevice(c->device));
+        if (c->have_mesh && (c->mesh.n_ext > 0 || !c->mesh.ext_rows.empty()))
+            set_mesh_extension(*c, 0, {}, {}, {});
+        c->formulation = formulation;
+        c->src_row = c->enode;
+        c->collect_last_k = false;
+        if (c->have_elec) c->d_src_row.upload(c->src_row, c->stream);
+        invalidate_derived(*c);
+    });
+}
+
+int ertgb_set_extension(ertgb_ctx *ctx, int n_ext, int64_t n_entries, const int32_t *rows, const int32_t *cols,
+                        const double *vals, const int32_t *src_row, const double *src_center, int collect_last_k) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        if (!c->have_mesh || !c->have_elec) throw Error(ERTGB_STATE, "set the mesh and the electrodes before the extension");
+        if (c->formulation != ERTGB_FORMULATION_TOTAL_POTENTIAL)
+            throw Error(ERTGB_STATE, "a matrix extension needs the total-potential formulation");
+        ERTGB_REQUIRE(n_ext >= 0 && n_entries >= 0, "negative extension size");
+        ERTGB_REQUIRE(n_entries == 0 || (rows && cols && vals), "null extension entries");
+        ERTGB_REQUIRE(src_row, "null source rows");
+        const int64_t N = c->mesh.nn + n_ext;
+        ERTGB_REQUIRE(N <= INT32_MAX && n_entries <= INT32_MAX, "extension too large for int32 indices");
+        std::vector<int32_t> r(rows, rows + n_entries), q(cols, cols + n_entries);
+        std::vector<double> v(vals, vals + n_entries);
+        for (int64_t i = 0; i < n_entries; i++) {
+            ERTGB_REQUIRE(r[i] >= 0 && r[i] < N && q[i] >= 0 && q[i] < N, "extension entry out of range");
+            ERTGB_REQUIRE(std::isfinite(v[i]), "extension value not finite");
+        }
+        std::vector<int32_t> sr(src_row, src_row + c->nE);
+        for (int32_t x : sr) ERTGB_REQUIRE(x >= 0 && x < N, "electrode source row out of range");
+        ERTGB_CUDA(cudaSetDevice(c->device));
+        set_mesh_extension(*c, n_ext, std::move(r), std::move(q), std::move(v));
+        c->src_row = sr;
+        c->d_src_row.upload(c->src_row, c->stream);
+        if (src_center)
+            for (int d = 0; d < 3; d++) c->src_center[d] = src_center[d];
+        c->collect_last_k = collect_last_k != 0;
+        ERTGB_CUDA(cudaStreamSynchronize(c->stream));
         invalidate_derived(*c);
     });
 }
@@ -519,6 +618,8 @@ int ertgb_get_primary(ertgb_ctx *ctx, double *prim) {
     Context *c = reinterpret_cast<Context *>(ctx);
     return guard(c, [&] {
         ERTGB_REQUIRE(prim, "null buffer");
+        if (c->formulation == ERTGB_FORMULATION_TOTAL_POTENTIAL)
+            throw Error(ERTGB_STATE, "the total-potential formulation has no primary potentials");
         ensure_derived(*c);
         ERTGB_CUDA(cudaStreamSynchronize(c->stream));
         copy_blocked(*c, c->d_up.p, prim);
@@ -658,6 +759,8 @@ int ertgb_batch_response(ertgb_ctx *const *ctxs, int n, const double *const *rho
             cs[i] = reinterpret_cast<Context *>(ctxs[i]);
             ERTGB_REQUIRE(cs[i] && rho[i] && rhoa[i], "null context or buffer in the batch");
             ERTGB_REQUIRE(cs[i]->device == cs[0]->device, "all problems of a batch must be on one device");
+            ERTGB_REQUIRE(cs[i]->formulation == ERTGB_FORMULATION_SINGULARITY_REMOVAL,
+                          "batched responses use the singularity-removal formulation");
             for (int j = 0; j < i; j++) ERTGB_REQUIRE(cs[j] != cs[i], "a context appears twice in the batch");
         }
         Context &c0 = *cs[0];

@@ -853,6 +853,9 @@ int complex_response(Context &c, const double *rho_re, const double *rho_im, dou
                      cudaStream_t s) {
     MeshData &m = c.mesh;
     ComplexState &x = c.cx;
+    if (m.n_ext > 0 || !m.ext_rows.empty())
+        throw Error(ERTGB_BAD_INPUT, "complex resistivity takes no matrix extension (the reference's complete "
+                                     "electrode model is real-valued only, dcfemmodelling.cpp:423-428)");
     const int64_t n = m.n, nnz = m.nnz, Rpad = c.Rpad, R = c.R;
     x.have_pot = false;
     // 1 / rho* per cell

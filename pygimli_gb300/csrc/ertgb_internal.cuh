@@ -68,7 +68,8 @@ template <class T> struct DBuf {
 // Mesh-dependent structures.
 struct MeshData {
     int dim = 0, order = 1, nv = 0, nvb = 0;  // nv / nvb: nodes per cell / boundary
-    int64_t n = 0, C = 0, B = 0;  // nodes, cells, mixed boundaries
+    int64_t n = 0, C = 0, B = 0;  // matrix rows (nodes + extension rows), cells, mixed boundaries
+    int64_t nn = 0;               // mesh nodes (the first nn rows)
     int64_t nnz = 0;
     int64_t P = 0;                // parameters = max(cell marker) + 1
     std::vector<double> xyz;      // host copy (n x 3)
@@ -86,6 +87,14 @@ struct MeshData {
     DBuf<double> d_K, d_M;           // per-cell element matrices (C x nv*nv)
     DBuf<int32_t> d_bnd_nodes, d_bnd_cell;
     DBuf<double> d_bnd_mass, d_bnd_center, d_bnd_normal;  // B x nvb^2, B x 3, B x 3
+    // constant matrix extension (complete electrode model, bypass resistors):
+    // n_ext rows after the nodes; entries added after assembly, per slot in
+    // the order given (ext_ptr: nnz + 1 offsets into ext_val)
+    int64_t n_ext = 0;
+    std::vector<int32_t> ext_rows, ext_cols;
+    std::vector<double> ext_vals;
+    DBuf<int32_t> d_ext_ptr;
+    DBuf<double> d_ext_val;
     // parameter -> cells (sorted by parameter), for the Jacobian
     std::vector<int32_t> pcell_ptr, pcell;
     DBuf<int32_t> d_pcell_ptr, d_pcell;
@@ -163,6 +172,13 @@ struct Context {
     std::vector<double> emin_r;              // singular radius per electrode
     std::vector<int32_t> ecell_ptr, ecell;   // incident cells per electrode
     DBuf<int32_t> d_enode, d_ecell_ptr, d_ecell;
+    // formulation (ertgb_formulation); total potential: the row of each
+    // electrode's current and potential, and the CEM collect of the last
+    // wavenumber only
+    int formulation = ERTGB_FORMULATION_SINGULARITY_REMOVAL;
+    std::vector<int32_t> src_row;
+    DBuf<int32_t> d_src_row;
+    bool collect_last_k = false;
     DBuf<double> d_emin_r, d_epos;
     bool have_elec = false;
     // wavenumbers
@@ -242,6 +258,8 @@ void compute_rhs_scale(Context &c, cudaStream_t s);
 constexpr double kRhsFloor2 = 1e-6;
 void finish_potentials(Context &c, cudaStream_t s);
 void collect_response(Context &c, double *rhoa, cudaStream_t s);
+// total potential: unit currents at the electrodes' source rows into d_r
+void build_rhs_total(Context &c, cudaStream_t s);
 void check_rho(Context &c, const double *rho_cell, cudaStream_t s);
 // pcg.cu
 // mask: warm start (x kept) on the columns with mask[t] != 0; nullptr = cold start, all columns
@@ -292,6 +310,7 @@ void build_assembly_map(MeshData &m, std::vector<int32_t> &cptr, std::vector<int
                         std::vector<int32_t> &diag);
 void build_jacobian_tiles(Context &c);
 void build_lower_pattern(MeshData &m);
+void build_extension_map(const MeshData &m, std::vector<int32_t> &ptr, std::vector<double> &val);
 // fsai.cu
 void fsai_setup(Context &c, cudaStream_t s);
 // batch.cu: batched mixed-precision PCG over the contexts' assembled systems

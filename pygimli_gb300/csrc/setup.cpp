@@ -3,7 +3,10 @@
 //
 // Pattern: same content and order as SparseMatrix::buildSparsityPattern
 // (core/src/sparsematrix.h:966-1024): for every node the set of nodes that
-// share a cell with it, diagonal included, rows and columns ascending, int32.
+// share a cell with it, diagonal included, rows and columns ascending, int32;
+// with a matrix extension (complete electrode model, bypass resistors) the
+// positions of its entries are merged in and its rows follow the nodes, as
+// the reference's map matrix grows (dcfemmodelling.cpp:315-414, 701-708).
 //
 // Assembly map: for every CSR slot the list of element-matrix entries that
 // land on it, cell entries first in ascending cell order, then mixed-boundary
@@ -18,37 +21,56 @@
 namespace ertgb {
 
 void build_pattern(MeshData &m) {
-    const int64_t n = m.n, C = m.C;
+    const int64_t n = m.n, nn = m.nn, C = m.C;
     const int nv = m.nv;
     // node -> cells
-    std::vector<int64_t> nc_ptr(n + 1, 0);
+    std::vector<int64_t> nc_ptr(nn + 1, 0);
     for (int64_t c = 0; c < C; c++)
         for (int i = 0; i < nv; i++) nc_ptr[m.cells[c * nv + i] + 1]++;
-    for (int64_t i = 0; i < n; i++) nc_ptr[i + 1] += nc_ptr[i];
-    std::vector<int32_t> nc(nc_ptr[n]);
+    for (int64_t i = 0; i < nn; i++) nc_ptr[i + 1] += nc_ptr[i];
+    std::vector<int32_t> nc(nc_ptr[nn]);
     {
         std::vector<int64_t> pos(nc_ptr.begin(), nc_ptr.end() - 1);
         for (int64_t c = 0; c < C; c++)
             for (int i = 0; i < nv; i++) nc[pos[m.cells[c * nv + i]]++] = (int32_t)c;
+    }
+    // extension entries by row
+    const size_t nx = m.ext_rows.size();
+    std::vector<int64_t> x_ptr(n + 1, 0);
+    for (size_t q = 0; q < nx; q++) x_ptr[m.ext_rows[q] + 1]++;
+    for (int64_t i = 0; i < n; i++) x_ptr[i + 1] += x_ptr[i];
+    std::vector<int32_t> x_col(nx);
+    {
+        std::vector<int64_t> pos(x_ptr.begin(), x_ptr.end() - 1);
+        for (size_t q = 0; q < nx; q++) x_col[pos[m.ext_rows[q]]++] = m.ext_cols[q];
     }
     // rows
     m.rowptr.assign(n + 1, 0);
     std::vector<int32_t> mark(n, -1);
     std::vector<int32_t> row;
     std::vector<int32_t> cols;
-    cols.reserve((size_t)C * nv * 4);
+    cols.reserve((size_t)C * nv * 4 + nx);
     for (int64_t r = 0; r < n; r++) {
         row.clear();
-        for (int64_t q = nc_ptr[r]; q < nc_ptr[r + 1]; q++) {
-            const int32_t *cn = &m.cells[(int64_t)nc[q] * nv];
-            for (int i = 0; i < nv; i++) {
-                if (mark[cn[i]] != (int32_t)r) {
-                    mark[cn[i]] = (int32_t)r;
-                    row.push_back(cn[i]);
+        if (r < nn) {
+            for (int64_t q = nc_ptr[r]; q < nc_ptr[r + 1]; q++) {
+                const int32_t *cn = &m.cells[(int64_t)nc[q] * nv];
+                for (int i = 0; i < nv; i++) {
+                    if (mark[cn[i]] != (int32_t)r) {
+                        mark[cn[i]] = (int32_t)r;
+                        row.push_back(cn[i]);
+                    }
                 }
             }
+            if (row.empty()) throw Error(ERTGB_BAD_INPUT, "mesh has a node that belongs to no cell");
         }
-        if (row.empty()) throw Error(ERTGB_BAD_INPUT, "mesh has a node that belongs to no cell");
+        for (int64_t q = x_ptr[r]; q < x_ptr[r + 1]; q++) {
+            if (mark[x_col[q]] != (int32_t)r) {
+                mark[x_col[q]] = (int32_t)r;
+                row.push_back(x_col[q]);
+            }
+        }
+        if (row.empty()) throw Error(ERTGB_BAD_INPUT, "extension row without entries");
         std::sort(row.begin(), row.end());
         cols.insert(cols.end(), row.begin(), row.end());
         if (cols.size() > (size_t)INT32_MAX) throw Error(ERTGB_BAD_INPUT, "matrix too large for int32 indices");
@@ -99,6 +121,25 @@ void build_assembly_map(MeshData &m, std::vector<int32_t> &cptr, std::vector<int
     for (int64_t e = 0; e < B * nvb2; e++) centry[pos[bnd_slot[e]]++] = base + (int32_t)e;
     diag.resize(m.n);
     for (int64_t r = 0; r < m.n; r++) diag[r] = find_slot(m, (int32_t)r, (int32_t)r);
+}
+
+// Per-slot lists of the extension entries, each list in the order the
+// entries were given, so that their sum after the domain and boundary terms
+// rounds as the reference's additions into its map matrix do.
+void build_extension_map(const MeshData &m, std::vector<int32_t> &ptr, std::vector<double> &val) {
+    const size_t nx = m.ext_rows.size();
+    ptr.assign(m.nnz + 1, 0);
+    val.clear();
+    if (nx == 0) return;
+    std::vector<int32_t> slot(nx);
+    for (size_t q = 0; q < nx; q++) {
+        slot[q] = find_slot(m, m.ext_rows[q], m.ext_cols[q]);
+        ptr[slot[q] + 1]++;
+    }
+    for (int64_t i = 0; i < m.nnz; i++) ptr[i + 1] += ptr[i];
+    val.assign(nx, 0.0);
+    std::vector<int32_t> pos(ptr.begin(), ptr.end() - 1);
+    for (size_t q = 0; q < nx; q++) val[pos[slot[q]]++] = m.ext_vals[q];
 }
 
 // Lower-triangular pattern of A (the FSAI factor G) and its transpose:

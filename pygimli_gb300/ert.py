@@ -2,7 +2,10 @@
 
 Mirrors the method surface of pyGIMLi's ``pg.physics.ert.ERTModelling``
 (pygimli/physics/ert/ertModelling.py:73-246) over the singularity-removal
-operator ``DCSRMultiElectrodeModelling`` (core/src/bert/dcfemmodelling.h:344):
+operator ``DCSRMultiElectrodeModelling`` (core/src/bert/dcfemmodelling.h:344)
+or, with ``sr=False``, the total-potential operator
+``DCMultiElectrodeModelling`` (dcfemmodelling.h:105) with complete-electrode-
+model and bypass electrodes:
 ``setMesh``, ``setData``, ``response(model)``, ``createJacobian(model)``,
 ``jacobian()``, ``mesh()``, ``parameterCount``, ``solution()``,
 ``calcGeometricFactor``, ``mapERTModel``, ``setkValues/setWeights``.
@@ -10,9 +13,10 @@ Every numerical step runs in libertgb.so (hand-written sm_103a CUDA behind
 the C ABI of include/ertgb.h); this module only does setup bookkeeping
 (electrode search, wavenumbers, model mapping) and moves buffers.
 
-Scope (raises otherwise): real resistivity, node electrodes (marker -99),
-flat surface with mixed far-field boundaries, pole current pattern (the
-reference's default when there is no reference electrode).
+Scope (raises otherwise): node electrodes (marker -99; with sr=False also
+CEM and bypass electrodes), flat surface with mixed far-field boundaries,
+pole current pattern (the reference's default when there is no reference
+electrode).
 """
 from __future__ import annotations
 
@@ -21,6 +25,7 @@ import ctypes
 import numpy as np
 
 from . import _native
+from .cem import electrode_setup, has_cem_markers
 from .data import DataContainerERT, geometricFactors
 from .kwave import init_kwave_list
 from .mesh import MARKER_BOUND_HOMOGEN_NEUMANN, MARKER_BOUND_MIXED, MARKER_NODE_ELECTRODE, Mesh
@@ -75,17 +80,26 @@ def surface_info(mesh):
 
 
 class ERTModelling:
-    """ERT forward operator (singularity removal) on one GB300."""
+    """ERT forward operator on one GB300.
+
+    sr=True (default): singularity removal (pyGIMLi's
+    DCSRMultiElectrodeModelling).  sr=False: total potentials
+    (DCMultiElectrodeModelling, pygimli/physics/ert/ertModelling.py:102-106),
+    the formulation that also takes complete-electrode-model (CEM) and bypass
+    electrodes from the mesh markers (see ``pygimli_gb300.cem``)."""
 
     def __init__(self, sr=True, verbose=False, device=0, rtol=1e-10, maxIter=20000, precision="fp64",
                  precond="jacobi", weights=None):
-        if not sr:
-            raise NotImplementedError("only the singularity-removal operator (sr=True) is provided")
         self.verbose = verbose
         self._lib = _native.load()
         self._ctx = ctypes.c_void_p()
         _native.check(None, self._lib.ertgb_create(ctypes.byref(self._ctx), int(device)))
         self.device = int(device)
+        self._sr = bool(sr)
+        self._check(self._lib.ertgb_set_formulation(self._ctx, 0 if self._sr else 1))
+        self._contact_z = None    # setContactImpedances
+        self._bypass_r = None     # setBypassResistances
+        self._electrodes = None   # electrode setup of the total-potential operator
         self._mesh = None
         self._data = None
         self._k = None
@@ -257,11 +271,44 @@ class ERTModelling:
     def data(self):
         return self._data
 
+    def setContactImpedances(self, zi):
+        """Contact impedances (Ohm m^2) of the CEM electrodes, one per
+        electrode then per passive body (DCMultiElectrodeModelling::
+        setContactImpedances, dcfemmodelling.cpp:786-788; default 1).  Point
+        electrodes always couple with 1 (dcfemmodelling.cpp:344-350)."""
+        self._contact_z = None if zi is None else np.asarray(zi, np.float64).copy()
+        self._J = None
+        if self._mesh is not None and self._data is not None:
+            self._update_data()
+
+    def setBypassResistances(self, resistances):
+        """Bypass resistances {node marker: Ohm} (the reference reads them
+        from electrodeBypassResistances.map, dcfemmodelling.cpp:672-686;
+        default 1e-6 Ohm)."""
+        self._bypass_r = None if resistances is None else dict(resistances)
+        self._J = None
+        if self._mesh is not None and self._data is not None:
+            self._update_data()
+
     def _update_data(self):
         mesh, data = self._mesh, self._data
-        self._elec_nodes = search_electrodes(mesh, data.sensorPositions())
+        if self._sr:
+            if has_cem_markers(mesh):
+                raise ValueError("complete-electrode-model and bypass electrodes need the total-potential "
+                                 "operator: ERTModelling(sr=False)")
+            self._elec_nodes = search_electrodes(mesh, data.sensorPositions())
+            self._electrodes = None
+        else:
+            setup = electrode_setup(mesh, data.sensorPositions(), self._contact_z, self._bypass_r)
+            self._electrodes = setup
+            self._elec_nodes = setup.enode
         self._check(self._lib.ertgb_set_electrodes(self._ctx, len(self._elec_nodes),
                                                    _ptr(self._elec_nodes), float(self._surface_z)))
+        if self._electrodes is not None and (self._electrodes.cem or len(self._electrodes.rows)):
+            e = self._electrodes
+            self._check(self._lib.ertgb_set_extension(
+                self._ctx, int(e.n_ext), len(e.rows), _ptr(e.rows), _ptr(e.cols), _ptr(e.vals), _ptr(e.src_row),
+                _ptr(e.src_center), 1 if e.cem else 0))
         if not self._kw_user:
             self._k, self._w = init_kwave_list(mesh.dim(), data.sensorPositions())
         self._push_kw()
@@ -399,8 +446,11 @@ class ERTModelling:
 
     def calcGeometricFactor(self, data=None):
         """Analytic geometric factors (flat surface, calcGeometricFactor,
-        core/src/bert/dcfemmodelling.cpp:1527-1557)."""
+        core/src/bert/dcfemmodelling.cpp:1527-1557).  With CEM electrodes the
+        reference needs them given (response, :1088-1097)."""
         data = self._data if data is None else data
+        if self._electrodes is not None and self._electrodes.cem:
+            raise ValueError("data contains no K-factors: the complete electrode model needs them given")
         return geometricFactors(data, self._mesh.dim())
 
     def mapERTModel(self, model, background=-9e99):
