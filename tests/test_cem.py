@@ -182,9 +182,17 @@ def test_total_potential_golden(torch, golden_dir, name, form):
     resistivities and the Jacobian.  The PCG runs to rtol 1e-10 where the
     reference factors: rhoa within 1e-8, J within 1e-6 (relative norm); the
     bypass case's 1e-6 Ohm resistors raise the condition number by ~1e8,
-    so there rhoa 2e-6 and J 1e-5."""
+    so there rhoa 2e-6 and J 1e-5.  The 2.5-D CEM response is the last
+    wavenumber's unweighted electrode potential (the reference's collect):
+    its far-electrode values are ~1e-8 while the response rounds to 1e-10,
+    so the FP64 Jacobi solve runs to rtol 1e-12 there (at 1e-10 the error
+    of ~5e-11 moves one voltage by half a rounding step; the same Jacobi PCG
+    on the CPU reproduces both)."""
     z, mesh, zc = load(golden_dir, name)
-    fop = _fop(z, mesh, zc, **FORMS[form])
+    kw = dict(FORMS[form])
+    if name == "ert2d_cem_small" and form == "fp64":
+        kw["rtol"] = 1e-12
+    fop = _fop(z, mesh, zc, **kw)
     rhoa = fop.response(z["rho"])
     R = ref_matrix(z)
     rp, ci = fop.pattern()
