@@ -56,6 +56,9 @@ def parse():
     ap.add_argument("--weights", default=None, help="learned preconditioner weights (.npz); default: the "
                     "packaged weights trained for the workload")
     ap.add_argument("--no-plain", action="store_true", help="skip the comparison runs (plain FP64 Jacobi, FSAI)")
+    ap.add_argument("--cem-only", action="store_true", help="with --no-plain: still time the CEM form")
+    ap.add_argument("--cem-patch", type=float, default=4.0 / 3.0,
+                    help="surface cell size of the workload mesh (CEM patch = the triangles within one diagonal)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--gn", action="store_true", help="also time one full Gauss-Newton iteration per form "
@@ -363,6 +366,45 @@ def run_ours(args, world, rank, local):
         del Jp, fop_p
         return out
 
+    def time_cem(precision, precond, jac_dtype, label):
+        """The total-potential operator (ERTModelling(sr=False)) on the same
+        mesh with every electrode a complete-electrode-model patch (the
+        surface triangles within one cell diagonal of it, contact impedance
+        1 Ohm m^2): one extension row per electrode; response + Jacobian,
+        1 warm-up and 1 timed step."""
+        from pygimli_gb300.cem import mark_cem_electrodes
+        h = float(args.cem_patch)
+        mesh_c = mark_cem_electrodes(mesh, data.sensorPositions()[:, :2], h * np.sqrt(2.0) * (1.0 + 1e-6))
+        fop_c = ERTModelling(sr=False, device=local, rtol=args.rtol, precision=precision, precond=precond)
+        fop_c.setData(data)
+        fop_c.setMesh(mesh_c, ignoreRegionManager=True)
+        Jc = torch.empty((D, P), dtype=torch.float64 if jac_dtype == 0 else torch.float32, device=dev)
+        out_c = torch.empty(D, dtype=torch.float64, device=dev)
+
+        def step_c():
+            fop_c._response_dev(rho_d, out_c)
+            stream = torch.cuda.current_stream(dev).cuda_stream
+            fop_c._check(L.ertgb_jacobian(fop_c._ctx, ctypes.c_void_p(rho_d.data_ptr()), C,
+                                          ctypes.c_void_p(Jc.data_ptr()), jac_dtype, ctypes.c_void_p(stream)))
+
+        step_c()
+        torch.cuda.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record()
+        step_c()
+        f1.record()
+        torch.cuda.synchronize()
+        stc = fop_c.stats()
+        e = fop_c._electrodes
+        res = {"value": f0.elapsed_time(f1) / 1e3, "unit": UNIT, "steps": 1, "solver": label,
+               "electrodes": "CEM", "extension_rows": int(e.n_ext), "extension_entries": int(len(e.rows)),
+               "pcg_iterations": stc["iterations"], "ms_solve": stc["ms_solve"], "ms_jacobian": stc["ms_jacobian"],
+               "columns_finished_fp64": stc["stalled_columns"],
+               "jacobian": "FP64" if jac_dtype == 0 else "FP32 (FP64 differences)"}
+        del Jc, fop_c
+        return res
+
     def time_complex(precision):
         """Complex resistivity (IP) on the same workload: the reference's
         total-potential complex formulation, block COCG + complex Jacobian;
@@ -401,9 +443,17 @@ def run_ours(args, world, rank, local):
         del Jc, fop_c
         return res
 
-    plain = fsai_form = cx_form = None
+    plain = fsai_form = cx_form = cem_form = None
     if not args.no_plain:
         cx_form = {"mixed": time_complex("mixed"), "fp64": time_complex("fp64")}
+    if (not args.no_plain or args.cem_only) and mesh.dim() == 3:
+        cem_form = {}
+        for key, (prec, pc, jd, lab) in {"mixed_fsai": ("mixed", "fsai", 1, "block PCG (FSAI), mixed, total potential"),
+                                        "fp64": ("fp64", "jacobi", 0, "block PCG (Jacobi), FP64, total potential")}.items():
+            try:
+                cem_form[key] = time_cem(prec, pc, jd, lab)
+            except Exception as exc:  # the record reports it; the headline line stays
+                cem_form[key] = {"error": f"{type(exc).__name__}: {exc}"}
     if not args.no_plain and (args.precision, args.precond) != ("fp64", "jacobi"):
         plain = time_form("fp64", "jacobi", 0, "block PCG (Jacobi), FP64")
     if not args.no_plain and args.precond == "learned":
@@ -498,7 +548,7 @@ def run_ours(args, world, rank, local):
                               f"{mesh.nodeCount() * 96 * 8 / 1e6:.0f} MB, J {D * P * 8 / 1e9:.1f} GB"),
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
                "plain_fp64_gpu_pcg": plain, "fsai_form": fsai_form, "gn_iteration": gn,
-               "refine_h2": refine_rec, "complex_form": cx_form,
+               "refine_h2": refine_rec, "complex_form": cx_form, "cem_form": cem_form,
                "learned_weights": os.path.relpath(weights, ROOT) if weights else None,
                "clocks": clk, "step_ms": step_ms,
                "breakdown_ms": {"assemble": st["ms_assemble"], "rhs": st["ms_rhs"], "solve": st["ms_solve"],

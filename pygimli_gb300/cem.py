@@ -28,8 +28,8 @@ device after every assembly.
 The reference also reads map files from its working directory
 (``bypass.map``, ``electrodeBypassResistances.map``, ``contactImpedance.map``,
 ``contactResistance.map``); here contact impedances and bypass resistances
-are arguments.  Free electrodes inside cells, reference and calibration
-nodes are not supported.
+are arguments.  CEM electrodes made of cells, free electrodes inside cells,
+reference and calibration nodes are not supported.
 """
 from __future__ import annotations
 
@@ -230,6 +230,9 @@ def electrode_setup(mesh, sensors, contact_impedance=None, bypass_resistance=Non
     default 1; setContactImpedances); point electrodes always use 1.
     bypass_resistance: {node marker: Ohm} (default 1e-6 Ohm)."""
     electrodes, passive, bypass_markers, ent_nodes, ent_corners = search_electrodes(mesh, sensors)
+    if any(k == "c" for el in electrodes + passive for k, _ in el.entities):
+        raise NotImplementedError("CEM electrodes made of cells (cell marker -10000 - i) are not supported; "
+                                  "mark the electrode's boundaries instead")
     nn = mesh.nodeCount()
     nE = len(electrodes)
     cem = any(e.kind == "cem" for e in electrodes) or len(passive) > 0
