@@ -11,7 +11,7 @@ from .data import DataContainerERT, createData, geometricFactors  # noqa: F401
 from .mesh import Mesh, create_box_mesh_3d, create_para_mesh_2d  # noqa: F401
 
 __all__ = ["DataContainerERT", "createData", "geometricFactors", "Mesh", "create_box_mesh_3d",
-           "create_para_mesh_2d", "ERTModelling", "simulate", "load"]
+           "create_para_mesh_2d", "ERTModelling", "simulate", "createGeometricFactors", "load"]
 
 
 def load(fileName, **kwargs):
@@ -25,7 +25,7 @@ def load(fileName, **kwargs):
 
 
 def __getattr__(name):
-    if name in ("ERTModelling", "simulate"):
+    if name in ("ERTModelling", "simulate", "createGeometricFactors"):
         from . import ert
         return getattr(ert, name)
     raise AttributeError(name)

@@ -240,8 +240,10 @@ class ERTModelling:
 
     def _set_fwd_mesh(self, mesh):
         surf, topo = surface_info(mesh)
-        if topo:
-            raise NotImplementedError("meshes with topography need numerical primary potentials (not supported)")
+        if topo and self._sr:
+            raise NotImplementedError("meshes with topography need numerical primary potentials for singularity "
+                                      "removal (not supported); the total-potential operator "
+                                      "ERTModelling(sr=False) takes them")
         bm = mesh.boundary_markers
         if mesh.dim() == 3 and not np.any(bm == MARKER_BOUND_MIXED):
             raise NotImplementedError("Neumann-only domains are not supported")
@@ -618,10 +620,26 @@ class ERTModelling:
         return out
 
     def solution(self):
-        """k-summed potentials per electrode source (nE x nodes), the
-        reference's solutions_ (dcfemmodelling.cpp:1707-1729)."""
+        """k-summed potentials per electrode source (nE x rows), the
+        reference's solutions_ (dcfemmodelling.cpp:1707-1729): the first
+        wavenumber's term, then the others added in order."""
         u = self.subPotentials()
-        return np.einsum("k,ken->en", self._w, u)
+        sol = u[0] * self._w[0]
+        for ki in range(1, len(self._w)):
+            sol += u[ki] * self._w[ki]
+        return sol
+
+    def electrodePotentials(self):
+        """U[e, f]: potential at electrode f for the unit current at electrode
+        e after the last response -- the reference's DataMap
+        (DataMap::collect, core/src/bert/datamap.cpp:57-98): the k-summed
+        solution at the electrodes' rows; with CEM the extension rows of the
+        last wavenumber, unweighted (dcfemmodelling.cpp:1642-1644)."""
+        e = self._electrodes
+        if e is not None and e.cem:
+            return self.subPotentials()[-1][:, e.src_row].copy()
+        rows = e.src_row if e is not None else self._elec_nodes
+        return self.solution()[:, rows]
 
     def stats(self):
         s = _native.Stats()
@@ -656,6 +674,42 @@ def _cell_values(mesh, res):
     return arr, False
 
 
+def datamap_voltages(U, abmn):
+    """Voltages of the scheme from the electrode potential matrix, without
+    rounding or reciprocity (DataMap::data, core/src/bert/datamap.cpp:
+    159-231): (U[a,m] - U[a,n]) - (U[b,m] - U[b,n]), index -1 = infinity."""
+    U = np.asarray(U, np.float64)
+    ab = np.asarray(abmn, np.int64).reshape(-1, 4)
+
+    def g(i, j):
+        ok = (i != -1) & (j != -1)
+        return np.where(ok, U[np.where(ok, i, 0), np.where(ok, j, 0)], 0.0)
+
+    a, b, m, n = ab[:, 0], ab[:, 1], ab[:, 2], ab[:, 3]
+    return (g(a, m) - g(a, n)) - (g(b, m) - g(b, n))
+
+
+def createGeometricFactors(scheme, numerical=None, mesh=None, dim=3, h2=True, p2=True, verbose=False, **kwargs):
+    """Geometric factors (pg.physics.ert.createGeometricFactors,
+    pygimli/physics/ert/ert.py:323-397): analytic half-space factors, or
+    with ``numerical`` the inverse voltages of a unit-resistivity
+    total-potential simulation on ``mesh`` refined by H2 then P2 (``h2``,
+    ``p2``), which holds topography.  A mesh must be given: the reference's
+    default inversion mesh needs a mesh generator.  Keywords of
+    ERTModelling (device, precision, ...) are passed on."""
+    if not numerical and mesh is None:
+        return geometricFactors(scheme, dim)
+    if mesh is None:
+        raise NotImplementedError("numerical geometric factors need a mesh (no mesh generator here)")
+    m = mesh
+    if h2:
+        m = m.createH2()
+    if p2:
+        m = m.createP2()
+    d = simulate(m, scheme, 1.0, sr=False, calcOnly=True, **kwargs)
+    return 1.0 / d["u"]
+
+
 def simulate(mesh, scheme, res, **kwargs):
     """Simulate an ERT measurement (pg.physics.ert.simulate,
     pygimli/physics/ert/ert.py:12-285): apparent resistivities of ``res`` for
@@ -663,14 +717,17 @@ def simulate(mesh, scheme, res, **kwargs):
     resistivity; ``noiseLevel`` > 0 adds Gaussian noise with the errors of
     ``estimateError`` (``noiseAbs`` V at 1 A; ``seed`` fixes it, numpy's
     generator: the draws differ from pyGIMLi's); ``returnArray`` returns
-    rhoa (and phia) instead of the container.  Keywords of ERTModelling
-    (device, precision, precond, ...) are passed on.  Not provided:
-    calcOnly, returnFields, contact impedances (CEM)."""
+    rhoa (and phia) instead of the container.  ``calcOnly``: the voltages
+    only ('r' per unit current, 'i' = ``current``, 'u'), no geometric
+    factors (ert.py:186-201); ``returnFields``: the k-summed potentials per
+    source; ``contactImpedances`` (a value or one per electrode): CEM contact
+    impedances of the total-potential operator (``sr=False``) -- the
+    reference passes fixed values there instead (ert.py:123-128).  Keywords
+    of ERTModelling (sr, device, precision, precond, ...) are passed on."""
     from .data import estimateError
-    for k in ("calcOnly", "returnFields", "contactImpedances"):
-        if kwargs.get(k):
-            raise NotImplementedError(f"simulate({k}=...) is not provided")
-        kwargs.pop(k, None)
+    calc_only = bool(kwargs.pop("calcOnly", False))
+    return_fields = bool(kwargs.pop("returnFields", False))
+    contact = kwargs.pop("contactImpedances", None)
     kwargs.pop("verbose", None)
     return_array = kwargs.pop("returnArray", False)
     noise_level = float(kwargs.pop("noiseLevel", 0.0))
@@ -680,15 +737,40 @@ def simulate(mesh, scheme, res, **kwargs):
     current = kwargs.pop("current", 1.0)
     return_fop = kwargs.pop("returnFOP", False)
     fop = ERTModelling(**kwargs)
+    if contact is not None:
+        z = np.asarray(contact, np.float64)
+        fop.setContactImpedances(np.full(scheme.sensorCount(), float(z)) if z.ndim == 0 else z)
     data = scheme.copy()
     vals, rows = _cell_values(mesh, res)
     cplx = np.iscomplexobj(vals)
     fop.setComplex(cplx)
-    if not data.allNonZero("k"):
+    k_given = data.allNonZero("k")
+    if calc_only:
+        if cplx:
+            raise NotImplementedError("simulate(calcOnly=True) with complex resistivity (the reference has none)")
+        if rows:
+            raise ValueError("simulate(calcOnly=True) takes one resistivity per cell")
+        # the scheme's factors only scale apparent resistivities, which calcOnly does not return
+        k_saved = data["k"].copy() if data.exists("k") else None
+        data.set("k", np.ones(data.size()))
+    elif not k_given:
         data.set("k", geometricFactors(data, mesh.dim()))
     fop.setData(data)
     fop.setMesh(mesh, ignoreRegionManager=True)
     D = data.size()
+    if calc_only:
+        fop.response(vals)
+        if return_fields:
+            return fop.solution()
+        r = datamap_voltages(fop.electrodePotentials(), data.abmn())
+        if k_saved is not None:
+            data.set("k", k_saved)
+        else:
+            data.set("k", np.zeros(D))
+        data.set("r", r)
+        data.set("i", np.full(D, float(current)))
+        data.set("u", r * float(current))
+        return data
     for t in ("u", "i", "r"):
         data.set(t, np.zeros(D))
 
@@ -711,6 +793,8 @@ def simulate(mesh, scheme, res, **kwargs):
         data.set("rhoa", rhoa)
         if cplx:
             data.set("phia", phia)
+    if return_fields:
+        return fop.solution()
     if noise_level > 0 and not rows:
         rng = np.random.default_rng(seed)
         if not data.allNonZero("err"):

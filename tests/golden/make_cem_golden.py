@@ -16,6 +16,10 @@ wavenumber, apparent resistivities and the Jacobian):
                       beside 2 node electrodes
   ert2d_bypass_small  2.5-D, electrodes 2 and 5 as bypass electrodes (four
                       nodes down from the surface, default 1e-6 Ohm)
+  ert2d_topo_tp_small 2.5-D node electrodes on a sinusoidal surface; also the
+  ert3d_topo_tp_small 3-D likewise; both also hold the reference's k-summed
+                      electrode potential matrices for the model (U) and for
+                      1 Ohm m (U1)
 
 Run from the repository root; the working directory must hold none of the
 reference's map files (bypass.map, contactImpedance.map, ...).
@@ -44,7 +48,17 @@ def _resistivity(mesh, seed):
     return np.exp(rng.uniform(np.log(50.0), np.log(200.0), mesh.cellCount()))
 
 
-def case(name, mesh, data, seed, contact_impedance=None):
+def _electrode_potentials(R, k, w, nE):
+    """The reference's k-summed electrode potential matrix (solutions_ at
+    the electrode nodes, dcfemmodelling.cpp:1707-1729, DataMap::collect)."""
+    sub = R.subpotentials().reshape(len(k), nE, -1)
+    sol = sub[0] * w[0]
+    for ki in range(1, len(k)):
+        sol += sub[ki] * w[ki]
+    return sol[:, R.electrode_nodes()]
+
+
+def case(name, mesh, data, seed, contact_impedance=None, potentials=False):
     if only and name not in only:
         return
     for f in ("bypass.map", "electrodeBypassResistances.map", "contactImpedance.map", "contactResistance.map"):
@@ -58,8 +72,13 @@ def case(name, mesh, data, seed, contact_impedance=None):
     rp, ci, va = R.matrices[0]
     sub = R.subpotentials().reshape(len(k), data.sensorCount(), -1)
     J = R.jacobian(rho)
+    extra = {}
+    if potentials:  # node electrodes only: U for the model and for 1 Ohm m
+        extra["U"] = _electrode_potentials(R, k, w, data.sensorCount())
+        R.response(np.ones(mesh.cellCount()))
+        extra["U1"] = _electrode_potentials(R, k, w, data.sensorCount())
     np.savez_compressed(
-        os.path.join(OUT, name + ".npz"),
+        os.path.join(OUT, name + ".npz"), **extra,
         dim=mesh.dim(), nodes=mesh.nodes, cells=mesh.cells, cell_markers=mesh.cell_markers,
         node_markers=mesh.node_markers, boundaries=mesh.boundaries,
         boundary_markers=mesh.boundary_markers, boundary_cells=mesh.boundary_cells,
@@ -103,6 +122,40 @@ def main():
     m2b = Mesh(2, m2.nodes, m2.cells, m2.cell_markers, nmb, m2.boundaries, m2.boundary_markers, m2.boundary_cells,
                check=False)
     case("ert2d_bypass_small", m2b, d2, seed=25)
+    # topography (total potential only): a smooth surface, electrodes on it
+    case("ert2d_topo_tp_small", *_topo_2d(m2, xs), seed=26, potentials=True)
+    m3n = Mesh(3, m3.nodes, m3.cells, m3.cell_markers, m3.node_markers, m3.boundaries, m3.boundary_markers,
+               m3.boundary_cells, check=False)
+    case("ert3d_topo_tp_small", *_topo_3d(m3n, e, ab3), seed=27, potentials=True)
+
+
+def _bend(nodes, axis, t):
+    """Raise the surface (coordinate 0 on ``axis``) by t(x[, y]), fading
+    linearly to zero at the bottom of the mesh."""
+    out = nodes.copy()
+    H = -nodes[:, axis].min()
+    out[:, axis] = nodes[:, axis] + t * (1.0 + nodes[:, axis] / H)
+    return out
+
+
+def _topo_2d(m, xs):
+    t = 0.4 * np.sin(2.0 * np.pi * m.nodes[:, 0] / 6.0)
+    mt = Mesh(2, _bend(m.nodes, 1, t), m.cells, m.cell_markers, m.node_markers, m.boundaries, m.boundary_markers,
+              m.boundary_cells, check=False)
+    en = [int(np.nonzero((np.abs(m.nodes[:, 0] - x) < 1e-9) & (m.node_markers == -99))[0][0]) for x in xs]
+    d = DataContainerERT(mt.nodes[en], createData(xs, "dd").abmn())
+    d["k"] = geometricFactors(d, 2)
+    return mt, d
+
+
+def _topo_3d(m, e, ab):
+    t = 0.3 * np.sin(2.0 * np.pi * m.nodes[:, 0] / 8.0) * np.cos(2.0 * np.pi * m.nodes[:, 1] / 10.0)
+    mt = Mesh(3, _bend(m.nodes, 2, t), m.cells, m.cell_markers, m.node_markers, m.boundaries, m.boundary_markers,
+              m.boundary_cells, check=False)
+    en = [int(np.nonzero(np.linalg.norm(m.nodes[:, :2] - p, axis=1) + np.abs(m.nodes[:, 2]) < 1e-9)[0][0]) for p in e]
+    d = DataContainerERT(mt.nodes[en], ab)
+    d["k"] = geometricFactors(d, 3)
+    return mt, d
 
 
 if __name__ == "__main__":

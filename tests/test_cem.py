@@ -26,7 +26,9 @@ from pygimli_gb300 import cem  # noqa: E402
 from pygimli_gb300.data import DataContainerERT  # noqa: E402
 from pygimli_gb300.mesh import Mesh  # noqa: E402
 
-CASES = ["ert2d_tp_small", "ert2d_cem_small", "ert3d_cem_small", "ert2d_bypass_small"]
+CASES = ["ert2d_tp_small", "ert2d_cem_small", "ert3d_cem_small", "ert2d_bypass_small", "ert2d_topo_tp_small",
+         "ert3d_topo_tp_small"]
+TOPO = ["ert2d_topo_tp_small", "ert3d_topo_tp_small"]
 
 
 def load(golden_dir, name):
@@ -100,6 +102,21 @@ def test_host_extension_matches_reference(golden_dir, name):
     assert [e.kind for e in setup.electrodes] == [e.kind for e in P.electrodes]
 
 
+@pytest.mark.parametrize("name", TOPO)
+def test_oracle_electrode_potentials_topography(golden_dir, name):
+    """On a surface with topography (total potential only) the oracle's
+    k-summed electrode potential matrix equals the reference's for the model
+    and for 1 Ohm m, and the product's DataMap voltages equal the oracle's."""
+    from pygimli_gb300.ert import datamap_voltages
+    z, mesh, _ = load(golden_dir, name)
+    P = CO.TotalPotentialProblem(mesh, z["sensors"], z["abmn"], z["kfac"], z["k"], z["w"])
+    U = P.collect(P.solve(z["rho"]))
+    U1 = P.collect(P.solve(np.ones(mesh.cellCount())))
+    assert np.abs(U - z["U"]).max() <= 1e-13 * np.abs(z["U"]).max()
+    assert np.abs(U1 - z["U1"]).max() <= 1e-13 * np.abs(z["U1"]).max()
+    np.testing.assert_array_equal(datamap_voltages(U, z["abmn"]), CO.Problem.data_u(P, U))
+
+
 def test_entity_integrals_closed_form():
     """Closed-form integrals of the product against the oracle's quadrature
     for every entity type (linear and quadratic)."""
@@ -169,7 +186,8 @@ def _fop(z, mesh, zc, **kw):
 GPU_CASES = [("ert2d_tp_small", "fp64"), ("ert2d_tp_small", "mixed"), ("ert2d_tp_small", "mixed-fsai"),
              ("ert2d_cem_small", "fp64"), ("ert2d_cem_small", "mixed-fsai"),
              ("ert3d_cem_small", "fp64"), ("ert3d_cem_small", "mixed"), ("ert3d_cem_small", "mixed-fsai"),
-             ("ert2d_bypass_small", "fp64")]
+             ("ert2d_bypass_small", "fp64"), ("ert2d_topo_tp_small", "fp64"), ("ert2d_topo_tp_small", "mixed-fsai"),
+             ("ert3d_topo_tp_small", "fp64"), ("ert3d_topo_tp_small", "mixed-fsai")]
 FORMS = {"fp64": dict(precision="fp64"), "mixed": dict(precision="mixed"),
          "mixed-fsai": dict(precision="mixed", precond="fsai")}
 
@@ -232,3 +250,25 @@ def test_total_potential_guards(torch, golden_dir):
     fop.setComplex(True)
     with pytest.raises(RuntimeError):
         fop.response(np.concatenate([z["rho"], -0.01 * z["rho"]]))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", TOPO)
+def test_simulate_calc_only_and_numerical_factors(torch, golden_dir, name):
+    """simulate(sr=False, calcOnly=True) returns the reference's DataMap
+    voltages (no rounding, no reciprocity) on a topographic surface;
+    createGeometricFactors(numerical=True) is 1 / those voltages at 1 Ohm m;
+    returnFields the k-summed potentials per source."""
+    from pygimli_gb300.ert import createGeometricFactors, datamap_voltages, simulate
+    z, mesh, _ = load(golden_dir, name)
+    scheme = DataContainerERT(z["sensors"], z["abmn"])
+    d = simulate(mesh, scheme, z["rho"], sr=False, calcOnly=True, current=2.0)
+    u_ref = datamap_voltages(z["U"], z["abmn"])
+    assert np.max(np.abs(d["r"] - u_ref) / np.abs(u_ref)) <= 1e-8
+    np.testing.assert_allclose(d["u"], 2.0 * d["r"], rtol=1e-15)
+    assert not scheme.allNonZero("k")
+    k_num = createGeometricFactors(scheme, numerical=True, mesh=mesh, h2=False, p2=False)
+    k_ref = 1.0 / datamap_voltages(z["U1"], z["abmn"])
+    assert np.max(np.abs(k_num - k_ref) / np.abs(k_ref)) <= 1e-8
+    sol = simulate(mesh, scheme, z["rho"], sr=False, calcOnly=True, returnFields=True)
+    assert sol.shape == (scheme.sensorCount(), mesh.nodeCount())
