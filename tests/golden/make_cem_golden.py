@@ -14,6 +14,9 @@ wavenumber, apparent resistivities and the Jacobian):
                       contact impedances 0.5-2 Ohm m^2) and one passive body
   ert3d_cem_small     3-D, 2 x 2 CEM electrodes (2 x 2 m surface patches)
                       beside 2 node electrodes
+  ert2d_cem_p2_small  ert2d_cem_small and
+  ert3d_cem_p2_small  ert3d_cem_small on the reference's createP2 of the mesh
+                      (the 3-D one without the assembled matrix: size)
   ert2d_bypass_small  2.5-D, electrodes 2 and 5 as bypass electrodes (four
                       nodes down from the surface, default 1e-6 Ohm)
   ert2d_topo_tp_small 2.5-D node electrodes on a sinusoidal surface; also the
@@ -58,18 +61,21 @@ def _electrode_potentials(R, k, w, nE):
     return sol[:, R.electrode_nodes()]
 
 
-def case(name, mesh, data, seed, contact_impedance=None, potentials=False):
+def case(name, mesh, data, seed, contact_impedance=None, potentials=False, p2=False, matrix=True):
+    """One fixture; with p2 the reference refines the mesh itself
+    (Mesh::createP2) and the resistivity is one value per refined cell;
+    matrix=False leaves the assembled matrix out (size)."""
     if only and name not in only:
         return
     for f in ("bypass.map", "electrodeBypassResistances.map", "contactImpedance.map", "contactResistance.map"):
         if os.path.exists(f):
             raise SystemExit(f"{f} in the working directory would change the reference's result")
     R = RefModelling(mesh, data.sensorPositions(), data.abmn(), data["k"], keep_matrices=True, sr=False,
-                     contact_impedance=contact_impedance)
+                     contact_impedance=contact_impedance, p2=p2)
     k, w = R.kw()
     rho = _resistivity(mesh, seed)
     rhoa = R.response(rho)
-    rp, ci, va = R.matrices[0]
+    rp, ci, va = R.matrices[0] if matrix else (np.zeros(0, np.int32), np.zeros(0, np.int32), np.zeros(0))
     sub = R.subpotentials().reshape(len(k), data.sensorCount(), -1)
     J = R.jacobian(rho)
     extra = {}
@@ -83,10 +89,11 @@ def case(name, mesh, data, seed, contact_impedance=None, potentials=False):
         node_markers=mesh.node_markers, boundaries=mesh.boundaries,
         boundary_markers=mesh.boundary_markers, boundary_cells=mesh.boundary_cells,
         sensors=data.sensorPositions(), abmn=data.abmn(), kfac=data["k"], k=k, w=w, rho=rho, rhoa=rhoa,
-        rowptr=rp, colidx=ci, S=va, subpot_first=sub[0], subpot_last=sub[-1], J=J,
-        contact_impedance=np.zeros(0) if contact_impedance is None else np.asarray(contact_impedance, float))
+        rowptr=rp, colidx=ci, S=va, subpot_first=sub[0], subpot_last=sub[-1] if len(k) > 1 else np.zeros(0), J=J,
+        contact_impedance=np.zeros(0) if contact_impedance is None else np.asarray(contact_impedance, float),
+        p2=int(bool(p2)))
     R.close()
-    print(name, mesh, len(data), "k:", len(k), "matrix rows:", len(rp) - 1, "J:", J.shape)
+    print(name, mesh, len(data), "k:", len(k), "matrix rows:", max(len(rp) - 1, 0), "J:", J.shape)
 
 
 def main():
@@ -114,6 +121,9 @@ def main():
     d3 = DataContainerERT(np.column_stack([e, np.zeros(len(e))]), ab3)
     d3["k"] = geometricFactors(d3, 3)
     case("ert3d_cem_small", m3c, d3, seed=24)
+    # quadratic elements: CEM on Edge3 / Triangle6 boundaries
+    case("ert2d_cem_p2_small", m2c, d2, seed=28, contact_impedance=zc, p2=True)
+    case("ert3d_cem_p2_small", m3c, d3, seed=29, p2=True, matrix=False)
     # bypass electrodes: the surface node and the three below it
     nmb = m2.node_markers.copy()
     for i in (2, 5):

@@ -27,7 +27,7 @@ from pygimli_gb300.data import DataContainerERT  # noqa: E402
 from pygimli_gb300.mesh import Mesh  # noqa: E402
 
 CASES = ["ert2d_tp_small", "ert2d_cem_small", "ert3d_cem_small", "ert2d_bypass_small", "ert2d_topo_tp_small",
-         "ert3d_topo_tp_small"]
+         "ert3d_topo_tp_small", "ert2d_cem_p2_small", "ert3d_cem_p2_small"]
 TOPO = ["ert2d_topo_tp_small", "ert3d_topo_tp_small"]
 
 
@@ -35,6 +35,8 @@ def load(golden_dir, name):
     z = np.load(os.path.join(golden_dir, name + ".npz"))
     mesh = Mesh(int(z["dim"]), z["nodes"], z["cells"], z["cell_markers"], z["node_markers"], z["boundaries"],
                 z["boundary_markers"], z["boundary_cells"], check=False)
+    if "p2" in z.files and int(z["p2"]) == 1:
+        mesh = mesh.createP2()   # the reference's numbering (tests/test_refine.py)
     zc = z["contact_impedance"]
     return z, mesh, (zc if len(zc) else None)
 
@@ -54,10 +56,11 @@ def test_oracle_matches_reference(golden_dir, name):
     reference and of scipy then differ in the 9th digit."""
     z, mesh, zc = load(golden_dir, name)
     P = CO.TotalPotentialProblem(mesh, z["sensors"], z["abmn"], z["kfac"], z["k"], z["w"], contact_impedance=zc)
-    R = ref_matrix(z)
-    A = P.matrix(z["rho"], 0)
-    assert A.shape == R.shape and A.nnz == R.nnz
-    assert abs(A - R).max() <= 1e-15 * abs(R).max()
+    if len(z["S"]):
+        R = ref_matrix(z)
+        A = P.matrix(z["rho"], 0)
+        assert A.shape == R.shape and A.nnz == R.nnz
+        assert abs(A - R).max() <= 1e-15 * abs(R).max()
     rhoa, u = P.response(z["rho"])
     J = P.jacobian(u, z["rho"])
     tol = 1e-7 if "bypass" in name else 1e-12
@@ -87,9 +90,11 @@ def test_host_extension_matches_reference(golden_dir, name):
     z, mesh, zc = load(golden_dir, name)
     setup = cem.electrode_setup(mesh, z["sensors"], contact_impedance=zc)
     P = CO.TotalPotentialProblem(mesh, z["sensors"], z["abmn"], z["kfac"], z["k"], z["w"], contact_impedance=zc)
+    # without the reference's matrix in the fixture: the oracle's, which
+    # reproduces the reference's apparent resistivities and Jacobian
+    R = ref_matrix(z) if len(z["S"]) else P.matrix(z["rho"], 0)
     P.ext, P.ext_diag = {}, {}
     fem = P.matrix(z["rho"], 0)
-    R = ref_matrix(z)
     N = R.shape[0]
     assert mesh.nodeCount() + setup.n_ext == N
     X = sp.csr_matrix((setup.vals, (setup.rows, setup.cols)), shape=(N, N))
@@ -187,7 +192,7 @@ GPU_CASES = [("ert2d_tp_small", "fp64"), ("ert2d_tp_small", "mixed"), ("ert2d_tp
              ("ert2d_cem_small", "fp64"), ("ert2d_cem_small", "mixed-fsai"),
              ("ert3d_cem_small", "fp64"), ("ert3d_cem_small", "mixed"), ("ert3d_cem_small", "mixed-fsai"),
              ("ert2d_bypass_small", "fp64"), ("ert2d_topo_tp_small", "fp64"), ("ert2d_topo_tp_small", "mixed-fsai"),
-             ("ert3d_topo_tp_small", "fp64"), ("ert3d_topo_tp_small", "mixed-fsai")]
+             ("ert3d_topo_tp_small", "fp64"), ("ert3d_topo_tp_small", "mixed-fsai"), ("ert3d_cem_p2_small", "fp64")]
 FORMS = {"fp64": dict(precision="fp64"), "mixed": dict(precision="mixed"),
          "mixed-fsai": dict(precision="mixed", precond="fsai")}
 
@@ -200,7 +205,9 @@ def test_total_potential_golden(torch, golden_dir, name, form):
     resistivities and the Jacobian.  The PCG runs to rtol 1e-10 where the
     reference factors: rhoa within 1e-8, J within 1e-6 (relative norm); the
     bypass case's 1e-6 Ohm resistors raise the condition number by ~1e8,
-    so there rhoa 2e-6 and J 1e-5.  The 2.5-D CEM response is the last
+    so there rhoa 2e-6 and J 1e-5.  (The 2.5-D P2 CEM fixture has voltages
+    of one rounding step, 8e-13 from a rounding boundary: it is checked by
+    the oracle only.)  The 2.5-D CEM response is the last
     wavenumber's unweighted electrode potential (the reference's collect):
     its far-electrode values are ~1e-8 while the response rounds to 1e-10,
     so the FP64 Jacobi solve runs to rtol 1e-12 there (at 1e-10 the error
@@ -212,11 +219,12 @@ def test_total_potential_golden(torch, golden_dir, name, form):
         kw["rtol"] = 1e-12
     fop = _fop(z, mesh, zc, **kw)
     rhoa = fop.response(z["rho"])
-    R = ref_matrix(z)
-    rp, ci = fop.pattern()
-    assert len(rp) - 1 == R.shape[0]
-    S = sp.csr_matrix((fop.matrix(0), ci, rp), shape=R.shape)
-    assert abs(S - R).max() <= 1e-12 * abs(R).max()
+    if len(z["S"]):
+        R = ref_matrix(z)
+        rp, ci = fop.pattern()
+        assert len(rp) - 1 == R.shape[0]
+        S = sp.csr_matrix((fop.matrix(0), ci, rp), shape=R.shape)
+        assert abs(S - R).max() <= 1e-12 * abs(R).max()
     J = fop.createJacobian(z["rho"]).cpu().numpy()
     e_r = float(np.max(np.abs(rhoa - z["rhoa"]) / np.abs(z["rhoa"])))
     e_j = float(np.linalg.norm(J - z["J"]) / np.linalg.norm(z["J"]))
