@@ -18,7 +18,9 @@ beside it on the same workload.
 events around K steps on the launching stream).  ``e2e`` is the same step
 through the public Python API with host numpy inputs and the apparent
 resistivities and the full Jacobian copied back to pinned host memory.
-``--impl reference`` times the CPU oracle port (the reference's algorithm
+``cem_form`` times the total-potential operator (``ERTModelling(sr=False)``)
+on the 3-D workload's mesh with every electrode a complete-electrode-model
+patch.  ``--impl reference`` times the CPU oracle port (the reference's algorithm
 restated in numpy/scipy with a SuperLU direct solve) on a bounded,
 extrapolated sample.  With N > 1 ranks (torchrun) every rank runs an
 independent replica of the workload (the operator uses one GPU).
