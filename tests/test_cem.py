@@ -122,6 +122,21 @@ def test_oracle_electrode_potentials_topography(golden_dir, name):
     np.testing.assert_array_equal(datamap_voltages(U, z["abmn"]), CO.Problem.data_u(P, U))
 
 
+def test_datamap_voltages_with_poles():
+    """DataMap voltages with electrodes at infinity (index -1 in a, b or n)
+    equal the oracle's restatement of DataMap::data."""
+    from pygimli_gb300.ert import datamap_voltages
+    rng = np.random.default_rng(5)
+    U = rng.normal(size=(6, 6))
+    ab = np.array([[0, 1, 2, 3], [0, -1, 2, 3], [-1, 1, 4, 5], [2, 3, 4, -1], [5, -1, 0, -1], [1, 4, 3, 2]])
+
+    class _P:
+        abmn = ab
+
+    np.testing.assert_array_equal(datamap_voltages(U, ab), CO.Problem.data_u(_P, U))
+    assert datamap_voltages(U, ab)[4] == U[5, 0]
+
+
 def test_entity_integrals_closed_form():
     """Closed-form integrals of the product against the oracle's quadrature
     for every entity type (linear and quadratic)."""
