@@ -50,7 +50,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["box_3d", "box_3d_probe", "box_3d_large", "box_3d_large_p2", "line_2d"],
+    ap.add_argument("--workload", choices=["box_3d", "box_3d_probe", "box_3d_coarse", "box_3d_large",
+                                           "box_3d_large_p2", "line_2d"],
                     default="box_3d")
     ap.add_argument("--rtol", type=float, default=1e-10)
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
@@ -65,7 +66,56 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--gn", action="store_true", help="also time one full Gauss-Newton iteration per form "
                     "(response, Jacobian, 200 CGLS iterations on the GPU, line-search responses)")
+    ap.add_argument("--case", choices=["complex", "refine", "jacobian"], default=None,
+                    help="run one single workload for a profiler instead of the bench and print one line: "
+                    "'complex' = one complex-resistivity response + complex Jacobian (-10 mrad, --precision), "
+                    "'refine' = the GPU H2 refinement of the workload mesh, twice, "
+                    "'jacobian' = one response (--precision, --precond) and three Jacobians (FP32 with "
+                    "--precision mixed, else FP64)")
     return ap.parse_args()
+
+
+def run_case(args):
+    """One single workload (``--case``) for ``ncu`` launch lists and captures."""
+    import torch
+    from pygimli_gb300 import build as _build
+    _build.build()
+    mesh, data, rho, _ = workload(args.workload)
+    if args.case == "refine":
+        from pygimli_gb300 import refine
+        for _ in range(2):
+            t0 = time.perf_counter()
+            h = refine.createH2(mesh, 0)
+        print(f"refine {args.workload}: H2 of {mesh.cellCount()} cells -> {h.cellCount()} in "
+              f"{time.perf_counter() - t0:.4f} s")
+        return
+    from pygimli_gb300.ert import ERTModelling
+    if args.case == "jacobian":
+        weights = (args.weights or default_weights(args.workload)) if args.precond == "learned" else None
+        fop = ERTModelling(precision=args.precision, precond=args.precond, weights=weights)
+        fop.setData(data)
+        fop.setMesh(mesh, ignoreRegionManager=True)
+        fop.response(rho)
+        ms = []
+        for _ in range(3):
+            J = fop.createJacobian(rho, dtype="float32" if args.precision == "mixed" else "float64")
+            ms.append(fop.stats()["ms_jacobian"])
+            del J
+        print(f"jacobian {args.workload} {args.precision}: {data.size()} x {fop.parameterCount} J, "
+              f"ms per launch {', '.join(f'{x:.3f}' for x in ms)}")
+        return
+    fop = ERTModelling(precision=args.precision)
+    fop.setData(data)
+    fop.setMesh(mesh, ignoreRegionManager=True)
+    fop.setComplex(True)
+    z = rho * np.exp(-0.01j)
+    t0 = time.perf_counter()
+    fop.response(z)
+    fop.createJacobian(z)
+    torch.cuda.synchronize()
+    st = fop.stats()
+    print(f"complex {args.workload} {args.precision}: {time.perf_counter() - t0:.3f} s, COCG iterations "
+          f"{st['iterations']}, columns finished in FP64 {st['stalled_columns']}")
 
 
 def workload(name):
@@ -80,7 +130,10 @@ def workload(name):
                            f"{mesh.nodeCount()} nodes, {mesh.cellCount()} tetrahedra, "
                            f"{'P2' if name.endswith('p2') else 'P1'}"}
     else:
-        mesh, data, rho = synthetic.box_3d(scheme="inline" if name == "box_3d_probe" else "full")
+        # box_3d_coarse: the box_3d scheme on a para mesh of 4 m cells (124k
+        # tetrahedra, a 2.6 GB FP32 Jacobian) for profiler captures
+        mesh, data, rho = synthetic.box_3d(scheme="inline" if name == "box_3d_probe" else "full",
+                                           **({"h": 4.0} if name == "box_3d_coarse" else {}))
         cfg = {"workload": f"{name}: 3-D, 96 electrodes (12x8 @4 m), {data.size()} ABMN, "
                            f"{mesh.nodeCount()} nodes, {mesh.cellCount()} tetrahedra, P1"}
     return mesh, data, rho, cfg
@@ -297,7 +350,6 @@ def run_ours(args, world, rank, local):
     rhoa_d = torch.empty(D, dtype=torch.float64, device=dev)
     jdt = 0 if args.precision == "fp64" else 1
     J_d = torch.empty((D, P), dtype=torch.float64 if jdt == 0 else torch.float32, device=dev)
-    J_scratch = J_d if jdt == 0 else None
     import ctypes
 
     def step():
@@ -466,23 +518,21 @@ def run_ours(args, world, rank, local):
     by = ctypes.c_double()
     fl = ctypes.c_double()
     prof = {}
-    if J_scratch is None:
-        J_scratch = torch.empty((D, P), dtype=torch.float64, device=dev)
     spmm_kind = ("spmm", 0) if args.precision == "fp64" else ("spmm32", 3)
-    for name, kid, reps in ((spmm_kind[0], spmm_kind[1], 20), ("jacobian", 1, 2), ("assemble", 2, 10)):
-        fop._check(L.ertgb_profile_kernel(fop._ctx, kid, reps, ctypes.c_void_p(J_scratch.data_ptr()),
+    # the Jacobian is timed in the precision of the step (kernel 1: FP64 J, 4: FP32 J) into its own J buffer
+    for name, kid, reps in ((spmm_kind[0], spmm_kind[1], 20), ("jacobian", 1 if jdt == 0 else 4, 3),
+                            ("assemble", 2, 10)):
+        fop._check(L.ertgb_profile_kernel(fop._ctx, kid, reps, ctypes.c_void_p(J_d.data_ptr()),
                                           ctypes.byref(ms), ctypes.byref(by), ctypes.byref(fl)))
         prof[name] = (ms.value, by.value, fl.value)
-    if J_scratch is not J_d:
-        del J_scratch
     per_step = {spmm_kind[0]: prof[spmm_kind[0]][0] * st["iterations"],
-                "jacobian": prof["jacobian"][0] * (0.5 if jdt == 1 else 1.0),
+                "jacobian": prof["jacobian"][0],
                 "assemble": prof["assemble"][0]}
     dom = max(per_step, key=per_step.get)
     peak, peak_kind = measured_peaks()
     d_ms, d_bytes, d_flops = prof[dom]
     achieved = d_bytes / (d_ms * 1e-3) / 1e9
-    traffic = ncu_traffic(f"{dom}_{args.precision}_{args.workload}.txt")
+    traffic = ncu_traffic(f"{dom}{'32' if dom == 'jacobian' and jdt == 1 else ''}_{args.precision}_{args.workload}.txt")
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                 "algorithmic_bytes": d_bytes, "ms_per_launch": d_ms,
@@ -563,6 +613,9 @@ def run_ours(args, world, rank, local):
 
 def main():
     args = parse()
+    if args.case:
+        run_case(args)
+        return
     world, rank, local = dist_init(args.gpus if args.impl == "ours" else 0)
     if args.impl == "reference":
         run_reference(args, world, rank)

@@ -76,7 +76,8 @@ typedef enum {
     ERTGB_KERNEL_SPMM = 0,     /* PCG operator q = A p with column dots       */
     ERTGB_KERNEL_JACOBIAN = 1, /* Jacobian of the last response (FP64 J)      */
     ERTGB_KERNEL_ASSEMBLE = 2, /* system matrices of the last response        */
-    ERTGB_KERNEL_SPMM32 = 3    /* FP32 operator of the mixed-precision PCG    */
+    ERTGB_KERNEL_SPMM32 = 3,   /* FP32 operator of the mixed-precision PCG    */
+    ERTGB_KERNEL_JACOBIAN32 = 4 /* Jacobian of the last response (FP32 J)     */
 } ertgb_kernel;
 
 /* Create a context on CUDA device ``device``.  Replaces the construction of

@@ -56,18 +56,22 @@ void invalidate_derived(Context &c) {
     c.have_S = false;
 }
 
-// Join the caller's stream into the context stream and back.
+// Join the caller's stream into the context stream and back.  A null stream
+// is the caller's legacy default stream: the context stream is created
+// non-blocking, so it is ordered against the legacy stream explicitly
+// (work the caller queued there, such as the copy of the model, comes first).
 struct StreamJoin {
     Context &c;
     cudaStream_t user;
-    StreamJoin(Context &ctx, void *stream) : c(ctx), user((cudaStream_t)stream) {
-        if (user && user != c.stream) {
+    StreamJoin(Context &ctx, void *stream)
+        : c(ctx), user(stream ? (cudaStream_t)stream : cudaStreamLegacy) {
+        if (user != c.stream) {
             ERTGB_CUDA(cudaEventRecord(c.ev[6], user));
             ERTGB_CUDA(cudaStreamWaitEvent(c.stream, c.ev[6], 0));
         }
     }
     void done() {
-        if (user && user != c.stream) {
+        if (user != c.stream) {
             ERTGB_CUDA(cudaEventRecord(c.ev[7], c.stream));
             ERTGB_CUDA(cudaStreamWaitEvent(user, c.ev[7], 0));
         }
@@ -661,8 +665,9 @@ int ertgb_profile_kernel(ertgb_ctx *ctx, int kernel, int reps, void *J_scratch, 
         switch (kernel) {
             case ERTGB_KERNEL_SPMM: profile_spmm(*c, reps, ms, bytes, flops); break;
             case ERTGB_KERNEL_JACOBIAN:
+            case ERTGB_KERNEL_JACOBIAN32:
                 ERTGB_REQUIRE(J_scratch, "Jacobian profile needs a scratch J");
-                profile_jacobian(*c, reps, (double *)J_scratch, ms, bytes, flops);
+                profile_jacobian(*c, reps, J_scratch, kernel == ERTGB_KERNEL_JACOBIAN ? 0 : 1, ms, bytes, flops);
                 break;
             case ERTGB_KERNEL_ASSEMBLE: profile_assemble(*c, reps, ms, bytes, flops); break;
             case ERTGB_KERNEL_SPMM32: profile_spmm32(*c, reps, ms, bytes, flops); break;

@@ -119,6 +119,20 @@ struct JacTiles {
     std::vector<std::unique_ptr<JacChunk>> chunks;  // empty: the whole scheme in one pass
 };
 
+// Plan of the stiffness-only Jacobian kernel (one wavenumber k = 0, at most
+// one cell per parameter) for one J precision: tiles of 16 parameters, data
+// chunks (descriptors of 12 ints) with their electrode lists, dipoles in
+// chunk-local electrode indices, and the data of each chunk sorted by current
+// dipole (4 ints per datum: datum, current dipole, potential dipole, 0).
+struct JacStiff {
+    bool ok = false;
+    int nchunks = 0, G = 0;   // data chunks, cells staged at a time
+    int64_t ntiles = 0;
+    size_t buf_bytes = 0;     // one table buffer (two are resident)
+    size_t smem = 0;
+    DBuf<int32_t> d_pc, d_el, d_dipa, d_dipm, d_chunks, d_meta;
+};
+
 // Learned preconditioner (learned.cu): graph of the system matrix, network
 // weights, activations of every layer and the training buffers.  bf16
 // tensors are stored as uint16_t.
@@ -196,6 +210,8 @@ struct Context {
     int nA = 0, nM = 0;
     DBuf<int32_t> d_dip_a, d_dip_m, d_data_dip;  // nA x 2, nM x 2, D x 2 (ia, im)
     JacTiles jtiles[2];                          // FP64 and FP32 tables
+    JacStiff jstiff[2];                          // stiffness-only plans (FP64, FP32 J)
+    DBuf<float2> d_xhl;                          // FP32 J: potentials split into (hi, lo)
     bool jac_ready = false;
     DBuf<char> d_jscale;                         // per-datum / per-parameter scales
     // solver
@@ -301,7 +317,7 @@ void refined_free(Refined *r);
 void check_spmm_args(int64_t n, int64_t nnz, const void *rowptr, const void *colidx, const void *vals, int n_k,
                      int n_per_k, int64_t ld, const void *X, const void *Y, const void *dots);
 void profile_assemble(Context &c, int reps, double *ms, double *bytes, double *flops);
-void profile_jacobian(Context &c, int reps, double *J, double *ms, double *bytes, double *flops);
+void profile_jacobian(Context &c, int reps, void *J, int dtype, double *ms, double *bytes, double *flops);
 // jacobian.cu
 void jacobian(Context &c, const double *model, int n_model, void *J, int dtype, cudaStream_t s);
 // setup.cpp

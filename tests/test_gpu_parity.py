@@ -34,13 +34,25 @@ def torch():
 
 
 FORMS = {"fp64": dict(precision="fp64"), "mixed": dict(precision="mixed"),
-         "mixed-fsai": dict(precision="mixed", precond="fsai")}
+         "mixed-fsai": dict(precision="mixed", precond="fsai"),
+         "learned": dict(precision="mixed", precond="learned")}
+WEIGHTS = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "pygimli_gb300", "weights")
+
+
+def learned_weights(mesh):
+    """Packaged network weights for the mesh's kind of matrix: line_2d for
+    2-D meshes, box_3d for linear and box_3d_p2 for quadratic tetrahedra."""
+    if mesh.dim() == 2:
+        return os.path.join(WEIGHTS, "line_2d.npz")
+    return os.path.join(WEIGHTS, "box_3d_p2.npz" if mesh.cells.shape[1] == 10 else "box_3d.npz")
 
 
 def fop_for(mesh, data, k=None, w=None, form=None, **kw):
     from pygimli_gb300 import ERTModelling
     if form is not None:
         kw.update(FORMS[form])
+        if kw.get("precond") == "learned":
+            kw["weights"] = learned_weights(mesh)
     fop = ERTModelling(**kw)
     if k is not None:
         fop.setkValues(k)
