@@ -465,6 +465,7 @@ int ertgb_set_scheme(ertgb_ctx *ctx, int n_data, const int32_t *abmn, const doub
         c->abmn_h.assign(abmn, abmn + (size_t)4 * n_data);
         c->d_abmn.upload(abmn, (size_t)4 * n_data, c->stream);
         c->d_kfac.upload(kfac, (size_t)n_data, c->stream);
+        c->kfac_h.assign(kfac, kfac + n_data);
         // distinct current and potential dipoles, in order of first use
         std::map<std::pair<int32_t, int32_t>, int32_t> amap, mmap;
         std::vector<int32_t> dip_a, dip_m, data_dip((size_t)2 * n_data);

@@ -120,17 +120,19 @@ struct JacTiles {
 };
 
 // Plan of the stiffness-only Jacobian kernel (one wavenumber k = 0, at most
-// one cell per parameter) for one J precision: tiles of 16 parameters, data
-// chunks (descriptors of 12 ints) with their electrode lists, dipoles in
-// chunk-local electrode indices, and the data of each chunk sorted by current
-// dipole (4 ints per datum: datum, current dipole, potential dipole, 0).
+// one cell per parameter) for one J precision: tiles of 32 parameters with
+// their distinct nodes (node list per tile; local node index per slot and
+// cell node, 0xff for an empty slot), data chunks (descriptors of 12 ints)
+// with their dipoles as potential-row columns (nE = the electrode at
+// infinity), and the records of each chunk sorted by current dipole (datum,
+// ia | im << 16, geometric factor).
 struct JacStiff {
     bool ok = false;
-    int nchunks = 0, G = 0;   // data chunks, cells staged at a time
+    int nchunks = 0, RS = 0;  // chunks, staged row length (columns)
     int64_t ntiles = 0;
-    size_t buf_bytes = 0;     // one table buffer (two are resident)
-    size_t smem = 0;
-    DBuf<int32_t> d_pc, d_el, d_dipa, d_dipm, d_chunks, d_meta;
+    size_t tab_bytes = 0, stage_bytes = 0, smem = 0;
+    DBuf<int32_t> d_pc, d_nptr, d_tnodes, d_dipa, d_dipm, d_chunks, d_meta;
+    DBuf<uint8_t> d_lidx;
 };
 
 // Learned preconditioner (learned.cu): graph of the system matrix, network
@@ -205,6 +207,7 @@ struct Context {
     std::vector<int32_t> abmn_h;  // host copy of the scheme (D x 4)
     DBuf<int32_t> d_abmn;
     DBuf<double> d_kfac;
+    std::vector<double> kfac_h;   // host copy of the geometric factors
     bool have_scheme = false;
     // distinct current (a, b) and potential (m, n) dipoles of the scheme
     int nA = 0, nM = 0;

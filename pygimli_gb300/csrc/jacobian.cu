@@ -40,8 +40,7 @@ namespace {
 constexpr int kThreads = 512;
 constexpr size_t kSmemBudget = 110 * 1024;       // two blocks per SM
 constexpr size_t kSmemBudgetLarge = 220 * 1024;  // one block per SM (many wavenumbers x dipoles)
-constexpr size_t kStiffSmem = 220 * 1024;       // stiffness kernel: two table buffers + staging
-constexpr size_t kStiffStage = 24 * 1024;       // stiffness kernel: staging of the producers
+constexpr size_t kStiffSmem = 226 * 1024;      // stiffness kernel: one block per SM (227 KB max)
 
 template <int NV, typename CT, int TW>
 __global__ void __launch_bounds__(kThreads)
@@ -219,229 +218,243 @@ __global__ void k_jac_scales(int64_t D, int64_t P, const double *__restrict__ kf
 // dipole, and the sum has nv-1 instead of nv terms.  The FP64 J forms every
 // difference and product in FP64.  The FP32 J splits each FP64 potential
 // exactly into hi + lo (hi = fl32(u), lo = fl32(u - hi)) once per response and
-// forms the differences as (hi_x - hi_y) + (lo_x - lo_y): where the two
-// potentials cancel, hi_x - hi_y is exact (Sterbenz), so the result is the
-// FP64 difference rounded to FP32 up to 2^-47 of the potentials; products
-// and the J store are FP32.
+// forms the four-potential differences as
+//   ((hi_a,j - hi_a,0) - (hi_b,j - hi_b,0)) + ((lo_a,j - lo_a,0) - (lo_b,j - lo_b,0)):
+// where potentials cancel the hi differences are exact (Sterbenz), so the
+// result is the FP64 difference rounded to FP32 up to 2^-47 of the
+// potentials; products and the J store are FP32.
 //
-// One block per TW-parameter tile (thread = (datum sub-row, parameter)),
-// persistent over tiles.  Per data chunk the block builds, in shared memory,
-//   TA[ia][slot] = (K_c g_ab)_{1..nv-1}   for every distinct current dipole,
-//   TM[im][slot] = g_mn,{1..nv-1}         for every distinct potential dipole,
-// then each warp streams a balanced range of the chunk's data (sorted by
-// current dipole, so a TA row stays in registers across its group): one table
-// row load, nv-1 FMAs and one store per (datum, parameter); a warp writes
-// 32 / TW row segments of TW consecutive parameters.
+// One block of 1024 threads per SM, persistent over tiles of 32 parameters.
+// Per tile the block copies the potential rows of the tile's distinct nodes
+// into shared memory with asynchronous 16-byte copies (cp.async; a tile of 32
+// tetrahedra has at most ~30 distinct nodes against 128 cell nodes), once for
+// every data chunk.  Per data chunk it then builds the tables
+//   TA[ia] = w_0 / model^2 * (K_c g_ab)_{1..nv-1}  for every distinct current dipole,
+//   TM[im] = g_mn,{1..nv-1}                        for every distinct potential dipole,
+// each row component-major with the 32 slots fastest, and streams the chunk's
+// data: every warp takes a balanced range of the data records (datum,
+// ia | im << 16, geometric factor), sorted by current dipole so a lane's TA
+// values stay in registers across a group, staged 16 at a time in shared
+// memory with the next batch loaded ahead; 16 lanes per record, each lane two
+// adjacent parameters: nv-1 conflict-free 8-byte table loads, 2(nv-1) FMAs and
+// one 8-byte J store (two 4-byte stores when P is odd).
 // ---------------------------------------------------------------------------
 
-constexpr int kSJT = 512;    // threads of the stiffness kernel (one block per SM)
-constexpr int kSJProd = 4;   // producer warps (tables); the other warps stream J rows
-constexpr int kSTW = 16;     // parameters per tile
-// named barriers (0 is __syncthreads): buffer full / empty, producers only
-constexpr int kBarFull0 = 1, kBarEmpty0 = 3, kBarProd = 5;
+constexpr int kSJT = 1024;  // threads of the stiffness kernel (one block per SM)
+constexpr int kSTW = 32;    // parameters per tile
+constexpr int kNREC = 16;   // data records staged per warp batch
 
-__device__ __forceinline__ void named_sync(int id, int n) {
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
-}
-__device__ __forceinline__ void named_arrive(int id, int n) {
-    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
-}
-
-// chunk descriptor: data range of the sorted list, electrodes, dipoles and
-// their offsets into the concatenated lists, cells staged at a time
+// chunk descriptor: data range of the sorted records, dipoles and their offsets
 struct StiffChunk {
-    int32_t s0, s1, nEl, nA, nM, off_el, off_a, off_m, G, pad[3];
+    int32_t s0, s1, nA, nM, off_a, off_m, pad[6];
 };
 static_assert(sizeof(StiffChunk) == 12 * sizeof(int32_t), "chunk descriptor layout");
 
-template <typename OT> __host__ __device__ constexpr int nvp_of(int nm1) {
-    return sizeof(OT) == 4 ? (nm1 + 3) / 4 * 4 : (nm1 + 1) / 2 * 2;
-}
+// two adjacent slots of a table component (one 8- or 16-byte access)
+template <typename OT> struct Pair { using type = double2; };
+template <> struct Pair<float> { using type = float2; };
 
-// electrode-level staging element: FP32 (hi, lo) difference pair or FP64
+// staged potential element: FP32 (hi, lo) pair or FP64
 template <typename OT> struct StageOf { using type = double; };
 template <> struct StageOf<float> { using type = float2; };
 
-__device__ __forceinline__ float stage_diff(float2 x, float2 y) { return (x.x - y.x) + (x.y - y.y); }
-__device__ __forceinline__ double stage_diff(double x, double y) { return x - y; }
-__device__ __forceinline__ float2 stage_sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ double stage_sub(double a, double b) { return a - b; }
-
-// one table row of NVP values (NVP * sizeof(OT) a multiple of 16 bytes, rows 16-byte aligned)
-template <typename OT, int NVP> __device__ __forceinline__ void load_row(const OT *p, OT *v) {
-    static_assert(NVP * sizeof(OT) % 16 == 0, "table rows are whole 16-byte units");
-    const int4 *q = reinterpret_cast<const int4 *>(p);
-#pragma unroll
-    for (int i = 0; i < (int)(NVP * sizeof(OT) / 16); i++) reinterpret_cast<int4 *>(v)[i] = q[i];
+// (x_j - x_0) - (y_j - y_0) for the hi and the lo parts, summed
+__device__ __forceinline__ float dipole_shift(float2 xj, float2 x0, float2 yj, float2 y0) {
+    return ((xj.x - x0.x) - (yj.x - y0.x)) + ((xj.y - x0.y) - (yj.y - y0.y));
 }
-template <typename OT, int NVP> __device__ __forceinline__ void store_row(OT *p, const OT *v) {
-    int4 *q = reinterpret_cast<int4 *>(p);
-#pragma unroll
-    for (int i = 0; i < (int)(NVP * sizeof(OT) / 16); i++) q[i] = reinterpret_cast<const int4 *>(v)[i];
+__device__ __forceinline__ double dipole_shift(double xj, double x0, double yj, double y0) {
+    return (xj - x0) - (yj - y0);
 }
 
-template <int NV, typename OT>
+// per-datum scale (the geometric factor) carried in a data record: FP32 in .z, FP64 in (.z, .w)
+template <typename OT> __device__ __forceinline__ OT record_scale(int4 m);
+template <> __device__ __forceinline__ float record_scale<float>(int4 m) { return __int_as_float(m.z); }
+template <> __device__ __forceinline__ double record_scale<double>(int4 m) {
+    return __hiloint2double(m.w, m.z);
+}
+
+// asynchronous 16-byte global -> shared copy (both addresses 16-byte aligned)
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
+template <int NV, typename OT, bool V2>
 __global__ void __launch_bounds__(kSJT, 1)
-    k_jac_stiff(int64_t ntiles, int64_t P, const int32_t *__restrict__ pc, const int32_t *__restrict__ cells,
-                const double *__restrict__ K, const typename StageOf<OT>::type *__restrict__ pot, int64_t Rpad,
-                const StiffChunk *__restrict__ chunks, int nchunks, int buf_bytes, int G,
-                const int32_t *__restrict__ el, const int32_t *__restrict__ dipa, const int32_t *__restrict__ dipm,
-                const int4 *__restrict__ meta, const OT *__restrict__ sd, const OT *__restrict__ sp, OT w0,
+    k_jac_stiff(int64_t ntiles, int64_t P, const int32_t *__restrict__ pc, const double *__restrict__ K,
+                const typename StageOf<OT>::type *__restrict__ pot, int64_t Rpad, int nE, int RS,
+                const int32_t *__restrict__ tile_nptr, const int32_t *__restrict__ tnodes,
+                const uint8_t *__restrict__ lidx, const StiffChunk *__restrict__ chunks, int nchunks,
+                int tab_bytes, int stage_bytes, const int32_t *__restrict__ dipa, const int32_t *__restrict__ dipm,
+                const int4 *__restrict__ meta, int scale_data, const OT *__restrict__ sp, OT w0,
                 OT *__restrict__ J) {
     using ST = typename StageOf<OT>::type;
+    using OT2 = typename Pair<OT>::type;
     constexpr int TW = kSTW;
     constexpr int NM1 = NV - 1;
-    constexpr int NVP = nvp_of<OT>(NM1);
-    constexpr int SUB = 32 / TW;                  // data rows per warp step
-    constexpr int NPT = kSJProd * 32;             // producer threads
-    constexpr int NCW = kSJT / 32 - kSJProd;      // consumer warps
+    constexpr int NW = kSJT / 32;      // warps = data streams
+    constexpr int LPR = TW / 2;        // lanes per record (two adjacent slots each)
+    constexpr int RPW = 32 / LPR;      // records per warp step
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    // [TA | TM tables: row = NM1 x TW values, slot fastest][staged rows Us]
+    // [Ks: TW x NM1^2][sps: TW][lid: TW x NV bytes][records: NW x kNREC x (scale, datum, dipoles)]
+    OT *tabs = reinterpret_cast<OT *>(smem_raw);
+    ST *Us = reinterpret_cast<ST *>(smem_raw + tab_bytes);
+    OT *Ks = reinterpret_cast<OT *>(smem_raw + tab_bytes + stage_bytes);
+    OT *sps = Ks + TW * NM1 * NM1;
+    uint8_t *lid = reinterpret_cast<uint8_t *>(sps + TW);
+    OT *rec_f = reinterpret_cast<OT *>(lid + TW * NV);
+    int32_t *rec_d = reinterpret_cast<int32_t *>(rec_f + NW * kNREC);
+    int32_t *rec_p = rec_d + NW * kNREC;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int64_t nitems = ntiles * nchunks;
-    // buffer b: [TA | TM] tables, then sps[TW] (w_0 / model^2 per slot), node_s[TW * NV]
-    auto buf = [&](int b) { return smem_raw + (size_t)b * buf_bytes; };
-    const size_t tab_bytes = (size_t)buf_bytes - TW * sizeof(OT) - TW * NV * sizeof(int32_t);
-    ST *Eg = reinterpret_cast<ST *>(smem_raw + 2 * (size_t)buf_bytes);
+    const int s2 = 2 * (lane % LPR), sub = lane / LPR;  // pair phase: slots s2, s2 + 1 of record sub
+    const int nE2 = nE & ~1;  // columns copied in 16-byte units
+    const int P32 = (int)P;   // parameters < 2^31: 32 x 32 -> 64-bit row offsets
 
-    if (warp < kSJProd) {
-        // ---------------- producers: tables of item i into buffer i & 1
-        const int t = threadIdx.x;
-        int i = 0;
-        for (int64_t item = blockIdx.x; item < nitems; item += gridDim.x, i++) {
-            const int b = i & 1;
-            if (i >= 2) named_sync(kBarEmpty0 + b, kSJT);  // consumers are done with buffer b
-            const int64_t tile = item / nchunks;
-            const StiffChunk cd = chunks[item % nchunks];
-            const int64_t p0 = tile * TW;
-            const int TP = (int)(P - p0 < (int64_t)TW ? P - p0 : (int64_t)TW);
-            OT *TA = reinterpret_cast<OT *>(buf(b));
-            OT *TM = TA + (size_t)cd.nA * TW * NVP;
-            OT *sps = reinterpret_cast<OT *>(buf(b) + tab_bytes);
-            int32_t *node_s = reinterpret_cast<int32_t *>(sps + TW);
-            OT *Ks = reinterpret_cast<OT *>(Eg + (size_t)G * NM1 * cd.nEl);
-            for (int q = t; q < TW * NV; q += NPT) {
-                const int g = q / NV, k = q - g * NV;
-                const int cell = g < TP ? pc[p0 + g] : -1;
-                node_s[q] = cell < 0 ? -1 : cells[(int64_t)cell * NV + k];
+    // shifted dipole potentials g_j = (u_a - u_b)(node j) - (u_a - u_b)(node 0), j = 1..nv-1,
+    // of the cell in slot g; false for an empty slot
+    auto shifted = [&](int g, int a, int b, OT *gv) -> bool {
+        const int l0 = lid[g * NV];
+        if (l0 == 0xff) return false;
+        const ST *U0 = Us + (size_t)l0 * RS;
+        const ST a0 = U0[a], b0 = U0[b];
+#pragma unroll
+        for (int j = 0; j < NM1; j++) {
+            const ST *Uj = Us + (size_t)lid[g * NV + j + 1] * RS;
+            gv[j] = (OT)dipole_shift(Uj[a], a0, Uj[b], b0);
+        }
+        return true;
+    };
+
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t p0 = tile * TW;
+        const int TP = (int)(P - p0 < (int64_t)TW ? P - p0 : (int64_t)TW);
+        const int n0 = tile_nptr[tile], nn = tile_nptr[tile + 1] - n0;
+        __syncthreads();  // the previous tile is done with every shared buffer
+        // the tile's node rows: columns [0, nE2) by 16-byte copies, an odd last column by a
+        // plain load, column nE (the electrode at infinity) zero
+        {
+            const int per = nE2 / 2;
+            for (int q = threadIdx.x; q < nn * per; q += kSJT) {
+                const int i = q / per, c2 = 2 * (q - i * per);
+                cp_async16(Us + (size_t)i * RS + c2, pot + (int64_t)tnodes[n0 + i] * Rpad + c2);
             }
-            for (int q = t; q < TW; q += NPT) sps[q] = (sp && q < TP) ? w0 * sp[p0 + q] : w0;
-            const int32_t *elc = el + cd.off_el;
+            for (int i = threadIdx.x; i < nn; i += kSJT) {
+                if (nE2 < nE) Us[(size_t)i * RS + nE2] = pot[(int64_t)tnodes[n0 + i] * Rpad + nE2];
+                Us[(size_t)i * RS + nE] = ST{};
+            }
+        }
+        for (int q = threadIdx.x; q < TW * NV; q += kSJT) lid[q] = lidx[tile * TW * NV + q];
+        for (int q = threadIdx.x; q < TW; q += kSJT) sps[q] = (sp && q < TP) ? w0 * sp[p0 + q] : w0;
+        for (int q = threadIdx.x; q < TW * NM1 * NM1; q += kSJT) {
+            const int g = q / (NM1 * NM1), ij = q - g * NM1 * NM1;
+            const int r = ij / NM1 + 1, j = ij % NM1 + 1;
+            const int cell = g < TP ? pc[p0 + g] : -1;
+            Ks[q] = cell < 0 ? (OT)0 : (OT)K[(int64_t)cell * NV * NV + r * NV + j];
+        }
+        cp_async_wait_all();
+        for (int ch = 0; ch < nchunks; ch++) {
+            const StiffChunk cd = chunks[ch];
             const int32_t *dac = dipa + 2 * cd.off_a;
             const int32_t *dmc = dipm + 2 * cd.off_m;
-            named_sync(kBarProd, NPT);
-            for (int g0 = 0; g0 < TW; g0 += G) {
-                const int gn = min(G, TW - g0);
-                // electrode-level shifted potentials u_e(node j) - u_e(node 0), j = 1..nv-1
-                const int nst = gn * NM1 * cd.nEl;
-                for (int q = t; q < nst; q += NPT) {
-                    const int e = q % cd.nEl;
-                    const int gj = q / cd.nEl;  // g * NM1 + (j - 1)
-                    const int g = gj / NM1, j = gj - g * NM1 + 1;
-                    const int n0 = node_s[(g0 + g) * NV], nj = node_s[(g0 + g) * NV + j];
-                    const int ge = elc[e];
-                    ST v{};
-                    if (n0 >= 0 && ge >= 0) v = stage_sub(pot[(int64_t)nj * Rpad + ge], pot[(int64_t)n0 * Rpad + ge]);
-                    Eg[q] = v;
-                }
-                for (int q = t; q < gn * NM1 * NM1; q += NPT) {
-                    const int g = q / (NM1 * NM1), ij = q - g * NM1 * NM1;
-                    const int r = ij / NM1 + 1, j = ij % NM1 + 1;
-                    const int cell = (g0 + g) < TP ? pc[p0 + g0 + g] : -1;
-                    Ks[q] = cell < 0 ? (OT)0 : (OT)K[(int64_t)cell * NV * NV + r * NV + j];
-                }
-                named_sync(kBarProd, NPT);
-                // TA rows (w_0 / model^2 * K_c g_ab) and TM rows (g_mn) of the staged cells
-                for (int q = t; q < (cd.nA + cd.nM) * gn; q += NPT) {
-                    const int g = q % gn;
-                    int dp = q / gn;
-                    const bool isA = dp < cd.nA;
-                    if (!isA) dp -= cd.nA;
-                    const int32_t *dd = isA ? dac : dmc;
-                    const int a = dd[2 * dp], bb = dd[2 * dp + 1];
-                    const ST *Ea = Eg + (size_t)g * NM1 * cd.nEl;
-                    OT gv[NM1];
+            OT *TA = tabs;
+            OT *TM = tabs + (size_t)cd.nA * NM1 * TW;
+            __syncthreads();  // staged rows, lid, sps, Ks visible; the previous chunk's pair phase is done
+            // TA rows (w_0 / model^2 * K_c g_ab) and TM rows (g_mn) of the chunk's dipoles:
+            // thread = (dipole, slot), slot fastest
+            for (int q = threadIdx.x; q < (cd.nA + cd.nM) * TW; q += kSJT) {
+                const int g = q % TW;
+                int dp = q / TW;
+                const bool isA = dp < cd.nA;
+                if (!isA) dp -= cd.nA;
+                const int32_t *dd = isA ? dac : dmc;
+                OT gv[NM1], out[NM1];
+                const bool ok = shifted(g, dd[2 * dp], dd[2 * dp + 1], gv);
+                if (isA) {
+                    const OT *Kg = Ks + (size_t)g * NM1 * NM1;
+                    const OT f = sps[g];
 #pragma unroll
-                    for (int j = 0; j < NM1; j++) gv[j] = (OT)stage_diff(Ea[j * cd.nEl + a], Ea[j * cd.nEl + bb]);
-                    OT out[NVP];
-                    if (isA) {
-                        const OT *Kg = Ks + (size_t)g * NM1 * NM1;
-                        const OT f = sps[g0 + g];
+                    for (int i = 0; i < NM1; i++) {
+                        OT sacc = 0;
 #pragma unroll
-                        for (int r = 0; r < NM1; r++) {
-                            OT s = 0;
-#pragma unroll
-                            for (int j = 0; j < NM1; j++) s = fma(Kg[r * NM1 + j], gv[j], s);
-                            out[r] = s * f;
-                        }
-                    } else {
-#pragma unroll
-                        for (int r = 0; r < NM1; r++) out[r] = gv[r];
+                        for (int j = 0; j < NM1; j++) sacc = fma(Kg[i * NM1 + j], gv[j], sacc);
+                        out[i] = ok ? sacc * f : (OT)0;
                     }
+                } else {
 #pragma unroll
-                    for (int r = NM1; r < NVP; r++) out[r] = 0;
-                    store_row<OT, NVP>((isA ? TA : TM) + ((size_t)dp * TW + g0 + g) * NVP, out);
+                    for (int i = 0; i < NM1; i++) out[i] = ok ? gv[i] : (OT)0;
                 }
-                named_sync(kBarProd, NPT);  // Eg / Ks reused by the next cells
+                OT *dst = (isA ? TA : TM) + (size_t)dp * NM1 * TW + g;
+#pragma unroll
+                for (int i = 0; i < NM1; i++) dst[i * TW] = out[i];
             }
-            __threadfence_block();
-            named_arrive(kBarFull0 + b, kSJT);
-        }
-        // match the consumers' releases of the last two items
-        for (int k = (i >= 2 ? i - 2 : 0); k < i; k++) named_sync(kBarEmpty0 + (k & 1), kSJT);
-    } else {
-        // ---------------- consumers: stream the J rows of item i from buffer i & 1
-        const int cw = warp - kSJProd;
-        const int slot = lane % TW, sub = lane / TW;
-        int i = 0;
-        for (int64_t item = blockIdx.x; item < nitems; item += gridDim.x, i++) {
-            const int b = i & 1;
-            named_sync(kBarFull0 + b, kSJT);
-            const int64_t tile = item / nchunks;
-            const StiffChunk cd = chunks[item % nchunks];
-            const int64_t p0 = tile * TW;
-            const int TP = (int)(P - p0 < (int64_t)TW ? P - p0 : (int64_t)TW);
-            const OT *TA = reinterpret_cast<const OT *>(buf(b));
-            const OT *TM = TA + (size_t)cd.nA * TW * NVP;
-            // consumer warp cw streams a balanced range of the chunk's data; per
-            // batch of 32 data one coalesced load of their (datum, dipoles) and
-            // scale, broadcast by shuffles; the SUB lane groups of a warp take
-            // consecutive data of the batch
+            __syncthreads();
+            // pair phase: warp w streams a balanced range of the chunk's records (sorted by
+            // current dipole, so a lane's TA values stay in registers across a group), staged
+            // kNREC at a time with the next batch loaded ahead; RPW lane groups take
+            // consecutive records, each lane two adjacent parameters
             const int len = cd.s1 - cd.s0;
-            const int sb = cd.s0 + (int)((int64_t)len * cw / NCW);
-            const int se = cd.s0 + (int)((int64_t)len * (cw + 1) / NCW);
+            const int sb = cd.s0 + (int)((int64_t)len * warp / NW);
+            const int se = cd.s0 + (int)((int64_t)len * (warp + 1) / NW);
+            const bool st0 = s2 < TP, st1 = s2 + 1 < TP;
+            const int tm0 = cd.nA * NM1 * TW + s2;  // element offset of this lane's TM slots
+            OT *Jt = J + p0 + s2;
+            OT *rf = rec_f + warp * kNREC;
+            int32_t *rdd = rec_d + warp * kNREC, *rpp = rec_p + warp * kNREC;
             int cur = -1;
-            OT ta[NVP];
+            OT2 ta[NM1];
 #pragma unroll
-            for (int r = 0; r < NVP; r++) ta[r] = 0;
-            for (int base = sb; base < se; base += 32) {
-                const int sl = base + lane;
-                int4 mm = make_int4(0, 0, 0, 0);
-                OT sdl = (OT)1;
-                if (sl < se) {
-                    mm = meta[sl];
-                    if (sd) sdl = sd[mm.x];
+            for (int i = 0; i < NM1; i++) ta[i] = OT2{};
+            int4 nxt = make_int4(0, 0, 0, 0);
+            if (lane < kNREC && sb + lane < se) nxt = meta[sb + lane];
+            for (int base = sb; base < se; base += kNREC) {
+                __syncwarp();
+                if (lane < kNREC) {
+                    rdd[lane] = nxt.x;
+                    rpp[lane] = nxt.y;
+                    rf[lane] = record_scale<OT>(nxt);
                 }
-#pragma unroll 4
-                for (int k = 0; k < 32 / SUB; k++) {
-                    const int src = k * SUB + sub;
-                    const int dm = __shfl_sync(0xffffffffu, mm.x, src);
-                    const int ia = __shfl_sync(0xffffffffu, mm.y, src);
-                    const int im = __shfl_sync(0xffffffffu, mm.z, src);
-                    const OT sdk = __shfl_sync(0xffffffffu, sdl, src);
-                    if (base + src >= se) continue;
-                    if (ia != cur) {
-                        cur = ia;
-                        load_row<OT, NVP>(TA + ((size_t)cur * TW + slot) * NVP, ta);
-                    }
-                    OT tm[NVP];
-                    load_row<OT, NVP>(TM + ((size_t)im * TW + slot) * NVP, tm);
-                    OT acc = 0;
+                __syncwarp();
+                if (lane < kNREC && base + kNREC + lane < se) nxt = meta[base + kNREC + lane];
+                const int cnt = min(kNREC, se - base);  // warp-uniform
 #pragma unroll
-                    for (int r = 0; r < NM1; r++) acc = fma(ta[r], tm[r], acc);
-                    if (slot < TP) J[(int64_t)dm * P + p0 + slot] = acc * sdk;
+                for (int kk = 0; kk < kNREC / RPW; kk++) {
+                    const int k = RPW * kk + sub;
+                    if (k >= cnt) break;
+                    const int pk = rpp[k];
+                    const int ia = pk & 0xffff, im = pk >> 16;
+                    if (__builtin_expect(ia != cur, 0)) {
+                        cur = ia;
+#pragma unroll
+                        for (int i = 0; i < NM1; i++)
+                            ta[i] = *reinterpret_cast<const OT2 *>(TA + s2 + (cur * NM1 + i) * TW);
+                    }
+                    const int o = tm0 + im * (NM1 * TW);
+                    OT acc0 = 0, acc1 = 0;
+#pragma unroll
+                    for (int i = 0; i < NM1; i++) {
+                        const OT2 t = *reinterpret_cast<const OT2 *>(tabs + o + i * TW);
+                        acc0 = fma(ta[i].x, t.x, acc0);
+                        acc1 = fma(ta[i].y, t.y, acc1);
+                    }
+                    if (scale_data) {
+                        const OT f = rf[k];
+                        acc0 *= f;
+                        acc1 *= f;
+                    }
+                    OT *dst = Jt + (int64_t)rdd[k] * P32;
+                    if (V2 && st1) {
+                        *reinterpret_cast<OT2 *>(dst) = OT2{acc0, acc1};
+                    } else {
+                        if (st0) dst[0] = acc0;
+                        if (st1) dst[1] = acc1;
+                    }
                 }
             }
-            named_arrive(kBarEmpty0 + b, kSJT);
         }
     }
 }
@@ -471,7 +484,7 @@ bool plan(const Context &c, int dtype, int *TW, int *G, int ndip = -1) {
 }
 
 template <typename CT>
-void launch_stiff(Context &c, const CT *sd, const CT *sp, CT *J, int dtype, cudaStream_t s) {
+void launch_stiff(Context &c, bool scaled, const CT *sp, CT *J, int dtype, cudaStream_t s) {
     using ST = typename StageOf<CT>::type;
     MeshData &m = c.mesh;
     JacStiff &S = c.jstiff[dtype];
@@ -489,16 +502,19 @@ void launch_stiff(Context &c, const CT *sd, const CT *sp, CT *J, int dtype, cuda
     const CT w0 = (CT)c.w[0];
     auto go = [&](auto kern) {
         ERTGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S.smem));
-        const int64_t grid = std::min<int64_t>(S.ntiles * S.nchunks, (int64_t)nsm);
-        kern<<<(unsigned)grid, kSJT, S.smem, s>>>(S.ntiles, m.P, S.d_pc.p, m.d_cells.p, m.d_K.p, pot, c.Rpad,
-                                                  reinterpret_cast<const StiffChunk *>(S.d_chunks.p), S.nchunks,
-                                                  (int)S.buf_bytes, S.G, S.d_el.p, S.d_dipa.p, S.d_dipm.p,
-                                                  reinterpret_cast<const int4 *>(S.d_meta.p), sd, sp, w0, J);
+        const int64_t grid = std::min<int64_t>(S.ntiles, (int64_t)nsm);
+        kern<<<(unsigned)grid, kSJT, S.smem, s>>>(
+            S.ntiles, m.P, S.d_pc.p, m.d_K.p, pot, c.Rpad, c.nE, S.RS, S.d_nptr.p, S.d_tnodes.p, S.d_lidx.p,
+            reinterpret_cast<const StiffChunk *>(S.d_chunks.p), S.nchunks, (int)S.tab_bytes, (int)S.stage_bytes,
+            S.d_dipa.p, S.d_dipm.p, reinterpret_cast<const int4 *>(S.d_meta.p), scaled ? 1 : 0, sp, w0, J);
         ERTGB_CUDA(cudaGetLastError());
     };
+    // paired stores when every row's pair of adjacent parameters starts on a 2-element boundary
+    const bool v2 = m.P % 2 == 0 && reinterpret_cast<uintptr_t>(J) % (2 * sizeof(CT)) == 0;
     auto by_tw = [&](auto nvc) {
         constexpr int NV = decltype(nvc)::value;
-        go(k_jac_stiff<NV, CT>);
+        if (v2) go(k_jac_stiff<NV, CT, true>);
+        else go(k_jac_stiff<NV, CT, false>);
     };
     switch (m.nv) {
         case 3: by_tw(std::integral_constant<int, 3>()); break;
@@ -529,7 +545,7 @@ void launch(Context &c, const double *model, CT *J, int dtype, cudaStream_t s) {
         sp = base + c.D;
     }
     if (c.jstiff[dtype].ok) {
-        launch_stiff<CT>(c, sd, sp, J, dtype, s);
+        launch_stiff<CT>(c, sd != nullptr, sp, J, dtype, s);
         return;
     }
     auto go = [&](auto kern) {
@@ -605,58 +621,80 @@ static void build_chunks(Context &c, int cap, JacTiles &T) {
 
 // Plan of the stiffness kernel for one J precision (dt 0: FP64, 1: FP32).
 // Applies with one wavenumber k = 0 (3-D) and at most one cell per parameter.
-// Shared memory: two table buffers (tables of one data chunk for a tile of
-// kSTW parameters, the slot scales and the tile's cell nodes) and the
-// producers' staging of G cells.  Data are split into contiguous chunks whose
-// tables fit one buffer and whose electrodes fit the staging with G >= 2.
+// Shared memory of one block (one per SM): the potential rows of the tile's
+// distinct nodes (staged once per tile), the TA and TM tables of one data chunk, the
+// tile's K blocks, slot scales and local node indices, and the warps' record
+// batches.  Data are split into contiguous chunks whose dipoles fit the
+// table space left by the staging.
 static void build_stiff_plan(Context &c, int dt) {
     JacStiff &S = c.jstiff[dt];
     S.ok = false;
     MeshData &m = c.mesh;
-    if (c.nK != 1 || c.k[0] != 0.0 || c.D == 0 || m.P == 0) return;
+    if (c.nK != 1 || c.k[0] != 0.0 || c.D == 0 || m.P == 0 || m.P > INT32_MAX) return;
     if (m.nv != 3 && m.nv != 4 && m.nv != 6 && m.nv != 10) return;
+    if ((int64_t)c.kfac_h.size() != c.D) return;
     std::vector<int32_t> pc((size_t)m.P, -1);
     for (int64_t p = 0; p < m.P; p++) {
         const int32_t cnt = m.pcell_ptr[p + 1] - m.pcell_ptr[p];
         if (cnt > 1) return;
         if (cnt == 1) pc[p] = m.pcell[m.pcell_ptr[p]];
     }
-    const int TW = kSTW;
-    const int nm1 = m.nv - 1;
+    const int TW = kSTW, NV = m.nv;
+    const int nm1 = NV - 1;
     const size_t sz = dt == 0 ? 8 : 4;
-    const size_t nvp = dt == 0 ? (nm1 + 1) / 2 * 2 : (nm1 + 3) / 4 * 4;
-    const size_t per_dip = (size_t)TW * nvp * sz;                   // table bytes per dipole
-    const size_t fixed = (size_t)TW * sz + (size_t)TW * m.nv * 4;   // slot scales + cell nodes
-    const size_t per_el = (size_t)nm1 * 8;                          // staging bytes per electrode and cell
-    const size_t ks = (size_t)nm1 * nm1 * sz;                       // staging of K per cell
-    const int el_cap = (int)((kStiffStage / 2 - ks) / per_el);      // G >= 2
-    const size_t tab_cap = ((kStiffSmem - kStiffStage) / 2 - fixed) / 16 * 16;
+    const size_t per_dip = (size_t)TW * nm1 * sz;  // table bytes per dipole
+    const int RS = (c.nE + 2) / 2 * 2;             // staged row: nE columns + the zero column, even
+    const size_t row_bytes = (size_t)RS * 8;
+    const size_t fixed = (size_t)TW * nm1 * nm1 * sz + (size_t)TW * sz + (size_t)TW * NV +
+                         (size_t)(kSJT / 32) * kNREC * (sz + 8);
+    // distinct nodes of every tile and the local index of each (slot, cell node)
+    S.ntiles = ceil_div(m.P, TW);
+    std::vector<int32_t> nptr(1, 0), tnodes;
+    std::vector<uint8_t> lidx((size_t)S.ntiles * TW * NV, 0xff);
+    int nl_tile = 0;
+    for (int64_t t = 0; t < S.ntiles; t++) {
+        std::vector<int32_t> v;
+        for (int g = 0; g < TW && t * TW + g < m.P; g++) {
+            const int32_t cell = pc[t * TW + g];
+            if (cell >= 0) v.insert(v.end(), &m.cells[(size_t)cell * NV], &m.cells[(size_t)cell * NV] + NV);
+        }
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+        if (v.size() > 254) return;  // 0xff marks an empty slot
+        for (int g = 0; g < TW && t * TW + g < m.P; g++) {
+            const int32_t cell = pc[t * TW + g];
+            if (cell < 0) continue;
+            for (int k = 0; k < NV; k++)
+                lidx[((size_t)t * TW + g) * NV + k] = (uint8_t)(
+                    std::lower_bound(v.begin(), v.end(), m.cells[(size_t)cell * NV + k]) - v.begin());
+        }
+        nl_tile = std::max(nl_tile, (int)v.size());
+        tnodes.insert(tnodes.end(), v.begin(), v.end());
+        nptr.push_back((int32_t)tnodes.size());
+    }
+    const size_t stage = (size_t)nl_tile * row_bytes;
+    if (kStiffSmem < fixed + stage + 2 * per_dip) return;
+    const size_t tab_cap = (kStiffSmem - fixed - stage) / 16 * 16;
     const std::vector<int32_t> &ab = c.abmn_h;
+    auto col = [&](int32_t e) { return e < 0 ? c.nE : e; };
     std::vector<StiffChunk> chunks;
-    std::vector<int32_t> el, dipa, dipm;
+    std::vector<int32_t> dipa, dipm;
     std::vector<int4> meta;
     meta.reserve((size_t)c.D);
     size_t tab_max = 0;
-    int el_max = 0;
     int64_t d = 0;
     while (d < c.D) {
-        std::map<int32_t, int32_t> emap;
         std::map<std::pair<int32_t, int32_t>, int32_t> amap, mmap;
         std::vector<std::array<int32_t, 3>> rows;  // (ia, d, im) of the chunk
         const int64_t d0 = d;
         for (; d < c.D; d++) {
             const int32_t *q = &ab[4 * d];
-            std::set<int32_t> newe;
-            for (int i = 0; i < 4; i++)
-                if (!emap.count(q[i])) newe.insert(q[i]);
-            const int ne = (int)(emap.size() + newe.size());
             const int na = (int)amap.size() + (amap.count({q[0], q[1]}) ? 0 : 1);
             const int nmm = (int)mmap.size() + (mmap.count({q[2], q[3]}) ? 0 : 1);
-            if ((size_t)(na + nmm) * per_dip > tab_cap || ne > el_cap) {
+            if ((size_t)(na + nmm) * per_dip > tab_cap || na > 65535 || nmm > 32767) {
                 if (d == d0) return;  // one datum does not fit: no plan
                 break;
             }
-            for (int i = 0; i < 4; i++) emap.emplace(q[i], (int32_t)emap.size());
             const int32_t ia = amap.emplace(std::make_pair(q[0], q[1]), (int32_t)amap.size()).first->second;
             const int32_t im = mmap.emplace(std::make_pair(q[2], q[3]), (int32_t)mmap.size()).first->second;
             rows.push_back({ia, (int32_t)d, im});
@@ -664,40 +702,46 @@ static void build_stiff_plan(Context &c, int dt) {
         StiffChunk cd{};
         cd.s0 = (int32_t)meta.size();
         cd.s1 = cd.s0 + (int32_t)rows.size();
-        cd.nEl = (int32_t)emap.size();
         cd.nA = (int32_t)amap.size();
         cd.nM = (int32_t)mmap.size();
-        cd.off_el = (int32_t)el.size();
         cd.off_a = (int32_t)(dipa.size() / 2);
         cd.off_m = (int32_t)(dipm.size() / 2);
         tab_max = std::max(tab_max, (size_t)(cd.nA + cd.nM) * per_dip);
-        el_max = std::max(el_max, cd.nEl);
-        std::vector<int32_t> eloc(emap.size());
-        for (auto &kv : emap) eloc[kv.second] = kv.first;
-        el.insert(el.end(), eloc.begin(), eloc.end());
         std::vector<int32_t> da(2 * amap.size()), dm(2 * mmap.size());
         for (auto &kv : amap) {
-            da[2 * kv.second] = emap[kv.first.first];
-            da[2 * kv.second + 1] = emap[kv.first.second];
+            da[2 * kv.second] = col(kv.first.first);
+            da[2 * kv.second + 1] = col(kv.first.second);
         }
         for (auto &kv : mmap) {
-            dm[2 * kv.second] = emap[kv.first.first];
-            dm[2 * kv.second + 1] = emap[kv.first.second];
+            dm[2 * kv.second] = col(kv.first.first);
+            dm[2 * kv.second + 1] = col(kv.first.second);
         }
         dipa.insert(dipa.end(), da.begin(), da.end());
         dipm.insert(dipm.end(), dm.begin(), dm.end());
         std::sort(rows.begin(), rows.end());
-        for (auto &r : rows) meta.push_back(make_int4(r[1], r[0], r[2], 0));
+        for (auto &r : rows) {
+            // (datum, ia | im << 16, geometric factor: FP32 bits in .z or FP64 bits in .z/.w)
+            const double kf = c.kfac_h[r[1]];
+            int4 rec = make_int4(r[1], r[0] | (r[2] << 16), 0, 0);
+            if (dt == 1) {
+                const float f = (float)kf;
+                std::memcpy(&rec.z, &f, 4);
+            } else {
+                std::memcpy(&rec.z, &kf, 8);
+            }
+            meta.push_back(rec);
+        }
         chunks.push_back(cd);
     }
-    const size_t per_cell = (size_t)el_max * per_el + ks;
-    S.G = (int)std::max<size_t>(2, std::min<size_t>(8, kStiffStage / per_cell));
-    S.buf_bytes = (tab_max + 15) / 16 * 16 + fixed;
-    S.smem = 2 * S.buf_bytes + (size_t)S.G * per_cell;
-    S.ntiles = ceil_div(m.P, TW);
+    S.RS = RS;
+    S.tab_bytes = (tab_max + 15) / 16 * 16;
+    S.stage_bytes = stage;
+    S.smem = S.tab_bytes + stage + fixed;
     S.nchunks = (int)chunks.size();
     S.d_pc.upload(pc, c.stream);
-    S.d_el.upload(el, c.stream);
+    S.d_nptr.upload(nptr, c.stream);
+    S.d_tnodes.upload(tnodes, c.stream);
+    S.d_lidx.upload(lidx, c.stream);
     S.d_dipa.upload(dipa, c.stream);
     S.d_dipm.upload(dipm, c.stream);
     std::vector<int32_t> cw(chunks.size() * 12);
@@ -706,6 +750,7 @@ static void build_stiff_plan(Context &c, int dt) {
     std::vector<int32_t> mw(meta.size() * 4);
     std::memcpy(mw.data(), meta.data(), mw.size() * sizeof(int32_t));
     S.d_meta.upload(mw, c.stream);
+    ERTGB_CUDA(cudaStreamSynchronize(c.stream));  // host lists are freed on return
     S.ok = true;
 }
 
