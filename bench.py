@@ -4,25 +4,28 @@
 One step = one Gauss-Newton iteration's operator work: ``response(model)``
 (assembly, SR right-hand sides, multi-RHS PCG over all current sources,
 collect, apparent resistivities) followed by ``createJacobian(model)``
-(dense D x P Jacobian), on a seeded synthetic workload (default ``box_3d``:
-96 electrodes, 5336 data, ~486k tetrahedra, ~88k nodes).  The headline form
-is the mixed-precision block PCG with the learned preconditioner (packaged
-weights trained for the workload) to an FP64 true relative residual of
-1e-10, with an FP32 Jacobian built from FP64 potential differences; the
-plain FP64 Jacobi block PCG (FP64 Jacobian) and the FSAI form are timed
-beside it on the same workload.
+(dense D x P Jacobian), on a seeded synthetic workload (default
+``box_3d_large``: 256 electrodes on 16 x 16, 7392 data, 806,760 tetrahedra,
+144,648 nodes).  The headline form is the mixed-precision block PCG with the
+learned preconditioner (packaged weights) to an FP64 true relative residual
+of 1e-10, with an FP32 Jacobian built from FP64-exact potential differences;
+the plain FP64 Jacobi block PCG (FP64 Jacobian) and the FSAI form are timed
+beside it on the same workload, and the three forms on ``box_3d`` (96
+electrodes, 5336 data, 485,640 tetrahedra) in ``box_3d_forms``.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 ``value`` is device time per step with the inputs resident in HBM (CUDA
 events around K steps on the launching stream).  ``e2e`` is the same step
-through the public Python API with host numpy inputs and the apparent
-resistivities and the full Jacobian copied back to pinned host memory.
-``cem_form`` times the total-potential operator (``ERTModelling(sr=False)``)
-on the 3-D workload's mesh with every electrode a complete-electrode-model
-patch.  ``--impl reference`` times the CPU oracle port (the reference's algorithm
-restated in numpy/scipy with a SuperLU direct solve) on a bounded,
-extrapolated sample.  With N > 1 ranks (torchrun) every rank runs an
+through the reference-facing C ABI with host buffers (ertgb_response_host,
+ertgb_jacobian_host): the model copied in, the apparent resistivities and the
+full Jacobian copied out.  ``complex_form`` and ``cem_form`` time complex
+resistivity and the total-potential operator with complete-electrode-model
+patches on ``box_3d``.  ``cpu_baseline`` and ``--impl reference`` time the
+CPU oracle port (the reference's algorithm restated in numpy/scipy with a
+SuperLU direct solve) on bounded samples of the workload (one core beside the
+GPU timings, resp. every host thread).  ``--case`` runs single workloads for
+profiler captures.  With N > 1 ranks (torchrun) every rank runs an
 independent replica of the workload (the operator uses one GPU).
 """
 from __future__ import annotations
@@ -52,7 +55,7 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["box_3d", "box_3d_probe", "box_3d_coarse", "box_3d_large",
                                            "box_3d_large_p2", "line_2d"],
-                    default="box_3d")
+                    default="box_3d_large")
     ap.add_argument("--rtol", type=float, default=1e-10)
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
     ap.add_argument("--precond", choices=["jacobi", "fsai", "learned"], default="learned")
@@ -118,25 +121,28 @@ def run_case(args):
           f"{st['iterations']}, columns finished in FP64 {st['stalled_columns']}")
 
 
+def workload_label(name, mesh, data, rho=None):
+    if name == "line_2d":
+        return (f"line_2d: 2.5-D, 41 electrodes, 741 dipole-dipole, {mesh.nodeCount()} nodes, "
+                f"{mesh.cellCount()} triangles, 17 wavenumbers")
+    ne = "256 electrodes (16x16 @4 m)" if name.startswith("box_3d_large") else "96 electrodes (12x8 @4 m)"
+    order = "P2" if name.endswith("p2") else "P1"
+    return (f"{name}: 3-D, {ne}, {data.size()} ABMN, {mesh.nodeCount()} nodes, {mesh.cellCount()} tetrahedra, "
+            f"{order}")
+
+
 def workload(name):
     from pygimli_gb300 import synthetic
     if name == "line_2d":
         mesh, data, rho = synthetic.line_2d()
-        cfg = {"workload": "line_2d: 2.5-D, 41 electrodes, 741 dipole-dipole, "
-                           f"{mesh.nodeCount()} nodes, {mesh.cellCount()} triangles, 17 wavenumbers"}
     elif name.startswith("box_3d_large"):
         mesh, data, rho = synthetic.box_3d_large(p2=name.endswith("p2"))
-        cfg = {"workload": f"{name}: 3-D, 256 electrodes (16x16 @4 m), {data.size()} ABMN, "
-                           f"{mesh.nodeCount()} nodes, {mesh.cellCount()} tetrahedra, "
-                           f"{'P2' if name.endswith('p2') else 'P1'}"}
     else:
         # box_3d_coarse: the box_3d scheme on a para mesh of 4 m cells (124k
         # tetrahedra, a 2.6 GB FP32 Jacobian) for profiler captures
         mesh, data, rho = synthetic.box_3d(scheme="inline" if name == "box_3d_probe" else "full",
                                            **({"h": 4.0} if name == "box_3d_coarse" else {}))
-        cfg = {"workload": f"{name}: 3-D, 96 electrodes (12x8 @4 m), {data.size()} ABMN, "
-                           f"{mesh.nodeCount()} nodes, {mesh.cellCount()} tetrahedra, P1"}
-    return mesh, data, rho, cfg
+    return mesh, data, rho, {"workload": workload_label(name, mesh, data, rho)}
 
 
 def default_weights(name):
@@ -255,6 +261,13 @@ def max_over_ranks(ms, world, device=None):
 
 
 def run_reference(args, world, rank):
+    """The reference's CPU algorithm for the path (the oracle port: the
+    reference's own C++ needs its sources, which are not on the machine that
+    runs the benchmark) on the same workload with every host thread.  Each of
+    the K steps runs a bounded sample: the factorization is timed once (in
+    the first step) and charged to every step, the Jacobian's per-electrode
+    products run over all cells every step, 16 source solves and 64 Jacobian
+    rows are sampled per step and scaled (oracle/cpu_baseline.py)."""
     if rank != 0:
         return
     from oracle.cpu_baseline import SampledBaseline, host_threads
@@ -263,25 +276,24 @@ def run_reference(args, world, rank):
     k, w = init_kwave_list(mesh.dim(), data.sensorPositions())
     base = SampledBaseline(mesh, data, k, w)
     threads = host_threads()
-    # light warm-up: assembly only (the timed steps each factor the full matrix)
-    for _ in range(max(1, min(args.warmup, 1))):
+    for _ in range(max(1, min(args.warmup, 1))):  # light warm-up: one assembly
         base.P.assemble(rho, 0)
-    steps = args.steps
-    times, desc = [], ""
-    t_start = time.perf_counter()
-    for i in range(steps):
-        t, desc = base.step(rho, n_src=8, n_rows=64, threads=threads, seed=i)
+    times, descs, walls = [], [], []
+    for i in range(args.steps):
+        t0 = time.perf_counter()
+        t, desc = base.step(rho, n_src=16, n_rows=64, threads=threads, seed=i)
+        walls.append(time.perf_counter() - t0)
         times.append(t)
-        if time.perf_counter() - t_start > 150.0 and i >= 0:
-            break
+        descs.append(desc)
     value = float(np.mean(times))
+    sample = (descs[-1] + f"; {len(times)} steps, sample wall {walls[0]:.1f} s (first step, with the "
+              f"factorization) then {np.mean(walls[1:]) if len(walls) > 1 else 0.0:.1f} s per step")
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": len(times),
-           "steps_requested": steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
+           "warmup": args.warmup, "ms_per_step": value * 1e3,
            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded)", "impl": "reference",
            "config": dict(cfg, parallelism="cpu", solver="SuperLU direct (CHOLMOD stand-in)"),
-           "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                            "sample": desc},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
@@ -326,7 +338,35 @@ def gn_iteration(args, mesh, data, rho, local, weights):
     return out
 
 
+def _cpu_baseline_worker(name, n_src, n_rows, q):
+    """CPU baseline in its own (spawned) process: the oracle port on one host
+    core, on a bounded sample of the workload (oracle/cpu_baseline.py)."""
+    sys.path.insert(0, ROOT)
+    from oracle.cpu_baseline import SampledBaseline
+    from pygimli_gb300.kwave import init_kwave_list
+    try:
+        mesh, data, rho, _ = workload(name)
+        k, w = init_kwave_list(mesh.dim(), data.sensorPositions())
+        base = SampledBaseline(mesh, data, k, w)
+        t0 = time.perf_counter()
+        t, desc = base.step(rho, n_src=n_src, n_rows=n_rows, threads=1)
+        q.put({"value": t, "desc": desc, "wall_s": time.perf_counter() - t0})
+    except Exception as exc:  # reported in the bench line
+        q.put({"error": f"{type(exc).__name__}: {exc}"})
+
+
 def run_ours(args, world, rank, local):
+    cpu_q = cpu_p = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        # the CPU baseline runs on one host core beside the GPU timings (it needs
+        # no GPU); started before CUDA is initialised, in a spawned process
+        import multiprocessing as mp
+        ctx = mp.get_context("spawn")
+        cpu_q = ctx.Queue()
+        cpu_p = ctx.Process(target=_cpu_baseline_worker, args=(args.workload, 4, 32, cpu_q), daemon=True)
+        cpu_p.start()
+    import ctypes
+
     import torch
     from pygimli_gb300 import _native
     from pygimli_gb300 import build as _build
@@ -334,6 +374,7 @@ def run_ours(args, world, rank, local):
     _build.build()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    L = _native.load()
     mesh, data, rho, cfg = workload(args.workload)
     t_setup = time.perf_counter()
     weights = None
@@ -344,13 +385,11 @@ def run_ours(args, world, rank, local):
     fop.setData(data)
     fop.setMesh(mesh, ignoreRegionManager=True)
     setup_s = time.perf_counter() - t_setup
-    L = _native.load()
     D, P, C = data.size(), fop.parameterCount, mesh.cellCount()
     rho_d = torch.from_numpy(rho).to(dev)
     rhoa_d = torch.empty(D, dtype=torch.float64, device=dev)
     jdt = 0 if args.precision == "fp64" else 1
     J_d = torch.empty((D, P), dtype=torch.float64 if jdt == 0 else torch.float32, device=dev)
-    import ctypes
 
     def step():
         fop._response_dev(rho_d, rhoa_d)
@@ -383,62 +422,70 @@ def run_ours(args, world, rank, local):
     total_ms = max_over_ranks(total_ms, world, dev)
     value = total_ms / 1e3 / (args.steps * world)
 
-    def time_form(precision, precond, jac_dtype, label):
-        """The same step with another solver form on the same workload (CUDA
-        events, up to 3 timed steps after 2 warm-up steps)."""
-        fop_p = ERTModelling(device=local, rtol=args.rtol, precision=precision, precond=precond)
-        fop_p.setData(data)
-        fop_p.setMesh(mesh, ignoreRegionManager=True)
-        Jp = torch.empty((D, P), dtype=torch.float64 if jac_dtype == 0 else torch.float32, device=dev)
-        rhoa_p = torch.empty(D, dtype=torch.float64, device=dev)
+    def time_form(wl, precision, precond, jac_dtype, label, weights_=None, n_steps=3, n_warm=2, ref_rhoa=None):
+        """One step of another solver form on workload ``wl`` = (mesh, data,
+        rho): CUDA events over ``n_steps`` steps after ``n_warm`` warm-up steps."""
+        m_, d_, r_ = wl
+        fop_p = ERTModelling(device=local, rtol=args.rtol, precision=precision, precond=precond, weights=weights_)
+        fop_p.setData(d_)
+        fop_p.setMesh(m_, ignoreRegionManager=True)
+        Dp, Pp, Cp = d_.size(), fop_p.parameterCount, m_.cellCount()
+        rp = torch.from_numpy(r_).to(dev)
+        Jp = torch.empty((Dp, Pp), dtype=torch.float64 if jac_dtype == 0 else torch.float32, device=dev)
+        rhoa_p = torch.empty(Dp, dtype=torch.float64, device=dev)
 
         def step_p():
-            fop_p._response_dev(rho_d, rhoa_p)
+            fop_p._response_dev(rp, rhoa_p)
             stream = torch.cuda.current_stream(dev).cuda_stream
-            fop_p._check(L.ertgb_jacobian(fop_p._ctx, ctypes.c_void_p(rho_d.data_ptr()), C,
+            fop_p._check(L.ertgb_jacobian(fop_p._ctx, ctypes.c_void_p(rp.data_ptr()), Cp,
                                           ctypes.c_void_p(Jp.data_ptr()), jac_dtype, ctypes.c_void_p(stream)))
 
-        np_steps = max(1, min(args.steps, 3))
-        for _ in range(max(1, min(args.warmup, 2))):
+        for _ in range(n_warm):
             step_p()
         torch.cuda.synchronize()
         f0 = torch.cuda.Event(enable_timing=True)
         f1 = torch.cuda.Event(enable_timing=True)
         f0.record()
-        for _ in range(np_steps):
+        for _ in range(n_steps):
             step_p()
         f1.record()
         torch.cuda.synchronize()
         stp = fop_p.stats()
-        t_p = f0.elapsed_time(f1) / 1e3 / np_steps
-        rel = float(torch.max(torch.abs(rhoa_d - rhoa_p) / torch.abs(rhoa_p)).item())
-        out = {"value": t_p, "unit": UNIT, "steps": np_steps, "solver": label,
+        out = {"value": f0.elapsed_time(f1) / 1e3 / n_steps, "unit": UNIT, "steps": n_steps, "solver": label,
                "jacobian": "FP64" if jac_dtype == 0 else "FP32 (FP64 differences)",
                "pcg_iterations": stp["iterations"], "ms_solve": stp["ms_solve"],
-               "ms_jacobian": stp["ms_jacobian"], "ratio_to_value": t_p / (total_ms / 1e3 / args.steps),
-               "max_rel_diff_rhoa_vs_value_form": rel}
+               "ms_jacobian": stp["ms_jacobian"]}
+        if ref_rhoa is not None:
+            out["max_rel_diff_rhoa_vs_headline_form"] = float(torch.max(torch.abs(ref_rhoa - rhoa_p) /
+                                                                        torch.abs(rhoa_p)).item())
+        else:
+            out["rhoa"] = rhoa_p.clone()
         del Jp, fop_p
+        torch.cuda.empty_cache()
         return out
 
-    def time_cem(precision, precond, jac_dtype, label):
-        """The total-potential operator (ERTModelling(sr=False)) on the same
-        mesh with every electrode a complete-electrode-model patch (the
-        surface triangles within one cell diagonal of it, contact impedance
-        1 Ohm m^2): one extension row per electrode; response + Jacobian,
-        1 warm-up and 1 timed step."""
+    def time_cem(wl, precision, precond, jac_dtype, label):
+        """The total-potential operator (ERTModelling(sr=False)) on workload
+        ``wl``'s mesh with every electrode a complete-electrode-model patch
+        (the surface triangles within one cell diagonal of it, contact
+        impedance 1 Ohm m^2): one extension row per electrode; response +
+        Jacobian, 1 warm-up and 1 timed step."""
         from pygimli_gb300.cem import mark_cem_electrodes
+        m_, d_, r_ = wl
         h = float(args.cem_patch)
-        mesh_c = mark_cem_electrodes(mesh, data.sensorPositions()[:, :2], h * np.sqrt(2.0) * (1.0 + 1e-6))
+        mesh_c = mark_cem_electrodes(m_, d_.sensorPositions()[:, :2], h * np.sqrt(2.0) * (1.0 + 1e-6))
         fop_c = ERTModelling(sr=False, device=local, rtol=args.rtol, precision=precision, precond=precond)
-        fop_c.setData(data)
+        fop_c.setData(d_)
         fop_c.setMesh(mesh_c, ignoreRegionManager=True)
-        Jc = torch.empty((D, P), dtype=torch.float64 if jac_dtype == 0 else torch.float32, device=dev)
-        out_c = torch.empty(D, dtype=torch.float64, device=dev)
+        Dc, Pc, Cc = d_.size(), fop_c.parameterCount, m_.cellCount()
+        rc = torch.from_numpy(r_).to(dev)
+        Jc = torch.empty((Dc, Pc), dtype=torch.float64 if jac_dtype == 0 else torch.float32, device=dev)
+        out_c = torch.empty(Dc, dtype=torch.float64, device=dev)
 
         def step_c():
-            fop_c._response_dev(rho_d, out_c)
+            fop_c._response_dev(rc, out_c)
             stream = torch.cuda.current_stream(dev).cuda_stream
-            fop_c._check(L.ertgb_jacobian(fop_c._ctx, ctypes.c_void_p(rho_d.data_ptr()), C,
+            fop_c._check(L.ertgb_jacobian(fop_c._ctx, ctypes.c_void_p(rc.data_ptr()), Cc,
                                           ctypes.c_void_p(Jc.data_ptr()), jac_dtype, ctypes.c_void_p(stream)))
 
         step_c()
@@ -457,20 +504,23 @@ def run_ours(args, world, rank, local):
                "columns_finished_fp64": stc["stalled_columns"],
                "jacobian": "FP64" if jac_dtype == 0 else "FP32 (FP64 differences)"}
         del Jc, fop_c
+        torch.cuda.empty_cache()
         return res
 
-    def time_complex(precision):
-        """Complex resistivity (IP) on the same workload: the reference's
+    def time_complex(wl, precision):
+        """Complex resistivity (IP) on workload ``wl``: the reference's
         total-potential complex formulation, block COCG + complex Jacobian;
         phases of -10 mrad on the workload's amplitudes."""
+        m_, d_, r_ = wl
         fop_c = ERTModelling(device=local, rtol=args.rtol, precision=precision)
-        fop_c.setData(data)
-        fop_c.setMesh(mesh, ignoreRegionManager=True)
+        fop_c.setData(d_)
+        fop_c.setMesh(m_, ignoreRegionManager=True)
         fop_c.setComplex(True)
-        zr = torch.from_numpy(rho * np.cos(-0.01)).to(dev)
-        zi = torch.from_numpy(rho * np.sin(-0.01)).to(dev)
-        out_c = torch.empty((2, D), dtype=torch.float64, device=dev)
-        Jc = torch.empty((D, P), dtype=torch.complex128, device=dev)
+        Dc, Cc = d_.size(), m_.cellCount()
+        zr = torch.from_numpy(r_ * np.cos(-0.01)).to(dev)
+        zi = torch.from_numpy(r_ * np.sin(-0.01)).to(dev)
+        out_c = torch.empty((2, Dc), dtype=torch.float64, device=dev)
+        Jc = torch.empty((Dc, fop_c.parameterCount), dtype=torch.complex128, device=dev)
 
         def step_c():
             stream = torch.cuda.current_stream(dev).cuda_stream
@@ -478,7 +528,7 @@ def run_ours(args, world, rank, local):
                                                   ctypes.c_void_p(zi.data_ptr()), ctypes.c_void_p(out_c[0].data_ptr()),
                                                   ctypes.c_void_p(out_c[1].data_ptr()), ctypes.c_void_p(stream)))
             fop_c._check(L.ertgb_jacobian_complex(fop_c._ctx, ctypes.c_void_p(zr.data_ptr()),
-                                                  ctypes.c_void_p(zi.data_ptr()), C, ctypes.c_void_p(Jc.data_ptr()),
+                                                  ctypes.c_void_p(zi.data_ptr()), Cc, ctypes.c_void_p(Jc.data_ptr()),
                                                   ctypes.c_void_p(stream)))
 
         step_c()
@@ -495,23 +545,48 @@ def run_ours(args, world, rank, local):
                "cocg_iterations": stc["iterations"],
                "columns_finished_fp64": stc["stalled_columns"], "jacobian": "complex FP64"}
         del Jc, fop_c
+        torch.cuda.empty_cache()
         return res
 
-    plain = fsai_form = cx_form = cem_form = None
+    wl_main = (mesh, data, rho)
+    plain = fsai_form = cx_form = cem_form = c2_forms = None
+    if not args.no_plain and (args.precision, args.precond) != ("fp64", "jacobi"):
+        plain = time_form(wl_main, "fp64", "jacobi", 0, "block PCG (Jacobi), FP64",
+                          n_steps=max(1, min(args.steps, 2)), n_warm=1, ref_rhoa=rhoa_d)
+        plain["ratio_to_value"] = plain["value"] / value
+    if not args.no_plain and args.precond == "learned":
+        fsai_form = time_form(wl_main, args.precision, "fsai", jdt, f"block PCG (FSAI), {args.precision}",
+                              ref_rhoa=rhoa_d)
+        fsai_form["ratio_to_value"] = fsai_form["value"] / value
+    # the 96-electrode configuration beside the target one, and the variants
+    # (complex resistivity, CEM electrodes) on it
+    if not args.no_plain or args.cem_only:
+        if args.workload == "box_3d":
+            wl_c2 = wl_main
+        else:
+            m2, d2, r2, _ = workload("box_3d")
+            wl_c2 = (m2, d2, r2)
+    if not args.no_plain and args.workload != "box_3d":
+        head = time_form(wl_c2, args.precision, args.precond, jdt, f"block PCG ({args.precond}), {args.precision}",
+                         weights_=default_weights("box_3d") if args.precond == "learned" else None)
+        ref2 = head.pop("rhoa")
+        c2_forms = {"workload": workload_label("box_3d", *wl_c2), "headline_form": head,
+                    "plain_fp64_gpu_pcg": time_form(wl_c2, "fp64", "jacobi", 0, "block PCG (Jacobi), FP64",
+                                                    ref_rhoa=ref2)}
+        if args.precond == "learned":
+            c2_forms["fsai_form"] = time_form(wl_c2, args.precision, "fsai", jdt,
+                                              f"block PCG (FSAI), {args.precision}", ref_rhoa=ref2)
+        c2_forms["ratio_plain_to_headline"] = c2_forms["plain_fp64_gpu_pcg"]["value"] / head["value"]
     if not args.no_plain:
-        cx_form = {"mixed": time_complex("mixed"), "fp64": time_complex("fp64")}
+        cx_form = {"workload": "box_3d", "mixed": time_complex(wl_c2, "mixed"), "fp64": time_complex(wl_c2, "fp64")}
     if (not args.no_plain or args.cem_only) and mesh.dim() == 3:
-        cem_form = {}
+        cem_form = {"workload": "box_3d"}
         for key, (prec, pc, jd, lab) in {"mixed_fsai": ("mixed", "fsai", 1, "block PCG (FSAI), mixed, total potential"),
                                         "fp64": ("fp64", "jacobi", 0, "block PCG (Jacobi), FP64, total potential")}.items():
             try:
-                cem_form[key] = time_cem(prec, pc, jd, lab)
+                cem_form[key] = time_cem(wl_c2, prec, pc, jd, lab)
             except Exception as exc:  # the record reports it; the headline line stays
                 cem_form[key] = {"error": f"{type(exc).__name__}: {exc}"}
-    if not args.no_plain and (args.precision, args.precond) != ("fp64", "jacobi"):
-        plain = time_form("fp64", "jacobi", 0, "block PCG (Jacobi), FP64")
-    if not args.no_plain and args.precond == "learned":
-        fsai_form = time_form(args.precision, "fsai", jdt, f"block PCG (FSAI), {args.precision}")
 
     # roofline of the dominant kernel (CUDA events on the context stream)
     ms = ctypes.c_double()
@@ -537,27 +612,38 @@ def run_ours(args, world, rank, local):
                 "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                 "algorithmic_bytes": d_bytes, "ms_per_launch": d_ms,
                 "tflops": d_flops / (d_ms * 1e-3) / 1e12,
-                "share_of_step": per_step[dom] / (total_ms / args.steps)}
+                "share_of_step": per_step[dom] / (total_ms / args.steps),
+                "kernels": {k: {"ms_per_launch": v[0], "algorithmic_bytes": v[1],
+                                "gbs": v[1] / (v[0] * 1e-3) / 1e9, "frac": v[1] / (v[0] * 1e-3) / 1e9 / peak}
+                            for k, v in prof.items()}}
+    del J_d
+    torch.cuda.empty_cache()
 
-    # end to end through the public API, host buffers
+    # end to end through the reference-facing C ABI with host buffers: the
+    # per-cell model copied in for the response and for the Jacobian's
+    # scaling, the apparent resistivities and the full Jacobian copied out
     e2e = None
     if not args.no_e2e:
-        Jh = torch.empty((D, P), dtype=J_d.dtype, pin_memory=True)
-        model = rho.copy()
-        tt = []
+        rho_h = np.ascontiguousarray(rho, np.float64)
+        rhoa_h = np.empty(D, np.float64)
+        Jh = torch.empty((D, P), dtype=torch.float64 if jdt == 0 else torch.float32, pin_memory=True)
+        tt, tr, its = [], [], []
         for i in range(max(1, min(args.steps, 3)) + 1):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            r = fop.response(model)
-            J = fop.createJacobian(model, dtype="float64" if jdt == 0 else "float32")
-            Jh.copy_(J, non_blocking=True)
-            torch.cuda.synchronize()
+            fop._check(L.ertgb_response_host(fop._ctx, rho_h.ctypes.data, rhoa_h.ctypes.data))
+            t1 = time.perf_counter()
+            fop._check(L.ertgb_jacobian_host(fop._ctx, rho_h.ctypes.data, C, ctypes.c_void_p(Jh.data_ptr()), jdt))
             if i > 0:
                 tt.append(time.perf_counter() - t0)
-            del J
-        e2e = {"value": float(np.mean(tt)), "unit": UNIT, "h2d_bytes_per_step": int(C * 8 + P * 8),
-               "d2h_bytes_per_step": int(D * 8 + D * P * J_d.element_size()), "steps": len(tt),
-               "check_rhoa_vs_device": float(np.max(np.abs(r - rhoa_d.cpu().numpy()) / r))}
+                tr.append(t1 - t0)
+                its.append(fop.stats()["iterations"])
+        e2e = {"value": float(np.mean(tt)), "unit": UNIT, "h2d_bytes_per_step": int(2 * C * 8),
+               "d2h_bytes_per_step": int(D * 8 + D * P * Jh.element_size()), "steps": len(tt),
+               "path": "ertgb_response_host + ertgb_jacobian_host (host buffers; J into pinned memory)",
+               "response_s": float(np.mean(tr)), "jacobian_with_copy_s": float(np.mean(tt) - np.mean(tr)),
+               "pcg_iterations": its,
+               "check_rhoa_vs_device": float(np.max(np.abs(rhoa_h - rhoa_d.cpu().numpy()) / rhoa_h))}
         del Jh
 
     gn = None
@@ -581,11 +667,17 @@ def run_ours(args, world, rank, local):
         del mh
 
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        from oracle.cpu_baseline import SampledBaseline
-        base = SampledBaseline(mesh, data, fop.kValues(), fop.weights())
-        t, desc = base.step(rho, n_src=4, n_rows=32, threads=1)
-        cpu = {"value": t, "unit": UNIT, "cores": 1, "kind": "port", "sample": desc}
+    if cpu_p is not None:
+        try:
+            r = cpu_q.get(timeout=600)
+        except Exception as exc:  # queue.Empty: the baseline did not finish in time
+            r = {"error": f"CPU baseline did not finish: {type(exc).__name__}"}
+        cpu_p.join(timeout=5)
+        if "error" in r:
+            cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "port", "sample": r["error"]}
+        else:
+            cpu = {"value": r["value"], "unit": UNIT, "cores": 1, "kind": "port",
+                   "sample": r["desc"] + f"; sample wall {r['wall_s']:.1f} s (ran beside the GPU timings)"}
 
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -597,10 +689,11 @@ def run_ours(args, world, rank, local):
                               solver=f"block PCG ({args.precond}), {args.precision}",
                               jacobian="FP64" if jdt == 0 else "FP32 (FP64 differences)",
                               rtol=args.rtol, l2="working set > L2: PCG blocks 4 x "
-                              f"{mesh.nodeCount() * 96 * 8 / 1e6:.0f} MB, J {D * P * 8 / 1e9:.1f} GB"),
+                              f"{mesh.nodeCount() * fop.sizes()[3] * 8 / 1e6:.0f} MB, J "
+                              f"{D * P * (8 if jdt == 0 else 4) / 1e9:.1f} GB"),
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-               "plain_fp64_gpu_pcg": plain, "fsai_form": fsai_form, "gn_iteration": gn,
-               "refine_h2": refine_rec, "complex_form": cx_form, "cem_form": cem_form,
+               "plain_fp64_gpu_pcg": plain, "fsai_form": fsai_form, "box_3d_forms": c2_forms,
+               "gn_iteration": gn, "refine_h2": refine_rec, "complex_form": cx_form, "cem_form": cem_form,
                "learned_weights": os.path.relpath(weights, ROOT) if weights else None,
                "clocks": clk, "step_ms": step_ms,
                "breakdown_ms": {"assemble": st["ms_assemble"], "rhs": st["ms_rhs"], "solve": st["ms_solve"],

@@ -128,6 +128,7 @@ __global__ void __launch_bounds__(256) k_spmm32_dot(int64_t n, int64_t nnz, int 
 // DOT: 0 = column dots p . q (the PCG operator), 1 = none, 2 = w . q.
 constexpr int kQThreads = 256;
 constexpr int kQGroups = kQThreads / 8;
+constexpr int kQTileRows = 128;  // rows per tile of the FP32 operator (a multiple of kQGroups)
 
 template <int CH, int DOT>
 __global__ void __launch_bounds__(kQThreads, 2) k_spmm32_q(int64_t n, int64_t Rpad, const int32_t *__restrict__ rowptr,
@@ -138,13 +139,16 @@ __global__ void __launch_bounds__(kQThreads, 2) k_spmm32_q(int64_t n, int64_t Rp
     __shared__ float red[DOT == 1 ? 1 : kQGroups][DOT == 1 ? 1 : 32 * CH + 1];
     const int l8 = threadIdx.x & 7, g = threadIdx.x >> 3;
     const int64_t t0 = (int64_t)blockIdx.y * 32 * CH + l8 * 4;
-    const int64_t per_block = (n + gridDim.x - 1) / gridDim.x;
-    const int64_t r_begin = (int64_t)blockIdx.x * per_block;
-    const int64_t r_end = min(n, r_begin + per_block);
     float4 dot[CH];
 #pragma unroll
     for (int j = 0; j < CH; j++) dot[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int64_t row = r_begin + g; row < r_end; row += kQGroups) {
+    // tiles of kQTileRows consecutive rows in grid-stride order: the rows in
+    // flight at a time form one window of consecutive rows, so the rows of p
+    // that neighbouring matrix rows share stay in L2 when p exceeds it
+    const int64_t ntile = (n + kQTileRows - 1) / kQTileRows;
+    for (int64_t tile = blockIdx.x; tile < ntile; tile += gridDim.x)
+    for (int64_t row = tile * kQTileRows + g, r_end = min(n, (tile + 1) * kQTileRows); row < r_end;
+         row += kQGroups) {
         float4 acc[CH];
 #pragma unroll
         for (int j = 0; j < CH; j++) acc[j] = make_float4(0.f, 0.f, 0.f, 0.f);

@@ -105,6 +105,7 @@ class ERTModelling:
         self._k = None
         self._w = None
         self._kw_user = False
+        self._topo = False        # forward mesh surface is not flat (set by setMesh)
         self._J = None
         self._elec_nodes = None
         self._last_model = None
@@ -254,6 +255,7 @@ class ERTModelling:
             _ptr(mesh.boundary_markers), _ptr(mesh.boundary_cells)))
         self._mesh = mesh
         self._surface_z = surf
+        self._topo = bool(topo)
         self._J = None
         if self._data is not None:
             self._update_data()
@@ -327,6 +329,12 @@ class ERTModelling:
         if data.size() == 0:
             raise ValueError("data container is empty")
         if np.min(np.abs(kf)) < TOLERANCE:
+            # the reference computes missing factors analytically only for a flat
+            # surface without CEM electrodes (DCMultiElectrodeModelling::response,
+            # core/src/bert/dcfemmodelling.cpp:1088-1097)
+            if self._topo or (self._electrodes is not None and self._electrodes.cem):
+                raise ValueError("data contains no K-factors (topography or complete electrode model: "
+                                 "give them, e.g. from calcGeometricFactor)")
             kf = self.calcGeometricFactor(data)
             data.set("k", kf)
         ab = np.ascontiguousarray(data.abmn(), np.int32)
@@ -447,13 +455,32 @@ class ERTModelling:
         return J
 
     def calcGeometricFactor(self, data=None):
-        """Analytic geometric factors (flat surface, calcGeometricFactor,
-        core/src/bert/dcfemmodelling.cpp:1527-1557).  With CEM electrodes the
-        reference needs them given (response, :1088-1097)."""
+        """Geometric factors (DCMultiElectrodeModelling::calcGeometricFactor,
+        core/src/bert/dcfemmodelling.cpp:1527-1557): analytic half-space
+        factors for a flat surface without CEM electrodes, otherwise
+        numerical ones, 1 / (u + 1e-12) with u the voltages of this operator
+        (its formulation, forward mesh, electrodes and contact impedances) for
+        a unit resistivity."""
         data = self._data if data is None else data
-        if self._electrodes is not None and self._electrodes.cem:
-            raise ValueError("data contains no K-factors: the complete electrode model needs them given")
-        return geometricFactors(data, self._mesh.dim())
+        cem = self._electrodes is not None and self._electrodes.cem
+        if not (getattr(self, "_topo", False) or cem):
+            return geometricFactors(data, self._mesh.dim())
+        fop = ERTModelling(sr=self._sr, device=self.device, rtol=self._rtol, maxIter=self._maxIter,
+                           precision=self.precision)
+        if self._contact_z is not None:
+            fop.setContactImpedances(self._contact_z)
+        if self._bypass_r is not None:
+            fop.setBypassResistances(self._bypass_r)
+        if self._kw_user:
+            fop.setkValues(self._k)
+            fop.setWeights(self._w)
+        unit = data.copy()
+        unit.set("k", np.ones(unit.size()))
+        fop.setData(unit)
+        fop.setMesh(self._mesh, ignoreRegionManager=True)
+        fop.response(np.ones(self._mesh.cellCount()))
+        u = datamap_voltages(fop.electrodePotentials(), data.abmn())
+        return 1.0 / (u + TOLERANCE)
 
     def mapERTModel(self, model, background=-9e99):
         fixed = self._rm.fixedValues() if self._rm is not None else None

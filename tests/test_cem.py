@@ -254,7 +254,9 @@ def test_total_potential_golden(torch, golden_dir, name, form):
 def test_total_potential_guards(torch, golden_dir):
     """Refusals of the formulation: the SR operator on a CEM mesh, the
     learned preconditioner and complex resistivity with a matrix extension,
-    numerical geometric factors with CEM."""
+    data without geometric factors on a CEM mesh (the reference's response
+    refuses them, dcfemmodelling.cpp:1088-1097); calcGeometricFactor there
+    gives numerical factors: unit resistivity then has apparent resistivity 1."""
     from pygimli_gb300 import ERTModelling
     z, mesh, zc = load(golden_dir, "ert3d_cem_small")
     data = DataContainerERT(z["sensors"], z["abmn"])
@@ -268,8 +270,16 @@ def test_total_potential_guards(torch, golden_dir):
     with pytest.raises(RuntimeError):
         fop.response(z["rho"])
     fop = _fop(z, mesh, zc)
-    with pytest.raises(ValueError):
-        fop.calcGeometricFactor()
+    bare = DataContainerERT(z["sensors"], z["abmn"])
+    with pytest.raises(ValueError, match="no K-factors"):
+        fop.setData(bare)
+    fop = _fop(z, mesh, zc)
+    k_num = fop.calcGeometricFactor()
+    unit = DataContainerERT(z["sensors"], z["abmn"])
+    unit.set("k", k_num)
+    fop.setData(unit)
+    rhoa = fop.response(np.ones(mesh.cellCount()))
+    assert np.max(np.abs(rhoa - 1.0)) <= 1e-6
     fop.setComplex(True)
     with pytest.raises(RuntimeError):
         fop.response(np.concatenate([z["rho"], -0.01 * z["rho"]]))
@@ -295,3 +305,30 @@ def test_simulate_calc_only_and_numerical_factors(torch, golden_dir, name):
     assert np.max(np.abs(k_num - k_ref) / np.abs(k_ref)) <= 1e-8
     sol = simulate(mesh, scheme, z["rho"], sr=False, calcOnly=True, returnFields=True)
     assert sol.shape == (scheme.sensorCount(), mesh.nodeCount())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", TOPO)
+def test_numerical_factors_on_topography(torch, golden_dir, name):
+    """On a topographic surface the operator refuses data without geometric
+    factors (the reference computes them analytically only for a flat
+    surface) and calcGeometricFactor gives the numerical ones: 1 / (u + 1e-12)
+    with u the voltages at unit resistivity, pinned to the reference's own
+    unit-resistivity electrode potentials (core/src/bert/dcfemmodelling.cpp:
+    1527-1557)."""
+    from pygimli_gb300 import ERTModelling
+    from pygimli_gb300.ert import datamap_voltages
+    z, mesh, _ = load(golden_dir, name)
+    fop = ERTModelling(sr=False)
+    fop.setkValues(z["k"])
+    fop.setWeights(z["w"])
+    with pytest.raises(ValueError, match="no K-factors"):
+        fop.setData(DataContainerERT(z["sensors"], z["abmn"]))
+        fop.setMesh(mesh, ignoreRegionManager=True)
+    data = DataContainerERT(z["sensors"], z["abmn"])
+    data.set("k", np.ones(data.size()))
+    fop.setData(data)
+    fop.setMesh(mesh, ignoreRegionManager=True)
+    k_num = fop.calcGeometricFactor(DataContainerERT(z["sensors"], z["abmn"]))
+    k_ref = 1.0 / (datamap_voltages(z["U1"], z["abmn"]) + 1e-12)
+    assert np.max(np.abs(k_num - k_ref) / np.abs(k_ref)) <= 1e-8
