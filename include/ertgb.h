@@ -152,6 +152,25 @@ int ertgb_set_extension(ertgb_ctx *ctx, int n_ext, int64_t n_entries, const int3
  * (core/src/bert/dcfemmodelling.h:239-243). */
 int ertgb_set_kw(ertgb_ctx *ctx, int n_k, const double *k_host, const double *w_host);
 
+/* Unit primary potentials for singularity removal (host, n_k x n_elec x
+ * n_nodes, node fastest), used instead of the analytic half-space
+ * potentials until the mesh, electrodes or wavenumbers change: the numerical
+ * primaries of a topographic surface.  Replaces setPrimaryPotential
+ * (core/src/bert/dcfemmodelling.h:374) and the topography branch of
+ * DCSRMultiElectrodeModelling::checkPrimpotentials_
+ * (core/src/bert/dcfemmodelling.cpp:2008-2068), whose total-potential solve
+ * on createP2 the caller runs (ERTModelling does it on the GPU). */
+int ertgb_set_primary(ertgb_ctx *ctx, int n_k, int n_elec, int64_t n_nodes, const double *up_host);
+
+/* Potentials of a homogeneous model of resistivity rho without a solve: the
+ * analytic half-space potentials of every source (with the source node's
+ * singular value) times rho, as the sub-potentials of the next Jacobian.
+ * Replaces the analytic branch of prepareJacobianT_
+ * (core/src/bert/dcfemmodelling.cpp:1262-1301: createJacobian before any
+ * response on a model with standard deviation <= 1e-7, calculateKAnalyt
+ * 1737-1753, scaled by model[0]).  Node electrodes, flat surface. */
+int ertgb_analytic_potentials(ertgb_ctx *ctx, double rho);
+
 /* Measurement scheme: the a b m n columns (-1 = at infinity) and geometric
  * factors k of DataContainerERT (core/src/bert/bertDataContainer.h:62),
  * as read by DataMap::data (core/src/bert/datamap.cpp:159-231). */

@@ -329,7 +329,10 @@ class Problem:
     """Mesh + electrodes + scheme with everything that does not depend on the
     resistivity model precomputed."""
 
-    def __init__(self, mesh, sensors, abmn, kfac, k=None, w=None):
+    def __init__(self, mesh, sensors, abmn, kfac, k=None, w=None, primary=None):
+        """``primary``: unit primary potentials u_p[kIdx, e, node] given (the
+        numerical ones of a topographic surface, ``numerical_primary``);
+        default the analytic half-space potentials."""
         self.mesh = mesh
         self.dim = mesh.dim()
         nodes = mesh.nodes
@@ -362,7 +365,10 @@ class Problem:
         self.alpha = [mixed_bc_alpha(self.dim, self.bnd_c, self.bnd_n, self.src_center, kk)
                       for kk in self.k]
         self._slot_maps()
-        self.up = self._primary()
+        if primary is not None:
+            self.up = np.asarray(primary, np.float64).reshape(len(self.k), self.nE, self.n).copy()
+        else:
+            self.up = self._primary()
 
     # electrode search (dcfemmodelling.cpp:790-1030), node electrodes only
     def _search_electrodes(self, sensors):
@@ -700,3 +706,23 @@ def prolongate_empty(mesh, vals, background):
             raise ValueError("cannot prolongate empty cells")
         for c, v in upd.items():
             vals[c] = v
+
+
+def numerical_primary(mesh, sensors, abmn, kfac, k, w):
+    """Unit primary potentials of a topographic surface
+    (DCSRMultiElectrodeModelling::checkPrimpotentials_,
+    core/src/bert/dcfemmodelling.cpp:2008-2068): the total potential at 1
+    Ohm m on createP2 of the mesh (cem_oracle.TotalPotentialProblem, direct
+    solve), taken at the mesh's own nodes (createP2 keeps them first; the
+    reference's interpolation to a vertex is its nodal value).
+    Returns u_p[kIdx, e, node]."""
+    import os
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    if here not in sys.path:
+        sys.path.insert(0, here)
+    from cem_oracle import TotalPotentialProblem
+    m2 = mesh.createP2()
+    T = TotalPotentialProblem(m2, sensors, abmn, kfac, k, w)
+    u = T.solve(np.ones(m2.cellCount()))
+    return u[:, :, :mesh.nodeCount()].copy()

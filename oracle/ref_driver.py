@@ -60,6 +60,7 @@ def lib():
         L.ref_response_complex.argtypes = [vp, vp, ctypes.c_int, vp]
         L.ref_jacobian_complex.argtypes = [vp, vp, ctypes.c_int, vp, vp, vp, vp]
         L.ref_set_kw.argtypes = [vp, ctypes.c_int, vp, vp]
+        L.ref_set_primary.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp]
         L.ref_kw_count.argtypes = [vp]
         L.ref_get_kw.argtypes = [vp, vp, vp]
         L.ref_electrode_nodes.argtypes = [vp, vp]
@@ -252,6 +253,13 @@ class RefModelling:
         self.matrices = []
         _check(lib().ref_response(self.h, _p(m), len(m), _p(out)))
         return out
+
+    def set_primary(self, prim):
+        """Primary potentials (rows = source + k * nE, cols = nodes) for the
+        singularity-removal operator (setPrimaryPotential)."""
+        P = np.ascontiguousarray(prim, np.float64)
+        self._prim = P
+        _check(lib().ref_set_primary(self.h, P.shape[0], P.shape[1], _p(P)))
 
     def subpotentials(self):
         r = ctypes.c_int()

@@ -123,6 +123,7 @@ struct RefHandle {
     void (*detach)(DCMultiElectrodeModelling *) = nullptr;
     CallbackSolver *solver = nullptr;
     RMatrix subpots;          // collected sub-potentials (nE*nK x nNodes)
+    RMatrix prim;             // primary potentials given to the singularity-removal operator
     RefHandle(int dim) : mesh(dim) {}
     ~RefHandle() { delete fop; delete solver; }
 };
@@ -256,6 +257,22 @@ int ref_mesh_arrays(void *hp, double *xyz, int *nodeMarker, int *cells, int *cel
             for (Index j = 0; j < bd.nodeCount(); j++) bnd[b * bd.nodeCount() + j] = (int)bd.node(j).id();
             bndMarker[b] = bd.marker();
         }
+    });
+}
+
+// Primary potentials of the singularity-removal operator given by the caller
+// (rows = current source + wavenumber * sources, cols = nodes): the
+// reference's setPrimaryPotential (core/src/bert/dcfemmodelling.h:374);
+// checkPrimpotentials_ (dcfemmodelling.cpp:1986-2141) then takes them as they are.
+int ref_set_primary(void *hp, int rows, int cols, const double *P) {
+    RefHandle *h = (RefHandle *)hp;
+    return guarded([&] {
+        auto *sr = dynamic_cast<DCSRMultiElectrodeModelling *>(h->fop);
+        if (!sr) throwError("primary potentials need the singularity-removal operator");
+        h->prim.resize(rows, cols);
+        for (int i = 0; i < rows; i++)
+            for (int j = 0; j < cols; j++) h->prim[i][j] = P[(size_t)i * cols + j];
+        sr->setPrimaryPotential(h->prim);
     });
 }
 

@@ -52,6 +52,8 @@ SIGNATURES = {
     "ertgb_set_mesh": (_ci, [_vp, _ci, _ci, _ci, _vp, _ci, _vp, _vp, _ci, _vp, _vp, _vp]),
     "ertgb_set_electrodes": (_ci, [_vp, _ci, _vp, _d]),
     "ertgb_set_kw": (_ci, [_vp, _ci, _vp, _vp]),
+    "ertgb_set_primary": (_ci, [_vp, _ci, _ci, _i64, _vp]),
+    "ertgb_analytic_potentials": (_ci, [_vp, _d]),
     "ertgb_set_scheme": (_ci, [_vp, _ci, _vp, _vp]),
     "ertgb_set_solver": (_ci, [_vp, _d, _ci, _ci]),
     "ertgb_set_precision": (_ci, [_vp, _ci]),

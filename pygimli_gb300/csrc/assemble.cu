@@ -718,6 +718,38 @@ void compute_primary(Context &c) {
     ERTGB_CUDA(cudaGetLastError());
 }
 
+__global__ void k_scale(int64_t total, double f, double *__restrict__ x) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] *= f;
+}
+
+void analytic_potentials(Context &c, double rho, double *out) {
+    MeshData &m = c.mesh;
+    const int fullspace = (c.surface_z == -DBL_MAX || std::isnan(c.surface_z)) ? 1 : 0;
+    const int64_t total = m.n * c.Rpad;
+    k_primary<<<grid1(total, kThreads, 1 << 16), kThreads, 0, c.stream>>>(
+        m.n, c.nE, c.nK, c.Rpad, m.d_xyz.p, c.d_epos.p, c.d_enode.p, c.d_emin_r.p, c.d_k.p, c.surface_z, fullspace,
+        out);
+    ERTGB_CUDA(cudaGetLastError());
+    k_scale<<<grid1(total, kThreads, 1 << 16), kThreads, 0, c.stream>>>(total, rho, out);
+    ERTGB_CUDA(cudaGetLastError());
+}
+
+void upload_primary(Context &c) {
+    MeshData &m = c.mesh;
+    const int64_t n = m.n;
+    std::vector<double> tmp((size_t)n * c.Rpad, 0.0);
+    for (int ki = 0; ki < c.nK; ki++)
+        for (int e = 0; e < c.nE; e++) {
+            const double *src = c.up_user.data() + ((size_t)ki * c.nE + e) * n;
+            const int64_t t = (int64_t)ki * c.nE + e;
+            for (int64_t i = 0; i < n; i++) tmp[(size_t)i * c.Rpad + t] = src[i];
+        }
+    c.d_up.alloc((size_t)n * c.Rpad);
+    ERTGB_CUDA(cudaMemcpyAsync(c.d_up.p, tmp.data(), sizeof(double) * tmp.size(), cudaMemcpyHostToDevice, c.stream));
+    ERTGB_CUDA(cudaStreamSynchronize(c.stream));
+}
+
 void assemble_all(Context &c, const double *rho_cell, double *vals, cudaStream_t s) {
     MeshData &m = c.mesh;
     dim3 grid(grid1(m.nnz, kThreads, 1 << 16), c.nK);

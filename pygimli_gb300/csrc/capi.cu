@@ -50,6 +50,7 @@ template <class F> int guard(Context *c, F &&f) {
 
 void invalidate_derived(Context &c) {
     c.fp64_k.clear();
+    c.up_user.clear();  // given primaries belong to the mesh, electrodes and wavenumbers they were set for
     c.prim_ready = false;
     c.s1_ready = false;
     c.have_pot = false;
@@ -113,6 +114,7 @@ void ensure_derived(Context &c) {
         c.Rpad = ceil_div(c.R, c.rhs_align) * c.rhs_align;
         compute_boundary_alpha(c);
         if (total) c.d_up.release();  // no primary field
+        else if (!c.up_user.empty()) upload_primary(c);
         else compute_primary(c);
         c.prim_ready = true;
         c.s1_ready = false;
@@ -434,6 +436,43 @@ int ertgb_set_extension(ertgb_ctx *ctx, int n_ext, int64_t n_entries, const int3
         c->collect_last_k = collect_last_k != 0;
         ERTGB_CUDA(cudaStreamSynchronize(c->stream));
         invalidate_derived(*c);
+    });
+}
+
+int ertgb_analytic_potentials(ertgb_ctx *ctx, double rho) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        ERTGB_REQUIRE(std::isfinite(rho) && rho > 0.0, "resistivity must be positive");
+        ensure_derived(*c);
+        if (c->mesh.n_ext > 0 || !c->mesh.ext_rows.empty())
+            throw Error(ERTGB_STATE, "no analytic potentials with complete-electrode-model or bypass electrodes");
+        if (!c->up_user.empty())
+            throw Error(ERTGB_STATE, "no analytic potentials on a topographic surface");
+        for (int32_t v : c->enode)
+            if (v < 0) throw Error(ERTGB_STATE, "analytic potentials need node electrodes");
+        c->d_x.alloc((size_t)c->mesh.n * c->Rpad);
+        analytic_potentials(*c, rho, c->d_x.p);
+        ERTGB_CUDA(cudaStreamSynchronize(c->stream));
+        c->have_pot = true;
+    });
+}
+
+int ertgb_set_primary(ertgb_ctx *ctx, int n_k, int n_elec, int64_t n_nodes, const double *up) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        if (c->formulation != ERTGB_FORMULATION_SINGULARITY_REMOVAL)
+            throw Error(ERTGB_STATE, "primary potentials belong to the singularity-removal formulation");
+        if (!c->have_mesh || !c->have_elec || !c->have_kw)
+            throw Error(ERTGB_STATE, "set mesh, electrodes and wavenumbers before the primary potentials");
+        ERTGB_REQUIRE(up, "null buffer");
+        ERTGB_REQUIRE(n_k == c->nK && n_elec == c->nE && n_nodes == c->mesh.n,
+                      "primary potentials must be n_k x n_elec x n_nodes of the context");
+        const size_t total = (size_t)n_k * n_elec * n_nodes;
+        for (size_t i = 0; i < total; i++) ERTGB_REQUIRE(std::isfinite(up[i]), "non-finite primary potential");
+        c->up_user.assign(up, up + total);
+        c->prim_ready = false;
+        c->have_pot = false;
+        c->have_S = false;
     });
 }
 

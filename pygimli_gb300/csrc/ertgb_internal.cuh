@@ -228,6 +228,7 @@ struct Context {
     bool prim_ready = false;
     DBuf<double> d_alpha;         // nK x B mixed-boundary coefficients
     DBuf<double> d_up;            // unit primary potential  n x Rpad
+    std::vector<double> up_user;  // given unit primary potentials (nK x nE x n), empty: analytic
     DBuf<double> d_S1;            // nK x nnz (unit resistivity)
     bool s1_ready = false;
     // per response
@@ -266,6 +267,11 @@ struct Context {
 void build_mesh_device(Context &c);
 void compute_boundary_alpha(Context &c);
 void compute_primary(Context &c);
+// given primary potentials (c.up_user, nK x nE x n) into d_up (n x Rpad)
+void upload_primary(Context &c);
+// analytic half-space potentials of every source (the unit primaries, with
+// the source node's singular value) times rho into out (n x Rpad)
+void analytic_potentials(Context &c, double rho, double *out);
 void assemble_all(Context &c, const double *rho_cell, double *vals_out, cudaStream_t s);
 void assemble_unit(Context &c, cudaStream_t s);
 void compute_source_rho(Context &c, const double *rho_cell, cudaStream_t s);

@@ -241,10 +241,9 @@ class ERTModelling:
 
     def _set_fwd_mesh(self, mesh):
         surf, topo = surface_info(mesh)
-        if topo and self._sr:
-            raise NotImplementedError("meshes with topography need numerical primary potentials for singularity "
-                                      "removal (not supported); the total-potential operator "
-                                      "ERTModelling(sr=False) takes them")
+        if topo and self._sr and mesh.order != 1:
+            raise NotImplementedError("singularity removal on a topographic surface computes its primary "
+                                      "potentials on createP2 of the mesh: the mesh must be linear")
         bm = mesh.boundary_markers
         if mesh.dim() == 3 and not np.any(bm == MARKER_BOUND_MIXED):
             raise NotImplementedError("Neumann-only domains are not supported")
@@ -316,7 +315,33 @@ class ERTModelling:
         if not self._kw_user:
             self._k, self._w = init_kwave_list(mesh.dim(), data.sensorPositions())
         self._push_kw()
+        if self._sr and self._topo:
+            self._push_numerical_primary()
         self._push_scheme()
+
+    def _push_numerical_primary(self):
+        """Primary potentials of singularity removal on a topographic surface
+        (DCSRMultiElectrodeModelling::checkPrimpotentials_, core/src/bert/
+        dcfemmodelling.cpp:2008-2068): the total potential at 1 Ohm m on
+        createP2 of the forward mesh (GPU refinement, total-potential operator
+        in FP64 to rtol 1e-12, this operator's wavenumbers), taken at the
+        forward mesh's nodes, which createP2 keeps first (the reference's
+        interpolation to a vertex is its nodal value)."""
+        from . import refine
+        mesh = self._mesh
+        m2 = refine.createP2(mesh, self.device)
+        fop = ERTModelling(sr=False, device=self.device, rtol=1e-12, maxIter=max(self._maxIter, 100000),
+                           precision="fp64")
+        fop.setkValues(self._k)
+        fop.setWeights(self._w)
+        unit = self._data.copy()
+        unit.set("k", np.ones(unit.size()))
+        fop.setData(unit)
+        fop.setMesh(m2, ignoreRegionManager=True)
+        fop.response(np.ones(m2.cellCount()))
+        up = np.ascontiguousarray(fop.subPotentials()[:, :, :mesh.nodeCount()])
+        del fop
+        self._check(self._lib.ertgb_set_primary(self._ctx, up.shape[0], up.shape[1], up.shape[2], _ptr(up)))
 
     def _push_kw(self):
         k = np.ascontiguousarray(self._k, np.float64)
@@ -601,11 +626,33 @@ class ERTModelling:
             md = torch.from_numpy(np.ascontiguousarray(model, np.float64)).to(dev)
         J = torch.empty((D, P), dtype=tdt, device=dev)
         stream = torch.cuda.current_stream(dev).cuda_stream
-        self._check(self._lib.ertgb_jacobian(self._ctx, ctypes.c_void_p(md.data_ptr()), int(md.numel()),
-                                             ctypes.c_void_p(J.data_ptr()), 0 if tdt == torch.float64 else 1,
-                                             ctypes.c_void_p(stream)))
+
+        def run():
+            return self._lib.ertgb_jacobian(self._ctx, ctypes.c_void_p(md.data_ptr()), int(md.numel()),
+                                            ctypes.c_void_p(J.data_ptr()), 0 if tdt == torch.float64 else 1,
+                                            ctypes.c_void_p(stream))
+
+        rc = run()
+        if rc == _native.STATE:
+            self._potentials_for_jacobian(md.cpu().numpy() if isinstance(model, torch.Tensor) else model)
+            rc = run()
+        self._check(rc)
         self._J = J
         return J
+
+    def _potentials_for_jacobian(self, model):
+        """Sub-potentials for a Jacobian requested before any response
+        (prepareJacobianT_, core/src/bert/dcfemmodelling.cpp:1262-1301): for a
+        homogeneous model (standard deviation <= 1e-7) on a flat surface
+        without CEM electrodes the analytic half-space potentials scaled by
+        model[0]; otherwise the potentials of a response to the model."""
+        m = np.asarray(model, np.float64).ravel()
+        sd = float(np.std(m, ddof=1)) if m.size > 1 else 0.0
+        cem = self._electrodes is not None and (self._electrodes.cem or len(self._electrodes.rows) > 0)
+        if sd <= TOLERANCE * 1e5 and not self._topo and not cem:
+            self._check(self._lib.ertgb_analytic_potentials(self._ctx, float(m[0])))
+        else:
+            self.response(model)
 
     def jacobian(self):
         return self._J
