@@ -110,9 +110,22 @@ int ertgb_set_mesh(ertgb_ctx *ctx, int dim, int order, int n_nodes, const double
  * (updateMeshDependency_, :727-745).  Replaces that search's results; the
  * mean electrode position (sourceCenterPos_, :1026-1030), the singular
  * radii (core/src/bert/electrode.cpp:154-197) and the incident cells
- * (electrode.cpp:102-127) are derived here. */
+ * (electrode.cpp:102-127) are derived here.  Node -1: an electrode given by
+ * a matrix extension row (ertgb_set_extension) or by the cell that holds it
+ * (ertgb_set_electrode_shapes). */
 int ertgb_set_electrodes(ertgb_ctx *ctx, int n_elec, const int32_t *elec_node_host,
                          double surface_z);
+
+/* Electrodes that are not mesh nodes (after ertgb_set_electrodes, which gives
+ * them node -1): cell_host[e] >= 0 is the cell holding electrode e (linear
+ * cells), pos_host[3e..3e+2] its position in mesh coordinates; -1 keeps the
+ * node electrode.  The source enters with the cell's shape functions at the
+ * position, the electrode potential is the interpolation there, the source
+ * resistivity of singularity removal is the cell's.  Replaces
+ * ElectrodeShapeEntity (core/src/bert/electrode.cpp:252-290) as chosen by
+ * DCMultiElectrodeModelling::searchElectrodes_
+ * (core/src/bert/dcfemmodelling.cpp:924-937). */
+int ertgb_set_electrode_shapes(ertgb_ctx *ctx, int n_elec, const int32_t *cell_host, const double *pos_host);
 
 /* Formulation of the forward operator.  SINGULARITY_REMOVAL (default):
  * DCSRMultiElectrodeModelling, pyGIMLi ERTModelling(sr=True)

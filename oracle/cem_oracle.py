@@ -46,7 +46,7 @@ import scipy.sparse as sp
 import scipy.sparse.linalg as spla
 
 from ert_oracle import (TOLERANCE, Problem, _p2_shape, _rule_tet_deg4, _rule_tri_deg4, boundary_center_normal,
-                        boundary_mass, element_matrices, mixed_bc_alpha, sparsity_pattern)
+                        boundary_mass, element_matrices, find_cell, mixed_bc_alpha, sparsity_pattern)
 
 MARKER_BOUND_ELECTRODE = -10000
 MARKER_FIXEDVALUE_REGION = -1000000
@@ -178,7 +178,12 @@ def search_electrodes(mesh, sensors):
                     hit = Electrode("node", mesh.nodes[nd], node=int(nd))
                     break
         if hit is None:
-            raise ValueError("There is a requested electrode that does not match the given mesh.")
+            # no electrode node: the cell that holds the sensor (ElectrodeShapeEntity)
+            cell, wts = find_cell(mesh, p)
+            if cell < 0:
+                raise ValueError("There is a requested electrode that does not match the given mesh.")
+            hit = Electrode("entity", p.copy())
+            hit.rows, hit.wts = mesh.cells[cell].astype(np.int64), wts
         electrodes.append(hit)
     return electrodes, passive, bypass_markers
 
@@ -273,6 +278,11 @@ class TotalPotentialProblem:
             self.src_row = self.n + np.arange(self.nE)
         else:
             self.src_row = np.array([e.node for e in self.electrodes], np.int64)
+        # source / collect weights per electrode: its row, or an entity electrode's cell nodes
+        self.erows = [getattr(e, "rows", None) if e.kind == "entity" else np.array([self.src_row[i]])
+                      for i, e in enumerate(self.electrodes)]
+        self.ewts = [getattr(e, "wts", None) if e.kind == "entity" else np.ones(1)
+                     for e in self.electrodes]
         bm = mesh.boundary_markers
         self.mixed = np.nonzero(bm == -2)[0]
         bnd = mesh.boundaries[self.mixed]
@@ -311,7 +321,7 @@ class TotalPotentialProblem:
             lu = spla.splu(self.matrix(rho_cell, ki).tocsc(), permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=0.0)
             for e in range(self.nE):
                 rhs = np.zeros(self.N)
-                rhs[self.src_row[e]] = 1.0
+                rhs[self.erows[e]] = self.ewts[e]
                 u[ki, e] = lu.solve(rhs)
         return u
 
@@ -319,7 +329,7 @@ class TotalPotentialProblem:
         if self.cem:
             return u[-1][:, self.src_row].copy()
         sol = np.einsum("k,ken->en", self.w, u)
-        return sol[:, self.src_row]
+        return np.stack([sol[:, r] @ w for r, w in zip(self.erows, self.ewts)], axis=1)
 
     def response(self, rho_cell):
         if np.min(rho_cell) < TOLERANCE:

@@ -325,6 +325,24 @@ def sparsity_pattern(n, cells):
     return rowptr, cols
 
 
+def find_cell(mesh, p, tol=1e-12):
+    """Cell that holds point p (linear triangles / tetrahedra) and the cell's
+    shape functions at p (barycentric coordinates): the lowest cell index
+    whose coordinates are all >= -tol.  (-1, None) if none."""
+    d = mesh.dim()
+    if mesh.cells.shape[1] != d + 1:
+        raise NotImplementedError("electrodes inside cells need linear cells")
+    x = mesh.nodes[mesh.cells][:, :, :d]                       # C x (d+1) x d
+    A = np.transpose(x[:, 1:, :] - x[:, :1, :], (0, 2, 1))      # C x d x d
+    rhs = p[:d][None, :] - x[:, 0, :]
+    lam = np.linalg.solve(A, rhs[:, :, None])[:, :, 0]
+    bary = np.column_stack([1.0 - lam.sum(axis=1), lam])
+    ok = np.nonzero(np.all(bary >= -tol, axis=1))[0]
+    if len(ok) == 0:
+        return -1, None
+    return int(ok[0]), bary[ok[0]]
+
+
 class Problem:
     """Mesh + electrodes + scheme with everything that does not depend on the
     resistivity model precomputed."""
@@ -380,25 +398,44 @@ class Problem:
             if zvar and not yvar and np.max(np.abs(ePos[:, 1])) < 1e-8:
                 ePos[:, [1, 2]] = ePos[:, [2, 1]]
         cand = list(np.nonzero(mesh.node_markers == -99)[0])
-        enodes = []
+        enodes, epos, erows, ewts, ecell_ent = [], [], [], [], []
         for p in ePos:
             hit = None
             for j, nid in enumerate(cand):
                 if np.linalg.norm(p - mesh.nodes[nid]) < 0.01:
                     hit = j
                     break
-            if hit is None:
+            if hit is not None:
+                nd = cand.pop(hit)
+                enodes.append(nd)
+                epos.append(mesh.nodes[nd])
+                erows.append(np.array([nd]))
+                ewts.append(np.ones(1))
+                ecell_ent.append(-1)
+                continue
+            # no electrode node: the cell that holds the sensor (ElectrodeShapeEntity,
+            # dcfemmodelling.cpp:924-937, electrode.cpp:252-290)
+            cell, wts = find_cell(mesh, p)
+            if cell < 0:
                 raise ValueError("There is a requested electrode that does not match the given mesh.")
-            enodes.append(cand.pop(hit))
+            enodes.append(-1)
+            epos.append(p.copy())
+            erows.append(mesh.cells[cell].astype(np.int64))
+            ewts.append(wts)
+            ecell_ent.append(cell)
         self.enodes = np.array(enodes, np.int64)
-        self.epos = mesh.nodes[self.enodes]
+        self.epos = np.array(epos, np.float64)
+        self.erows, self.ewts = erows, ewts
         self.nE = len(self.enodes)
         self.src_center = self.epos.sum(axis=0) / self.nE
-        # incident cells and neighbour distance per electrode node
+        # incident cells and neighbour distance per electrode node (the cell of an entity electrode)
         cells = mesh.cells
         self.ecells = []
-        self.eminr = np.empty(self.nE)
+        self.eminr = np.zeros(self.nE)
         for i, nd in enumerate(self.enodes):
+            if nd < 0:
+                self.ecells.append(np.array([ecell_ent[i]]))
+                continue
             cs = np.nonzero(np.any(cells == nd, axis=1))[0]
             self.ecells.append(cs)
             nb = np.setdiff1d(np.unique(cells[cs]), [nd])
@@ -446,7 +483,9 @@ class Problem:
                     u = (besselK0(rs * kk) + besselK0(rm * kk)) / (2.0 * PI)
                 u[zero] = 0.0
                 mr = self.eminr[e]
-                if kk > 0.0:
+                if self.enodes[e] < 0:
+                    pass  # entity electrode: no node at the source
+                elif kk > 0.0:
                     u[self.enodes[e]] = besselK0(np.array([mr / 6.0 * kk]))[0] / PI
                 else:
                     u[self.enodes[e]] = 1.0 / (2.0 * PI * mr / 2.0)
@@ -512,7 +551,7 @@ class Problem:
     def collect(self, u):
         """Electrode potential matrix U[e, f] = sum_k w_k u_k[e](node f)."""
         sol = np.einsum("k,ken->en", self.w, u)
-        return sol[:, self.enodes]
+        return np.stack([sol[:, r] @ w for r, w in zip(self.erows, self.ewts)], axis=1)
 
     def data_u(self, U, reciprocity=False):
         ab = self.abmn
@@ -598,7 +637,7 @@ class Problem:
             lu = spla.splu(S.tocsc(), permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=0.0)
             for e in range(self.nE):
                 rhs = np.zeros(self.n, complex)
-                rhs[self.enodes[e]] = 1.0
+                rhs[self.erows[e]] = self.ewts[e]
                 u[ki, e] = lu.solve(rhs)
         return u
 

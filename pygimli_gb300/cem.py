@@ -109,8 +109,9 @@ def entity_integrals(nvert, corners):
 @dataclass
 class ElectrodeShape:
     """One electrode or passive body: ``kind`` "node" (a node electrode or a
-    bypass electrode at its first node), "cem" or "passive"; ``entities``
-    are ("b", boundary) / ("c", cell) pairs."""
+    bypass electrode at its first node), "cem", "passive" or "entity" (a
+    point inside the cell ``entities[0]``); ``entities`` are ("b", boundary) /
+    ("c", cell) pairs."""
     kind: str
     pos: np.ndarray
     node: int = -1
@@ -133,6 +134,7 @@ class ElectrodeSetup:
     src_row: np.ndarray          # row of each electrode's current and potential (int32)
     enode: np.ndarray            # node of each electrode, -1 for CEM electrodes (int32)
     src_center: np.ndarray       # mean electrode position (mixed boundary condition)
+    search: object = None        # ert.ElectrodeSearch when an electrode lies inside a cell
 
 
 def _sensor_positions(dim, sensors):
@@ -217,8 +219,14 @@ def search_electrodes(mesh, sensors):
                     hit = ElectrodeShape("node", nodes[nd].copy(), node=int(nd))
                     break
         if hit is None:
-            raise ValueError(f"There is a requested electrode that does not match the given mesh: sensor {i} "
-                             f"at {p} (electrodes inside cells are not supported)")
+            # no electrode node: the cell that holds the sensor (ElectrodeShapeEntity,
+            # dcfemmodelling.cpp:924-937)
+            from .ert import find_cell
+            cell = find_cell(mesh, p)
+            if cell < 0:
+                raise ValueError(f"There is a requested electrode that does not match the given mesh: sensor {i} "
+                                 f"at {p}")
+            hit = ElectrodeShape("entity", p.copy(), entities=[("c", int(cell))])
         electrodes.append(hit)
     return electrodes, passive, bypass_markers, ent_nodes, ent_corners
 
@@ -230,7 +238,10 @@ def electrode_setup(mesh, sensors, contact_impedance=None, bypass_resistance=Non
     default 1; setContactImpedances); point electrodes always use 1.
     bypass_resistance: {node marker: Ohm} (default 1e-6 Ohm)."""
     electrodes, passive, bypass_markers, ent_nodes, ent_corners = search_electrodes(mesh, sensors)
-    if any(k == "c" for el in electrodes + passive for k, _ in el.entities):
+    entity = [e for e in electrodes if e.kind == "entity"]
+    if entity and (any(e.kind == "cem" for e in electrodes) or passive):
+        raise NotImplementedError("electrodes inside cells together with complete-electrode-model electrodes")
+    if any(k == "c" for el in electrodes + passive if el.kind != "entity" for k, _ in el.entities):
         raise NotImplementedError("CEM electrodes made of cells (cell marker -10000 - i) are not supported; "
                                   "mark the electrode's boundaries instead")
     nn = mesh.nodeCount()
@@ -288,9 +299,16 @@ def electrode_setup(mesh, sensors, contact_impedance=None, bypass_resistance=Non
         src_row = np.array([e.node for e in electrodes])
     enode = np.array([e.node if e.kind == "node" else -1 for e in electrodes])
     center = sum(e.pos for e in electrodes) / nE
+    search = None
+    if entity:
+        from .ert import ElectrodeSearch
+        search = ElectrodeSearch(enode.astype(np.int32),
+                                 np.array([e.entities[0][1] if e.kind == "entity" else -1 for e in electrodes],
+                                          np.int32),
+                                 np.array([e.pos for e in electrodes], np.float64))
     return ElectrodeSetup(electrodes, passive, bypass_markers, cem, n_ext, np.asarray(rows, np.int32),
                           np.asarray(cols, np.int32), np.asarray(vals, np.float64), src_row.astype(np.int32),
-                          enode.astype(np.int32), np.asarray(center, np.float64))
+                          enode.astype(np.int32), np.asarray(center, np.float64), search)
 
 
 def mark_cem_electrodes(mesh, positions, radius, passive=None):

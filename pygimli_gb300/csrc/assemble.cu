@@ -587,34 +587,46 @@ __global__ void k_finish_pot(int64_t n, int nE, int64_t R, int64_t Rpad, const d
 // reference's k loop (first term a product, then accumulate).
 // last_k: the last wavenumber's potential, unweighted (the complete
 // electrode model's collect, core/src/bert/dcfemmodelling.cpp:1829, 1912).
-__global__ void k_collect(int nE, int nK, int64_t Rpad, const int32_t *__restrict__ enode,
+// U[e][f]: potential at electrode f for the source at electrode e, the
+// k-summed solution at f's rows weighted by f's weights (a node electrode: its
+// row with weight 1; an electrode inside a cell: the cell's shape functions
+// there, ElectrodeShapeEntity::pot, core/src/bert/electrode.cpp:273-275)
+__global__ void k_collect(int nE, int nK, int64_t Rpad, const int32_t *__restrict__ ew_ptr,
+                          const int32_t *__restrict__ ew_row, const double *__restrict__ ew_w,
                           const double *__restrict__ w, const double *__restrict__ x,
                           double *__restrict__ U, int last_k) {
     const int64_t total = (int64_t)nE * nE;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
          t += (int64_t)gridDim.x * blockDim.x) {
         const int e = (int)(t / nE), f = (int)(t % nE);
-        const double *row = x + (int64_t)enode[f] * Rpad;
-        if (last_k) {
-            U[t] = row[(int64_t)(nK - 1) * nE + e];
-            continue;
+        double u = 0.0;
+        for (int q = ew_ptr[f]; q < ew_ptr[f + 1]; q++) {
+            const double *row = x + (int64_t)ew_row[q] * Rpad;
+            double acc;
+            if (last_k) {
+                acc = row[(int64_t)(nK - 1) * nE + e];
+            } else {
+                acc = row[e] * w[0];
+                for (int ki = 1; ki < nK; ki++) acc += row[(int64_t)ki * nE + e] * w[ki];
+            }
+            u = q == ew_ptr[f] ? ew_w[q] * acc : fma(ew_w[q], acc, u);
         }
-        double acc = row[e] * w[0];
-        for (int ki = 1; ki < nK; ki++) acc += row[(int64_t)ki * nE + e] * w[ki];
-        U[t] = acc;
+        U[t] = u;
     }
 }
 
-// Total potential: column t = k * nE + e carries a unit current on the
-// source row of electrode e (ElectrodeShapeNode / ElectrodeShapeDomain::
-// assembleRHS, core/src/bert/electrode.cpp:133-150, 341-355); b is zeroed
-// before.
-__global__ void k_rhs_total(int nE, int64_t R, int64_t Rpad, const int32_t *__restrict__ src_row,
+// Total potential: column t = k * nE + e carries a unit current at electrode
+// e: its source row (ElectrodeShapeNode / ElectrodeShapeDomain::assembleRHS,
+// core/src/bert/electrode.cpp:133-150, 341-355) or the shape functions of
+// the cell holding it (ElectrodeShapeEntity::assembleRHS, 278-290); b is
+// zeroed before.
+__global__ void k_rhs_total(int nE, int64_t R, int64_t Rpad, const int32_t *__restrict__ ew_ptr,
+                            const int32_t *__restrict__ ew_row, const double *__restrict__ ew_w,
                             double *__restrict__ b) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t >= R) return;
     const int e = (int)(t % nE);
-    b[(int64_t)src_row[e] * Rpad + t] = 1.0;
+    for (int q = ew_ptr[e]; q < ew_ptr[e + 1]; q++) b[(int64_t)ew_row[q] * Rpad + t] = ew_w[q];
 }
 
 __device__ inline double abmn_u(const double *U, int nE, int a, int b, int m, int n) {
@@ -735,6 +747,30 @@ void analytic_potentials(Context &c, double rho, double *out) {
     ERTGB_CUDA(cudaGetLastError());
 }
 
+void build_electrode_weights(Context &c) {
+    const bool total = c.formulation == ERTGB_FORMULATION_TOTAL_POTENTIAL;
+    const int nv = c.mesh.nv;
+    std::vector<int32_t> ptr(1, 0), row;
+    std::vector<double> wt;
+    for (int e = 0; e < c.nE; e++) {
+        const int32_t cell = e < (int)c.ent_cell.size() ? c.ent_cell[e] : -1;
+        if (cell >= 0) {
+            for (int i = 0; i < nv; i++) {
+                row.push_back(c.mesh.cells[(size_t)cell * nv + i]);
+                wt.push_back(c.ent_w[(size_t)e * nv + i]);
+            }
+        } else {
+            row.push_back(total ? c.src_row[e] : c.enode[e]);
+            wt.push_back(1.0);
+        }
+        ptr.push_back((int32_t)row.size());
+    }
+    c.d_ew_ptr.upload(ptr, c.stream);
+    c.d_ew_row.upload(row, c.stream);
+    c.d_ew_w.upload(wt, c.stream);
+    ERTGB_CUDA(cudaStreamSynchronize(c.stream));
+}
+
 void upload_primary(Context &c) {
     MeshData &m = c.mesh;
     const int64_t n = m.n;
@@ -800,7 +836,8 @@ void build_rhs(Context &c, cudaStream_t s) {
 void build_rhs_total(Context &c, cudaStream_t s) {
     MeshData &m = c.mesh;
     ERTGB_CUDA(cudaMemsetAsync(c.d_r.p, 0, sizeof(double) * (size_t)m.n * c.Rpad, s));
-    k_rhs_total<<<(unsigned)ceil_div(c.R, kThreads), kThreads, 0, s>>>(c.nE, c.R, c.Rpad, c.d_src_row.p, c.d_r.p);
+    k_rhs_total<<<(unsigned)ceil_div(c.R, kThreads), kThreads, 0, s>>>(c.nE, c.R, c.Rpad, c.d_ew_ptr.p, c.d_ew_row.p,
+                                                                       c.d_ew_w.p, c.d_r.p);
     ERTGB_CUDA(cudaGetLastError());
     c.d_pnorm2.release();  // no primary field: the reference norm is ||b||
 }
@@ -828,9 +865,9 @@ void finish_potentials(Context &c, cudaStream_t s) {
 void collect_response(Context &c, double *rhoa, cudaStream_t s) {
     c.d_U.alloc((size_t)c.nE * c.nE);
     const bool total = c.formulation == ERTGB_FORMULATION_TOTAL_POTENTIAL;
-    k_collect<<<grid1((int64_t)c.nE * c.nE), kThreads, 0, s>>>(c.nE, c.nK, c.Rpad,
-                                                               total ? c.d_src_row.p : c.d_enode.p, c.d_w.p,
-                                                               c.d_x.p, c.d_U.p, total && c.collect_last_k ? 1 : 0);
+    k_collect<<<grid1((int64_t)c.nE * c.nE), kThreads, 0, s>>>(c.nE, c.nK, c.Rpad, c.d_ew_ptr.p, c.d_ew_row.p,
+                                                               c.d_ew_w.p, c.d_w.p, c.d_x.p, c.d_U.p,
+                                                               total && c.collect_last_k ? 1 : 0);
     ERTGB_CUDA(cudaGetLastError());
     k_response<<<grid1(c.D), kThreads, 0, s>>>(c.D, c.nE, c.d_abmn.p, c.d_kfac.p, c.d_U.p, rhoa);
     ERTGB_CUDA(cudaGetLastError());

@@ -102,14 +102,16 @@ void ensure_derived(Context &c) {
     const bool total = c.formulation == ERTGB_FORMULATION_TOTAL_POTENTIAL;
     if (total) {
         if ((int)c.src_row.size() != c.nE) throw Error(ERTGB_STATE, "electrode source rows do not match the electrodes");
-        for (int32_t r : c.src_row)
-            if (r < 0 || r >= c.mesh.n)
+        for (int e = 0; e < c.nE; e++)
+            if ((c.src_row[e] < 0 || c.src_row[e] >= c.mesh.n) && c.ent_cell[e] < 0)
                 throw Error(ERTGB_STATE, "an electrode has no source row (set the matrix extension after the electrodes)");
     } else {
-        for (int32_t v : c.enode)
-            if (v < 0) throw Error(ERTGB_STATE, "singularity removal needs a node for every electrode");
+        for (int e = 0; e < c.nE; e++)
+            if (c.enode[e] < 0 && c.ent_cell[e] < 0)
+                throw Error(ERTGB_STATE, "singularity removal needs a node or a cell for every electrode");
     }
     if (!c.prim_ready) {
+        build_electrode_weights(c);
         c.R = (int64_t)c.nE * c.nK;
         c.Rpad = ceil_div(c.R, c.rhs_align) * c.rhs_align;
         compute_boundary_alpha(c);
@@ -320,10 +322,11 @@ int ertgb_set_electrodes(ertgb_ctx *ctx, int n_elec, const int32_t *elec_node, d
         MeshData &m = c->mesh;
         c->nE = n_elec;
         c->enode.assign(elec_node, elec_node + n_elec);
-        const bool total = c->formulation == ERTGB_FORMULATION_TOTAL_POTENTIAL;
         std::set<int32_t> uniq;
         for (int32_t v : c->enode) {
-            if (v == -1 && total) continue;  // an electrode given by its extension row
+            // -1: an electrode given by its extension row (total potential) or by
+            // the cell that holds it (ertgb_set_electrode_shapes)
+            if (v == -1) continue;
             ERTGB_REQUIRE(v >= 0 && v < m.nn, "electrode node index out of range");
             ERTGB_REQUIRE(uniq.insert(v).second, "two electrodes on the same node");
         }
@@ -337,6 +340,9 @@ int ertgb_set_electrodes(ertgb_ctx *ctx, int n_elec, const int32_t *elec_node, d
                 sc[d] += epos[3 * e + d];
             }
         for (int d = 0; d < 3; d++) c->src_center[d] = sc[d] / (double)n_elec;
+        c->epos_h = epos;
+        c->ent_cell.assign(n_elec, -1);
+        c->ent_w.assign((size_t)n_elec * m.nv, 0.0);
         // incident cells and smallest neighbour distance per electrode node
         std::vector<std::vector<int32_t>> inc(n_elec);
         std::vector<int> slot(m.nn, -1);
@@ -390,6 +396,77 @@ int ertgb_set_electrodes(ertgb_ctx *ctx, int n_elec, const int32_t *elec_node, d
     });
 }
 
+int ertgb_set_electrode_shapes(ertgb_ctx *ctx, int n_elec, const int32_t *cell, const double *pos) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        if (!c->have_elec) throw Error(ERTGB_STATE, "set the electrodes first");
+        ERTGB_REQUIRE(n_elec == c->nE && cell && pos, "one cell and position per electrode");
+        MeshData &m = c->mesh;
+        const int d = m.dim;
+        for (int e = 0; e < n_elec; e++) {
+            if (cell[e] < 0) continue;
+            ERTGB_REQUIRE(c->enode[e] < 0, "an electrode inside a cell must have no node");
+            ERTGB_REQUIRE(cell[e] < m.C, "electrode cell out of range");
+            ERTGB_REQUIRE(m.order == 1 && m.nv == d + 1, "electrodes inside cells need linear cells");
+            // barycentric coordinates = the linear shape functions at the electrode
+            const int32_t *cn = &m.cells[(size_t)cell[e] * m.nv];
+            double A[3][3] = {{0}}, r[3] = {0}, lam[3] = {0};
+            for (int i = 0; i < d; i++) {
+                for (int j = 0; j < d; j++) A[i][j] = m.xyz[3 * (size_t)cn[j + 1] + i] - m.xyz[3 * (size_t)cn[0] + i];
+                r[i] = pos[3 * e + i] - m.xyz[3 * (size_t)cn[0] + i];
+            }
+            // Gaussian elimination with partial pivoting (d <= 3)
+            int piv[3] = {0, 1, 2};
+            for (int k = 0; k < d; k++) {
+                int b = k;
+                for (int i = k + 1; i < d; i++)
+                    if (std::fabs(A[piv[i]][k]) > std::fabs(A[piv[b]][k])) b = i;
+                std::swap(piv[k], piv[b]);
+                ERTGB_REQUIRE(std::fabs(A[piv[k]][k]) > 0.0, "degenerate electrode cell");
+                for (int i = k + 1; i < d; i++) {
+                    const double f = A[piv[i]][k] / A[piv[k]][k];
+                    for (int j = k; j < d; j++) A[piv[i]][j] -= f * A[piv[k]][j];
+                    r[piv[i]] -= f * r[piv[k]];
+                }
+            }
+            for (int k = d - 1; k >= 0; k--) {
+                double s2 = r[piv[k]];
+                for (int j = k + 1; j < d; j++) s2 -= A[piv[k]][j] * lam[j];
+                lam[k] = s2 / A[piv[k]][k];
+            }
+            double l0 = 1.0;
+            for (int i = 0; i < d; i++) l0 -= lam[i];
+            ERTGB_REQUIRE(l0 >= -1e-9 && lam[0] >= -1e-9 && lam[1] >= -1e-9 && (d < 3 || lam[2] >= -1e-9),
+                          "electrode position outside its cell");
+            c->ent_cell[e] = cell[e];
+            c->ent_w[(size_t)e * m.nv] = l0;
+            for (int i = 0; i < d; i++) c->ent_w[(size_t)e * m.nv + i + 1] = lam[i];
+            for (int i = 0; i < 3; i++) c->epos_h[3 * e + i] = pos[3 * e + i];
+            c->emin_r[e] = 0.0;
+        }
+        // source resistivity of an electrode inside a cell: that cell's
+        std::vector<int32_t> ptr(1, 0), lst;
+        for (int e = 0; e < c->nE; e++) {
+            if (c->ent_cell[e] >= 0) lst.push_back(c->ent_cell[e]);
+            else lst.insert(lst.end(), c->ecell.begin() + c->ecell_ptr[e], c->ecell.begin() + c->ecell_ptr[e + 1]);
+            ptr.push_back((int32_t)lst.size());
+        }
+        c->ecell_ptr.swap(ptr);
+        c->ecell.swap(lst);
+        double sc[3] = {0, 0, 0};
+        for (int e = 0; e < c->nE; e++)
+            for (int i = 0; i < 3; i++) sc[i] += c->epos_h[3 * e + i];
+        for (int i = 0; i < 3; i++) c->src_center[i] = sc[i] / (double)c->nE;
+        cudaStream_t s = c->stream;
+        c->d_epos.upload(c->epos_h, s);
+        c->d_emin_r.upload(c->emin_r, s);
+        c->d_ecell_ptr.upload(c->ecell_ptr, s);
+        c->d_ecell.upload(c->ecell, s);
+        ERTGB_CUDA(cudaStreamSynchronize(s));
+        invalidate_derived(*c);
+    });
+}
+
 int ertgb_set_formulation(ertgb_ctx *ctx, int formulation) {
     Context *c = reinterpret_cast<Context *>(ctx);
     return guard(c, [&] {
@@ -426,7 +503,9 @@ int ertgb_set_extension(ertgb_ctx *ctx, int n_ext, int64_t n_entries, const int3
             ERTGB_REQUIRE(std::isfinite(v[i]), "extension value not finite");
         }
         std::vector<int32_t> sr(src_row, src_row + c->nE);
-        for (int32_t x : sr) ERTGB_REQUIRE(x >= 0 && x < N, "electrode source row out of range");
+        for (int e = 0; e < c->nE; e++)  // an electrode inside a cell has no source row
+            ERTGB_REQUIRE((sr[e] >= 0 && sr[e] < N) || (e < (int)c->ent_cell.size() && c->ent_cell[e] >= 0),
+                          "electrode source row out of range");
         ERTGB_CUDA(cudaSetDevice(c->device));
         set_mesh_extension(*c, n_ext, std::move(r), std::move(q), std::move(v));
         c->src_row = sr;

@@ -856,6 +856,8 @@ int complex_response(Context &c, const double *rho_re, const double *rho_im, dou
     if (m.n_ext > 0 || !m.ext_rows.empty())
         throw Error(ERTGB_BAD_INPUT, "complex resistivity takes no matrix extension (the reference's complete "
                                      "electrode model is real-valued only, dcfemmodelling.cpp:423-428)");
+    for (int32_t cell : c.ent_cell)
+        if (cell >= 0) throw Error(ERTGB_BAD_INPUT, "complex resistivity needs node electrodes");
     const int64_t n = m.n, nnz = m.nnz, Rpad = c.Rpad, R = c.R;
     x.have_pot = false;
     // 1 / rho* per cell

@@ -186,6 +186,11 @@ struct Context {
     double surface_z = 0.0;
     double src_center[3] = {0, 0, 0};
     std::vector<double> emin_r;              // singular radius per electrode
+    std::vector<double> epos_h;              // electrode positions (nE x 3)
+    std::vector<int32_t> ent_cell;           // cell holding an electrode that is no node (-1: none)
+    std::vector<double> ent_w;               // nE x nv: shape functions of that cell at the electrode
+    DBuf<int32_t> d_ew_ptr, d_ew_row;        // source / collect rows and weights per electrode
+    DBuf<double> d_ew_w;
     std::vector<int32_t> ecell_ptr, ecell;   // incident cells per electrode
     DBuf<int32_t> d_enode, d_ecell_ptr, d_ecell;
     // formulation (ertgb_formulation); total potential: the row of each
@@ -285,6 +290,9 @@ void finish_potentials(Context &c, cudaStream_t s);
 void collect_response(Context &c, double *rhoa, cudaStream_t s);
 // total potential: unit currents at the electrodes' source rows into d_r
 void build_rhs_total(Context &c, cudaStream_t s);
+// rows and weights of every electrode's source and potential (its node / source
+// row with weight 1, or the shape functions of the cell holding it)
+void build_electrode_weights(Context &c);
 void check_rho(Context &c, const double *rho_cell, cudaStream_t s);
 // pcg.cu
 // mask: warm start (x kept) on the columns with mask[t] != 0; nullptr = cold start, all columns

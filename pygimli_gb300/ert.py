@@ -43,29 +43,73 @@ def _ptr(a):
     return ctypes.c_void_p(a.ctypes.data)
 
 
-def search_electrodes(mesh, sensors):
-    """Node electrodes as DCMultiElectrodeModelling::searchElectrodes_ finds
-    them (core/src/bert/dcfemmodelling.cpp:790-1030): sensor i takes the first
-    still-unused node with marker -99 within 1 cm.  2-D sensors given as
-    (x, 0, z) are swapped to (x, z) first (:859-867)."""
+def sensor_positions(mesh, sensors):
+    """Sensor positions in mesh coordinates: 2-D sensors given as (x, 0, z)
+    are swapped to (x, z) (dcfemmodelling.cpp:859-867)."""
     ePos = np.asarray(sensors, dtype=np.float64).reshape(-1, 3).copy()
     if mesh.dim() == 2:
         zvar = np.ptp(ePos[:, 2]) > 0 or np.max(np.abs(ePos[:, 2])) > 0
         yvar = np.ptp(ePos[:, 1]) > 0
         if zvar and not yvar and np.max(np.abs(ePos[:, 1])) < 1e-8:
             ePos[:, [1, 2]] = ePos[:, [2, 1]]
+    return ePos
+
+
+def find_cell(mesh, p, tol=1e-12):
+    """The cell that holds point p (linear cells; the lowest cell index whose
+    barycentric coordinates are all >= -tol, as Mesh::findCell returns the
+    one holding cell), or -1."""
+    d = mesh.dim()
+    if mesh.cells.shape[1] != d + 1:
+        raise NotImplementedError("electrodes inside cells need linear cells")
+    x = mesh.nodes[mesh.cells][:, :, :d]
+    near = np.nonzero(np.all((x.min(axis=1) <= p[:d] + 1e-9) & (x.max(axis=1) >= p[:d] - 1e-9), axis=1))[0]
+    if len(near) == 0:
+        return -1
+    xs = x[near]
+    A = np.transpose(xs[:, 1:, :] - xs[:, :1, :], (0, 2, 1))
+    lam = np.linalg.solve(A, (p[:d][None, :] - xs[:, 0, :])[:, :, None])[:, :, 0]
+    bary = np.column_stack([1.0 - lam.sum(axis=1), lam])
+    ok = np.nonzero(np.all(bary >= -tol, axis=1))[0]
+    return int(near[ok[0]]) if len(ok) else -1
+
+
+class ElectrodeSearch:
+    """Electrodes of the singularity-removal operator in data order: a node
+    (nodes[i] >= 0) or, with no electrode node within 1 cm, the cell that
+    holds the sensor (cells[i] >= 0, ElectrodeShapeEntity); pos: the sensor
+    positions in mesh coordinates."""
+
+    def __init__(self, nodes, cells, pos):
+        self.nodes, self.cells, self.pos = nodes, cells, pos
+
+    @property
+    def entity(self):
+        return bool(np.any(self.cells >= 0))
+
+
+def search_electrodes(mesh, sensors):
+    """Electrodes as DCMultiElectrodeModelling::searchElectrodes_ finds them
+    for node and free electrodes (core/src/bert/dcfemmodelling.cpp:790-1030):
+    sensor i takes the first still-unused node with marker -99 within 1 cm,
+    else the cell that holds it (:924-937)."""
+    ePos = sensor_positions(mesh, sensors)
     cand = np.nonzero(mesh.node_markers == MARKER_NODE_ELECTRODE)[0]
     used = np.zeros(len(cand), bool)
-    out = np.empty(len(ePos), np.int32)
+    nodes = np.full(len(ePos), -1, np.int32)
+    cells = np.full(len(ePos), -1, np.int32)
     cpos = mesh.nodes[cand]
     for i, p in enumerate(ePos):
         d = np.linalg.norm(cpos - p, axis=1)
         ok = np.nonzero((d < 0.01) & ~used)[0]
-        if len(ok) == 0:
+        if len(ok):
+            used[ok[0]] = True
+            nodes[i] = cand[ok[0]]
+            continue
+        cells[i] = find_cell(mesh, p)
+        if cells[i] < 0:
             raise ValueError(f"There is a requested electrode that does not match the given mesh: {p}")
-        used[ok[0]] = True
-        out[i] = cand[ok[0]]
-    return out
+    return ElectrodeSearch(nodes, cells, ePos)
 
 
 def surface_info(mesh):
@@ -299,14 +343,21 @@ class ERTModelling:
             if has_cem_markers(mesh):
                 raise ValueError("complete-electrode-model and bypass electrodes need the total-potential "
                                  "operator: ERTModelling(sr=False)")
-            self._elec_nodes = search_electrodes(mesh, data.sensorPositions())
+            es = search_electrodes(mesh, data.sensorPositions())
+            self._elec_nodes = es.nodes
             self._electrodes = None
         else:
             setup = electrode_setup(mesh, data.sensorPositions(), self._contact_z, self._bypass_r)
             self._electrodes = setup
             self._elec_nodes = setup.enode
+            es = setup.search
         self._check(self._lib.ertgb_set_electrodes(self._ctx, len(self._elec_nodes),
                                                    _ptr(self._elec_nodes), float(self._surface_z)))
+        self._entity = es is not None and es.entity
+        if self._entity:
+            cells = np.ascontiguousarray(es.cells, np.int32)
+            pos = np.ascontiguousarray(es.pos, np.float64)
+            self._check(self._lib.ertgb_set_electrode_shapes(self._ctx, len(cells), _ptr(cells), _ptr(pos)))
         if self._electrodes is not None and (self._electrodes.cem or len(self._electrodes.rows)):
             e = self._electrodes
             self._check(self._lib.ertgb_set_extension(

@@ -67,7 +67,7 @@ def test_host_setup_matches_reference(golden_dir, name):
     z, mesh = load_case(golden_dir, name)
     k, w = init_kwave_list(mesh.dim(), z["sensors"])
     assert np.array_equal(k, z["k"]) and np.array_equal(w, z["w"])
-    assert np.array_equal(search_electrodes(mesh, z["sensors"]), z["electrode_nodes"])
+    assert np.array_equal(search_electrodes(mesh, z["sensors"]).nodes, z["electrode_nodes"])
     d = DataContainerERT(z["sensors"], z["abmn"])
     kf = geometricFactors(d, mesh.dim())
     assert np.max(np.abs(kf - z["kfac_ref"]) / np.abs(z["kfac_ref"])) < 1e-14
