@@ -95,7 +95,10 @@ const char *ertgb_last_error(const ertgb_ctx *ctx);
  * Tetrahedron10 in the node order of Mesh::createP2, core/src/mesh.cpp:
  * 1284-1600).  xyz: n_nodes x 3.  cell_nodes: n_cells x (dim+1) for order 1,
  * x 6 / 10 for order 2.  bnd_nodes: n_bnd x dim (order 1) or x 3 / 6
- * (order 2), bnd_marker -1 Neumann / -2 mixed,
+ * (order 2), bnd_marker -1 Neumann / -2 mixed / -3 homogeneous Dirichlet
+ * (the boundary's nodes get Dirichlet rows and columns, diagonal 1:
+ * dcfemBoundaryAssembleStiffnessMatrix, core/src/bert/dcfemmodelling.cpp:
+ * 279-298; -4 is refused as by the reference, :293),
  * bnd_cell: adjacent cell of each boundary.  Builds the CSR pattern
  * (core/src/sparsematrix.h:966-1024), the per-slot assembly map and the
  * element matrices (core/src/elementmatrix.cpp:683-1122). */
@@ -126,6 +129,22 @@ int ertgb_set_electrodes(ertgb_ctx *ctx, int n_elec, const int32_t *elec_node_ho
  * DCMultiElectrodeModelling::searchElectrodes_
  * (core/src/bert/dcfemmodelling.cpp:924-937). */
 int ertgb_set_electrode_shapes(ertgb_ctx *ctx, int n_elec, const int32_t *cell_host, const double *pos_host);
+
+/* Current reference and calibration (after ertgb_set_electrodes; setting the
+ * mesh or the electrodes clears them).  The pattern of electrode e then
+ * carries +1 at e and -1 at the reference electrode: electrode ref_electrode
+ * (its own pattern is empty) or mesh node ref_node; both -1: the current
+ * leaves at infinity.  Replaces DCMultiElectrodeModelling::searchElectrodes_
+ * (core/src/bert/dcfemmodelling.cpp:1011-1073: node marker -999, or the
+ * last electrode in a 3-D domain without mixed and Dirichlet boundaries) and
+ * createCurrentPattern (:1515-1523).  Singularity removal subtracts the
+ * reference's primary potential (:2085-2090) and averages the two source
+ * resistivities (:2236-2266).  calib_host: n_calib calibration nodes (node
+ * marker -1000, else node 0, in such a closed 3-D domain): Dirichlet rows
+ * and columns in every system matrix (:1835, 2182-2192) and a zero
+ * singularity-removal right-hand side there (:2281-2283).  A closed 3-D
+ * domain needs at least one. */
+int ertgb_set_reference(ertgb_ctx *ctx, int ref_electrode, int ref_node, int n_calib, const int32_t *calib_host);
 
 /* Formulation of the forward operator.  SINGULARITY_REMOVAL (default):
  * DCSRMultiElectrodeModelling, pyGIMLi ERTModelling(sr=True)

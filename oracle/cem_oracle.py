@@ -34,8 +34,15 @@ Reference code restated (paths inside pyGIMLi):
 
 Not restated: the map files the reference reads from the working directory
 (bypass.map, electrodeBypassResistances.map, contactImpedance.map,
-contactResistance.map) -- their values enter here as arguments; free
-electrodes inside cells; reference and calibration nodes.
+contactResistance.map) -- their values enter here as arguments; a
+reference electrode together with CEM electrodes.
+
+Reference and calibration nodes, Neumann domains and homogeneous Dirichlet
+boundaries follow ert_oracle.BoundarySetup: Dirichlet rows cleaned before
+the extensions (dcfemBoundaryAssembleStiffnessMatrix,
+core/src/bert/dcfemmodelling.cpp:279-298), calibration rows after them
+(1835), the pattern of electrode e carrying +1 there and -1 at the reference
+electrode (1515-1523, 1862-1864).
 """
 from __future__ import annotations
 
@@ -45,7 +52,7 @@ import numpy as np
 import scipy.sparse as sp
 import scipy.sparse.linalg as spla
 
-from ert_oracle import (TOLERANCE, Problem, _p2_shape, _rule_tet_deg4, _rule_tri_deg4, boundary_center_normal,
+from ert_oracle import (TOLERANCE, BoundarySetup, Problem, _p2_shape, _rule_tet_deg4, _rule_tri_deg4, boundary_center_normal,
                         boundary_mass, element_matrices, find_cell, mixed_bc_alpha, sparsity_pattern)
 
 MARKER_BOUND_ELECTRODE = -10000
@@ -292,6 +299,11 @@ class TotalPotentialProblem:
         self.alpha = [mixed_bc_alpha(self.dim, bc, bn, self.src_center, kk) for kk in self.k]
         self.bnd_nodes = bnd
         Problem._slot_maps(self)
+        self.epos = np.array([e.pos for e in self.electrodes], np.float64)
+        Problem._patterns(self)
+        self.dirichlet = self.bc.dirichlet
+        if self.sink is not None and self.n_ext:
+            raise NotImplementedError("a reference electrode with complete-electrode-model electrodes")
 
     def matrix(self, rho_cell, kidx):
         """FEM matrix (domain, mixed boundaries) plus the extensions, N x N."""
@@ -305,12 +317,19 @@ class TotalPotentialProblem:
         if len(self.mixed):
             bc = self.bnd_mass * (self.alpha[kidx] / rho_cell[self.bnd_cell])[:, None, None]
             np.add.at(vals, self.bnd_slot.ravel(), bc.ravel())
+        diag_slot = Problem._diag_slots(self)
+        if len(self.dirichlet):
+            Problem._clean_rows_cols(self, vals, self.dirichlet, diag_slot)
         A = sp.csr_matrix((vals, self.cols, self.rowptr), shape=(self.n, self.n))
         A = sp.block_diag([A, sp.csr_matrix((self.n_ext, self.n_ext))]).tolil() if self.n_ext else A.tolil()
         for (r, c), v in self.ext.items():
             A[r, c] += v
         for r, v in self.ext_diag.items():
             A[r, r] = v
+        for r in self.calib:
+            A[r, :] = 0.0
+            A[:, r] = 0.0
+            A[r, r] = 1.0
         return A.tocsr()
 
     def solve(self, rho_cell):
@@ -321,7 +340,9 @@ class TotalPotentialProblem:
             lu = spla.splu(self.matrix(rho_cell, ki).tocsc(), permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=0.0)
             for e in range(self.nE):
                 rhs = np.zeros(self.N)
-                rhs[self.erows[e]] = self.ewts[e]
+                rhs[self.erows[e]] += self.ewts[e]
+                if self.sink is not None:
+                    rhs[self.sink[0]] -= self.sink[1]
                 u[ki, e] = lu.solve(rhs)
         return u
 

@@ -27,6 +27,12 @@ Each step cites the reference code it restates (paths inside pyGIMLi):
   Jacobian           core/src/bert/bertJacobian.cpp:70-119 (calc2),
                      267-421; scaling dcfemmodelling.cpp:1377-1384
   electrode search   core/src/bert/dcfemmodelling.cpp:790-1030
+  Neumann domains    core/src/bert/dcfemmodelling.cpp:711-773 (detection),
+                     1011-1073 (reference electrode, calibration nodes),
+                     1515-1523 (current patterns), 2182-2192 and 2281-2283
+                     (calibration rows), 2236-2266 (source resistivity of a
+                     pattern); homogeneous Dirichlet boundaries 279-298 and
+                     142-154; reference-electrode data datamap.cpp:203-214
   model mapping      core/src/modellingbase.cpp:401-497,
                      core/src/mesh.cpp:2247-2316 prolongateEmptyCellsValues
 """
@@ -40,6 +46,65 @@ import scipy.sparse.linalg as spla
 
 TOLERANCE = 1e-12
 PI = math.pi
+MARKER_BOUND_HOMOGEN_NEUMANN = -1
+MARKER_BOUND_MIXED = -2
+MARKER_BOUND_HOMOGEN_DIRICHLET = -3
+MARKER_BOUND_DIRICHLET = -4
+MARKER_NODE_REFERENCEELECTRODE = -999
+MARKER_NODE_CALIBRATION = -1000
+
+
+class BoundarySetup:
+    """Boundary conditions and current patterns of a mesh
+    (updateMeshDependency_, core/src/bert/dcfemmodelling.cpp:711-773;
+    searchElectrodes_, 799-802 and 1011-1073):
+
+    neumann    no mixed and no Dirichlet boundary (in 2-D only the topography
+               flag follows from it)
+    topography a Neumann-boundary centre off the first one's height, or a
+               Neumann domain (any dimension)
+    dirichlet  nodes of homogeneous Dirichlet boundaries (-3), sorted
+    calib      calibration nodes of a 3-D Neumann domain: node marker -1000,
+               else node 0
+    ref_node   the first node with marker -999 (-1: none); its patterns
+               (e, ref) hold for every domain
+    ref_elec   a 3-D Neumann domain without reference node: the last
+               electrode (its own pattern is empty), else -1
+    """
+
+    def __init__(self, mesh, n_elec):
+        bm = np.asarray(mesh.boundary_markers)
+        if np.any(bm == MARKER_BOUND_DIRICHLET):
+            raise NotImplementedError("inhomogeneous Dirichlet boundaries (-4) are not implemented")
+        self.neumann = not np.any((bm == MARKER_BOUND_MIXED) | (bm == MARKER_BOUND_HOMOGEN_DIRICHLET))
+        neu = np.nonzero(bm == MARKER_BOUND_HOMOGEN_NEUMANN)[0]
+        topo = False
+        if len(neu):
+            cz = mesh.nodes[mesh.boundaries[neu]].mean(axis=1)[:, mesh.dim() - 1]
+            topo = bool(np.any(cz != cz[0]))
+        self.topography = topo or self.neumann
+        dnodes = mesh.boundaries[bm == MARKER_BOUND_HOMOGEN_DIRICHLET]
+        self.dirichlet = np.unique(dnodes.ravel()).astype(np.int64) if len(dnodes) else np.zeros(0, np.int64)
+        nm = np.asarray(mesh.node_markers)
+        refs = np.nonzero(nm == MARKER_NODE_REFERENCEELECTRODE)[0]
+        self.ref_node = int(refs[0]) if len(refs) else -1
+        self.ref_elec = -1
+        neumann3 = self.neumann and mesh.dim() == 3
+        if neumann3:
+            cal = np.nonzero(nm == MARKER_NODE_CALIBRATION)[0]
+            self.calib = cal.astype(np.int64) if len(cal) else np.zeros(1, np.int64)
+            if self.ref_node < 0 and n_elec > 0:
+                self.ref_elec = n_elec - 1
+        else:
+            self.calib = np.zeros(0, np.int64)
+        self.clean = np.union1d(self.dirichlet, self.calib).astype(np.int64)
+
+
+def node_min_radius(mesh, nd):
+    """Smallest distance from node nd to the nodes of its cells."""
+    cs = np.nonzero(np.any(mesh.cells == nd, axis=1))[0]
+    nb = np.setdiff1d(np.unique(mesh.cells[cs]), [nd])
+    return float(np.min(np.linalg.norm(mesh.nodes[nb] - mesh.nodes[nd], axis=1))), cs
 
 
 # ---------------------------------------------------------------- Bessel --
@@ -373,8 +438,7 @@ class Problem:
         self.bnd_mass = boundary_mass(self.dim, nodes, bnd)
         self.bnd_c, self.bnd_n = boundary_center_normal(self.dim, nodes, bnd)
         neu = np.nonzero(bm == -1)[0]
-        if len(self.mixed) == 0 and len(np.nonzero(bm == -3)[0]) == 0:
-            raise NotImplementedError("Neumann-only domains are not supported")
+        self._patterns()
         if len(neu):
             cz = boundary_center_normal(self.dim, nodes, mesh.boundaries[neu])[0][:, self.dim - 1]
             self.surfaceZ = float(cz[0])
@@ -441,6 +505,25 @@ class Problem:
             nb = np.setdiff1d(np.unique(cells[cs]), [nd])
             self.eminr[i] = np.min(np.linalg.norm(mesh.nodes[nb] - mesh.nodes[nd], axis=1))
 
+    def _patterns(self):
+        """Reference electrode and calibration/Dirichlet nodes (BoundarySetup):
+        pattern e carries +1 at electrode e and -1 at the reference (sink rows
+        and weights; none: the current leaves at infinity)."""
+        bc = BoundarySetup(self.mesh, self.nE)
+        self.bc = bc
+        self.calib, self.clean = bc.calib, bc.clean
+        self.ref_minr, self.ref_cells = 0.0, np.zeros(0, np.int64)
+        if bc.ref_node >= 0:
+            self.sink = (np.array([bc.ref_node]), np.ones(1))
+            self.ref_pos = self.mesh.nodes[bc.ref_node].copy()
+            self.ref_minr, self.ref_cells = node_min_radius(self.mesh, bc.ref_node)
+        elif bc.ref_elec >= 0:
+            r = bc.ref_elec
+            self.sink = (self.erows[r], self.ewts[r])
+            self.ref_pos = self.epos[r].copy()
+        else:
+            self.sink = None
+
     def _slot_maps(self):
         """(cell, i, j) -> CSR slot and (boundary, i, j) -> CSR slot."""
         n = self.n
@@ -459,37 +542,50 @@ class Problem:
         else:
             self.bnd_slot = np.zeros((0, self.dim, self.dim), np.int64)
 
-    def _primary(self):
-        """u_p[kIdx, e, node] for unit current (exactDCSolution + setSingValue)."""
+    def _unit_primary(self, src, node, mr, kk):
+        """Unit-current half-space potential of a source at src for
+        wavenumber kk at every node, with the singular value at its node
+        (exactDCSolution + setSingValue)."""
         nodes = self.mesh.nodes
+        ax = 1 if kk > 0 else 2
+        r = np.linalg.norm(nodes - src, axis=1)
+        mir = src.copy()
+        mir[ax] = 2.0 * self.surfaceZ - src[ax]
+        rm = np.linalg.norm(nodes - mir, axis=1)
+        zero = r < TOLERANCE
+        rs = np.where(zero, 1.0, r)
+        rm = np.where(zero, 1.0, rm)
+        if kk == 0.0:
+            u = (1.0 / rs + 1.0 / rm) / (4.0 * PI)
+        elif np.array_equal(src, mir):
+            u = besselK0(rs * kk) / PI
+        else:
+            u = (besselK0(rs * kk) + besselK0(rm * kk)) / (2.0 * PI)
+        u[zero] = 0.0
+        if node < 0:
+            pass  # entity electrode: no node at the source
+        elif kk > 0.0:
+            u[node] = besselK0(np.array([mr / 6.0 * kk]))[0] / PI
+        else:
+            u[node] = 1.0 / (2.0 * PI * mr / 2.0)
+        return u
+
+    def _primary(self):
+        """u_p[kIdx, e, node] for the unit-current pattern of electrode e
+        (exactDCSolution + setSingValue; minus the reference electrode's,
+        checkPrimpotentials_, dcfemmodelling.cpp:2085-2090)."""
         up = np.zeros((len(self.k), self.nE, self.n))
-        surfaceZ = self.surfaceZ
         for ki, kk in enumerate(self.k):
-            ax = 1 if kk > 0 else 2
+            ref = None
+            if self.bc.ref_node >= 0:
+                ref = self._unit_primary(self.ref_pos, self.bc.ref_node, self.ref_minr, kk)
+            elif self.bc.ref_elec >= 0:
+                r = self.bc.ref_elec
+                ref = self._unit_primary(self.epos[r], self.enodes[r], self.eminr[r], kk)
             for e in range(self.nE):
-                src = self.epos[e]
-                r = np.linalg.norm(nodes - src, axis=1)
-                mir = src.copy()
-                mir[ax] = 2.0 * surfaceZ - src[ax]
-                rm = np.linalg.norm(nodes - mir, axis=1)
-                zero = r < TOLERANCE
-                rs = np.where(zero, 1.0, r)
-                rm = np.where(zero, 1.0, rm)
-                if kk == 0.0:
-                    u = (1.0 / rs + 1.0 / rm) / (4.0 * PI)
-                elif np.array_equal(src, mir):
-                    u = besselK0(rs * kk) / PI
-                else:
-                    u = (besselK0(rs * kk) + besselK0(rm * kk)) / (2.0 * PI)
-                u[zero] = 0.0
-                mr = self.eminr[e]
-                if self.enodes[e] < 0:
-                    pass  # entity electrode: no node at the source
-                elif kk > 0.0:
-                    u[self.enodes[e]] = besselK0(np.array([mr / 6.0 * kk]))[0] / PI
-                else:
-                    u[self.enodes[e]] = 1.0 / (2.0 * PI * mr / 2.0)
-                up[ki, e] = u
+                up[ki, e] = self._unit_primary(self.epos[e], self.enodes[e], self.eminr[e], kk)
+                if ref is not None:
+                    up[ki, e] -= ref
         return up
 
     # ---------------------------------------------------------- assembly --
@@ -511,6 +607,8 @@ class Problem:
             rb = rho_cell[self.bnd_cell]
             bc = self.bnd_mass * (self.alpha[kidx] / rb)[:, None, None]
             np.add.at(vals, self.bnd_slot.ravel(), bc.ravel())
+        if len(self.clean):  # homogeneous Dirichlet boundaries, then calibration nodes
+            self._clean_rows_cols(vals, self.clean, diag_slot)
         return vals
 
     def _diag_slots(self):
@@ -529,8 +627,22 @@ class Problem:
 
     # ---------------------------------------------------------- forward --
     def source_rho(self, rho_cell):
-        """Geometric mean of the cells around each electrode node."""
-        return np.array([np.exp(np.mean(np.log(rho_cell[c]))) for c in self.ecells])
+        """Source resistivity of each electrode's pattern: the geometric mean
+        of the cells around the electrode node, averaged with the reference
+        electrode's over those above TOLERANCE (calculateK,
+        dcfemmodelling.cpp:2236-2266)."""
+        gm = np.array([np.exp(np.mean(np.log(rho_cell[c]))) for c in self.ecells])
+        if self.sink is None:
+            return gm
+        if self.bc.ref_node >= 0:
+            rr = float(np.exp(np.mean(np.log(rho_cell[self.ref_cells]))))
+        else:
+            rr = float(gm[self.bc.ref_elec])
+        out = np.empty_like(gm)
+        for e, ra in enumerate(gm):
+            v = [x for x in (ra, rr) if x > TOLERANCE]
+            out[e] = sum(v) / len(v)
+        return out
 
     def solve(self, rho_cell):
         """Sub-potentials u[kIdx, e, node] (SR total potentials per k)."""
@@ -545,6 +657,7 @@ class Problem:
             for e in range(self.nE):
                 prim = self.up[ki, e] * rs[e]
                 rhs = S1 @ prim / rs[e] - S @ prim
+                rhs[self.calib] = 0.0
                 u[ki, e] = lu.solve(rhs) + prim
         return u
 

@@ -54,6 +54,7 @@ SIGNATURES = {
     "ertgb_set_kw": (_ci, [_vp, _ci, _vp, _vp]),
     "ertgb_set_primary": (_ci, [_vp, _ci, _ci, _i64, _vp]),
     "ertgb_set_electrode_shapes": (_ci, [_vp, _ci, _vp, _vp]),
+    "ertgb_set_reference": (_ci, [_vp, _ci, _ci, _ci, _vp]),
     "ertgb_analytic_potentials": (_ci, [_vp, _d]),
     "ertgb_set_scheme": (_ci, [_vp, _ci, _vp, _vp]),
     "ertgb_set_solver": (_ci, [_vp, _d, _ci, _ci]),

@@ -380,12 +380,42 @@ __global__ void k_boundary_alpha(int64_t B, int nK, const double *__restrict__ k
     }
 }
 
-// Unit-current primary potential at every node for column t = k*nE + e
-// (exactDCSolution with the singular value at the source node).
+// Unit-current half-space potential at node (vx, vy, vz) of a source at s
+// whose node is snode (exactDCSolution with the singular value at that node,
+// radius mr).
+__device__ double unit_potential(int64_t node, double vx, double vy, double vz, const double *s, int64_t snode,
+                                 double mr, double k, double surface_z, int fullspace) {
+    if (node == snode) return (k > 0.0) ? as_k0(mr / 6.0 * k) / kPi : 1.0 / (2.0 * kPi * mr / 2.0);
+    const double dx = vx - s[0], dy = vy - s[1], dz = vz - s[2];
+    const double r = sqrt(dx * dx + dy * dy + dz * dz);
+    if (r < kTol) return 0.0;
+    const int ax = (k > 0.0) ? 1 : 2;
+    double m[3] = {s[0], s[1], s[2]};
+    m[ax] = 2.0 * surface_z - s[ax];
+    if (fullspace) return (k == 0.0) ? 1.0 / (4.0 * kPi * r) : as_k0(r * k) / (2.0 * kPi);
+    const double mx = vx - m[0], my = vy - m[1], mz = vz - m[2];
+    const double rm = sqrt(mx * mx + my * my + mz * mz);
+    if (k == 0.0) return (1.0 / r + 1.0 / rm) / (4.0 * kPi);
+    if (m[0] == s[0] && m[1] == s[1] && m[2] == s[2]) return as_k0(r * k) / kPi;
+    return (as_k0(r * k) + as_k0(rm * k)) / (2.0 * kPi);
+}
+
+// Where the current returns: electrode ref_e (>= 0), else a node (rnode >= 0,
+// at rpos with singular radius rmr), else nowhere (infinity).
+struct RefSource {
+    int ref_e;
+    int64_t rnode;
+    double rpos[3];
+    double rmr;
+};
+
+// Primary potential of the unit-current pattern of column t = k*nE + e at
+// every node: the source at electrode e minus the reference electrode's
+// (checkPrimpotentials_, core/src/bert/dcfemmodelling.cpp:2085-2090).
 __global__ void k_primary(int64_t n, int nE, int nK, int64_t Rpad, const double *__restrict__ xyz,
                           const double *__restrict__ epos, const int32_t *__restrict__ enode,
                           const double *__restrict__ emin_r, const double *__restrict__ kv,
-                          double surface_z, int fullspace, double *__restrict__ up) {
+                          double surface_z, int fullspace, RefSource ref, double *__restrict__ up) {
     const int64_t R = (int64_t)nE * nK;
     const int64_t total = n * Rpad;
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
@@ -399,36 +429,13 @@ __global__ void k_primary(int64_t n, int nE, int nK, int64_t Rpad, const double 
         const int ki = (int)(t / nE);
         const int e = (int)(t - (int64_t)ki * nE);
         const double k = kv[ki];
-        const double *s = epos + 3 * e;
         const double vx = xyz[3 * node], vy = xyz[3 * node + 1], vz = xyz[3 * node + 2];
-        double val;
-        if (node == enode[e]) {
-            const double mr = emin_r[e];
-            val = (k > 0.0) ? as_k0(mr / 6.0 * k) / kPi : 1.0 / (2.0 * kPi * mr / 2.0);
-        } else {
-            const double dx = vx - s[0], dy = vy - s[1], dz = vz - s[2];
-            const double r = sqrt(dx * dx + dy * dy + dz * dz);
-            if (r < kTol) {
-                val = 0.0;
-            } else {
-                const int ax = (k > 0.0) ? 1 : 2;
-                double m[3] = {s[0], s[1], s[2]};
-                m[ax] = 2.0 * surface_z - s[ax];
-                if (fullspace) {
-                    val = (k == 0.0) ? 1.0 / (4.0 * kPi * r) : as_k0(r * k) / (2.0 * kPi);
-                } else {
-                    const double mx = vx - m[0], my = vy - m[1], mz = vz - m[2];
-                    const double rm = sqrt(mx * mx + my * my + mz * mz);
-                    if (k == 0.0) {
-                        val = (1.0 / r + 1.0 / rm) / (4.0 * kPi);
-                    } else if (m[0] == s[0] && m[1] == s[1] && m[2] == s[2]) {
-                        val = as_k0(r * k) / kPi;
-                    } else {
-                        val = (as_k0(r * k) + as_k0(rm * k)) / (2.0 * kPi);
-                    }
-                }
-            }
-        }
+        double val = unit_potential(node, vx, vy, vz, epos + 3 * e, enode[e], emin_r[e], k, surface_z, fullspace);
+        if (ref.ref_e >= 0)
+            val -= unit_potential(node, vx, vy, vz, epos + 3 * ref.ref_e, enode[ref.ref_e], emin_r[ref.ref_e], k,
+                                  surface_z, fullspace);
+        else if (ref.rnode >= 0)
+            val -= unit_potential(node, vx, vy, vz, ref.rpos, ref.rnode, ref.rmr, k, surface_z, fullspace);
         up[idx] = val;
     }
 }
@@ -485,15 +492,31 @@ __global__ void k_dinv(int64_t n, int nK, int64_t nnz, const int32_t *__restrict
     }
 }
 
+__device__ double geo_mean(const int32_t *__restrict__ lst, int a, int b, const double *__restrict__ rho) {
+    double s = 0.0;
+    for (int q = a; q < b; q++) s += log(rho[lst[q]]);
+    return exp(s / (double)(b - a));
+}
+
+// Source resistivity of electrode e's pattern: the geometric mean of the
+// cells around the electrode, averaged with the reference electrode's
+// (electrode ref_e, or the nrc cells around the reference node) over those
+// above the tolerance (calculateK, core/src/bert/dcfemmodelling.cpp:2236-2266).
 __global__ void k_source_rho(int nE, const int32_t *__restrict__ ptr, const int32_t *__restrict__ ecell,
-                             const double *__restrict__ rho, double *__restrict__ out) {
+                             const double *__restrict__ rho, int ref_e, const int32_t *__restrict__ rcell, int nrc,
+                             double *__restrict__ out) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nE) return;
-    double s = 0.0;
-    const int a = ptr[e], b = ptr[e + 1];
-    for (int q = a; q < b; q++) s += log(rho[ecell[q]]);
-    s /= (double)(b - a);
-    out[e] = exp(s);
+    double rs = geo_mean(ecell, ptr[e], ptr[e + 1], rho);
+    if (ref_e >= 0 || nrc > 0) {
+        const double rr = ref_e >= 0 ? geo_mean(ecell, ptr[ref_e], ptr[ref_e + 1], rho) : geo_mean(rcell, 0, nrc, rho);
+        double sum = 0.0;
+        int cnt = 0;
+        if (rs > kTol) sum += rs, cnt++;
+        if (rr > kTol) sum += rr, cnt++;
+        if (cnt) rs = sum / cnt;
+    }
+    out[e] = rs;
 }
 
 __global__ void k_check_rho(int64_t C, const double *__restrict__ rho, int32_t *__restrict__ bad) {
@@ -618,15 +641,46 @@ __global__ void k_collect(int nE, int nK, int64_t Rpad, const int32_t *__restric
 // Total potential: column t = k * nE + e carries a unit current at electrode
 // e: its source row (ElectrodeShapeNode / ElectrodeShapeDomain::assembleRHS,
 // core/src/bert/electrode.cpp:133-150, 341-355) or the shape functions of
-// the cell holding it (ElectrodeShapeEntity::assembleRHS, 278-290); b is
-// zeroed before.
+// the cell holding it (ElectrodeShapeEntity::assembleRHS, 278-290), and the
+// reference electrode's rows with the weights negated (calculateK_,
+// core/src/bert/dcfemmodelling.cpp:1862-1864); b is zeroed before.
 __global__ void k_rhs_total(int nE, int64_t R, int64_t Rpad, const int32_t *__restrict__ ew_ptr,
-                            const int32_t *__restrict__ ew_row, const double *__restrict__ ew_w,
+                            const int32_t *__restrict__ ew_row, const double *__restrict__ ew_w, int n_sink,
+                            const int32_t *__restrict__ sink_row, const double *__restrict__ sink_w,
                             double *__restrict__ b) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t >= R) return;
     const int e = (int)(t % nE);
-    for (int q = ew_ptr[e]; q < ew_ptr[e + 1]; q++) b[(int64_t)ew_row[q] * Rpad + t] = ew_w[q];
+    for (int q = ew_ptr[e]; q < ew_ptr[e + 1]; q++) b[(int64_t)ew_row[q] * Rpad + t] += ew_w[q];
+    for (int q = 0; q < n_sink; q++) b[(int64_t)sink_row[q] * Rpad + t] -= sink_w[q];
+}
+
+// Homogeneous Dirichlet rows (assembleStiffnessMatrixHomogenDirichletBC,
+// core/src/bert/dcfemmodelling.cpp:141-154): on a fixed row every entry 0
+// but the diagonal 1, on a fixed column every entry 0; one warp per row.
+__global__ void k_clean_fixed(int64_t n, int nK, int64_t nnz, const int32_t *__restrict__ rowptr,
+                              const int32_t *__restrict__ colidx, const uint8_t *__restrict__ fixed,
+                              double *__restrict__ vals) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t row = warp; row < n; row += nwarps) {
+        const bool fr = fixed[row] != 0;
+        for (int32_t q = rowptr[row] + lane; q < rowptr[row + 1]; q += 32) {
+            const int32_t col = colidx[q];
+            if (!fr && !fixed[col]) continue;
+            const double v = (fr && col == row) ? 1.0 : 0.0;
+            for (int ki = 0; ki < nK; ki++) vals[(int64_t)ki * nnz + q] = v;
+        }
+    }
+}
+
+// Singularity removal: zero right-hand side on the calibration rows
+// (calculateK, core/src/bert/dcfemmodelling.cpp:2281-2283).
+__global__ void k_zero_rows(int n_rows, const int32_t *__restrict__ rows, int64_t Rpad, double *__restrict__ b) {
+    const int64_t total = (int64_t)n_rows * Rpad;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x)
+        b[(int64_t)rows[i / Rpad] * Rpad + i % Rpad] = 0.0;
 }
 
 __device__ inline double abmn_u(const double *U, int nE, int a, int b, int m, int n) {
@@ -720,13 +774,22 @@ void compute_boundary_alpha(Context &c) {
     }
 }
 
+static RefSource ref_source(const Context &c) {
+    RefSource r{};
+    r.ref_e = c.ref_elec;
+    r.rnode = c.ref_elec < 0 ? c.ref_node : -1;
+    for (int d = 0; d < 3; d++) r.rpos[d] = c.ref_pos[d];
+    r.rmr = c.ref_minr;
+    return r;
+}
+
 void compute_primary(Context &c) {
     MeshData &m = c.mesh;
     c.d_up.alloc((size_t)m.n * c.Rpad);
     const int fullspace = (c.surface_z == -DBL_MAX || std::isnan(c.surface_z)) ? 1 : 0;
     k_primary<<<grid1(m.n * c.Rpad, kThreads, 1 << 16), kThreads, 0, c.stream>>>(
         m.n, c.nE, c.nK, c.Rpad, m.d_xyz.p, c.d_epos.p, c.d_enode.p, c.d_emin_r.p, c.d_k.p, c.surface_z,
-        fullspace, c.d_up.p);
+        fullspace, ref_source(c), c.d_up.p);
     ERTGB_CUDA(cudaGetLastError());
 }
 
@@ -741,7 +804,7 @@ void analytic_potentials(Context &c, double rho, double *out) {
     const int64_t total = m.n * c.Rpad;
     k_primary<<<grid1(total, kThreads, 1 << 16), kThreads, 0, c.stream>>>(
         m.n, c.nE, c.nK, c.Rpad, m.d_xyz.p, c.d_epos.p, c.d_enode.p, c.d_emin_r.p, c.d_k.p, c.surface_z, fullspace,
-        out);
+        ref_source(c), out);
     ERTGB_CUDA(cudaGetLastError());
     k_scale<<<grid1(total, kThreads, 1 << 16), kThreads, 0, c.stream>>>(total, rho, out);
     ERTGB_CUDA(cudaGetLastError());
@@ -768,7 +831,41 @@ void build_electrode_weights(Context &c) {
     c.d_ew_ptr.upload(ptr, c.stream);
     c.d_ew_row.upload(row, c.stream);
     c.d_ew_w.upload(wt, c.stream);
+    // the reference electrode's rows and weights (negated in the right-hand side)
+    std::vector<int32_t> srow;
+    std::vector<double> sw;
+    if (c.ref_elec >= 0) {
+        srow.assign(row.begin() + ptr[c.ref_elec], row.begin() + ptr[c.ref_elec + 1]);
+        sw.assign(wt.begin() + ptr[c.ref_elec], wt.begin() + ptr[c.ref_elec + 1]);
+    } else if (c.ref_node >= 0) {
+        srow.push_back(c.ref_node);
+        sw.push_back(1.0);
+    }
+    c.n_sink = (int)srow.size();
+    c.d_sink_row.upload(srow, c.stream);
+    c.d_sink_w.upload(sw, c.stream);
+    c.d_ref_cells.upload(c.ref_cells, c.stream);
+    // fixed rows: Dirichlet boundary nodes and calibration nodes
+    const MeshData &m = c.mesh;
+    c.have_fixed = !m.dir_nodes.empty() || !c.calib.empty();
+    if (c.have_fixed) {
+        std::vector<uint8_t> fixed((size_t)m.n, 0);
+        for (int32_t v : m.dir_nodes) fixed[v] = 1;
+        for (int32_t v : c.calib) fixed[v] = 1;
+        c.d_fixed.upload(fixed, c.stream);
+    } else {
+        c.d_fixed.release();
+    }
+    c.d_calib.upload(c.calib, c.stream);
     ERTGB_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+void clean_fixed_rows(Context &c, double *vals, cudaStream_t s) {
+    if (!c.have_fixed) return;
+    MeshData &m = c.mesh;
+    k_clean_fixed<<<grid1(m.n * 32, kThreads, 1 << 14), kThreads, 0, s>>>(m.n, c.nK, m.nnz, m.d_rowptr.p,
+                                                                          m.d_colidx.p, c.d_fixed.p, vals);
+    ERTGB_CUDA(cudaGetLastError());
 }
 
 void upload_primary(Context &c) {
@@ -793,6 +890,7 @@ void assemble_all(Context &c, const double *rho_cell, double *vals, cudaStream_t
                                          c.d_alpha.p, m.d_bnd_cell.p, rho_cell, c.d_k.p, m.nv * m.nv,
                                          m.nvb * m.nvb, m.C, m.B, m.d_ext_ptr.p, m.d_ext_val.p, vals);
     ERTGB_CUDA(cudaGetLastError());
+    clean_fixed_rows(c, vals, s);
     if (rho_cell) {
         c.d_dinv.alloc((size_t)m.n * c.nK);
         k_dinv<<<grid1(m.n * c.nK), kThreads, 0, s>>>(m.n, c.nK, m.nnz, m.d_diag.p, vals, c.d_dinv.p);
@@ -820,8 +918,9 @@ void check_rho(Context &c, const double *rho_cell, cudaStream_t s) {
 
 void compute_source_rho(Context &c, const double *rho_cell, cudaStream_t s) {
     c.d_rhos.alloc(c.nE);
+    const int nrc = c.ref_elec < 0 && c.ref_node >= 0 ? (int)c.ref_cells.size() : 0;
     k_source_rho<<<(unsigned)ceil_div(c.nE, 128), 128, 0, s>>>(c.nE, c.d_ecell_ptr.p, c.d_ecell.p, rho_cell,
-                                                              c.d_rhos.p);
+                                                              c.ref_elec, c.d_ref_cells.p, nrc, c.d_rhos.p);
     ERTGB_CUDA(cudaGetLastError());
 }
 
@@ -831,13 +930,19 @@ void build_rhs(Context &c, cudaStream_t s) {
                                                                   m.d_colidx.p, c.d_S.p, c.d_S1.p, c.d_up.p,
                                                                   c.d_rhos.p, c.d_r.p);
     ERTGB_CUDA(cudaGetLastError());
+    if (!c.calib.empty()) {
+        k_zero_rows<<<grid1((int64_t)c.calib.size() * c.Rpad), kThreads, 0, s>>>((int)c.calib.size(), c.d_calib.p,
+                                                                                 c.Rpad, c.d_r.p);
+        ERTGB_CUDA(cudaGetLastError());
+    }
 }
 
 void build_rhs_total(Context &c, cudaStream_t s) {
     MeshData &m = c.mesh;
     ERTGB_CUDA(cudaMemsetAsync(c.d_r.p, 0, sizeof(double) * (size_t)m.n * c.Rpad, s));
     k_rhs_total<<<(unsigned)ceil_div(c.R, kThreads), kThreads, 0, s>>>(c.nE, c.R, c.Rpad, c.d_ew_ptr.p, c.d_ew_row.p,
-                                                                       c.d_ew_w.p, c.d_r.p);
+                                                                       c.d_ew_w.p, c.n_sink, c.d_sink_row.p,
+                                                                       c.d_sink_w.p, c.d_r.p);
     ERTGB_CUDA(cudaGetLastError());
     c.d_pnorm2.release();  // no primary field: the reference norm is ||b||
 }

@@ -48,6 +48,14 @@ template <class F> int guard(Context *c, F &&f) {
     }
 }
 
+void clear_reference(Context &c) {
+    c.ref_elec = -1;
+    c.ref_node = -1;
+    c.ref_minr = 0.0;
+    c.ref_cells.clear();
+    c.calib.clear();
+}
+
 void invalidate_derived(Context &c) {
     c.fp64_k.clear();
     c.up_user.clear();  // given primaries belong to the mesh, electrodes and wavenumbers they were set for
@@ -109,6 +117,21 @@ void ensure_derived(Context &c) {
         for (int e = 0; e < c.nE; e++)
             if (c.enode[e] < 0 && c.ent_cell[e] < 0)
                 throw Error(ERTGB_STATE, "singularity removal needs a node or a cell for every electrode");
+    }
+    const MeshData &m = c.mesh;
+    if (m.dim == 3 && m.B == 0 && m.dir_nodes.empty() && c.calib.empty())
+        throw Error(ERTGB_STATE, "a closed (Neumann-only) 3-D domain needs a calibration node (ertgb_set_reference)");
+    if (!m.ext_rows.empty() || m.n_ext > 0) {
+        if (c.ref_elec >= 0 || c.ref_node >= 0)
+            throw Error(ERTGB_STATE, "a reference electrode with complete-electrode-model or bypass electrodes "
+                                     "is not supported");
+        if (!m.dir_nodes.empty()) {
+            std::vector<uint8_t> fixed((size_t)m.nn, 0);
+            for (int32_t v : m.dir_nodes) fixed[v] = 1;
+            for (size_t i = 0; i < m.ext_rows.size(); i++)
+                if ((m.ext_rows[i] < m.nn && fixed[m.ext_rows[i]]) || (m.ext_cols[i] < m.nn && fixed[m.ext_cols[i]]))
+                    throw Error(ERTGB_STATE, "a complete-electrode-model or bypass entry on a Dirichlet boundary node");
+        }
     }
     if (!c.prim_ready) {
         build_electrode_weights(c);
@@ -285,13 +308,20 @@ int ertgb_set_mesh(ertgb_ctx *ctx, int dim, int order, int n_nodes, const double
         int32_t pmax = -1;
         for (int32_t v : m.marker) pmax = std::max(pmax, v);
         m.P = (int64_t)pmax + 1;
-        bool have_mixed = false;
+        std::set<int32_t> dir;
         for (int b = 0; b < n_bnd; b++) {
             const int mk = bnd_marker[b];
-            if (mk == -3 || mk == -4)
-                throw Error(ERTGB_BAD_INPUT, "Dirichlet boundary markers (-3, -4) are not supported");
+            if (mk == -4)  // the reference throws here as well (dcfemmodelling.cpp:293)
+                throw Error(ERTGB_BAD_INPUT, "inhomogeneous Dirichlet boundaries (marker -4) are not implemented");
+            if (mk == -3) {  // homogeneous Dirichlet: the boundary's nodes are fixed rows
+                for (int i = 0; i < m.nvb; i++) {
+                    const int32_t v = bnd_nodes[(size_t)b * m.nvb + i];
+                    ERTGB_REQUIRE(v >= 0 && v < n_nodes, "boundary node index out of range");
+                    dir.insert(v);
+                }
+                continue;
+            }
             if (mk != -2) continue;
-            have_mixed = true;
             for (int i = 0; i < m.nvb; i++) {
                 const int32_t v = bnd_nodes[(size_t)b * m.nvb + i];
                 ERTGB_REQUIRE(v >= 0 && v < n_nodes, "boundary node index out of range");
@@ -301,13 +331,13 @@ int ertgb_set_mesh(ertgb_ctx *ctx, int dim, int order, int n_nodes, const double
                           "mixed boundary without an adjacent cell");
             m.bnd_cell.push_back(bnd_cell[b]);
         }
-        if (!have_mixed && dim == 3)
-            throw Error(ERTGB_BAD_INPUT, "Neumann-only domains (no mixed boundary) are not supported");
+        m.dir_nodes.assign(dir.begin(), dir.end());
         m.B = (int64_t)m.bnd_cell.size();
         build_pattern(m);
         build_mesh_device(*c);
         c->have_mesh = true;
         c->have_elec = false;
+        clear_reference(*c);
         c->src_row.clear();
         c->collect_last_k = false;
         invalidate_derived(*c);
@@ -392,6 +422,51 @@ int ertgb_set_electrodes(ertgb_ctx *ctx, int n_elec, const int32_t *elec_node, d
         c->d_src_row.upload(c->src_row, s);
         ERTGB_CUDA(cudaStreamSynchronize(s));
         c->have_elec = true;
+        clear_reference(*c);
+        invalidate_derived(*c);
+    });
+}
+
+int ertgb_set_reference(ertgb_ctx *ctx, int ref_electrode, int ref_node, int n_calib, const int32_t *calib) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        if (!c->have_mesh || !c->have_elec) throw Error(ERTGB_STATE, "set the mesh and the electrodes first");
+        MeshData &m = c->mesh;
+        ERTGB_REQUIRE(ref_electrode >= -1 && ref_electrode < c->nE, "reference electrode out of range");
+        ERTGB_REQUIRE(ref_node >= -1 && ref_node < m.nn, "reference node out of range");
+        ERTGB_REQUIRE(ref_electrode < 0 || ref_node < 0, "give either a reference electrode or a reference node");
+        ERTGB_REQUIRE(n_calib >= 0 && (n_calib == 0 || calib), "null calibration nodes");
+        std::set<int32_t> cal;
+        for (int i = 0; i < n_calib; i++) {
+            ERTGB_REQUIRE(calib[i] >= 0 && calib[i] < m.nn, "calibration node out of range");
+            cal.insert(calib[i]);
+        }
+        clear_reference(*c);
+        c->ref_elec = ref_electrode;
+        c->ref_node = ref_node;
+        if (ref_node >= 0) {
+            for (int d = 0; d < 3; d++) c->ref_pos[d] = m.xyz[3 * (size_t)ref_node + d];
+            double mr = DBL_MAX;
+            for (int64_t cc = 0; cc < m.C; cc++) {
+                const int32_t *cn = &m.cells[(size_t)cc * m.nv];
+                bool has = false;
+                for (int i = 0; i < m.nv; i++) has |= cn[i] == ref_node;
+                if (!has) continue;
+                c->ref_cells.push_back((int32_t)cc);
+                for (int i = 0; i < m.nv; i++) {
+                    if (cn[i] == ref_node) continue;
+                    double d2 = 0;
+                    for (int d = 0; d < 3; d++) {
+                        const double dd = m.xyz[3 * (size_t)ref_node + d] - m.xyz[3 * (size_t)cn[i] + d];
+                        d2 += dd * dd;
+                    }
+                    mr = std::min(mr, std::sqrt(d2));
+                }
+            }
+            ERTGB_REQUIRE(!c->ref_cells.empty(), "reference node belongs to no cell");
+            c->ref_minr = mr;
+        }
+        c->calib.assign(cal.begin(), cal.end());
         invalidate_derived(*c);
     });
 }

@@ -858,6 +858,9 @@ int complex_response(Context &c, const double *rho_re, const double *rho_im, dou
                                      "electrode model is real-valued only, dcfemmodelling.cpp:423-428)");
     for (int32_t cell : c.ent_cell)
         if (cell >= 0) throw Error(ERTGB_BAD_INPUT, "complex resistivity needs node electrodes");
+    if (c.ref_elec >= 0 || c.ref_node >= 0 || c.have_fixed)
+        throw Error(ERTGB_BAD_INPUT, "complex resistivity with a reference electrode, calibration nodes or "
+                                     "Dirichlet boundaries is not supported");
     const int64_t n = m.n, nnz = m.nnz, Rpad = c.Rpad, R = c.R;
     x.have_pot = false;
     // 1 / rho* per cell

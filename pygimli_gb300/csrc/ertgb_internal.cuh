@@ -77,6 +77,7 @@ struct MeshData {
     std::vector<int32_t> marker;  // C
     std::vector<int32_t> rowptr, colidx;
     std::vector<int32_t> bnd_nodes, bnd_cell;  // mixed boundaries only
+    std::vector<int32_t> dir_nodes;            // nodes of homogeneous Dirichlet boundaries (sorted)
     // FSAI factor pattern: lower triangle of A and its transpose
     std::vector<int32_t> Lrowptr, Lcolidx, LtoA, Urowptr, Ucolidx, UtoL;
     DBuf<int32_t> d_Lrowptr, d_Lcolidx, d_LtoA, d_Urowptr, d_Ucolidx, d_UtoL;
@@ -193,6 +194,23 @@ struct Context {
     DBuf<double> d_ew_w;
     std::vector<int32_t> ecell_ptr, ecell;   // incident cells per electrode
     DBuf<int32_t> d_enode, d_ecell_ptr, d_ecell;
+    // current reference: the pattern of electrode e carries +1 at e and -1 at
+    // the reference electrode (an electrode, ref_elec, or a node, ref_node;
+    // neither: the current leaves at infinity)
+    int ref_elec = -1, ref_node = -1;
+    double ref_pos[3] = {0, 0, 0};
+    double ref_minr = 0.0;                   // singular radius of the reference node
+    std::vector<int32_t> ref_cells;          // cells around the reference node
+    DBuf<int32_t> d_ref_cells;
+    DBuf<int32_t> d_sink_row;                // rows and weights of the reference's -1
+    DBuf<double> d_sink_w;
+    int n_sink = 0;
+    // rows held at zero potential: calibration nodes (zero singularity-removal
+    // right-hand side) and Dirichlet nodes; fixed[row] = 1 cleans row and column
+    std::vector<int32_t> calib;
+    DBuf<int32_t> d_calib;
+    DBuf<uint8_t> d_fixed;
+    bool have_fixed = false;
     // formulation (ertgb_formulation); total potential: the row of each
     // electrode's current and potential, and the CEM collect of the last
     // wavenumber only
@@ -291,8 +309,12 @@ void collect_response(Context &c, double *rhoa, cudaStream_t s);
 // total potential: unit currents at the electrodes' source rows into d_r
 void build_rhs_total(Context &c, cudaStream_t s);
 // rows and weights of every electrode's source and potential (its node / source
-// row with weight 1, or the shape functions of the cell holding it)
+// row with weight 1, or the shape functions of the cell holding it), the
+// reference electrode's sink and the fixed-row flags
 void build_electrode_weights(Context &c);
+// homogeneous Dirichlet rows and columns (diagonal 1) of the fixed rows in
+// nK matrices of the pattern
+void clean_fixed_rows(Context &c, double *vals, cudaStream_t s);
 void check_rho(Context &c, const double *rho_cell, cudaStream_t s);
 // pcg.cu
 // mask: warm start (x kept) on the columns with mask[t] != 0; nullptr = cold start, all columns

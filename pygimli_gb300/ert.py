@@ -13,10 +13,12 @@ Every numerical step runs in libertgb.so (hand-written sm_103a CUDA behind
 the C ABI of include/ertgb.h); this module only does setup bookkeeping
 (electrode search, wavenumbers, model mapping) and moves buffers.
 
-Scope (raises otherwise): node electrodes (marker -99; with sr=False also
-CEM and bypass electrodes), flat surface with mixed far-field boundaries,
-pole current pattern (the reference's default when there is no reference
-electrode).
+Scope (raises otherwise): node electrodes (marker -99) and electrodes inside
+cells, with sr=False also CEM and bypass electrodes; mixed far-field,
+homogeneous Neumann and homogeneous Dirichlet (-3) boundaries, closed
+(Neumann-only) domains with calibration nodes (-1000) and a reference
+electrode (node marker -999 or the last electrode); pole current patterns
+or patterns against the reference electrode.
 """
 from __future__ import annotations
 
@@ -28,10 +30,14 @@ from . import _native
 from .cem import electrode_setup, has_cem_markers
 from .data import DataContainerERT, geometricFactors
 from .kwave import init_kwave_list
-from .mesh import MARKER_BOUND_HOMOGEN_NEUMANN, MARKER_BOUND_MIXED, MARKER_NODE_ELECTRODE, Mesh
+from .mesh import (MARKER_BOUND_HOMOGEN_DIRICHLET, MARKER_BOUND_HOMOGEN_NEUMANN, MARKER_BOUND_MIXED,
+                   MARKER_NODE_ELECTRODE, Mesh)
 from .modelmap import map_model
 
 TOLERANCE = 1e-12
+MARKER_BOUND_DIRICHLET = -4
+MARKER_NODE_REFERENCEELECTRODE = -999
+MARKER_NODE_CALIBRATION = -1000
 
 
 def _torch():
@@ -114,13 +120,52 @@ def search_electrodes(mesh, sensors):
 
 def surface_info(mesh):
     """surfaceZ and topography flag of updateMeshDependency_
-    (core/src/bert/dcfemmodelling.cpp:711-773)."""
+    (core/src/bert/dcfemmodelling.cpp:711-773); a domain without mixed and
+    Dirichlet boundaries counts as topography (:750-755)."""
     bm = mesh.boundary_markers
     neu = np.nonzero(bm == MARKER_BOUND_HOMOGEN_NEUMANN)[0]
+    closed = not np.any((bm == MARKER_BOUND_MIXED) | (bm == MARKER_BOUND_HOMOGEN_DIRICHLET))
     if len(neu) == 0:
-        return -np.finfo(np.float64).max, False
+        return -np.finfo(np.float64).max, closed
     c = mesh.nodes[mesh.boundaries[neu]].mean(axis=1)[:, mesh.dim() - 1]
-    return float(c[0]), bool(np.any(c != c[0]))
+    return float(c[0]), bool(np.any(c != c[0])) or closed
+
+
+class BoundarySetup:
+    """Boundary conditions and current reference of a mesh with n_elec
+    electrodes, as updateMeshDependency_ and searchElectrodes_ choose them
+    (core/src/bert/dcfemmodelling.cpp:711-773, 799-802, 1011-1073):
+    ``neumann`` (no mixed, no Dirichlet boundary), ``topography``,
+    ``dirichlet`` (nodes of -3 boundaries), ``calib`` (a closed 3-D domain:
+    the nodes with marker -1000, else node 0), ``ref_node`` (the first node
+    with marker -999, in any domain; -1: none) and ``ref_elec`` (a closed
+    3-D domain without reference node: the last electrode; else -1)."""
+
+    def __init__(self, neumann, topography, dirichlet, calib, ref_node, ref_elec):
+        self.neumann, self.topography = neumann, topography
+        self.dirichlet, self.calib = dirichlet, calib
+        self.ref_node, self.ref_elec = ref_node, ref_elec
+
+
+def boundary_setup(mesh, n_elec):
+    bm = np.asarray(mesh.boundary_markers)
+    if np.any(bm == MARKER_BOUND_DIRICHLET):
+        raise NotImplementedError("inhomogeneous Dirichlet boundaries (marker -4) are not implemented")
+    _, topo = surface_info(mesh)
+    neumann = not np.any((bm == MARKER_BOUND_MIXED) | (bm == MARKER_BOUND_HOMOGEN_DIRICHLET))
+    d = mesh.boundaries[bm == MARKER_BOUND_HOMOGEN_DIRICHLET]
+    dirichlet = np.unique(d) if d.size else np.zeros(0, np.int64)
+    nm = np.asarray(mesh.node_markers)
+    refs = np.flatnonzero(nm == MARKER_NODE_REFERENCEELECTRODE)
+    ref_node = int(refs[0]) if len(refs) else -1
+    calib, ref_elec = np.zeros(0, np.int64), -1
+    if neumann and mesh.dim() == 3:  # 2.5-D is never a Neumann domain (:758-766)
+        calib = np.flatnonzero(nm == MARKER_NODE_CALIBRATION)
+        if len(calib) == 0:
+            calib = np.zeros(1, np.int64)
+        if ref_node < 0 and n_elec > 0:
+            ref_elec = n_elec - 1
+    return BoundarySetup(neumann, topo, dirichlet, calib, ref_node, ref_elec)
 
 
 class ERTModelling:
@@ -288,9 +333,7 @@ class ERTModelling:
         if topo and self._sr and mesh.order != 1:
             raise NotImplementedError("singularity removal on a topographic surface computes its primary "
                                       "potentials on createP2 of the mesh: the mesh must be linear")
-        bm = mesh.boundary_markers
-        if mesh.dim() == 3 and not np.any(bm == MARKER_BOUND_MIXED):
-            raise NotImplementedError("Neumann-only domains are not supported")
+        boundary_setup(mesh, 0)  # refuses -4 boundaries
         b = np.ascontiguousarray(mesh.boundaries, np.int32)
         self._check(self._lib.ertgb_set_mesh(
             self._ctx, mesh.dim(), mesh.order, mesh.nodeCount(), _ptr(mesh.nodes), mesh.cellCount(),
@@ -363,6 +406,15 @@ class ERTModelling:
             self._check(self._lib.ertgb_set_extension(
                 self._ctx, int(e.n_ext), len(e.rows), _ptr(e.rows), _ptr(e.cols), _ptr(e.vals), _ptr(e.src_row),
                 _ptr(e.src_center), 1 if e.cem else 0))
+        bc = boundary_setup(mesh, len(self._elec_nodes))
+        if bc.ref_node >= 0 or bc.ref_elec >= 0:
+            if self._electrodes is not None and (self._electrodes.cem or len(self._electrodes.rows)):
+                raise NotImplementedError("a reference electrode with complete-electrode-model or bypass "
+                                          "electrodes is not supported")
+        calib = np.ascontiguousarray(bc.calib, np.int32)
+        self._check(self._lib.ertgb_set_reference(self._ctx, int(bc.ref_elec), int(bc.ref_node), len(calib),
+                                                  _ptr(calib) if len(calib) else None))
+        self._bc = bc
         if not self._kw_user:
             self._k, self._w = init_kwave_list(mesh.dim(), data.sensorPositions())
         self._push_kw()
