@@ -626,10 +626,13 @@ def run_ours(args, world, rank, local):
     if not args.no_e2e:
         rho_h = np.ascontiguousarray(rho, np.float64)
         rhoa_h = np.empty(D, np.float64)
-        # a plain host array: on Grace the device writes it over the coherent
-        # link at full speed (a pinned torch buffer of this size was slower)
+        # a plain host array allocated and touched once, as a Gauss-Newton
+        # loop reuses it (on the GB300 machine's host the copy into it ran at
+        # 40-190 GB/s from run to run; into page-locked or huge-page host
+        # buffers it was not faster)
         Jh = np.empty((D, P), dtype=np.float64 if jdt == 0 else np.float32)
-        tt, tr, its = [], [], []
+        Jh.reshape(-1)[:: 4096 // Jh.itemsize] = 0
+        tt, tr, its, tj = [], [], [], []
         for i in range(max(1, min(args.steps, 3)) + 1):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
@@ -640,10 +643,14 @@ def run_ours(args, world, rank, local):
                 tt.append(time.perf_counter() - t0)
                 tr.append(t1 - t0)
                 its.append(fop.stats()["iterations"])
+                tj.append(fop.stats()["ms_jacobian"] * 1e-3)
+        jbytes = D * P * Jh.itemsize
+        copy_s = float(np.mean(tt) - np.mean(tr) - np.mean(tj))
         e2e = {"value": float(np.mean(tt)), "unit": UNIT, "h2d_bytes_per_step": int(2 * C * 8),
-               "d2h_bytes_per_step": int(D * 8 + D * P * Jh.itemsize), "steps": len(tt),
-               "path": "ertgb_response_host + ertgb_jacobian_host (host numpy buffers)",
+               "d2h_bytes_per_step": int(D * 8 + jbytes), "steps": len(tt),
+               "path": "ertgb_response_host + ertgb_jacobian_host (host numpy buffers, allocated once)",
                "response_s": float(np.mean(tr)), "jacobian_with_copy_s": float(np.mean(tt) - np.mean(tr)),
+               "jacobian_copy_gbs": jbytes / copy_s / 1e9 if copy_s > 0 else None,
                "pcg_iterations": its,
                "check_rhoa_vs_device": float(np.max(np.abs(rhoa_h - rhoa_d.cpu().numpy()) / rhoa_h))}
         del Jh
