@@ -1,7 +1,9 @@
 """Test infrastructure only: FP64 numpy restatement of pyGIMLi's regularised
 CGLS (solveCGLSCDWWhtrans, core/src/solver.cpp:27-212), the checker of the
 GPU ``ertgb_cgls``.  Same operations in the same order, including the
-rounding of C (p wm) to 1e-10."""
+rounding of C (p wm) to 1e-10.  Pinned to the reference's own
+solveCGLSCDWWhtrans run through oracle/_ref (tests/golden/cgls_small.npz,
+tests/golden/make_cgls_golden.py; tests/test_inversion.py)."""
 from __future__ import annotations
 
 import numpy as np

@@ -98,6 +98,8 @@ def lib():
         L.ref_data_tokens.argtypes = [vp, cs, ctypes.c_int]
         L.ref_data_get.argtypes = [vp, cs, vp]
         L.ref_data_save.argtypes = [vp, cs, cs, cs, ctypes.c_int]
+        L.ref_cgls.argtypes = [ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp,
+                               ctypes.c_double, vp, ctypes.c_int, ctypes.c_double]
         _lib = L
     return _lib
 
@@ -450,3 +452,19 @@ def data_resave(path_in, path_out, fmt_data="all", fmt_sensor="x y z", no_filter
                                int(bool(no_filter))))
     finally:
         L.ref_data_free(h)
+
+
+def cgls(J, C, dW, b, x0, wc, wm, tm, td, lam, rough, max_iter=200, tol=-1.0):
+    """The reference's solveCGLSCDWWhtrans (core/src/solver.cpp:27-212): J
+    dense (nData x nModel), C = (rowptr, colidx, values, nModel) in CSR."""
+    rp, ci, cv, P = C
+    f = lambda a: np.ascontiguousarray(a, np.float64)  # noqa: E731
+    Jc = f(J)
+    rp = np.ascontiguousarray(rp, np.int32)
+    ci = np.ascontiguousarray(ci, np.int32)
+    arrs = [f(cv), f(dW), f(b), f(wc), f(wm), f(tm), f(td), f(rough)]
+    x = f(x0).copy()
+    cvv, dWv, bv, wcv, wmv, tmv, tdv, rv = arrs
+    _check(lib().ref_cgls(Jc.shape[0], Jc.shape[1], _p(Jc), len(rp) - 1, _p(rp), _p(ci), _p(cvv), _p(dWv), _p(bv),
+                          _p(x), _p(wcv), _p(wmv), _p(tmv), _p(tdv), float(lam), _p(rv), int(max_iter), float(tol)))
+    return x

@@ -16,6 +16,7 @@
 //   mesh / data I/O        core/src/mesh_io.cpp:391-662 (binary mesh v3),
 //                          mesh_io.cpp:674-992 exportVTK,
 //                          core/src/datacontainer.cpp:209-470 load, 518-615 save
+//   regularised CGLS       core/src/solver.cpp:27-212 solveCGLSCDWWhtrans
 //   solver injection       core/src/bert/dcfemmodelling.h:266 setSolver,
 //                          core/src/solverWrapper.h:26-56 SolverWrapper
 // The reference's default direct solver (CHOLMOD/UMFPACK) is not available,
@@ -33,6 +34,7 @@
 #include <bert/bertDataContainer.h>
 #include <bert/bertMisc.h>
 #include <bert/bertJacobian.h>
+#include <solver.h>
 
 #include <cstring>
 #include <exception>
@@ -644,6 +646,32 @@ int ref_data_get(void *dp, const char *token, double *out) {
 int ref_data_save(void *dp, const char *path, const char *fmtData, const char *fmtSensor, int noFilter) {
     DataContainerERT *d = (DataContainerERT *)dp;
     return guarded([&] { d->save(path, fmtData, fmtSensor, noFilter != 0, false); });
+}
+
+// The reference's regularised CGLS (solveCGLSCDWWhtrans, core/src/solver.cpp:
+// 27-212) on a dense J (nData x nModel, row-major) and a constraint matrix
+// given as CSR (nConst rows, built into the reference's RSparseMapMatrix);
+// x is the start vector on input and the solution on output.
+int ref_cgls(int nData, int nModel, const double *J, int nConst, const int *crp, const int *cci, const double *cv,
+             const double *dW, const double *b, double *x, const double *wc, const double *wm, const double *tm,
+             const double *td, double lambda, const double *rough, int maxIter, double tol) {
+    return guarded([&] {
+        RMatrix S(nData, nModel);
+        for (int i = 0; i < nData; i++)
+            for (int j = 0; j < nModel; j++) S[i][j] = J[(size_t)i * nModel + j];
+        RSparseMapMatrix C(nConst, nModel);
+        for (int i = 0; i < nConst; i++)
+            for (int q = crp[i]; q < crp[i + 1]; q++) C.setVal(i, cci[q], cv[q]);
+        auto vec = [](const double *v, int n) {
+            RVector r(n);
+            for (int i = 0; i < n; i++) r[i] = v[i];
+            return r;
+        };
+        RVector xv(vec(x, nModel));
+        solveCGLSCDWWhtrans(S, C, vec(dW, nData), vec(b, nData), xv, vec(wc, nConst), vec(wm, nModel),
+                            vec(tm, nModel), vec(td, nData), lambda, vec(rough, nConst), maxIter, tol, false);
+        for (int i = 0; i < nModel; i++) x[i] = xv[i];
+    });
 }
 
 }  // extern "C"

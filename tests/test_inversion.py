@@ -43,6 +43,25 @@ def test_oracle_cgls_solves_normal_equations():
     assert np.linalg.norm(x - xs) <= 1e-8 * np.linalg.norm(xs)
 
 
+def _golden(golden_dir):
+    z = np.load(golden_dir + "/cgls_small.npz")
+    C = (z["rp"], z["ci"], z["cv"], z["J"].shape[1])
+    args = (z["J"], C, z["dW"], z["b"], np.zeros(z["J"].shape[1]), z["wc"], z["wm"], z["tm"], z["td"], float(z["lam"]),
+            z["rough"])
+    return z, args
+
+
+def test_oracle_cgls_matches_reference(golden_dir):
+    """The oracle CGLS against the reference's own solveCGLSCDWWhtrans
+    (core/src/solver.cpp:27-212, fixture tests/golden/make_cgls_golden.py):
+    after 5 iterations and converged."""
+    z, args = _golden(golden_dir)
+    x5, _ = IO.cgls(*args, max_iter=5)
+    assert np.linalg.norm(x5 - z["x5"]) <= 1e-12 * np.linalg.norm(z["x5"])
+    xc, _ = IO.cgls(*args, max_iter=500, tol=1e-28)
+    assert np.linalg.norm(xc - z["xconv"]) <= 1e-9 * np.linalg.norm(z["xconv"])
+
+
 @pytest.fixture(scope="module")
 def torch():
     t = pytest.importorskip("torch")
@@ -99,3 +118,18 @@ def test_gauss_newton_step_lowers_objective(torch):
     # the anomaly is recovered as conductive
     inside = (np.abs(c[:, 0] - 10) < 2.0) & (c[:, 1] > -2.8) & (c[:, 1] < -1.2)
     assert np.median(model[inside]) < np.median(model[~inside])
+
+
+@pytest.mark.gpu
+def test_gpu_cgls_matches_reference(torch, golden_dir):
+    """The GPU CGLS (FP64 Jacobian) against the reference's own
+    solveCGLSCDWWhtrans after 5 iterations and converged."""
+    from pygimli_gb300.inversion import cgls
+    z, args = _golden(golden_dir)
+    Jd = torch.tensor(z["J"], dtype=torch.float64, device="cuda")
+    x5, _ = cgls(Jd, *args[1:], max_iter=5)
+    e5 = float(np.linalg.norm(x5 - z["x5"]) / np.linalg.norm(z["x5"]))
+    xc, _ = cgls(Jd, *args[1:], max_iter=500, tol=1e-28)
+    ec = float(np.linalg.norm(xc - z["xconv"]) / np.linalg.norm(z["xconv"]))
+    print(f"GPU CGLS vs reference: 5 iterations {e5:.2e}, converged {ec:.2e}")
+    assert e5 <= 1e-10 and ec <= 1e-8
