@@ -58,7 +58,7 @@ def parse():
                     default="box_3d_large")
     ap.add_argument("--rtol", type=float, default=1e-10)
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
-    ap.add_argument("--precond", choices=["jacobi", "fsai", "learned"], default="learned")
+    ap.add_argument("--precond", choices=["jacobi", "fsai", "learned", "ic0"], default="learned")
     ap.add_argument("--weights", default=None, help="learned preconditioner weights (.npz); default: the "
                     "packaged weights trained for the workload")
     ap.add_argument("--no-plain", action="store_true", help="skip the comparison runs (plain FP64 Jacobi, FSAI)")
@@ -549,11 +549,16 @@ def run_ours(args, world, rank, local):
         return res
 
     wl_main = (mesh, data, rho)
-    plain = fsai_form = cx_form = cem_form = c2_forms = None
+    plain = fsai_form = cx_form = cem_form = c2_forms = ic0_form = None
     if not args.no_plain and (args.precision, args.precond) != ("fp64", "jacobi"):
         plain = time_form(wl_main, "fp64", "jacobi", 0, "block PCG (Jacobi), FP64",
                           n_steps=max(1, min(args.steps, 2)), n_warm=1, ref_rhoa=rhoa_d)
         plain["ratio_to_value"] = plain["value"] / value
+    if not args.no_plain and args.precond != "ic0":
+        # the FP64 solver with the incomplete-Cholesky preconditioner
+        ic0_form = time_form(wl_main, "fp64", "ic0", 0, "block PCG (IC(0)), FP64",
+                             n_steps=max(1, min(args.steps, 2)), n_warm=1, ref_rhoa=rhoa_d)
+        ic0_form["ratio_to_value"] = ic0_form["value"] / value
     if not args.no_plain and args.precond == "learned":
         fsai_form = time_form(wl_main, args.precision, "fsai", jdt, f"block PCG (FSAI), {args.precision}",
                               ref_rhoa=rhoa_d)
@@ -701,7 +706,8 @@ def run_ours(args, world, rank, local):
                               f"{mesh.nodeCount() * fop.sizes()[3] * 8 / 1e6:.0f} MB, J "
                               f"{D * P * (8 if jdt == 0 else 4) / 1e9:.1f} GB"),
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-               "plain_fp64_gpu_pcg": plain, "fsai_form": fsai_form, "box_3d_forms": c2_forms,
+               "plain_fp64_gpu_pcg": plain, "fsai_form": fsai_form, "fp64_ic0_form": ic0_form,
+               "box_3d_forms": c2_forms,
                "gn_iteration": gn, "refine_h2": refine_rec, "complex_form": cx_form, "cem_form": cem_form,
                "learned_weights": os.path.relpath(weights, ROOT) if weights else None,
                "clocks": clk, "step_ms": step_ms,

@@ -40,7 +40,16 @@ typedef enum {
  * LEARNED: M^-1 = G^T G with G emitted by a message-passing network on the
  * graph of A (weights: ertgb_set_precond_weights), same pattern, same
  * application and the same FP64 Jacobi fallback as FSAI. */
-typedef enum { ERTGB_PRECOND_JACOBI = 0, ERTGB_PRECOND_FSAI = 1, ERTGB_PRECOND_LEARNED = 2 } ertgb_precond;
+/* IC0: incomplete Cholesky on A's lower pattern (no fill), factored on the
+ * device per response and wavenumber, level-scheduled triangular solves;
+ * FP64 precision only (the incomplete counterpart of the reference's CHOLMOD
+ * factorization, core/src/cholmodWrapper.cpp:309-420). */
+typedef enum {
+    ERTGB_PRECOND_JACOBI = 0,
+    ERTGB_PRECOND_FSAI = 1,
+    ERTGB_PRECOND_LEARNED = 2,
+    ERTGB_PRECOND_IC0 = 3
+} ertgb_precond;
 
 /* Length of the learned preconditioner's FP32 parameter vector: encoders
  * (2 x (64x4 + 64)), 4 layers of (W1 64x192, b1 64, W2 64x128, b2 64) and the

@@ -65,6 +65,14 @@ template <class T> struct DBuf {
     }
 };
 
+// Level schedule of the IC(0) factorization and triangular solves: rows of
+// the lower (forward) and upper (backward) pattern ordered by level.
+struct Ic0Plan {
+    bool ready = false;
+    std::vector<int32_t> frow, flev, brow, blev;
+    DBuf<int32_t> d_frow, d_brow;
+};
+
 // Mesh-dependent structures.
 struct MeshData {
     int dim = 0, order = 1, nv = 0, nvb = 0;  // nv / nvb: nodes per cell / boundary
@@ -81,6 +89,7 @@ struct MeshData {
     // FSAI factor pattern: lower triangle of A and its transpose
     std::vector<int32_t> Lrowptr, Lcolidx, LtoA, Urowptr, Ucolidx, UtoL;
     DBuf<int32_t> d_Lrowptr, d_Lcolidx, d_LtoA, d_Urowptr, d_Ucolidx, d_UtoL;
+    Ic0Plan ic0;  // built on first use of the IC(0) preconditioner
     // device
     DBuf<double> d_xyz;
     DBuf<int32_t> d_cells, d_rowptr, d_colidx, d_diag;
@@ -266,6 +275,11 @@ struct Context {
     DBuf<double> d_G;
     DBuf<float> d_G32, d_GT32, d_t32, d_z32;
     int32_t fsai_fallback_rows = 0;
+    // IC(0) preconditioner: factor values per wavenumber (lower pattern),
+    // its pivot-breakdown counter, and the preconditioned residual
+    DBuf<double> d_ic, d_z;
+    DBuf<int32_t> d_ic_bad;
+    int32_t ic0_breakdowns = 0;
     // mixed precision: wavenumbers whose columns stalled in FP32 in the last
     // response start in FP64 next time (cleared with the mesh / k / w)
     std::vector<uint8_t> fp64_k;
@@ -368,6 +382,11 @@ void build_lower_pattern(MeshData &m);
 void build_extension_map(const MeshData &m, std::vector<int32_t> &ptr, std::vector<double> &val);
 // fsai.cu
 void fsai_setup(Context &c, cudaStream_t s);
+// ic0.cu: factor every wavenumber's matrix (d_S) into d_ic; z = (L L^T)^-1 r
+// on all columns; kernel launches of one application
+void ic0_setup(Context &c, cudaStream_t s);
+void ic0_apply(Context &c, const double *r, double *z, cudaStream_t s);
+int ic0_launches(const Context &c);
 // batch.cu: batched mixed-precision PCG over the contexts' assembled systems
 int batch_solve(std::vector<Context *> &cs, cudaStream_t s, ertgb_batch_info *info, int *stalled);
 // cgls.cu: regularised Gauss-Newton update (all pointers device, vectors FP64)

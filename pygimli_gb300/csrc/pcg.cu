@@ -87,9 +87,10 @@ __global__ void __launch_bounds__(256) k_spmm_dot(int64_t n, int64_t nnz, int nE
 
 // Vector kernels: block (32, 8), grid (Rpad/32, NB); thread column t, rows
 // strided by 8*NB.  part_a / part_b receive per-block column partials.
+// z (may be null): the preconditioned residual given (IC(0)); null: z = D^-1 r
 __global__ void k_init(int64_t n, int nE, int nK, int64_t R, int64_t Rpad, const double *__restrict__ dinv,
                        const double *__restrict__ r, double *__restrict__ p, double *__restrict__ part_a,
-                       double *__restrict__ part_b) {
+                       double *__restrict__ part_b, const double *__restrict__ zg) {
     __shared__ double sa[kRowsPerBlock][32], sb[kRowsPerBlock][32];
     const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
     const int64_t ki = t < R ? t / nE : 0;
@@ -99,7 +100,7 @@ __global__ void k_init(int64_t n, int nE, int nK, int64_t R, int64_t Rpad, const
          row += (int64_t)gridDim.y * kRowsPerBlock) {
         const int64_t i = row * Rpad + t;
         const double rv = r[i];
-        const double z = t < R ? rv * dk[row] : 0.0;
+        const double z = t < R ? (zg ? zg[i] : rv * dk[row]) : 0.0;
         p[i] = z;
         a = fma(rv, z, a);
         b = fma(rv, rv, b);
@@ -224,7 +225,7 @@ __global__ void k_update_xr(int64_t n, int nE, int64_t R, int64_t Rpad, const do
     const bool act = active[t] != 0;
     const double alpha = col[ALPHA * Rpad + t];
     const int64_t ki = t < R ? t / nE : 0;
-    const double *dk = dinv + ki * n;
+    const double *dk = dinv ? dinv + ki * n : nullptr;
     double a = 0.0, b = 0.0;
     if (act) {
         for (int64_t row = (int64_t)blockIdx.y * kRowsPerBlock + threadIdx.y; row < n;
@@ -233,7 +234,7 @@ __global__ void k_update_xr(int64_t n, int nE, int64_t R, int64_t Rpad, const do
             x[i] = fma(alpha, p[i], x[i]);
             const double rv = fma(-alpha, q[i], r[i]);
             r[i] = rv;
-            a = fma(rv, rv * dk[row], a);
+            if (dinv) a = fma(rv, rv * dk[row], a);
             b = fma(rv, rv, b);
         }
     }
@@ -279,16 +280,38 @@ __global__ void k_finish_beta_w(int64_t Rpad, int NB, double rtol2, const double
 
 __global__ void k_update_p(int64_t n, int nE, int64_t R, int64_t Rpad, const double *__restrict__ dinv,
                            const double *__restrict__ col, const int32_t *__restrict__ active,
-                           const double *__restrict__ r, double *__restrict__ p) {
+                           const double *__restrict__ r, double *__restrict__ p, const double *__restrict__ zg) {
     const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
     if (!active[t]) return;
     const double beta = col[BETA * Rpad + t];
     const int64_t ki = t < R ? t / nE : 0;
-    const double *dk = dinv + ki * n;
+    const double *dk = dinv ? dinv + ki * n : nullptr;
     for (int64_t row = (int64_t)blockIdx.y * kRowsPerBlock + threadIdx.y; row < n;
          row += (int64_t)gridDim.y * kRowsPerBlock) {
         const int64_t i = row * Rpad + t;
-        p[i] = fma(beta, p[i], r[i] * dk[row]);
+        p[i] = fma(beta, p[i], zg ? zg[i] : r[i] * dk[row]);
+    }
+}
+
+// column partials of r . z (IC(0): z from the triangular solves)
+__global__ void k_dot_rz(int64_t n, int64_t Rpad, const int32_t *__restrict__ active, const double *__restrict__ r,
+                         const double *__restrict__ z, double *__restrict__ part_a) {
+    __shared__ double sa[kRowsPerBlock][32];
+    const int64_t t = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    double a = 0.0;
+    if (active[t]) {
+        for (int64_t row = (int64_t)blockIdx.y * kRowsPerBlock + threadIdx.y; row < n;
+             row += (int64_t)gridDim.y * kRowsPerBlock) {
+            const int64_t i = row * Rpad + t;
+            a = fma(r[i], z[i], a);
+        }
+    }
+    sa[threadIdx.y][threadIdx.x] = a;
+    __syncthreads();
+    if (threadIdx.y == 0) {
+        double s1 = 0.0;
+        for (int w = 0; w < kRowsPerBlock; w++) s1 += sa[w][threadIdx.x];
+        part_a[(int64_t)blockIdx.y * Rpad + t] = s1;
     }
 }
 
@@ -361,7 +384,18 @@ int pcg_solve(Context &c, cudaStream_t s, const int32_t *mask) {
         ERTGB_CUDA(cudaMemsetAsync(c.d_x.p, 0, sizeof(double) * n * Rpad, s));
     }
     ERTGB_CUDA(cudaMemsetAsync(nactive, 0, sizeof(int32_t), s));
-    k_init<<<vg, vb, 0, s>>>(n, c.nE, c.nK, R, Rpad, c.d_dinv.p, c.d_r.p, c.d_p.p, part_a, part_b);
+    // IC(0) (plain FP64 solve only; the FP64 finish of the mixed solver keeps Jacobi)
+    const bool ic0 = c.precond == ERTGB_PRECOND_IC0 && !mask;
+    const double *dv = ic0 ? nullptr : c.d_dinv.p;
+    const double *zg = nullptr;
+    if (ic0) {
+        ic0_setup(c, s);
+        c.d_z.alloc((size_t)n * Rpad);
+        ic0_apply(c, c.d_r.p, c.d_z.p, s);
+        zg = c.d_z.p;
+        c.stats.launches_response += ic0_launches(c);
+    }
+    k_init<<<vg, vb, 0, s>>>(n, c.nE, c.nK, R, Rpad, c.d_dinv.p, c.d_r.p, c.d_p.p, part_a, part_b, zg);
     k_finish_init<<<fg, fb, 0, s>>>(Rpad, R, NB, part_a, part_b, c.d_col.p, active, iters, nactive, mask,
                                     c.d_pnorm2.n >= (size_t)Rpad ? c.d_pnorm2.p : nullptr);
     ERTGB_CUDA(cudaGetLastError());
@@ -374,11 +408,15 @@ int pcg_solve(Context &c, cudaStream_t s, const int32_t *mask) {
         launch_spmm(ch, sg, s, n, m.nnz, c.nE, c.nK, Rpad, m.d_rowptr.p, m.d_colidx.p, c.d_S.p, c.d_p.p, c.d_q.p,
                     part_c, active);
         k_finish_alpha_w<<<fwg, 32 * kFinWarps, 0, s>>>(Rpad, NB, part_c, c.d_col.p, active, nactive);
-        k_update_xr<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, c.d_dinv.p, c.d_col.p, active, c.d_x.p, c.d_r.p,
+        k_update_xr<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, dv, c.d_col.p, active, c.d_x.p, c.d_r.p,
                                       c.d_p.p, c.d_q.p, part_a, part_b);
+        if (ic0) {
+            ic0_apply(c, c.d_r.p, c.d_z.p, s);
+            k_dot_rz<<<vg, vb, 0, s>>>(n, Rpad, active, c.d_r.p, c.d_z.p, part_a);
+        }
         k_finish_beta_w<<<fwg, 32 * kFinWarps, 0, s>>>(Rpad, NB, rtol2, part_a, part_b, c.d_col.p, active, iters,
                                                        nactive);
-        k_update_p<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, c.d_dinv.p, c.d_col.p, active, c.d_r.p, c.d_p.p);
+        k_update_p<<<vg, vb, 0, s>>>(n, c.nE, R, Rpad, dv, c.d_col.p, active, c.d_r.p, c.d_p.p, zg);
     }
     cudaError_t cap = cudaStreamEndCapture(s, &graph);
     if (cap != cudaSuccess) ERTGB_CUDA(cap);
@@ -401,7 +439,7 @@ int pcg_solve(Context &c, cudaStream_t s, const int32_t *mask) {
             }
             ERTGB_CUDA(cudaGraphLaunch(exec, s));
             iterations += kGraphIters;
-            c.stats.launches_response += 5 * kGraphIters;
+            c.stats.launches_response += (5 + (ic0 ? ic0_launches(c) + 1 : 0)) * kGraphIters;
             ERTGB_CUDA(cudaMemcpyAsync(&h_active, nactive, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
             ERTGB_CUDA(cudaStreamSynchronize(s));
         }

@@ -32,7 +32,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 FORMS = {"fp64": dict(precision="fp64", precond="jacobi"),
          "mixed": dict(precision="mixed", precond="jacobi"),
          "mixed-fsai": dict(precision="mixed", precond="fsai"),
-         "learned": dict(precision="mixed", precond="learned")}
+         "learned": dict(precision="mixed", precond="learned"),
+         "fp64-ic0": dict(precision="fp64", precond="ic0")}
 
 
 @pytest.fixture(scope="module")

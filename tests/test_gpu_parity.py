@@ -35,7 +35,8 @@ def torch():
 
 FORMS = {"fp64": dict(precision="fp64"), "mixed": dict(precision="mixed"),
          "mixed-fsai": dict(precision="mixed", precond="fsai"),
-         "learned": dict(precision="mixed", precond="learned")}
+         "learned": dict(precision="mixed", precond="learned"),
+         "fp64-ic0": dict(precision="fp64", precond="ic0")}
 WEIGHTS = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "pygimli_gb300", "weights")
 
 
