@@ -69,13 +69,72 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--gn", action="store_true", help="also time one full Gauss-Newton iteration per form "
                     "(response, Jacobian, 200 CGLS iterations on the GPU, line-search responses)")
-    ap.add_argument("--case", choices=["complex", "refine", "jacobian"], default=None,
+    ap.add_argument("--case", choices=["complex", "refine", "jacobian", "batch"], default=None,
                     help="run one single workload for a profiler instead of the bench and print one line: "
                     "'complex' = one complex-resistivity response + complex Jacobian (-10 mrad, --precision), "
                     "'refine' = the GPU H2 refinement of the workload mesh, twice, "
                     "'jacobian' = one response (--precision, --precond) and three Jacobians (FP32 with "
-                    "--precision mixed, else FP64)")
+                    "--precision mixed, else FP64), "
+                    "'batch' = the batched 2.5-D configuration (--batch-problems of the 64 seeded problems, "
+                    "21 explicit wavenumbers each): one batched response against the same problems' "
+                    "responses one after another (mixed and plain FP64)")
+    ap.add_argument("--batch-problems", type=int, default=64)
     return ap.parse_args()
+
+
+def run_batch_case(args):
+    """The batched 2.5-D configuration: seeded problems of 2k-60k nodes with
+    24-72 electrodes (dipole-dipole + Wenner), 21 explicit wavenumbers each
+    (setkValues / setWeights: 17 Gauss-Legendre + 4 Gauss-Laguerre points
+    over each problem's electrode distances), one batched mixed-precision
+    response against the same problems solved one after another."""
+    import torch
+    from pygimli_gb300 import synthetic
+    from pygimli_gb300.batch import BatchedERTModelling
+    from pygimli_gb300.ert import ERTModelling
+    from pygimli_gb300.kwave import kwave_list
+    probs = synthetic.batch_2d(64)[:args.batch_problems]
+
+    def fop_for(mesh, data, precision):
+        p = data.sensorPositions()
+        d = np.linalg.norm(p[:, None, :] - p[None, :, :], axis=2)
+        k, w = kwave_list(d[d > 0].min() / 2.0, d.max() * 2.0, 17, 4)
+        f = ERTModelling(precision=precision, rtol=args.rtol, maxIter=200000)
+        f.setkValues(k)
+        f.setWeights(w)
+        f.setData(data)
+        f.setMesh(mesh, ignoreRegionManager=True)
+        return f
+
+    models = [r for _, _, r in probs]
+    rec = {"case": "batch", "problems": len(probs), "wavenumbers": 21,
+           "nodes": [int(m.nodeCount()) for m, _, _ in probs],
+           "rhs_columns": int(sum(21 * d.sensorCount() for _, d, _ in probs))}
+    batch = BatchedERTModelling([fop_for(m, d, "mixed") for m, d, _ in probs])
+    for label in ("batched_mixed_first_s", "batched_mixed_s"):  # the first call also tunes the tile shape
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out_b = batch.response(models)
+        torch.cuda.synchronize()
+        rec[label] = time.perf_counter() - t0
+    rec["batch_info"] = {k: v for k, v in (batch.info or {}).items() if not isinstance(v, list)}
+    del batch
+    torch.cuda.empty_cache()
+    for precision in ("mixed", "fp64"):
+        t_seq, dev = 0.0, 0.0
+        for (m, d, r), rb in zip(probs, out_b):
+            f = fop_for(m, d, precision)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rs = f.response(r)
+            torch.cuda.synchronize()
+            t_seq += time.perf_counter() - t0
+            dev = max(dev, float(np.max(np.abs(np.asarray(rb) - rs) / rs)))
+            del f
+        rec[f"sequential_{precision}_s"] = t_seq
+        rec[f"max_rel_diff_rhoa_batched_vs_sequential_{precision}"] = dev
+    rec["ratio_sequential_mixed_to_batched"] = rec["sequential_mixed_s"] / rec["batched_mixed_s"]
+    print(json.dumps(rec), flush=True)
 
 
 def run_case(args):
@@ -83,6 +142,9 @@ def run_case(args):
     import torch
     from pygimli_gb300 import build as _build
     _build.build()
+    if args.case == "batch":
+        run_batch_case(args)
+        return
     mesh, data, rho, _ = workload(args.workload)
     if args.case == "refine":
         from pygimli_gb300 import refine
