@@ -76,8 +76,8 @@ def parse():
                     "'jacobian' = one response (--precision, --precond) and three Jacobians (FP32 with "
                     "--precision mixed, else FP64), "
                     "'batch' = the batched 2.5-D configuration (--batch-problems of the 64 seeded problems, "
-                    "21 explicit wavenumbers each): one batched response against the same problems' "
-                    "responses one after another (mixed and plain FP64)")
+                    "21 explicit wavenumbers each): batched responses (mixed; FP64 side by side) against the "
+                    "same problems' responses one after another (mixed and plain FP64)")
     ap.add_argument("--batch-problems", type=int, default=64)
     return ap.parse_args()
 
@@ -120,6 +120,16 @@ def run_batch_case(args):
     rec["batch_info"] = {k: v for k, v in (batch.info or {}).items() if not isinstance(v, list)}
     del batch
     torch.cuda.empty_cache()
+    # the same problems in FP64: their FP64 solves side by side (one stream each)
+    batch64 = BatchedERTModelling([fop_for(m, d, "fp64") for m, d, _ in probs])
+    for label in ("batched_fp64_first_s", "batched_fp64_s"):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out_b64 = batch64.response(models)
+        torch.cuda.synchronize()
+        rec[label] = time.perf_counter() - t0
+    del batch64
+    torch.cuda.empty_cache()
     for precision in ("mixed", "fp64"):
         t_seq, dev = 0.0, 0.0
         for (m, d, r), rb in zip(probs, out_b):
@@ -134,6 +144,9 @@ def run_batch_case(args):
         rec[f"sequential_{precision}_s"] = t_seq
         rec[f"max_rel_diff_rhoa_batched_vs_sequential_{precision}"] = dev
     rec["ratio_sequential_mixed_to_batched"] = rec["sequential_mixed_s"] / rec["batched_mixed_s"]
+    rec["ratio_sequential_fp64_to_batched_fp64"] = rec["sequential_fp64_s"] / rec["batched_fp64_s"]
+    rec["max_rel_diff_rhoa_batched_fp64_vs_mixed"] = float(max(np.max(np.abs(np.asarray(a) - np.asarray(b)) / np.asarray(b))
+                                                               for a, b in zip(out_b, out_b64)))
     print(json.dumps(rec), flush=True)
 
 

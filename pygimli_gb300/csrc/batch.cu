@@ -1,4 +1,5 @@
-// Batched mixed-precision block PCG over independent problems.
+// Batched mixed-precision block PCG over independent problems (problems that
+// are all FP64 run their own FP64 solves side by side instead).
 //
 // Every problem of the batch keeps its own context (mesh, matrices of all
 // wavenumbers, right-hand sides of all sources, FP64 solution); the batch
@@ -575,7 +576,58 @@ static Shape tune(std::vector<Context *> &cs, cudaStream_t s, DBuf<double> &part
     return best;
 }
 
+namespace {
+
+// Every problem in FP64 (the problems' own precision): the FP64 block PCG of
+// each problem with its own preconditioner, all problems side by side, each
+// on its own stream and host thread (there is no FP32 phase to share).
+int batch_solve_fp64(std::vector<Context *> &cs, cudaStream_t s, ertgb_batch_info *tuning) {
+    cudaEvent_t ready;
+    ERTGB_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+    ERTGB_CUDA(cudaEventRecord(ready, s));
+    std::vector<int> rcs(cs.size(), ERTGB_OK);
+    std::vector<std::exception_ptr> errs(cs.size());
+    std::vector<std::thread> th;
+    for (size_t f = 0; f < cs.size(); f++) {
+        th.emplace_back([&, f] {
+            try {
+                Context &c = *cs[f];
+                ERTGB_CUDA(cudaSetDevice(c.device));
+                ERTGB_CUDA(cudaStreamWaitEvent(c.stream, ready, 0));
+                rcs[f] = pcg_solve(c, c.stream);
+                ERTGB_CUDA(cudaStreamSynchronize(c.stream));
+            } catch (...) {
+                errs[f] = std::current_exception();
+            }
+        });
+    }
+    for (auto &t : th) t.join();
+    cudaEventDestroy(ready);
+    for (auto &e : errs)
+        if (e) std::rethrow_exception(e);
+    int status = ERTGB_OK, maxit = 0;
+    int64_t cols = 0;
+    for (size_t f = 0; f < cs.size(); f++) {
+        if (rcs[f] != ERTGB_OK) status = rcs[f];
+        maxit = std::max(maxit, cs[f]->stats.iterations);
+        cols += cs[f]->Rpad;
+    }
+    if (tuning) {
+        tuning->iterations = maxit;
+        tuning->columns = cols;
+    }
+    return status;
+}
+
+}  // namespace
+
 int batch_solve(std::vector<Context *> &cs, cudaStream_t s, ertgb_batch_info *tuning, int *stalled_out) {
+    bool all_fp64 = true;
+    for (Context *c : cs) all_fp64 = all_fp64 && c->precision == ERTGB_PRECISION_FP64;
+    if (all_fp64) {
+        if (stalled_out) *stalled_out = 0;
+        return batch_solve_fp64(cs, s, tuning);
+    }
     // per-problem FP32 operands and recurrence vectors
     for (Context *cp : cs) {
         Context &c = *cp;

@@ -2,7 +2,8 @@
 problem's apparent resistivities and Jacobian equal those of its own FP64
 solve (potentials / rhoa <= 1e-6, Jacobian <= 1e-5 relative), one small
 problem is checked against the oracle, and the autotuner's choice is one of
-its timed candidates and is cached for an identical batch."""
+its timed candidates and is cached for an identical batch.  A batch of FP64
+operators (their solves side by side) equals the single FP64 solves."""
 import numpy as np
 import pytest
 
@@ -63,6 +64,26 @@ def test_batch_matches_single_solves(torch):
     assert batch.info["cached"]
     for o2, o in zip(out2, out):
         assert float(np.max(np.abs(o2 - 2.0 * o) / (2.0 * o))) <= TOL_POT
+
+
+def test_fp64_batch_matches_single_solves(torch):
+    """A batch of FP64 operators runs every problem's own FP64 solve side by
+    side: the same responses and Jacobians as the single solves (1e-9)."""
+    from pygimli_gb300 import synthetic
+    from pygimli_gb300.batch import BatchedERTModelling
+    probs = synthetic.batch_2d(5, seed=13, nodes=(1500, 9000), electrodes=(12, 30))
+    singles = [_fop(m, d) for m, d, _ in probs]
+    ref = [f.response(r) for f, (_, _, r) in zip(singles, probs)]
+    batch = BatchedERTModelling([_fop(m, d, precision="fp64") for m, d, _ in probs])
+    out = batch.response([r for _, _, r in probs])
+    for i, (o, r) in enumerate(zip(out, ref)):
+        e = float(np.max(np.abs(o - r) / r))
+        assert e <= 1e-9, (i, e)
+    J = batch.createJacobian([r for _, _, r in probs])
+    for i, (f, (_, _, r)) in enumerate(zip(singles, probs)):
+        Jr = f.createJacobian(r).cpu().numpy()
+        assert np.linalg.norm(J[i].cpu().numpy() - Jr) <= 1e-9 * np.linalg.norm(Jr), i
+    assert batch.info["iterations"] > 0 and batch.info["stalled_columns"] == 0
 
 
 def test_batch_errors(torch):
