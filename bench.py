@@ -58,7 +58,7 @@ def parse():
                     default="box_3d_large")
     ap.add_argument("--rtol", type=float, default=1e-10)
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
-    ap.add_argument("--precond", choices=["jacobi", "fsai", "learned", "ic0"], default="learned")
+    ap.add_argument("--precond", choices=["jacobi", "fsai", "learned", "ic0", "band"], default="learned")
     ap.add_argument("--weights", default=None, help="learned preconditioner weights (.npz); default: the "
                     "packaged weights trained for the workload")
     ap.add_argument("--no-plain", action="store_true", help="skip the comparison runs (plain FP64 Jacobi, FSAI)")
@@ -95,11 +95,11 @@ def run_batch_case(args):
     from pygimli_gb300.kwave import kwave_list
     probs = synthetic.batch_2d(64)[:args.batch_problems]
 
-    def fop_for(mesh, data, precision):
+    def fop_for(mesh, data, precision, precond="jacobi"):
         p = data.sensorPositions()
         d = np.linalg.norm(p[:, None, :] - p[None, :, :], axis=2)
         k, w = kwave_list(d[d > 0].min() / 2.0, d.max() * 2.0, 17, 4)
-        f = ERTModelling(precision=precision, rtol=args.rtol, maxIter=200000)
+        f = ERTModelling(precision=precision, precond=precond, rtol=args.rtol, maxIter=200000)
         f.setkValues(k)
         f.setWeights(w)
         f.setData(data)
@@ -130,6 +130,29 @@ def run_batch_case(args):
         rec[label] = time.perf_counter() - t0
     del batch64
     torch.cuda.empty_cache()
+    # the banded direct solve (exact Cholesky per wavenumber): batched and one after another
+    batchb = BatchedERTModelling([fop_for(m, d, "fp64", "band") for m, d, _ in probs])
+    for label in ("batched_band_first_s", "batched_band_s"):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out_bb = batchb.response(models)
+        torch.cuda.synchronize()
+        rec[label] = time.perf_counter() - t0
+    del batchb
+    torch.cuda.empty_cache()
+    t_seq = 0.0
+    for m, d, r in probs:
+        f = fop_for(m, d, "fp64", "band")
+        f.response(r)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        f.response(r)
+        torch.cuda.synchronize()
+        t_seq += time.perf_counter() - t0
+        del f
+    rec["sequential_band_s"] = t_seq
+    rec["max_rel_diff_rhoa_band_vs_fp64_pcg"] = float(max(np.max(np.abs(np.asarray(a) - np.asarray(b)) /
+                                                                 np.asarray(b)) for a, b in zip(out_bb, out_b64)))
     for precision in ("mixed", "fp64"):
         t_seq, dev = 0.0, 0.0
         for (m, d, r), rb in zip(probs, out_b):
@@ -145,6 +168,8 @@ def run_batch_case(args):
         rec[f"max_rel_diff_rhoa_batched_vs_sequential_{precision}"] = dev
     rec["ratio_sequential_mixed_to_batched"] = rec["sequential_mixed_s"] / rec["batched_mixed_s"]
     rec["ratio_sequential_fp64_to_batched_fp64"] = rec["sequential_fp64_s"] / rec["batched_fp64_s"]
+    rec["ratio_sequential_band_to_batched_band"] = rec["sequential_band_s"] / rec["batched_band_s"]
+    rec["ratio_sequential_fp64_pcg_to_batched_band"] = rec["sequential_fp64_s"] / rec["batched_band_s"]
     rec["max_rel_diff_rhoa_batched_fp64_vs_mixed"] = float(max(np.max(np.abs(np.asarray(a) - np.asarray(b)) / np.asarray(b))
                                                                for a, b in zip(out_b, out_b64)))
     print(json.dumps(rec), flush=True)

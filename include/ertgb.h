@@ -43,12 +43,18 @@ typedef enum {
 /* IC0: incomplete Cholesky on A's lower pattern (no fill), factored on the
  * device per response and wavenumber, level-scheduled triangular solves;
  * FP64 precision only (the incomplete counterpart of the reference's CHOLMOD
- * factorization, core/src/cholmodWrapper.cpp:309-420). */
+ * factorization, core/src/cholmodWrapper.cpp:309-420).
+ * BAND: no iteration: the exact Cholesky factor of every wavenumber's matrix
+ * in band storage (the mesh's order or reverse Cuthill-McKee, bandwidth at
+ * most 256: the 2-D meshes of the 2.5-D path) and a forward and backward
+ * substitution per source, as the reference's direct solve
+ * (dcfemmodelling.cpp:2199-2210); FP64 precision only. */
 typedef enum {
     ERTGB_PRECOND_JACOBI = 0,
     ERTGB_PRECOND_FSAI = 1,
     ERTGB_PRECOND_LEARNED = 2,
-    ERTGB_PRECOND_IC0 = 3
+    ERTGB_PRECOND_IC0 = 3,
+    ERTGB_PRECOND_BAND = 4
 } ertgb_precond;
 
 /* Length of the learned preconditioner's FP32 parameter vector: encoders

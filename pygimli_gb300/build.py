@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libertgb.so")
-SOURCES = ["setup.cpp", "assemble.cu", "pcg.cu", "pcg_mixed.cu", "fsai.cu", "jacobian.cu", "capi.cu", "noalloc.cu", "learned.cu", "batch.cu", "cgls.cu", "refine.cu", "complex.cu", "ic0.cu"]
+SOURCES = ["setup.cpp", "assemble.cu", "pcg.cu", "pcg_mixed.cu", "fsai.cu", "jacobian.cu", "capi.cu", "noalloc.cu", "learned.cu", "batch.cu", "cgls.cu", "refine.cu", "complex.cu", "ic0.cu", "band.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-strict-aliasing"]
 

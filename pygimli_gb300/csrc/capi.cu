@@ -175,10 +175,11 @@ int do_response(Context &c, const double *rho, double *rhoa, void *stream) {
     MeshData &m = c.mesh;
     ERTGB_CUDA(cudaEventRecord(c.ev[0], s));
     const bool total = c.formulation == ERTGB_FORMULATION_TOTAL_POTENTIAL;
-    if (c.precision != ERTGB_PRECISION_MIXED && c.precond != ERTGB_PRECOND_JACOBI && c.precond != ERTGB_PRECOND_IC0)
+    const bool fp64_only = c.precond == ERTGB_PRECOND_IC0 || c.precond == ERTGB_PRECOND_BAND;
+    if (c.precision != ERTGB_PRECISION_MIXED && c.precond != ERTGB_PRECOND_JACOBI && !fp64_only)
         throw Error(ERTGB_BAD_INPUT, "the FSAI and learned preconditioners need mixed precision");
-    if (c.precision == ERTGB_PRECISION_MIXED && c.precond == ERTGB_PRECOND_IC0)
-        throw Error(ERTGB_BAD_INPUT, "the IC(0) preconditioner needs FP64 precision");
+    if (c.precision == ERTGB_PRECISION_MIXED && fp64_only)
+        throw Error(ERTGB_BAD_INPUT, "the IC(0) preconditioner and the banded direct solve need FP64 precision");
     if (c.precond == ERTGB_PRECOND_LEARNED && !m.ext_rows.empty())
         throw Error(ERTGB_BAD_INPUT, "the learned preconditioner does not cover a matrix extension (CEM, bypass)");
     c.d_S.alloc((size_t)c.nK * m.nnz);
@@ -692,7 +693,8 @@ int ertgb_set_solver(ertgb_ctx *ctx, double rtol, int max_iter, int precond) {
         ERTGB_REQUIRE(rtol > 0.0 && rtol < 1.0, "rtol must be in (0, 1)");
         ERTGB_REQUIRE(max_iter > 0, "max_iter must be positive");
         ERTGB_REQUIRE(precond == ERTGB_PRECOND_JACOBI || precond == ERTGB_PRECOND_FSAI ||
-                          precond == ERTGB_PRECOND_LEARNED || precond == ERTGB_PRECOND_IC0,
+                          precond == ERTGB_PRECOND_LEARNED || precond == ERTGB_PRECOND_IC0 ||
+                          precond == ERTGB_PRECOND_BAND,
                       "unknown preconditioner");
         c->rtol = rtol;
         c->max_iter = max_iter;

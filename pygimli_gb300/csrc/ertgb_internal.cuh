@@ -73,6 +73,16 @@ struct Ic0Plan {
     DBuf<int32_t> d_frow, d_brow;
 };
 
+// Band ordering of the direct solve: the mesh's own order or reverse
+// Cuthill-McKee, whichever has the smaller bandwidth b (usable if b <= kMaxBand).
+constexpr int kMaxBand = 256;
+struct BandPlan {
+    bool built = false, ok = false;
+    int b = 0;
+    std::vector<int32_t> perm, pos;  // band index -> row, row -> band index
+    DBuf<int32_t> d_perm, d_pos;
+};
+
 // Mesh-dependent structures.
 struct MeshData {
     int dim = 0, order = 1, nv = 0, nvb = 0;  // nv / nvb: nodes per cell / boundary
@@ -90,6 +100,7 @@ struct MeshData {
     std::vector<int32_t> Lrowptr, Lcolidx, LtoA, Urowptr, Ucolidx, UtoL;
     DBuf<int32_t> d_Lrowptr, d_Lcolidx, d_LtoA, d_Urowptr, d_Ucolidx, d_UtoL;
     Ic0Plan ic0;  // built on first use of the IC(0) preconditioner
+    BandPlan band;  // built on first use of the banded direct solve
     // device
     DBuf<double> d_xyz;
     DBuf<int32_t> d_cells, d_rowptr, d_colidx, d_diag;
@@ -278,6 +289,7 @@ struct Context {
     // IC(0) preconditioner: factor values per wavenumber (lower pattern),
     // its pivot-breakdown counter, and the preconditioned residual
     DBuf<double> d_ic, d_z;
+    DBuf<double> d_band;  // banded Cholesky factors, nK x n x (b + 1)
     DBuf<int32_t> d_ic_bad;
     int32_t ic0_breakdowns = 0;
     // mixed precision: wavenumbers whose columns stalled in FP32 in the last
@@ -387,6 +399,8 @@ void fsai_setup(Context &c, cudaStream_t s);
 void ic0_setup(Context &c, cudaStream_t s);
 void ic0_apply(Context &c, const double *r, double *z, cudaStream_t s);
 int ic0_launches(const Context &c);
+// band.cu: x = A^-1 b for every column (FP64 banded Cholesky per wavenumber)
+int band_solve(Context &c, cudaStream_t s);
 // batch.cu: batched mixed-precision PCG over the contexts' assembled systems
 int batch_solve(std::vector<Context *> &cs, cudaStream_t s, ertgb_batch_info *info, int *stalled);
 // cgls.cu: regularised Gauss-Newton update (all pointers device, vectors FP64)

@@ -346,6 +346,7 @@ void pcg_prepare(Context &c) {
 }
 
 int pcg_solve(Context &c, cudaStream_t s, const int32_t *mask) {
+    if (c.precond == ERTGB_PRECOND_BAND && !mask) return band_solve(c, s);  // direct, no iterations
     MeshData &m = c.mesh;
     const int64_t n = m.n, Rpad = c.Rpad, R = c.R;
     const int NB = (int)std::min<int64_t>(ceil_div(n, kRowsPerBlock), kPartRows);

@@ -249,7 +249,7 @@ class ERTModelling:
         ``"learned"`` (network-emitted factor; ``weights``: a
         LearnedPreconditioner, a weight array or an .npz path).  FSAI and
         learned need mixed precision; stalled columns finish with FP64 Jacobi."""
-        codes = {"jacobi": 0, "fsai": 1, "learned": 2, "ic0": 3}
+        codes = {"jacobi": 0, "fsai": 1, "learned": 2, "ic0": 3, "band": 4}
         if precond not in codes:
             raise ValueError(f"precond must be one of {sorted(codes)}")
         if weights is not None:
