@@ -12,8 +12,10 @@
 //   one block per wavenumber factors column by column (right-looking):
 //     L(j,j) = sqrt(a_jj);  L(j+i,j) = a_{j+i,j} / L(j,j);
 //     a_{j+i, j+l} -= L(j+i,j) L(j+l,j)   (1 <= l <= i <= b),
-//   then one block per wavenumber solves L y = b, L^T x = y for all of its
-//   columns (one thread per right-hand side, sequential over the band).
+//   then L y = b, L^T x = y for every column of the wavenumber (one thread
+//   per right-hand side, sequential over the band; for bandwidths up to 64
+//   the last b solution values stay in registers).  Bandwidths up to 31 are
+//   factored by one warp per wavenumber (lane d holds L(j+d, j)).
 //
 // Rows are visited in the chosen order through a permutation, so the
 // right-hand-side and solution blocks stay in the mesh's node order.  A pivot
@@ -80,6 +82,92 @@ __global__ void __launch_bounds__(kBandThreads) k_band_factor(int64_t n, int b, 
             for (int i = l + tid; i <= m; i += kBandThreads) Al[i] -= col[i] * cl;
         }
         __syncthreads();
+    }
+}
+
+// Narrow bands (b <= 31): one warp per wavenumber factors column by column
+// with lane d holding L(j+d, j); the update of the next columns is lane-
+// parallel, and __syncwarp orders it before the next column is read.
+__global__ void __launch_bounds__(128) k_band_factor_warp(int64_t n, int b, int nK, double *__restrict__ B,
+                                                           int32_t *__restrict__ bad) {
+    const int w = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (w >= nK) return;
+    double *A = B + (int64_t)w * n * (b + 1);
+    for (int64_t j = 0; j < n; j++) {
+        const int m = (int)(n - 1 - j < (int64_t)b ? n - 1 - j : (int64_t)b);
+        double *Aj = A + j * (b + 1);
+        double v = lane <= m ? Aj[lane] : 0.0;
+        double d = __shfl_sync(0xffffffffu, v, 0);
+        if (!(d > 0.0) || !isfinite(d)) {
+            if (lane == 0) atomicAdd(bad, 1);
+            d = 1.0;
+        }
+        const double ljj = sqrt(d);
+        v = lane == 0 ? ljj : v / ljj;
+        if (lane <= m) Aj[lane] = v;
+        for (int l = 1; l <= m; l++) {
+            const double cl = __shfl_sync(0xffffffffu, v, l);
+            if (lane >= l && lane <= m) A[(j + l) * (b + 1) + (lane - l)] -= v * cl;
+        }
+        __syncwarp();
+    }
+}
+
+// Narrow bands (b <= BW): one thread per right-hand side, the last BW
+// solution values of its column in registers (pull form): forward
+// y_j = (r_j - sum_{i=1..b} L(j, j-i) y_{j-i}) / L_jj with L(j, j-i) =
+// B[(j-i)(b+1) + i], backward x_j = (y_j - sum_i L(j+i, j) x_{j+i}) / L_jj.
+template <int BW>
+__global__ void __launch_bounds__(128) k_band_solve_reg(int64_t n, int b, int nE, int64_t Rpad,
+                                                         const double *__restrict__ B,
+                                                         const int32_t *__restrict__ perm,
+                                                         double *__restrict__ x) {
+    const int k = blockIdx.y;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nE) return;
+    const double *L = B + (int64_t)k * n * (b + 1);
+    double *xc = x + (int64_t)k * nE + e;
+    double win[BW];
+#pragma unroll
+    for (int i = 0; i < BW; i++) win[i] = 0.0;  // win[i] = y_{j-1-i}
+    for (int64_t j = 0; j < n; j++) {
+        const int64_t row = perm[j];
+        double s0 = xc[row * Rpad], s1 = 0.0;
+#pragma unroll
+        for (int i = 0; i < BW; i++) {
+            const int64_t c = j - 1 - i;  // column j-1-i holds L(j, c) at offset i+1
+            if (i < b && c >= 0) {
+                const double l = L[c * (b + 1) + i + 1];
+                if (i & 1) s1 = fma(-l, win[i], s1);
+                else s0 = fma(-l, win[i], s0);
+            }
+        }
+        const double y = (s0 + s1) / L[j * (b + 1)];
+        xc[row * Rpad] = y;
+#pragma unroll
+        for (int i = BW - 1; i > 0; i--) win[i] = win[i - 1];
+        win[0] = y;
+    }
+#pragma unroll
+    for (int i = 0; i < BW; i++) win[i] = 0.0;  // win[i] = x_{j+1+i}
+    for (int64_t j = n - 1; j >= 0; j--) {
+        const int64_t row = perm[j];
+        const double *Lj = L + j * (b + 1);
+        double s0 = xc[row * Rpad], s1 = 0.0;
+#pragma unroll
+        for (int i = 0; i < BW; i++) {
+            if (i < b && j + 1 + i < n) {
+                const double l = Lj[i + 1];
+                if (i & 1) s1 = fma(-l, win[i], s1);
+                else s0 = fma(-l, win[i], s0);
+            }
+        }
+        const double xv = (s0 + s1) / Lj[0];
+        xc[row * Rpad] = xv;
+#pragma unroll
+        for (int i = BW - 1; i > 0; i--) win[i] = win[i - 1];
+        win[0] = xv;
     }
 }
 
@@ -203,12 +291,25 @@ int band_solve(Context &c, cudaStream_t s) {
     DBuf<int32_t> &bad = c.d_ic_bad;
     bad.alloc(1);
     bad.zero(s);
-    k_band_factor<<<c.nK, kBandThreads, 0, s>>>(n, (int)b, c.d_band.p, bad.p);
+    if (b <= 31)
+        k_band_factor_warp<<<(unsigned)ceil_div((int64_t)c.nK * 32, 128), 128, 0, s>>>(n, (int)b, c.nK, c.d_band.p,
+                                                                                        bad.p);
+    else
+        k_band_factor<<<c.nK, kBandThreads, 0, s>>>(n, (int)b, c.d_band.p, bad.p);
     // the solution overwrites a copy of the right-hand sides (d_r keeps them)
     c.d_x.alloc((size_t)n * c.Rpad);
     ERTGB_CUDA(cudaMemcpyAsync(c.d_x.p, c.d_r.p, sizeof(double) * n * c.Rpad, cudaMemcpyDeviceToDevice, s));
-    k_band_solve<<<c.nK, std::min(kBandThreads, ((c.nE + 31) / 32) * 32), 0, s>>>(n, (int)b, c.nE, c.Rpad,
-                                                                                  c.d_band.p, P.d_perm.p, c.d_x.p);
+    const dim3 sg((unsigned)ceil_div(c.nE, 32), (unsigned)c.nK);
+    if (b <= 16)
+        k_band_solve_reg<16><<<sg, 32, 0, s>>>(n, (int)b, c.nE, c.Rpad, c.d_band.p, P.d_perm.p, c.d_x.p);
+    else if (b <= 32)
+        k_band_solve_reg<32><<<sg, 32, 0, s>>>(n, (int)b, c.nE, c.Rpad, c.d_band.p, P.d_perm.p, c.d_x.p);
+    else if (b <= 64)
+        k_band_solve_reg<64><<<sg, 32, 0, s>>>(n, (int)b, c.nE, c.Rpad, c.d_band.p, P.d_perm.p, c.d_x.p);
+    else
+        k_band_solve<<<c.nK, std::min(kBandThreads, ((c.nE + 31) / 32) * 32), 0, s>>>(n, (int)b, c.nE, c.Rpad,
+                                                                                      c.d_band.p, P.d_perm.p,
+                                                                                      c.d_x.p);
     ERTGB_CUDA(cudaGetLastError());
     int32_t h = 0;
     ERTGB_CUDA(cudaMemcpyAsync(&h, bad.p, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
