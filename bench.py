@@ -682,6 +682,18 @@ def run_ours(args, world, rank, local):
             c2_forms["fsai_form"] = time_form(wl_c2, args.precision, "fsai", jdt,
                                               f"block PCG (FSAI), {args.precision}", ref_rhoa=ref2)
         c2_forms["ratio_plain_to_headline"] = c2_forms["plain_fp64_gpu_pcg"]["value"] / head["value"]
+    c1_forms = None
+    if not args.no_plain and args.workload != "line_2d":
+        # the 2.5-D configuration (41 electrodes, 17 wavenumbers): the banded
+        # direct solve beside the plain FP64 PCG (FP64 Jacobians)
+        m1, d1, r1, _ = workload("line_2d")
+        wl_c1 = (m1, d1, r1)
+        band = time_form(wl_c1, "fp64", "band", 0, "banded Cholesky (direct), FP64")
+        ref1 = band.pop("rhoa")
+        c1_forms = {"workload": workload_label("line_2d", m1, d1), "band_direct": band,
+                    "plain_fp64_gpu_pcg": time_form(wl_c1, "fp64", "jacobi", 0, "block PCG (Jacobi), FP64",
+                                                    ref_rhoa=ref1)}
+        c1_forms["ratio_plain_to_band"] = c1_forms["plain_fp64_gpu_pcg"]["value"] / band["value"]
     if not args.no_plain:
         cx_form = {"workload": "box_3d", "mixed": time_complex(wl_c2, "mixed"), "fp64": time_complex(wl_c2, "fp64")}
     if (not args.no_plain or args.cem_only) and mesh.dim() == 3:
@@ -807,7 +819,7 @@ def run_ours(args, world, rank, local):
                               f"{D * P * (8 if jdt == 0 else 4) / 1e9:.1f} GB"),
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
                "plain_fp64_gpu_pcg": plain, "fsai_form": fsai_form, "fp64_ic0_form": ic0_form,
-               "box_3d_forms": c2_forms,
+               "box_3d_forms": c2_forms, "line_2d_forms": c1_forms,
                "gn_iteration": gn, "refine_h2": refine_rec, "complex_form": cx_form, "cem_form": cem_form,
                "learned_weights": os.path.relpath(weights, ROOT) if weights else None,
                "clocks": clk, "step_ms": step_ms,
