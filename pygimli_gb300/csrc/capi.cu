@@ -101,6 +101,41 @@ void ertgb::check_spmm_args(int64_t n, int64_t nnz, const void *rowptr, const vo
 
 namespace {
 
+// Device -> host copy of a large result.  Into page-locked (or device)
+// memory the copy engines run at full speed; into ordinary pageable memory
+// the driver's staged copy varied from call to call on the GB300 machine
+// (24-193 GB/s for the same array), while the GPU's own stores through the
+// host page tables (devices that report pageable memory access, as Grace
+// systems do) held 170 GB/s, so such destinations are written by a
+// grid-stride copy kernel.
+__global__ void k_copy_out16(uint4 *__restrict__ dst, const uint4 *__restrict__ src, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+__global__ void k_copy_out4(uint32_t *__restrict__ dst, const uint32_t *__restrict__ src, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+void copy_to_host(Context &c, void *dst, const void *src, size_t bytes) {
+    cudaPointerAttributes a{};
+    const bool known = cudaPointerGetAttributes(&a, dst) == cudaSuccess;
+    cudaGetLastError();  // an unregistered host pointer may leave an error on older drivers
+    int pageable = 0, sms = 1;
+    ERTGB_CUDA(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, c.device));
+    ERTGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device));
+    const bool unregistered = known && a.type == cudaMemoryTypeUnregistered;
+    if (!unregistered || !pageable || bytes % 4) {
+        ERTGB_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c.stream));
+        return;
+    }
+    if (((uintptr_t)dst % 16 == 0) && ((uintptr_t)src % 16 == 0) && bytes % 16 == 0)
+        k_copy_out16<<<(unsigned)(4 * sms), 512, 0, c.stream>>>((uint4 *)dst, (const uint4 *)src, bytes / 16);
+    else
+        k_copy_out4<<<(unsigned)(4 * sms), 512, 0, c.stream>>>((uint32_t *)dst, (const uint32_t *)src, bytes / 4);
+    ERTGB_CUDA(cudaGetLastError());
+}
+
 void ensure_derived(Context &c) {
     if (!c.have_mesh) throw Error(ERTGB_STATE, "no mesh set");
     if (!c.have_elec) throw Error(ERTGB_STATE, "no electrodes set");
@@ -759,7 +794,7 @@ int ertgb_jacobian_host(ertgb_ctx *ctx, const double *model, int n_model, void *
         const size_t bytes = (size_t)c->D * c->mesh.P * (dtype == 0 ? 8 : 4);
         c->d_J_tmp.alloc(bytes);
         do_jacobian(*c, md, n_model, c->d_J_tmp.p, dtype, nullptr);
-        ERTGB_CUDA(cudaMemcpyAsync(J, c->d_J_tmp.p, bytes, cudaMemcpyDeviceToHost, c->stream));
+        copy_to_host(*c, J, c->d_J_tmp.p, bytes);
         ERTGB_CUDA(cudaStreamSynchronize(c->stream));
     });
 }
