@@ -69,7 +69,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--gn", action="store_true", help="also time one full Gauss-Newton iteration per form "
                     "(response, Jacobian, 200 CGLS iterations on the GPU, line-search responses)")
-    ap.add_argument("--case", choices=["complex", "refine", "jacobian", "batch"], default=None,
+    ap.add_argument("--case", choices=["complex", "refine", "jacobian", "batch", "gn2d"], default=None,
                     help="run one single workload for a profiler instead of the bench and print one line: "
                     "'complex' = one complex-resistivity response + complex Jacobian (-10 mrad, --precision), "
                     "'refine' = the GPU H2 refinement of the workload mesh, twice, "
@@ -77,7 +77,8 @@ def parse():
                     "--precision mixed, else FP64), "
                     "'batch' = the batched 2.5-D configuration (--batch-problems of the 64 seeded problems, "
                     "21 explicit wavenumbers each): batched responses (mixed; FP64 side by side) against the "
-                    "same problems' responses one after another (mixed and plain FP64)")
+                    "same problems' responses one after another (mixed and plain FP64), "
+                    "'gn2d' = one Gauss-Newton iteration per solver form on the largest of those meshes")
     ap.add_argument("--batch-problems", type=int, default=64)
     return ap.parse_args()
 
@@ -175,6 +176,57 @@ def run_batch_case(args):
     print(json.dumps(rec), flush=True)
 
 
+def run_gn2d_case(args):
+    """One Gauss-Newton iteration (response, Jacobian, CGLS, line search) on
+    the largest mesh of the batched 2.5-D configuration's first 16 problems
+    (21 explicit wavenumbers), per solver form: the banded direct solve, the
+    plain FP64 PCG (Jacobi, IC(0)) and the mixed-precision PCG with the learned
+    preconditioner (line_2d weights) and with FSAI.  Observed data = the
+    model's response with 2 % noise; start = homogeneous median model."""
+    import torch
+    from pygimli_gb300 import synthetic
+    from pygimli_gb300.ert import ERTModelling
+    from pygimli_gb300.inversion import GaussNewton
+    from pygimli_gb300.kwave import kwave_list
+    probs = synthetic.batch_2d(64)[:16]
+    mesh, data, rho = max(probs, key=lambda t: t[0].nodeCount())
+    p = data.sensorPositions()
+    d = np.linalg.norm(p[:, None, :] - p[None, :, :], axis=2)
+    k, w = kwave_list(d[d > 0].min() / 2.0, d.max() * 2.0, 17, 4)
+    forms = {"band_direct_fp64": dict(precision="fp64", precond="band"),
+             "jacobi_fp64": dict(precision="fp64", precond="jacobi"),
+             "ic0_fp64": dict(precision="fp64", precond="ic0"),
+             "learned_mixed": dict(precision="mixed", precond="learned", weights=default_weights("line_2d")),
+             "fsai_mixed": dict(precision="mixed", precond="fsai")}
+    rec = {"case": "gn2d", "nodes": int(mesh.nodeCount()), "cells": int(mesh.cellCount()), "data": int(data.size()),
+           "electrodes": int(data.sensorCount()), "wavenumbers": 21}
+    obs = None
+    for name, f in forms.items():
+        fop = ERTModelling(rtol=args.rtol, maxIter=200000, **f)
+        fop.setkValues(k)
+        fop.setWeights(w)
+        fop.setData(data)
+        fop.setMesh(mesh, ignoreRegionManager=True)
+        if obs is None:
+            obs = fop.response(rho) * (1.0 + 0.02 * np.random.default_rng(3).normal(size=data.size()))
+        gn = GaussNewton(fop, obs, np.full(data.size(), 0.02), lam=20.0)
+        model = np.full(mesh.cellCount(), float(np.median(obs)))
+        resp = fop.response(model)
+        gn.step(model, resp)  # warm-up (allocations, graph capture, band ordering)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        resp = fop.response(model)
+        its = fop.stats()["iterations"]
+        _, _, info = gn.step(model, resp)
+        torch.cuda.synchronize()
+        rec[name] = {"value": time.perf_counter() - t0, "unit": "s", "pcg_iterations_first_response": its,
+                     "cgls_iterations": info["cgls_iterations"], "forward_responses": info["responses"] + 1,
+                     "phi_before": info["phi_before"], "phi_after": info["phi_after"]}
+        del fop, gn
+        torch.cuda.empty_cache()
+    print(json.dumps(rec), flush=True)
+
+
 def run_case(args):
     """One single workload (``--case``) for ``ncu`` launch lists and captures."""
     import torch
@@ -182,6 +234,9 @@ def run_case(args):
     _build.build()
     if args.case == "batch":
         run_batch_case(args)
+        return
+    if args.case == "gn2d":
+        run_gn2d_case(args)
         return
     mesh, data, rho, _ = workload(args.workload)
     if args.case == "refine":
