@@ -283,7 +283,10 @@ __device__ __forceinline__ void cp_async_wait_all() {
     asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
 
-template <int NV, typename OT, bool V2>
+// VEC: 4 = four adjacent parameters per lane and 16-byte stores (FP32 J with
+// a row length and base aligned to four), 2 = two per lane and paired
+// stores, 1 = two per lane, element stores
+template <int NV, typename OT, int VEC>
 __global__ void __launch_bounds__(kSJT, 1)
     k_jac_stiff(int64_t ntiles, int64_t P, const int32_t *__restrict__ pc, const double *__restrict__ K,
                 const typename StageOf<OT>::type *__restrict__ pot, int64_t Rpad, int nE, int RS,
@@ -297,8 +300,10 @@ __global__ void __launch_bounds__(kSJT, 1)
     constexpr int TW = kSTW;
     constexpr int NM1 = NV - 1;
     constexpr int NW = kSJT / 32;      // warps = data streams
-    constexpr int LPR = TW / 2;        // lanes per record (two adjacent slots each)
+    constexpr int PPL = VEC == 4 ? 4 : 2;  // adjacent parameters (slots) per lane
+    constexpr int LPR = TW / PPL;      // lanes per record
     constexpr int RPW = 32 / LPR;      // records per warp step
+    static_assert(VEC != 4 || sizeof(OT) == 4, "16-byte stores of four FP32 values");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     // [TA | TM tables: row = NM1 x TW values, slot fastest][staged rows Us]
     // [Ks: TW x NM1^2][sps: TW][lid: TW x NV bytes][records: NW x kNREC x (scale, datum, dipoles)]
@@ -311,7 +316,7 @@ __global__ void __launch_bounds__(kSJT, 1)
     int32_t *rec_d = reinterpret_cast<int32_t *>(rec_f + NW * kNREC);
     int32_t *rec_p = rec_d + NW * kNREC;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int s2 = 2 * (lane % LPR), sub = lane / LPR;  // pair phase: slots s2, s2 + 1 of record sub
+    const int s2 = PPL * (lane % LPR), sub = lane / LPR;  // pair phase: slots s2 .. s2 + PPL - 1 of record sub
     const int nE2 = nE & ~1;  // columns copied in 16-byte units
     const int P32 = (int)P;   // parameters < 2^31: 32 x 32 -> 64-bit row offsets
 
@@ -400,15 +405,17 @@ __global__ void __launch_bounds__(kSJT, 1)
             const int len = cd.s1 - cd.s0;
             const int sb = cd.s0 + (int)((int64_t)len * warp / NW);
             const int se = cd.s0 + (int)((int64_t)len * (warp + 1) / NW);
-            const bool st0 = s2 < TP, st1 = s2 + 1 < TP;
+            const bool st0 = s2 < TP, st1 = s2 + 1 < TP, stall = s2 + PPL - 1 < TP;
             const int tm0 = cd.nA * NM1 * TW + s2;  // element offset of this lane's TM slots
             OT *Jt = J + p0 + s2;
             OT *rf = rec_f + warp * kNREC;
             int32_t *rdd = rec_d + warp * kNREC, *rpp = rec_p + warp * kNREC;
             int cur = -1;
-            OT2 ta[NM1];
+            OT ta[NM1][PPL];
 #pragma unroll
-            for (int i = 0; i < NM1; i++) ta[i] = OT2{};
+            for (int i = 0; i < NM1; i++)
+#pragma unroll
+                for (int q = 0; q < PPL; q++) ta[i][q] = (OT)0;
             int4 nxt = make_int4(0, 0, 0, 0);
             if (lane < kNREC && sb + lane < se) nxt = meta[sb + lane];
             for (int base = sb; base < se; base += kNREC) {
@@ -430,28 +437,58 @@ __global__ void __launch_bounds__(kSJT, 1)
                     if (__builtin_expect(ia != cur, 0)) {
                         cur = ia;
 #pragma unroll
-                        for (int i = 0; i < NM1; i++)
-                            ta[i] = *reinterpret_cast<const OT2 *>(TA + s2 + (cur * NM1 + i) * TW);
+                        for (int i = 0; i < NM1; i++) {
+                            const OT *src = TA + s2 + (cur * NM1 + i) * TW;
+                            if constexpr (VEC == 4) {
+                                const float4 v = *reinterpret_cast<const float4 *>(src);
+                                ta[i][0] = v.x;
+                                ta[i][1] = v.y;
+                                ta[i][2] = v.z;
+                                ta[i][3] = v.w;
+                            } else {
+                                const OT2 v = *reinterpret_cast<const OT2 *>(src);
+                                ta[i][0] = v.x;
+                                ta[i][1] = v.y;
+                            }
+                        }
                     }
                     const int o = tm0 + im * (NM1 * TW);
-                    OT acc0 = 0, acc1 = 0;
+                    OT acc[PPL];
+#pragma unroll
+                    for (int q = 0; q < PPL; q++) acc[q] = (OT)0;
 #pragma unroll
                     for (int i = 0; i < NM1; i++) {
-                        const OT2 t = *reinterpret_cast<const OT2 *>(tabs + o + i * TW);
-                        acc0 = fma(ta[i].x, t.x, acc0);
-                        acc1 = fma(ta[i].y, t.y, acc1);
+                        if constexpr (VEC == 4) {
+                            const float4 t = *reinterpret_cast<const float4 *>(tabs + o + i * TW);
+                            acc[0] = fma(ta[i][0], t.x, acc[0]);
+                            acc[1] = fma(ta[i][1], t.y, acc[1]);
+                            acc[2] = fma(ta[i][2], t.z, acc[2]);
+                            acc[3] = fma(ta[i][3], t.w, acc[3]);
+                        } else {
+                            const OT2 t = *reinterpret_cast<const OT2 *>(tabs + o + i * TW);
+                            acc[0] = fma(ta[i][0], t.x, acc[0]);
+                            acc[1] = fma(ta[i][1], t.y, acc[1]);
+                        }
                     }
                     if (scale_data) {
                         const OT f = rf[k];
-                        acc0 *= f;
-                        acc1 *= f;
+#pragma unroll
+                        for (int q = 0; q < PPL; q++) acc[q] *= f;
                     }
                     OT *dst = Jt + (int64_t)rdd[k] * P32;
-                    if (V2 && st1) {
-                        *reinterpret_cast<OT2 *>(dst) = OT2{acc0, acc1};
+                    if constexpr (VEC == 4) {
+                        if (stall) {
+                            *reinterpret_cast<float4 *>(dst) = make_float4(acc[0], acc[1], acc[2], acc[3]);
+                        } else {
+#pragma unroll
+                            for (int q = 0; q < PPL; q++)
+                                if (s2 + q < TP) dst[q] = acc[q];
+                        }
+                    } else if (VEC == 2 && st1) {
+                        *reinterpret_cast<OT2 *>(dst) = OT2{acc[0], acc[1]};
                     } else {
-                        if (st0) dst[0] = acc0;
-                        if (st1) dst[1] = acc1;
+                        if (st0) dst[0] = acc[0];
+                        if (st1) dst[1] = acc[1];
                     }
                 }
             }
@@ -509,12 +546,20 @@ void launch_stiff(Context &c, bool scaled, const CT *sp, CT *J, int dtype, cudaS
             S.d_dipa.p, S.d_dipm.p, reinterpret_cast<const int4 *>(S.d_meta.p), scaled ? 1 : 0, sp, w0, J);
         ERTGB_CUDA(cudaGetLastError());
     };
-    // paired stores when every row's pair of adjacent parameters starts on a 2-element boundary
+    // 16-byte stores (FP32) when every row's group of four parameters starts on a
+    // four-element boundary, else paired stores on a two-element boundary
     const bool v2 = m.P % 2 == 0 && reinterpret_cast<uintptr_t>(J) % (2 * sizeof(CT)) == 0;
+    const bool v4 = sizeof(CT) == 4 && m.P % 4 == 0 && reinterpret_cast<uintptr_t>(J) % 16 == 0;
     auto by_tw = [&](auto nvc) {
         constexpr int NV = decltype(nvc)::value;
-        if (v2) go(k_jac_stiff<NV, CT, true>);
-        else go(k_jac_stiff<NV, CT, false>);
+        if constexpr (sizeof(CT) == 4 && NV <= 6) {  // 4 (NV - 1) TA registers: spills past NV = 6
+            if (v4) {
+                go(k_jac_stiff<NV, CT, 4>);
+                return;
+            }
+        }
+        if (v2) go(k_jac_stiff<NV, CT, 2>);
+        else go(k_jac_stiff<NV, CT, 1>);
     };
     switch (m.nv) {
         case 3: by_tw(std::integral_constant<int, 3>()); break;
