@@ -265,6 +265,14 @@ int ertgb_get_matrix(ertgb_ctx *ctx, int k_index, int which, double *vals_host);
 /* Sub-potentials of the last response, laid out [k][electrode][node]
  * like the reference's subSolutions_ rows (i + k*nElecs). */
 int ertgb_get_potentials(ertgb_ctx *ctx, double *pot_host);
+/* Electrode potential matrix of the last response, n_elec x n_elec row-major:
+ * U[e][f] = potential at electrode f for the unit current of pattern e,
+ * summed over the wavenumbers with their weights (the complete electrode
+ * model: its extension row, last wavenumber) -- the reference's DataMap
+ * (DataMap::collect, core/src/bert/datamap.cpp:57-98), from which
+ * DCMultiElectrodeModelling::calculate(DataContainerERT &)
+ * (core/src/bert/dcfemmodelling.cpp:1558-1618) takes its voltages. */
+int ertgb_get_electrode_potentials(ertgb_ctx *ctx, double *U_host);
 /* Unit-current primary potentials [k][electrode][node]. */
 int ertgb_get_primary(ertgb_ctx *ctx, double *prim_host);
 int ertgb_get_stats(const ertgb_ctx *ctx, ertgb_stats *stats);

@@ -256,8 +256,10 @@ def bypass_entries(mesh, bypass_markers, resistance=None):
 class TotalPotentialProblem:
     """Mesh + electrodes + scheme of the total-potential operator."""
 
-    def __init__(self, mesh, sensors, abmn, kfac, k, w, contact_impedance=None, bypass_resistance=None):
+    def __init__(self, mesh, sensors, abmn, kfac, k, w, contact_impedance=None, bypass_resistance=None,
+                 dipole=False):
         self.mesh = mesh
+        self.dipole = bool(dipole)  # patterns of the dipole current pattern (ert_oracle.BoundarySetup)
         self.dim = mesh.dim()
         nodes = mesh.nodes
         self.n = len(nodes)
@@ -351,6 +353,10 @@ class TotalPotentialProblem:
             return u[-1][:, self.src_row].copy()
         sol = np.einsum("k,ken->en", self.w, u)
         return np.stack([sol[:, r] @ w for r, w in zip(self.erows, self.ewts)], axis=1)
+
+    def calculate(self, rho_cell):
+        """Signed voltages of the data for a unit current (Problem.calculate)."""
+        return Problem.calculate(self, rho_cell)
 
     def response(self, rho_cell):
         if np.min(rho_cell) < TOLERANCE:

@@ -70,9 +70,15 @@ class BoundarySetup:
                (e, ref) hold for every domain
     ref_elec   a 3-D Neumann domain without reference node: the last
                electrode (its own pattern is empty), else -1
+
+    dipole=True (the dipole current pattern, setDipoleCurrentPattern): no
+    reference at all, since createCurrentPattern (1488-1513) pairs the data's
+    own a and b electrodes and searchElectrodes_ picks no last-electrode
+    reference then (1054); a pole datum (b = -1) of a closed domain drains
+    its current at the calibration nodes.
     """
 
-    def __init__(self, mesh, n_elec):
+    def __init__(self, mesh, n_elec, dipole=False):
         bm = np.asarray(mesh.boundary_markers)
         if np.any(bm == MARKER_BOUND_DIRICHLET):
             raise NotImplementedError("inhomogeneous Dirichlet boundaries (-4) are not implemented")
@@ -93,10 +99,12 @@ class BoundarySetup:
         if neumann3:
             cal = np.nonzero(nm == MARKER_NODE_CALIBRATION)[0]
             self.calib = cal.astype(np.int64) if len(cal) else np.zeros(1, np.int64)
-            if self.ref_node < 0 and n_elec > 0:
+            if self.ref_node < 0 and n_elec > 0 and not dipole:
                 self.ref_elec = n_elec - 1
         else:
             self.calib = np.zeros(0, np.int64)
+        if dipole:
+            self.ref_node = -1
         self.clean = np.union1d(self.dirichlet, self.calib).astype(np.int64)
 
 
@@ -412,11 +420,14 @@ class Problem:
     """Mesh + electrodes + scheme with everything that does not depend on the
     resistivity model precomputed."""
 
-    def __init__(self, mesh, sensors, abmn, kfac, k=None, w=None, primary=None):
+    def __init__(self, mesh, sensors, abmn, kfac, k=None, w=None, primary=None, dipole=False):
         """``primary``: unit primary potentials u_p[kIdx, e, node] given (the
         numerical ones of a topographic surface, ``numerical_primary``);
-        default the analytic half-space potentials."""
+        default the analytic half-space potentials.  ``dipole``: the
+        patterns of the dipole current pattern (BoundarySetup): one pure
+        pole per electrode, whose differences are the (a, b) dipoles."""
         self.mesh = mesh
+        self.dipole = bool(dipole)
         self.dim = mesh.dim()
         nodes = mesh.nodes
         self.n = len(nodes)
@@ -509,7 +520,7 @@ class Problem:
         """Reference electrode and calibration/Dirichlet nodes (BoundarySetup):
         pattern e carries +1 at electrode e and -1 at the reference (sink rows
         and weights; none: the current leaves at infinity)."""
-        bc = BoundarySetup(self.mesh, self.nE)
+        bc = BoundarySetup(self.mesh, self.nE, getattr(self, "dipole", False))
         self.bc = bc
         self.calib, self.clean = bc.calib, bc.clean
         self.ref_minr, self.ref_cells = 0.0, np.zeros(0, np.int64)
@@ -679,6 +690,13 @@ class Problem:
 
         uAM, uAN, uBM, uBN = g(a, m), g(a, n), g(b, m), g(b, n)
         return (uAM - uAN) - (uBM - uBN)
+
+    def calculate(self, rho_cell):
+        """Signed voltages of the data for a unit current, without rounding
+        or reciprocity (DCMultiElectrodeModelling::calculate(DataContainerERT
+        &), dcfemmodelling.cpp:1558-1618); with ``dipole`` the voltage of an
+        (a, b) pattern is the difference of the pure poles a and b."""
+        return Problem.data_u(self, self.collect(self.solve(rho_cell)))
 
     def response_from_u(self, u):
         U = self.collect(u)
@@ -860,7 +878,7 @@ def prolongate_empty(mesh, vals, background):
             vals[c] = v
 
 
-def numerical_primary(mesh, sensors, abmn, kfac, k, w):
+def numerical_primary(mesh, sensors, abmn, kfac, k, w, dipole=False):
     """Unit primary potentials of a topographic surface
     (DCSRMultiElectrodeModelling::checkPrimpotentials_,
     core/src/bert/dcfemmodelling.cpp:2008-2068): the total potential at 1
@@ -875,6 +893,6 @@ def numerical_primary(mesh, sensors, abmn, kfac, k, w):
         sys.path.insert(0, here)
     from cem_oracle import TotalPotentialProblem
     m2 = mesh.createP2()
-    T = TotalPotentialProblem(m2, sensors, abmn, kfac, k, w)
+    T = TotalPotentialProblem(m2, sensors, abmn, kfac, k, w, dipole=dipole)
     u = T.solve(np.ones(m2.cellCount()))
     return u[:, :, :mesh.nodeCount()].copy()

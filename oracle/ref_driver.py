@@ -66,6 +66,7 @@ def lib():
         L.ref_electrode_nodes.argtypes = [vp, vp]
         L.ref_geometric_factors.argtypes = [vp, vp]
         L.ref_response.argtypes = [vp, vp, ctypes.c_int, vp]
+        L.ref_calculate_dipole.argtypes = [vp, vp, ctypes.c_int, vp, vp]
         L.ref_subpot_shape.argtypes = [vp, vp, vp]
         L.ref_subpotentials.argtypes = [vp, vp]
         L.ref_jacobian.argtypes = [vp, vp, ctypes.c_int, vp, vp, vp]
@@ -255,6 +256,16 @@ class RefModelling:
         self.matrices = []
         _check(lib().ref_response(self.h, _p(m), len(m), _p(out)))
         return out
+
+    def calculate_dipole(self, model):
+        """Voltages (unit current) of the data with the dipole current
+        pattern (calculate(DataContainerERT &) with setDipoleCurrentPattern);
+        returns (u, number of (a, b) patterns solved)."""
+        m = np.ascontiguousarray(model, np.float64)
+        out = np.zeros(self.nData)
+        npat = ctypes.c_int()
+        _check(lib().ref_calculate_dipole(self.h, _p(m), len(m), _p(out), ctypes.byref(npat)))
+        return out, npat.value
 
     def set_primary(self, prim):
         """Primary potentials (rows = source + k * nE, cols = nodes) for the

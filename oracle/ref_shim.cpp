@@ -391,6 +391,28 @@ int ref_response(void *hp, const double *model, int nModel, double *rhoa) {
     });
 }
 
+// The dipole current pattern: setDipoleCurrentPattern(true), the model
+// mapped to the cells (mapERTModel), calculate(DataContainerERT &)
+// (dcfemmodelling.cpp:1558-1618: one solve per distinct (a, b) pair of the
+// data, createCurrentPattern 1488-1513), then the data's "u" (unit current)
+// and the number of patterns solved.  The operator is back in pole mode
+// afterwards.
+int ref_calculate_dipole(void *hp, const double *model, int nModel, double *u, int *n_patterns) {
+    RefHandle *h = (RefHandle *)hp;
+    int rc = guarded([&] {
+        RVector m(nModel);
+        for (int i = 0; i < nModel; i++) m[i] = model[i];
+        h->fop->setDipoleCurrentPattern(true);
+        h->fop->mapERTModel(m, -9e99);
+        h->fop->calculate(h->data, false);
+        const RVector &uu = h->data("u");
+        for (Index i = 0; i < uu.size(); i++) u[i] = uu[i];
+        *n_patterns = (int)h->data.currentPattern(false).size();
+    });
+    h->fop->setDipoleCurrentPattern(false);
+    return rc;
+}
+
 // Sub-potentials of the last response: rows (i + kIdx*nE), cols nodes.
 int ref_subpot_shape(void *hp, int *rows, int *cols) {
     RefHandle *h = (RefHandle *)hp;

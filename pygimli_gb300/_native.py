@@ -70,6 +70,7 @@ SIGNATURES = {
     "ertgb_get_pattern": (_ci, [_vp, _vp, _vp]),
     "ertgb_get_matrix": (_ci, [_vp, _ci, _ci, _vp]),
     "ertgb_get_potentials": (_ci, [_vp, _vp]),
+    "ertgb_get_electrode_potentials": (_ci, [_vp, _vp]),
     "ertgb_get_primary": (_ci, [_vp, _vp]),
     "ertgb_get_stats": (_ci, [_vp, ctypes.POINTER(Stats)]),
     "ertgb_csr_spmm_dot": (_ci, [_i64, _i64, _vp, _vp, _vp, _ci, _ci, _i64, _vp, _vp, _vp, _vp]),

@@ -967,13 +967,17 @@ void finish_potentials(Context &c, cudaStream_t s) {
     ERTGB_CUDA(cudaGetLastError());
 }
 
-void collect_response(Context &c, double *rhoa, cudaStream_t s) {
+void collect_potentials(Context &c, cudaStream_t s) {
     c.d_U.alloc((size_t)c.nE * c.nE);
     const bool total = c.formulation == ERTGB_FORMULATION_TOTAL_POTENTIAL;
     k_collect<<<grid1((int64_t)c.nE * c.nE), kThreads, 0, s>>>(c.nE, c.nK, c.Rpad, c.d_ew_ptr.p, c.d_ew_row.p,
                                                                c.d_ew_w.p, c.d_w.p, c.d_x.p, c.d_U.p,
                                                                total && c.collect_last_k ? 1 : 0);
     ERTGB_CUDA(cudaGetLastError());
+}
+
+void collect_response(Context &c, double *rhoa, cudaStream_t s) {
+    collect_potentials(c, s);
     k_response<<<grid1(c.D), kThreads, 0, s>>>(c.D, c.nE, c.d_abmn.p, c.d_kfac.p, c.d_U.p, rhoa);
     ERTGB_CUDA(cudaGetLastError());
 }

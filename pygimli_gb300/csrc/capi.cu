@@ -851,6 +851,18 @@ int ertgb_get_potentials(ertgb_ctx *ctx, double *pot) {
     });
 }
 
+int ertgb_get_electrode_potentials(ertgb_ctx *ctx, double *U) {
+    Context *c = reinterpret_cast<Context *>(ctx);
+    return guard(c, [&] {
+        if (!c->have_pot) throw Error(ERTGB_STATE, "no potentials yet");
+        ERTGB_REQUIRE(U, "null buffer");
+        collect_potentials(*c, c->stream);
+        ERTGB_CUDA(cudaMemcpyAsync(U, c->d_U.p, sizeof(double) * (size_t)c->nE * c->nE, cudaMemcpyDeviceToHost,
+                                   c->stream));
+        ERTGB_CUDA(cudaStreamSynchronize(c->stream));
+    });
+}
+
 int ertgb_get_primary(ertgb_ctx *ctx, double *prim) {
     Context *c = reinterpret_cast<Context *>(ctx);
     return guard(c, [&] {

@@ -331,6 +331,7 @@ void compute_rhs_scale(Context &c, cudaStream_t s);
 // where the singularity-removal right-hand side cancels (homogeneous ground around a source).
 constexpr double kRhsFloor2 = 1e-6;
 void finish_potentials(Context &c, cudaStream_t s);
+void collect_potentials(Context &c, cudaStream_t s);  // d_U = k-summed potentials at the electrodes
 void collect_response(Context &c, double *rhoa, cudaStream_t s);
 // total potential: unit currents at the electrodes' source rows into d_r
 void build_rhs_total(Context &c, cudaStream_t s);

@@ -18,7 +18,8 @@ cells, with sr=False also CEM and bypass electrodes; mixed far-field,
 homogeneous Neumann and homogeneous Dirichlet (-3) boundaries, closed
 (Neumann-only) domains with calibration nodes (-1000) and a reference
 electrode (node marker -999 or the last electrode); pole current patterns
-or patterns against the reference electrode.
+or patterns against the reference electrode, and the dipole current pattern
+(forward voltages, ``setDipoleCurrentPattern`` + ``calculate``).
 """
 from __future__ import annotations
 
@@ -147,7 +148,7 @@ class BoundarySetup:
         self.ref_node, self.ref_elec = ref_node, ref_elec
 
 
-def boundary_setup(mesh, n_elec):
+def boundary_setup(mesh, n_elec, dipole=False):
     bm = np.asarray(mesh.boundary_markers)
     if np.any(bm == MARKER_BOUND_DIRICHLET):
         raise NotImplementedError("inhomogeneous Dirichlet boundaries (marker -4) are not implemented")
@@ -163,8 +164,10 @@ def boundary_setup(mesh, n_elec):
         calib = np.flatnonzero(nm == MARKER_NODE_CALIBRATION)
         if len(calib) == 0:
             calib = np.zeros(1, np.int64)
-        if ref_node < 0 and n_elec > 0:
+        if ref_node < 0 and n_elec > 0 and not dipole:
             ref_elec = n_elec - 1
+    if dipole:  # the dipole current pattern pairs the data's own electrodes (no reference)
+        ref_node = -1
     return BoundarySetup(neumann, topo, dirichlet, calib, ref_node, ref_elec)
 
 
@@ -204,6 +207,8 @@ class ERTModelling:
         self._refineH2 = True
         self._refineP2 = False
         self._complex = False     # complex resistivity (setComplex)
+        self._dipole = False      # dipole current pattern (setDipoleCurrentPattern)
+        self._mapped = None       # cell resistivities of the last mapERTModel / response
         self._rm = None           # region manager of the parameter mesh (setMesh without ignoreRegionManager)
         self._fwd_parent = None   # forward-mesh cell -> parameter-mesh cell
         self.setSolverTolerance(rtol, maxIter)
@@ -396,6 +401,7 @@ class ERTModelling:
             es = setup.search
         self._check(self._lib.ertgb_set_electrodes(self._ctx, len(self._elec_nodes),
                                                    _ptr(self._elec_nodes), float(self._surface_z)))
+        self._esearch = es
         self._entity = es is not None and es.entity
         if self._entity:
             cells = np.ascontiguousarray(es.cells, np.int32)
@@ -406,7 +412,7 @@ class ERTModelling:
             self._check(self._lib.ertgb_set_extension(
                 self._ctx, int(e.n_ext), len(e.rows), _ptr(e.rows), _ptr(e.cols), _ptr(e.vals), _ptr(e.src_row),
                 _ptr(e.src_center), 1 if e.cem else 0))
-        bc = boundary_setup(mesh, len(self._elec_nodes))
+        bc = boundary_setup(mesh, len(self._elec_nodes), self._dipole)
         if bc.ref_node >= 0 or bc.ref_elec >= 0:
             if self._electrodes is not None and (self._electrodes.cem or len(self._electrodes.rows)):
                 raise NotImplementedError("a reference electrode with complete-electrode-model or bypass "
@@ -437,11 +443,12 @@ class ERTModelling:
                            precision="fp64")
         fop.setkValues(self._k)
         fop.setWeights(self._w)
+        fop._dipole = self._dipole  # the same current patterns (pure poles for the dipole pattern)
         unit = self._data.copy()
         unit.set("k", np.ones(unit.size()))
         fop.setData(unit)
         fop.setMesh(m2, ignoreRegionManager=True)
-        fop.response(np.ones(m2.cellCount()))
+        fop._forward(np.ones(m2.cellCount()))
         up = np.ascontiguousarray(fop.subPotentials()[:, :, :mesh.nodeCount()])
         del fop
         self._check(self._lib.ertgb_set_primary(self._ctx, up.shape[0], up.shape[1], up.shape[2], _ptr(up)))
@@ -611,8 +618,14 @@ class ERTModelling:
         return 1.0 / (u + TOLERANCE)
 
     def mapERTModel(self, model, background=-9e99):
+        """Cell resistivities of ``model`` (per cell or per parameter, the
+        region manager's fixed values and ``background`` for unmapped cells),
+        kept for ``calculate`` as the reference keeps them as cell attributes
+        (DCMultiElectrodeModelling::mapERTModel, dcfemmodelling.cpp:1211-1218)."""
         fixed = self._rm.fixedValues() if self._rm is not None else None
-        return map_model(self._mesh, model, background, fixed)
+        rho = map_model(self._mesh, model, background, fixed)
+        self._mapped = rho
+        return rho
 
     # ---------------------------------------------------------- forward
     def _ready(self):
@@ -627,6 +640,13 @@ class ERTModelling:
         CUDA tensor of per-cell resistivities -> CUDA tensor).  With
         setComplex(True): [Re..., Im...] of the complex apparent
         resistivities for a model [Re..., Im...] (or a complex array)."""
+        if self._dipole:
+            # DCMultiElectrodeModelling::response_ throws there (dcfemmodelling.cpp:1231-1233)
+            raise NotImplementedError("response with the dipole current pattern is not implemented (neither in "
+                                      "the reference); calculate(data) gives its voltages")
+        return self._forward(model)
+
+    def _forward(self, model):
         self._ready()
         if self._complex:
             return self._response_complex(model)
@@ -638,6 +658,7 @@ class ERTModelling:
             out = torch.empty(self._data.size(), dtype=torch.float64, device=rho.device)
             self._response_dev(rho, out)
             self._last_model = rho
+            self._mapped = rho
             return out
         m = np.asarray(model, np.float64)
         if np.min(m) < TOLERANCE:
@@ -649,6 +670,7 @@ class ERTModelling:
         out = torch.empty(self._data.size(), dtype=torch.float64, device=dev)
         self._response_dev(rho_d, out)
         self._last_model = m
+        self._mapped = rho
         return out.cpu().numpy()
 
     def _response_dev(self, rho, out):
@@ -717,6 +739,14 @@ class ERTModelling:
         torch = _torch()
         if self._mesh is None:
             raise RuntimeError("no mesh")
+        if self._dipole:
+            # the reference has no working dipole-pattern Jacobian: prepareJacobianT_
+            # takes one potential row per (a, b) pattern from calculate(DataContainerERT &)
+            # (dcfemmodelling.cpp:1290-1292), and the Jacobian's pattern branch
+            # (core/src/bert/bertJacobian.cpp:172-181) looks the pattern up from its
+            # zero-initialised a, b, m, n before it reads any datum's electrodes
+            raise NotImplementedError("createJacobian with the dipole current pattern is not implemented "
+                                      "(neither in the reference)")
         if self._complex:
             return self._jacobian_complex(model)
         P = self.parameterCount
@@ -807,16 +837,111 @@ class ERTModelling:
         return sol
 
     def electrodePotentials(self):
-        """U[e, f]: potential at electrode f for the unit current at electrode
+        """U[e, f]: potential at electrode f for the unit current of pattern
         e after the last response -- the reference's DataMap
         (DataMap::collect, core/src/bert/datamap.cpp:57-98): the k-summed
-        solution at the electrodes' rows; with CEM the extension rows of the
-        last wavenumber, unweighted (dcfemmodelling.cpp:1642-1644)."""
-        e = self._electrodes
-        if e is not None and e.cem:
-            return self.subPotentials()[-1][:, e.src_row].copy()
-        rows = e.src_row if e is not None else self._elec_nodes
-        return self.solution()[:, rows]
+        solution at the electrodes (a node, or the shape functions of the
+        cell that holds the electrode); with CEM the extension rows of the
+        last wavenumber, unweighted (dcfemmodelling.cpp:1642-1644).
+        Collected on the device (ertgb_get_electrode_potentials)."""
+        nE = len(self._elec_nodes)
+        U = np.zeros((nE, nE))
+        self._check(self._lib.ertgb_get_electrode_potentials(self._ctx, _ptr(U)))
+        return U
+
+    # ------------------------------------------------ dipole current pattern
+    def setDipoleCurrentPattern(self, dipole=True):
+        """One current pattern per distinct (a, b) pair of the data instead
+        of one per electrode (DCMultiElectrodeModelling::
+        setDipoleCurrentPattern, core/src/bert/dcfemmodelling.h:211;
+        createCurrentPattern, dcfemmodelling.cpp:1488-1513).  Forward only,
+        as in the reference: ``calculate(data)`` gives the voltages,
+        ``response`` and ``createJacobian`` refuse the mode.
+
+        The (a, b) pattern is solved as the difference of the pure poles a and
+        b: +1 at one electrode and no reference electrode (in a closed domain
+        the current drains at the calibration nodes).  The difference is the
+        dipole solution itself, not an approximation of it: each wavenumber
+        has one system matrix S for every source (its mixed boundaries use one
+        source centre, 2181-2182), the total-potential right-hand side is
+        linear in the source, and the singularity-removal potential u = u_p +
+        u_s solves S u = S1 (p_a - p_b) at the free nodes whatever the source
+        resistivity rho_s (u_p = rho_s (p_a - p_b), rhs = S1 u_p / rho_s -
+        S u_p, 2228-2254).  Only at the fixed-potential nodes of singularity
+        removal (calibration, homogeneous Dirichlet) does the reference keep
+        u = u_p with the pattern's own rho_s; ``calculate`` refuses a
+        measuring electrode there.  Solving the poles costs one solve per
+        electrode and wavenumber instead of one per (a, b) pattern."""
+        dipole = bool(dipole)
+        if dipole != self._dipole:
+            self._dipole = dipole
+            self._J = None
+            if self._mesh is not None and self._data is not None:
+                self._update_data()
+
+    def dipoleCurrentPattern(self):
+        return self._dipole
+
+    def calculate(self, data=None, reciprocity=False):
+        """Voltages for a unit current of ``data`` (default: the operator's
+        own) at the cell resistivities of the last ``mapERTModel`` or
+        ``response``, written to data 'u' and returned
+        (DCMultiElectrodeModelling::calculate(DataContainerERT &, bool),
+        core/src/bert/dcfemmodelling.cpp:1558-1618): u = (U[a,m] - U[a,n]) -
+        (U[b,m] - U[b,n]) of ``electrodePotentials``, signed, without the
+        rounding and the reciprocal mean of ``response``.  ``reciprocity``
+        changes nothing, as in the reference (1566, 1628-1639).  With the
+        dipole current pattern every datum's (a, b) pair must be one of the
+        operator's own data (the reference finds no pattern index otherwise,
+        1581-1586).  The operator's data need geometric factors where
+        ``response`` needs them (topography, CEM); their values do not enter."""
+        if self._complex:
+            raise NotImplementedError("calculate with complex resistivity is not implemented (the reference "
+                                      "refuses it, dcfemmodelling.cpp:1562)")
+        if self._mapped is None:
+            raise RuntimeError("no model: call mapERTModel(model) or response(model) first")
+        self._ready()
+        data = self._data if data is None else data
+        ab = np.asarray(data.abmn(), np.int64).reshape(-1, 4)
+        nE = len(self._elec_nodes)
+        if ab.size and (ab.max() >= nE or ab.min() < -1):
+            raise ValueError("electrode index out of range of the operator's electrodes")
+        if self._dipole:
+            own = {tuple(p) for p in np.asarray(self._data.abmn(), np.int64)[:, :2].tolist()}
+            for p in ab[:, :2].tolist():
+                if tuple(p) not in own:
+                    raise ValueError(f"current pattern (a, b) = {tuple(p)} is not among the operator's data")
+            if self._sr:
+                self._refuse_fixed_measuring(ab)
+        torch = _torch()
+        dev = torch.device("cuda", self.device)
+        rho = self._mapped
+        if isinstance(rho, torch.Tensor):
+            rho_d = rho.to(device=dev, dtype=torch.float64).contiguous()
+        else:
+            rho_d = torch.from_numpy(np.ascontiguousarray(rho, np.float64)).to(dev)
+        if rho_d.numel() != self._mesh.cellCount():
+            raise ValueError("the mapped model must give one resistivity per cell")
+        out = torch.empty(self._data.size(), dtype=torch.float64, device=dev)
+        self._response_dev(rho_d, out)
+        u = datamap_voltages(self.electrodePotentials(), ab)
+        data.set("u", u)
+        return u
+
+    def _refuse_fixed_measuring(self, ab):
+        """Singularity removal with the dipole pattern: no measuring
+        electrode on a calibration or homogeneous Dirichlet node."""
+        bc = self._bc
+        fixed = np.union1d(np.asarray(bc.calib, np.int64), np.asarray(bc.dirichlet, np.int64))
+        if not len(fixed):
+            return
+        es = self._esearch
+        for e in np.unique(ab[:, 2:][ab[:, 2:] >= 0]):
+            support = [es.nodes[e]] if es.nodes[e] >= 0 else self._mesh.cells[es.cells[e]]
+            if np.isin(support, fixed).any():
+                raise NotImplementedError(f"the dipole current pattern with singularity removal and measuring "
+                                          f"electrode {int(e)} on a fixed-potential (calibration or Dirichlet) "
+                                          f"node is not implemented")
 
     def stats(self):
         s = _native.Stats()
