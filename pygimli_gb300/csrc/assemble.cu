@@ -443,10 +443,21 @@ __global__ void k_primary(int64_t n, int nE, int nK, int64_t Rpad, const double 
 // ---------------------------------------------------------------- assembly
 // One thread per (slot, wavenumber).  Contributions are summed in the
 // reference's order: cells ascending, then mixed boundaries ascending.
+// 1/rho per cell (0 for a cell whose |rho| <= kTol, which adds nothing): one
+// FP64 division per cell instead of one per element entry in k_assemble
+__global__ void k_inv_rho(int64_t C, const double *__restrict__ rho, double *__restrict__ inv) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C;
+         c += (int64_t)gridDim.x * blockDim.x) {
+        const double r = rho[c];
+        inv[c] = fabs(r) > kTol ? 1.0 / r : 0.0;
+    }
+}
+
 __global__ void k_assemble(int64_t nnz, const int32_t *__restrict__ cptr, const int32_t *__restrict__ centry,
                            const double *__restrict__ K, const double *__restrict__ M,
                            const double *__restrict__ bmass, const double *__restrict__ alpha,
                            const int32_t *__restrict__ bcell, const double *__restrict__ rho,
+                           const double *__restrict__ inv_rho,
                            const double *__restrict__ kv, int nv2, int nvb2, int64_t C, int64_t B,
                            const int32_t *__restrict__ xptr, const double *__restrict__ xval,
                            double *__restrict__ vals) {
@@ -461,12 +472,9 @@ __global__ void k_assemble(int64_t nnz, const int32_t *__restrict__ cptr, const 
         for (int32_t q = cptr[s]; q < q1; q++) {
             const int64_t e = centry[q];
             if (e < cbase) {
-                const int64_t c = e / nv2;
-                const double r = rho ? rho[c] : 1.0;
-                if (fabs(r) > kTol) {
-                    const double se = (k > 0.0) ? M[e] * kk + K[e] : K[e];
-                    acc += (1.0 / r) * se;
-                }
+                const double ir = inv_rho ? inv_rho[e / nv2] : 1.0;
+                const double se = (k > 0.0) ? M[e] * kk + K[e] : K[e];
+                acc += ir * se;
             } else {
                 const int64_t eb = e - cbase;
                 const int64_t b = eb / nvb2;
@@ -885,10 +893,16 @@ void upload_primary(Context &c) {
 
 void assemble_all(Context &c, const double *rho_cell, double *vals, cudaStream_t s) {
     MeshData &m = c.mesh;
+    if (rho_cell) {
+        c.d_inv_rho.alloc((size_t)m.C);
+        k_inv_rho<<<grid1(m.C, kThreads, 4096), kThreads, 0, s>>>(m.C, rho_cell, c.d_inv_rho.p);
+        ERTGB_CUDA(cudaGetLastError());
+    }
     dim3 grid(grid1(m.nnz, kThreads, 1 << 16), c.nK);
     k_assemble<<<grid, kThreads, 0, s>>>(m.nnz, m.d_cptr.p, m.d_centry.p, m.d_K.p, m.d_M.p, m.d_bnd_mass.p,
-                                         c.d_alpha.p, m.d_bnd_cell.p, rho_cell, c.d_k.p, m.nv * m.nv,
-                                         m.nvb * m.nvb, m.C, m.B, m.d_ext_ptr.p, m.d_ext_val.p, vals);
+                                         c.d_alpha.p, m.d_bnd_cell.p, rho_cell, rho_cell ? c.d_inv_rho.p : nullptr,
+                                         c.d_k.p, m.nv * m.nv, m.nvb * m.nvb, m.C, m.B, m.d_ext_ptr.p,
+                                         m.d_ext_val.p, vals);
     ERTGB_CUDA(cudaGetLastError());
     clean_fixed_rows(c, vals, s);
     if (rho_cell) {
@@ -987,10 +1001,14 @@ void profile_assemble(Context &c, int reps, double *ms, double *bytes, double *f
     if (c.d_S.n < (size_t)c.nK * m.nnz || !c.d_rho_last) throw Error(ERTGB_STATE, "profile needs a completed response");
     cudaStream_t s = c.stream;
     dim3 grid(grid1(m.nnz, kThreads, 1 << 16), c.nK);
+    c.d_inv_rho.alloc((size_t)m.C);
+    k_inv_rho<<<grid1(m.C, kThreads, 4096), kThreads, 0, s>>>(m.C, c.d_rho_last, c.d_inv_rho.p);
+    ERTGB_CUDA(cudaGetLastError());
     auto go = [&] {
         k_assemble<<<grid, kThreads, 0, s>>>(m.nnz, m.d_cptr.p, m.d_centry.p, m.d_K.p, m.d_M.p, m.d_bnd_mass.p,
-                                             c.d_alpha.p, m.d_bnd_cell.p, c.d_rho_last, c.d_k.p, m.nv * m.nv,
-                                             m.nvb * m.nvb, m.C, m.B, m.d_ext_ptr.p, m.d_ext_val.p, c.d_S.p);
+                                             c.d_alpha.p, m.d_bnd_cell.p, c.d_rho_last, c.d_inv_rho.p, c.d_k.p,
+                                             m.nv * m.nv, m.nvb * m.nvb, m.C, m.B, m.d_ext_ptr.p, m.d_ext_val.p,
+                                             c.d_S.p);
     };
     go();
     ERTGB_CUDA(cudaEventRecord(c.ev[0], s));
@@ -1001,9 +1019,12 @@ void profile_assemble(Context &c, int reps, double *ms, double *bytes, double *f
     ERTGB_CUDA(cudaEventElapsedTime(&t, c.ev[0], c.ev[1]));
     *ms = (double)t / reps;
     const double entries = (double)m.C * m.nv * m.nv + (double)m.B * m.nvb * m.nvb;
-    // slot lists, element values (K and M), resistivity per cell, boundary
+    // slot lists, element values (K, and M where a wavenumber is positive: the
+    // 3-D operator has k = 0 and reads K alone), resistivity per cell, boundary
     // terms, matrix values written per wavenumber
-    *bytes = (double)(m.nnz + 1) * 4.0 + entries * 4.0 + (double)m.C * m.nv * m.nv * 16.0 + m.C * 8.0 +
+    bool any_k = false;
+    for (double kv : c.k) any_k = any_k || kv > 0.0;
+    *bytes = (double)(m.nnz + 1) * 4.0 + entries * 4.0 + (double)m.C * m.nv * m.nv * (any_k ? 16.0 : 8.0) + m.C * 8.0 +
              (double)m.B * (m.nvb * m.nvb * 8.0 + c.nK * 8.0 + 4.0) + (double)c.nK * m.nnz * 8.0;
     *flops = entries * c.nK * 3.0;
 }

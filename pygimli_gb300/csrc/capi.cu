@@ -240,9 +240,9 @@ int do_response(Context &c, const double *rho, double *rhoa, void *stream) {
     c.stats.ms_rhs = elapsed(c, 1, 2);
     c.stats.ms_solve = elapsed(c, 2, 3);
     c.stats.ms_collect = elapsed(c, 3, 4);
-    // check_rho, assemble, dinv, source_rho, rhs, finish_pot, collect, response
-    // (total potential: check_rho, assemble, dinv, rhs, collect, response)
-    c.stats.launches_response += total ? 6 : 8;
+    // check_rho, inv_rho, assemble, dinv, source_rho, rhs, finish_pot, collect, response
+    // (total potential: check_rho, inv_rho, assemble, dinv, rhs, collect, response)
+    c.stats.launches_response += total ? 7 : 9;
     c.have_pot = true;
     j.done();
     return status;

@@ -300,6 +300,7 @@ struct Context {
     DBuf<double> d_col;           // per-column scalars (see pcg.cu)
     DBuf<int32_t> d_active;
     DBuf<double> d_U;             // nE x nE collected electrode potentials
+    DBuf<double> d_inv_rho;       // 1/rho per cell of the last assembly
     DBuf<double> d_rhoa;
     bool have_pot = false;
     bool have_S = false;          // d_S holds the matrices of the current setup
