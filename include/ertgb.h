@@ -298,8 +298,10 @@ int ertgb_csr_spmm_dot(int64_t n, int64_t nnz, const int32_t *rowptr_dev, const 
  * (every GPU that loads the library holds it until exit), so ld is limited
  * to 1024 columns (larger ld: ERTGB_BAD_INPUT).  Calls no allocator.  The
  * first call on a device looks up the array's address and should come
- * before any stream capture.  All calls share the array: calls that overlap
- * on the GPU race and must be ordered by the caller. */
+ * before any stream capture; the address is kept for the life of the
+ * process, so no device may be reset (cudaDeviceReset) nor its primary
+ * context torn down while the library is loaded.  All calls share the array:
+ * calls that overlap on the GPU race and must be ordered by the caller. */
 int ertgb_csr_spmm_dot_noalloc(int64_t n, int64_t nnz, const int32_t *rowptr_dev, const int32_t *colidx_dev,
                                const double *vals_dev, int n_k, int n_per_k, int64_t ld, const double *X_dev,
                                double *Y_dev, double *dots_dev, void *stream);

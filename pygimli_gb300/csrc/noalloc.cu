@@ -21,7 +21,10 @@
 // host code it is a host-side stand-in), so the first call on each device
 // looks up the array's device address with cudaGetSymbolAddress, with that
 // device current, and caches it.  That first call per device should come
-// before any stream capture.
+// before any stream capture.  The cached address is that of the device's
+// primary context: a device reset (cudaDeviceReset) or a torn-down primary
+// context would leave it stale, so neither may happen while the library is
+// loaded.
 #include <mutex>
 #include <vector>
 
