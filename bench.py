@@ -24,7 +24,8 @@ resistivity and the total-potential operator with complete-electrode-model
 patches on ``box_3d``.  ``cpu_baseline`` and ``--impl reference`` time the
 CPU oracle port (the reference's algorithm restated in numpy/scipy with a
 SuperLU direct solve) on bounded samples of the workload (one core beside the
-GPU timings, resp. every host thread).  ``--case`` runs single workloads for
+GPU timings, resp. every host thread); ``--impl reference --ref-cpp`` times
+full steps of the reference's own C++ where its library was built.  ``--case`` runs single workloads for
 profiler captures.  With N > 1 ranks (torchrun) every rank runs an
 independent replica of the workload (the operator uses one GPU).
 """
@@ -66,6 +67,10 @@ def parse():
     ap.add_argument("--cem-patch", type=float, default=4.0 / 3.0,
                     help="surface cell size of the workload mesh (CEM patch = the triangles within one diagonal)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-cpp", action="store_true",
+                    help="with --impl reference: time full steps of the reference's own C++ "
+                         "(oracle/_ref/libgimli_ref.so, present only where the reference's sources were "
+                         "compiled) instead of the sampled port")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--gn", action="store_true", help="also time one full Gauss-Newton iteration per form "
                     "(response, Jacobian, 200 CGLS iterations on the GPU, line-search responses)")
@@ -425,6 +430,9 @@ def run_reference(args, world, rank):
     rows are sampled per step and scaled (oracle/cpu_baseline.py)."""
     if rank != 0:
         return
+    if args.ref_cpp:
+        run_reference_cpp(args)
+        return
     from oracle.cpu_baseline import SampledBaseline, host_threads
     from pygimli_gb300.kwave import init_kwave_list
     mesh, data, rho, cfg = workload(args.workload)
@@ -449,6 +457,47 @@ def run_reference(args, world, rank):
            "data": "synthetic (seeded)", "impl": "reference",
            "config": dict(cfg, parallelism="cpu", solver="SuperLU direct (CHOLMOD stand-in)"),
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def run_reference_cpp(args):
+    """Full steps (response + createJacobian, no sampling) of the reference's
+    own DCSRMultiElectrodeModelling compiled from its sources
+    (oracle/_ref/libgimli_ref.so), with every host thread
+    (setThreadCount) and SciPy's SuperLU as the stand-in for CHOLMOD
+    (the reference's setSolver hook).  The Jacobian stays in the
+    reference's FP64 RMatrix."""
+    from oracle import ref_driver
+    from oracle.cpu_baseline import host_threads
+    if not ref_driver.available():
+        raise SystemExit("--ref-cpp: oracle/_ref/libgimli_ref.so is not built here "
+                         "(make -C oracle needs the reference's sources)")
+    mesh, data, rho, cfg = workload(args.workload)
+    threads = host_threads()
+    t0 = time.perf_counter()
+    R = ref_driver.RefModelling(mesh, data.sensorPositions(), data.abmn(), data["k"], threads=threads, sr=True)
+    setup_s = time.perf_counter() - t0
+    times, resp = [], []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        R.response(rho)
+        t1 = time.perf_counter()
+        shape = R.create_jacobian(rho)
+        t2 = time.perf_counter()
+        if i >= args.warmup:
+            times.append(t2 - t0)
+            resp.append(t1 - t0)
+    R.close()
+    value = float(np.mean(times))
+    sample = (f"full steps of the reference's C++ (DCSRMultiElectrodeModelling, {threads} threads, SuperLU "
+              f"stand-in for CHOLMOD): response {np.mean(resp):.2f} s + createJacobian "
+              f"{value - np.mean(resp):.2f} s ({shape[0]} x {shape[1]} FP64); setup {setup_s:.1f} s")
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": len(times),
+           "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
+           "config": dict(cfg, parallelism="cpu", solver="SuperLU direct (CHOLMOD stand-in)"),
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "reference", "sample": sample},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 

@@ -299,6 +299,15 @@ class RefModelling:
         _check(lib().ref_jacobian_complex(self.h, _p(m), len(m), _p(Jr), _p(Ji), ctypes.byref(r), ctypes.byref(c)))
         return Jr + 1j * Ji
 
+    def create_jacobian(self, model):
+        """createJacobian(model) alone (the Jacobian stays in the reference's
+        RMatrix); returns its shape."""
+        m = np.ascontiguousarray(model, np.float64)
+        r = ctypes.c_int()
+        c = ctypes.c_int()
+        _check(lib().ref_jacobian(self.h, _p(m), len(m), None, ctypes.byref(r), ctypes.byref(c)))
+        return r.value, c.value
+
     def jacobian(self, model):
         m = np.ascontiguousarray(model, np.float64)
         r = ctypes.c_int()
