@@ -207,6 +207,7 @@ class ERTModelling:
         self._refineH2 = True
         self._refineP2 = False
         self._complex = False     # complex resistivity (setComplex)
+        self._conjImag = False    # complex start model flipped to a positive imaginary part
         self._dipole = False      # dipole current pattern (setDipoleCurrentPattern)
         self._mapped = None       # cell resistivities of the last mapERTModel / response
         self._rm = None           # region manager of the parameter mesh (setMesh without ignoreRegionManager)
@@ -522,17 +523,27 @@ class ERTModelling:
     def createStartModel(self, dataVals):
         """Start model: the median of the data values for every parameter
         (Modelling.createStartModel, pygimli/frameworks/modelling.py:231-244);
-        complex: medians of the real and imaginary parts, the imaginary part
-        flipped to positive (ertModelling.py:168-186, which then also flips
-        it back around response and Jacobian; that convention is left to the
-        caller here)."""
+        complex: medians of the real and imaginary parts, a negative
+        imaginary part flipped to positive, after which ``response`` and
+        ``createJacobian`` work on the flipped convention: the model's
+        imaginary part flipped before, the response's after, the Jacobian
+        conjugated (ertModelling.py:168-238)."""
         v = np.asarray(dataVals)
         if not self._complex:
             return np.full(self.parameterCount, float(np.median(v)))
         z = v if np.iscomplexobj(v) else v[:len(v) // 2] + 1j * v[len(v) // 2:]
         P = self._real_parameter_count()
         re, im = np.median(z.real), np.median(z.imag)
-        return np.concatenate([np.full(P, re), np.full(P, abs(im) if im < 0 else im)])
+        if im < 0:
+            self._conjImag = True
+            im = -im
+        return np.concatenate([np.full(P, re), np.full(P, im)])
+
+    def flipImagPart(self, v):
+        """[Re..., Im...] of ``v`` ([Re..., Im...] or complex) with the
+        imaginary part negated when the start model flipped it
+        (ERTModelling.flipImagPart, ertModelling.py:188-202)."""
+        return flip_imag(v, self._conjImag)
 
     def _complex_cells(self, model):
         """Per-cell (Re, Im) of a complex model [Re..., Im...]: one value per
@@ -649,7 +660,9 @@ class ERTModelling:
     def _forward(self, model):
         self._ready()
         if self._complex:
-            return self._response_complex(model)
+            if not self._conjImag:
+                return self._response_complex(model)
+            return self.flipImagPart(self._response_complex(self.flipImagPart(model)))
         torch = _torch()
         if isinstance(model, torch.Tensor) and model.is_cuda:
             rho = model.to(torch.float64).contiguous()
@@ -748,7 +761,11 @@ class ERTModelling:
             raise NotImplementedError("createJacobian with the dipole current pattern is not implemented "
                                       "(neither in the reference)")
         if self._complex:
-            return self._jacobian_complex(model)
+            if not self._conjImag:
+                return self._jacobian_complex(model)
+            J = self._jacobian_complex(self.flipImagPart(model))
+            J.imag.neg_()  # conjugate in place (the complex Jacobian can be tens of GB)
+            return J
         P = self.parameterCount
         D = self._data.size()
         tdt = torch.float64 if dtype in ("float64", torch.float64) else torch.float32
@@ -974,6 +991,21 @@ def _cell_values(mesh, res):
     if len(arr) != C:
         raise IndexError("Simulate called with wrong resistivity array.")
     return arr, False
+
+
+def flip_imag(v, conj):
+    """[Re..., Im...] of ``v`` ([Re..., Im...] or a complex array), the
+    imaginary part negated when ``conj`` (pg.utils.squeezeComplex(toComplex(v),
+    conj=...))."""
+    a = np.asarray(v)
+    if np.iscomplexobj(a):
+        re, im = a.real, a.imag
+    else:
+        a = a.astype(np.float64)
+        if len(a) % 2:
+            raise ValueError("a complex vector needs [Re..., Im...] (even length)")
+        re, im = a[:len(a) // 2], a[len(a) // 2:]
+    return np.concatenate([re, -im if conj else im]).astype(np.float64)
 
 
 def datamap_voltages(U, abmn):

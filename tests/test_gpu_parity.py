@@ -486,6 +486,33 @@ def test_complex_resistivity_golden(torch, golden_dir, name, precision):
     assert e_r <= 1e-7 and e_j <= 1e-6
 
 
+def test_complex_flip_convention(torch, golden_dir):
+    """A complex start model from data whose median imaginary part is
+    negative flips it to positive (ertModelling.py:168-186); response and
+    createJacobian then take and return that convention (:204-238):
+    response(flip(m)) = flip(response(m)) and the Jacobian conjugated, bit
+    for bit (the same deterministic solves)."""
+    z = np.load(os.path.join(golden_dir, "ert2d_complex_small.npz"))
+    mesh = Mesh(int(z["dim"]), z["nodes"], z["cells"], z["cell_markers"], z["node_markers"],
+                z["boundaries"], z["boundary_markers"], z["boundary_cells"])
+    data = DataContainerERT(z["sensors"], z["abmn"])
+    data.set("k", z["kfac"])
+    fop = fop_for(mesh, data, z["k"], z["w"], form="fp64")
+    fop.setComplex(True)
+    rho = z["rho"]
+    m = np.concatenate([rho.real, rho.imag])
+    r0 = fop.response(m)
+    J0 = fop.createJacobian(rho).cpu().numpy()
+    D = data.size()
+    sm = fop.createStartModel(np.concatenate([np.abs(r0[:D]), -np.abs(r0[D:]) - 1.0]))
+    P = mesh.cellCount()
+    assert fop._conjImag and np.all(sm[P:] > 0) and len(sm) == 2 * P
+    r1 = fop.response(fop.flipImagPart(m))
+    assert np.array_equal(r1, fop.flipImagPart(r0))
+    J1 = fop.createJacobian(np.conj(rho)).cpu().numpy()
+    assert np.array_equal(J1, np.conj(J0))
+
+
 def test_complex_sign_and_mirror_symmetry(torch):
     """The reference's complex simulate test (pygimli/testing/
     test_ERTManager_simulate.py) on this operator: layered complex

@@ -127,3 +127,15 @@ def test_data_container_editing():
     d.translate([1.0, 0.0])
     d.scale([2.0, 1.0, 1.0])
     assert np.isclose(d.sensorPosition(0)[0], 2.0)
+
+
+def test_flip_imag():
+    """The complex flip convention's vector helper (pg.utils.squeezeComplex
+    with conj): [Re..., Im...] out, the imaginary part negated on request."""
+    from pygimli_gb300.ert import flip_imag
+    v = np.array([1.0, 2.0, 3.0, -4.0])
+    assert np.array_equal(flip_imag(v, True), [1.0, 2.0, -3.0, 4.0])
+    assert np.array_equal(flip_imag(v, False), v)
+    assert np.array_equal(flip_imag(np.array([1 - 2j, 3 + 4j]), True), [1.0, 3.0, 2.0, -4.0])
+    with pytest.raises(ValueError):
+        flip_imag(np.ones(3), True)
