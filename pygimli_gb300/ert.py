@@ -315,6 +315,26 @@ class ERTModelling:
     def regionManager(self):
         return self._rm
 
+    def setDefaultBackground(self):
+        """With several regions, the one with the lowest marker becomes
+        background (MeshModelling.setDefaultBackground, pygimli/frameworks/
+        modelling.py:759-767; ERTModelling.setDefaultBackground,
+        ertModelling.py:131-144).  ``setMesh`` applies it already."""
+        if self._rm is None:
+            raise RuntimeError("no region manager: setMesh(mesh) without ignoreRegionManager first")
+        ids = self._rm.regionIdxs()
+        if len(ids) > 1:
+            self.setRegionProperties(ids[0], background=True)
+
+    def setDataPost(self, data):
+        """The framework's hook after setData (ertModelling.py:240-242)."""
+        self.setData(data)
+
+    def setMeshPost(self, mesh):
+        """The framework's hook after setMesh: the mesh as the forward mesh
+        (ertModelling.py:244-246)."""
+        self.setMesh(mesh, ignoreRegionManager=True)
+
     def setRegionProperties(self, regionNr, background=None, single=None, fix=None, **kwargs):
         """Background / single / fixed-value flags of a region ("*": all),
         as MeshModelling.setRegionProperties (pygimli/frameworks/

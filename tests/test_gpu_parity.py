@@ -440,6 +440,9 @@ def test_region_manager_forward(torch, dim):
     fop = ERTModelling()
     fop.setData(data)
     fop.setMesh(m)
+    P0 = fop.parameterCount
+    fop.setDefaultBackground()  # setMesh applied it already
+    assert fop.parameterCount == P0
     fop.setRegionProperties(3, fix=50.0)
     fop.setRegionProperties(4, single=True)
     P = fop.parameterCount
