@@ -91,6 +91,8 @@ def lib():
         L.ref_mesh_add_data.argtypes = [vp, cs, ctypes.c_int, vp]
         L.ref_mesh_export_vtk.argtypes = [vp, cs, ctypes.c_int]
         L.ref_regions.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, vp, ctypes.c_int, vp, vp, vp, vp, vp]
+        L.ref_region_constraints.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, vp, ctypes.c_int, vp,
+                                             vp, ctypes.c_int, vp, vp, vp, vp, vp, vp]
         L.ref_data_load.restype = vp
         L.ref_data_load.argtypes = [cs, ctypes.c_int, ctypes.c_int]
         L.ref_data_free.argtypes = [vp]
@@ -409,6 +411,26 @@ class RefMesh:
         _check(lib().ref_regions(self.h, int(default_background), len(background), _p(bg), len(single), _p(sg),
                                  len(fix), _p(fm), _p(fv), _p(out), ctypes.byref(npar), ctypes.byref(ncell)))
         return out, npar.value, ncell.value
+
+    def constraints(self, default_background=True, background=(), single=(), fix=None):
+        """The reference's RegionManager::fillConstraints for these region
+        settings: (rows, cols, vals, n_rows, n_cols), entries row-major."""
+        fix = fix or {}
+        bg = np.ascontiguousarray(list(background) or [0], np.int32)
+        sg = np.ascontiguousarray(list(single) or [0], np.int32)
+        fm = np.ascontiguousarray(list(fix) or [0], np.int32)
+        fv = np.ascontiguousarray(list(fix.values()) or [0.0], np.float64)
+        nr, nc, ne = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        args = (self.h, int(default_background), len(background), _p(bg), len(single), _p(sg), len(fix), _p(fm),
+                _p(fv))
+        _check(lib().ref_region_constraints(*args, 0, ctypes.byref(nr), ctypes.byref(nc), ctypes.byref(ne),
+                                            None, None, None))
+        r = np.zeros(max(ne.value, 1), np.int32)
+        c = np.zeros(max(ne.value, 1), np.int32)
+        v = np.zeros(max(ne.value, 1))
+        _check(lib().ref_region_constraints(*args, ne.value, ctypes.byref(nr), ctypes.byref(nc), ctypes.byref(ne),
+                                            _p(r), _p(c), _p(v)))
+        return r[:ne.value], c[:ne.value], v[:ne.value], nr.value, nc.value
 
     def add_data(self, name, values):
         v = np.ascontiguousarray(values, np.float64)

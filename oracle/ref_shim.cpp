@@ -620,6 +620,40 @@ int ref_regions(void *hp, int default_background, int n_bg, const int *bg, int n
     });
 }
 
+// The region manager's constraint matrix (RegionManager::fillConstraints,
+// core/src/regionManager.cpp:920-990, default first-order rows per region,
+// Region::fillConstraints 305-404) for the same region settings as
+// ref_regions: n_rows x n_param with its entries as (row, col, value)
+// triplets in row-major order.  Call with cap = 0 for the sizes first.
+int ref_region_constraints(void *hp, int default_background, int n_bg, const int *bg, int n_single,
+                           const int *single, int n_fix, const int *fix_marker, const double *fix_value, int cap,
+                           int *n_rows, int *n_cols, int *n_entries, int *rows, int *cols, double *vals) {
+    RefHandle *h = (RefHandle *)hp;
+    return guarded([&] {
+        RegionManager rm(false);
+        rm.setMesh(h->mesh);
+        IVector ids(rm.regionIdxs());
+        if (default_background && ids.size() > 1) rm.region(min(ids))->setBackground(true);
+        for (int i = 0; i < n_bg; i++) rm.region(bg[i])->setBackground(true);
+        for (int i = 0; i < n_single; i++) rm.region(single[i])->setSingle(true);
+        for (int i = 0; i < n_fix; i++) rm.region(fix_marker[i])->setFixValue(fix_value[i]);
+        rm.parameterCount();
+        RSparseMapMatrix C;
+        rm.fillConstraints(C);
+        *n_rows = (int)C.rows();
+        *n_cols = (int)C.cols();
+        *n_entries = (int)C.size();
+        if (cap >= (int)C.size()) {
+            int q = 0;
+            for (auto it = C.begin(); it != C.end(); it++, q++) {
+                rows[q] = (int)it->first.first;
+                cols[q] = (int)it->first.second;
+                vals[q] = it->second;
+            }
+        }
+    });
+}
+
 // DataContainerERT::load (unified data format).
 void *ref_data_load(const char *path, int fromOne, int removeInvalid) {
     DataContainerERT *d = nullptr;

@@ -52,7 +52,9 @@ class TransLog:
 def smoothness_constraints(mesh, n_params=None):
     """First-order smoothness constraint matrix (CSR rows of +1 / -1) over the
     faces shared by two cells whose markers (parameters) differ and are both
-    >= 0.  Rows follow the shared faces sorted by their node ids."""
+    >= 0, for a mesh whose cell markers are the parameters (no region
+    manager; with one, RegionManager.constraintMatrix).  Rows follow the
+    shared faces sorted by their node ids."""
     cells = mesh.cells[:, :mesh.dim() + 1].astype(np.int64)
     mk = mesh.cell_markers.astype(np.int64)
     nv = cells.shape[1]
@@ -139,7 +141,11 @@ class GaussNewton:
         self.line_search = line_search
         self.tD = TransLog
         self.tM = TransLog
-        self.C = smoothness_constraints(fop.mesh(), fop.parameterCount)
+        # with a region manager its constraint matrix over the parameter mesh
+        # (RegionManager::fillConstraints); on a mesh given as the forward mesh
+        # (ignoreRegionManager) first-order rows between its parameter cells
+        rm = fop.regionManager() if hasattr(fop, "regionManager") else None
+        self.C = rm.constraintMatrix() if rm is not None else smoothness_constraints(fop.mesh(), fop.parameterCount)
         import scipy.sparse as sp
         rp, ci, cv, P = self.C
         self._Cs = sp.csr_matrix((cv, ci, rp), shape=(len(rp) - 1, P))

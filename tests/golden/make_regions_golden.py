@@ -11,7 +11,8 @@ outside the parameter box, 2 inside, 3 and 4 two blocks); each case sets
 region flags the way pyGIMLi's MeshModelling does (lowest region background
 unless stated, then background / single / fixed-value regions) and stores
 the reference's renumbered cell markers, parameter count and para-domain
-cell count.
+cell count, and its constraint matrix (RegionManager::fillConstraints) as
+(row, column, value) triplets with its shape.
 """
 from __future__ import annotations
 
@@ -64,12 +65,16 @@ def main():
         rm = R.RefMesh(m)
         for c in CASES:
             fix = {int(k): v for k, v in c.get("fix", {}).items()}
-            mk, npar, ncell = rm.regions(c["default_background"], c.get("background", ()), c.get("single", ()), fix)
+            args = (c["default_background"], c.get("background", ()), c.get("single", ()), fix)
+            mk, npar, ncell = rm.regions(*args)
             key = f"{c['name']}_{dim}d"
             out["para_" + key] = mk
             out["npar_" + key] = npar
             out["ncell_" + key] = ncell
-            print(key, npar, ncell)
+            r, cc, v, nr, nc = rm.constraints(*args)
+            out["cons_" + key] = np.column_stack([r, cc, v])
+            out["cons_shape_" + key] = np.array([nr, nc])
+            print(key, npar, ncell, "constraints", nr, "x", nc)
         # more than 50 regions: every region single, lowest background
         mc = Mesh(dim, m.nodes, m.cells, np.arange(m.cellCount(), dtype=np.int32), m.node_markers, m.boundaries,
                   m.boundary_markers, m.boundary_cells)
@@ -78,7 +83,10 @@ def main():
         out[f"para_many_{dim}d"] = mk
         out[f"npar_many_{dim}d"] = npar
         out[f"ncell_many_{dim}d"] = ncell
-        print(f"many_{dim}d", npar, ncell)
+        r, cc, v, nr, nc = rmc.constraints(True)
+        out[f"cons_many_{dim}d"] = np.column_stack([r, cc, v])
+        out[f"cons_shape_many_{dim}d"] = np.array([nr, nc])
+        print(f"many_{dim}d", npar, ncell, "constraints", nr, "x", nc)
     np.savez_compressed(OUT, cases=json.dumps(CASES), **out)
 
 

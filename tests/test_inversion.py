@@ -133,3 +133,37 @@ def test_gpu_cgls_matches_reference(torch, golden_dir):
     ec = float(np.linalg.norm(xc - z["xconv"]) / np.linalg.norm(z["xconv"]))
     print(f"GPU CGLS vs reference: 5 iterations {e5:.2e}, converged {ec:.2e}")
     assert e5 <= 1e-10 and ec <= 1e-8
+
+
+@pytest.mark.gpu
+def test_gauss_newton_with_region_manager(torch):
+    """setMesh(mesh) through the region manager (four regions, H2 forward
+    mesh): the step takes the region manager's constraint matrix over the
+    parameter mesh (RegionManager::fillConstraints, pinned in
+    tests/test_regions.py), not rows over the refined forward mesh's faces,
+    and lowers the objective."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from make_regions_golden import region_mesh
+    from pygimli_gb300 import ERTModelling
+    from pygimli_gb300.data import createData, geometricFactors
+    from pygimli_gb300.inversion import GaussNewton
+    data = createData(np.arange(9.0), "dd")
+    data.set("k", geometricFactors(data, 2))
+    fop = ERTModelling()
+    fop.setData(data)
+    fop.setMesh(region_mesh(2))
+    P = fop.parameterCount
+    true = np.full(P, 100.0)
+    true[: P // 3] = 30.0
+    obs = fop.response(true) * (1 + 0.01 * np.random.default_rng(5).normal(size=data.size()))
+    gn = GaussNewton(fop, obs, np.full(data.size(), 0.02), lam=20.0)
+    rp, ci, cv, Pc = gn.C
+    ref = fop.regionManager().constraintMatrix()
+    assert Pc == P and np.array_equal(rp, ref[0]) and np.array_equal(ci, ref[1])
+    model = np.full(P, float(np.median(obs)))
+    resp = fop.response(model)
+    phi0 = gn.phi(model, resp)
+    model, resp, info = gn.step(model, resp)
+    assert gn.phi(model, resp) < phi0

@@ -2,7 +2,9 @@
 RegionManager (core/src/regionManager.cpp) on the fixtures of
 tests/golden/make_regions_golden.py: renumbered cell markers (parameter
 indices, -1 background, MARKER_FIXEDVALUE_REGION - region for fixed
-regions), parameter count and para-domain size."""
+regions), parameter count, para-domain size and the constraint matrix
+(RegionManager::fillConstraints: the same rows up to their order and sign,
+the same row and column counts)."""
 from __future__ import annotations
 
 import json
@@ -97,3 +99,41 @@ def test_para_domain_boundaries_and_data():
     # every kept boundary is a face of its cell
     for bnd, c in zip(pd.boundaries, pd.boundary_cells):
         assert set(bnd.tolist()) <= set(pd.cells[c].tolist())
+
+
+def _normalized_rows(rowptr, cols, vals):
+    """Rows as sorted (column, value) tuples, each scaled to +1 at its lowest
+    column: row order and sign leave C^T C unchanged."""
+    out = []
+    for i in range(len(rowptr) - 1):
+        c, v = cols[rowptr[i]:rowptr[i + 1]], vals[rowptr[i]:rowptr[i + 1]]
+        o = np.argsort(c)
+        c, v = c[o], v[o]
+        if len(v):
+            v = v * np.sign(v[0])
+        out.append(tuple(zip(c.tolist(), v.tolist())))
+    return sorted(out)
+
+
+def _reference_rows(key):
+    t = Z["cons_" + key]
+    nr, nc = (int(x) for x in Z["cons_shape_" + key])
+    r = t[:, 0].astype(np.int64)
+    o = np.lexsort((t[:, 1], r))
+    rowptr = np.searchsorted(r[o], np.arange(nr + 1))
+    return _normalized_rows(rowptr, t[o, 1].astype(np.int64), t[o, 2]), nr, nc
+
+
+@pytest.mark.parametrize("dim", (2, 3))
+@pytest.mark.parametrize("c", CASES + [{"name": "many"}], ids=[c["name"] for c in CASES] + ["many"])
+def test_constraints_match_reference(dim, c):
+    m = region_mesh(dim)
+    if c["name"] == "many":  # every cell its own region: all single, inter-region rows
+        m = Mesh(dim, m.nodes, m.cells, np.arange(m.cellCount(), dtype=np.int32), m.node_markers, m.boundaries,
+                 m.boundary_markers, m.boundary_cells)
+        c = {"name": "many", "default_background": True}
+    rm = _rm(m, c)
+    rowptr, cols, vals, P = rm.constraintMatrix()
+    ref, nr, nc = _reference_rows(f"{c['name']}_{dim}d")
+    assert (len(rowptr) - 1, P) == (nr, nc)
+    assert _normalized_rows(rowptr, cols, vals) == ref
