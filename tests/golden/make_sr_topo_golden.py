@@ -40,7 +40,6 @@ sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
 
 from make_cem_golden import _resistivity, _topo_2d, _topo_3d  # noqa: E402
 from oracle.ref_driver import RefModelling  # noqa: E402
-from pygimli_gb300.data import createData, geometricFactors  # noqa: E402
 from pygimli_gb300.mesh import Mesh, create_box_mesh_3d, create_para_mesh_2d  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
