@@ -139,3 +139,24 @@ def test_flip_imag():
     assert np.array_equal(flip_imag(np.array([1 - 2j, 3 + 4j]), True), [1.0, 3.0, 2.0, -4.0])
     with pytest.raises(ValueError):
         flip_imag(np.ones(3), True)
+
+
+def test_geometric_factors_hand_formula():
+    """Half-space geometric factors against the closed form with mirror
+    sources that the reference checks them with (pygimli/testing/
+    test_geometricFactors.py): surface and buried electrodes."""
+    from pygimli_gb300.data import DataContainerERT, geometricFactors
+
+    def hand(p):
+        d1, d2 = np.zeros(4), np.zeros(4)
+        for i, (c, q) in enumerate(((0, 2), (0, 3), (1, 2), (1, 3))):
+            d1[i] = np.sqrt(np.sum((p[c] - p[q]) ** 2))
+            d2[i] = np.sqrt(np.sum((p[c, :2] - p[q, :2]) ** 2) + (-p[c, 2] - p[q, 2]) ** 2)
+        dI = 1.0 / d1 + 1.0 / d2
+        return 4.0 * np.pi / (dI[0] - dI[1] - dI[2] + dI[3])
+
+    rng = np.random.default_rng(1)
+    for z in ((0.0, 0.0, 0.0, 0.0), (-1.0, -2.0, -0.5, -3.0), (0.0, -1.0, 0.0, -2.0)):
+        p = np.column_stack([np.arange(4.0), rng.normal(size=4), np.array(z)])
+        d = DataContainerERT(p, np.array([[0, 1, 2, 3]], np.int32))
+        np.testing.assert_allclose(geometricFactors(d, 3), [hand(p)], rtol=1e-13)
