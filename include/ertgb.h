@@ -265,7 +265,8 @@ int ertgb_get_matrix(ertgb_ctx *ctx, int k_index, int which, double *vals_host);
 /* Sub-potentials of the last response, laid out [k][electrode][node]
  * like the reference's subSolutions_ rows (i + k*nElecs). */
 int ertgb_get_potentials(ertgb_ctx *ctx, double *pot_host);
-/* Electrode potential matrix of the last response, n_elec x n_elec row-major:
+/* Electrode potential matrix of the last real-valued response (ertgb_response,
+ * ertgb_response_host, or the analytic potentials), n_elec x n_elec row-major:
  * U[e][f] = potential at electrode f for the unit current of pattern e,
  * summed over the wavenumbers with their weights (the complete electrode
  * model: its extension row, last wavenumber) -- the reference's DataMap
