@@ -30,6 +30,9 @@ Fixtures (inputs, k/w, resistivity, voltages ``u``, number of patterns):
   ert3d_dipole_closed_sr_small  and a reference node (-999, unused)
   ert2d_dipole_sr_small         2.5-D line with mixed boundaries
   ert2d_dipole_tp_small
+  ert2d_dipole_cem_small        the complete-electrode-model and bypass
+  ert3d_dipole_cem_small        meshes of make_cem_golden.py (total potential,
+  ert2d_dipole_bypass_small     their contact impedances and wavenumbers)
 
 Run from the repository root.
 """
@@ -37,6 +40,7 @@ from __future__ import annotations
 
 import os
 import sys
+import tempfile
 
 import numpy as np
 
@@ -60,11 +64,13 @@ def dipole_patterns(abmn, n_sensors):
     return np.column_stack([idx // (n_sensors + 1) - 1, idx % (n_sensors + 1) - 1])
 
 
-def case(name, mesh, data, seed, sr, numerical=False):
+def case(name, mesh, data, seed, sr, numerical=False, contact_impedance=None, kw=None, rho=None):
     if only and name not in only:
         return
     ones = np.ones(data.size())
-    R = RefModelling(mesh, data.sensorPositions(), data.abmn(), ones, sr=sr)
+    R = RefModelling(mesh, data.sensorPositions(), data.abmn(), ones, sr=sr, contact_impedance=contact_impedance)
+    if kw is not None:
+        R.set_kw(*kw)
     k, w = R.kw()
     prim = np.zeros(0)
     if numerical:
@@ -77,8 +83,14 @@ def case(name, mesh, data, seed, sr, numerical=False):
         R.set_kw(k, w)
         R.set_primary(full)
         prim = full[:len(full) // len(k)]
-    rho = _resistivity(mesh, seed)
-    u, npat = R.calculate_dipole(rho)
+    rho = _resistivity(mesh, seed) if rho is None else rho
+    here = os.getcwd()
+    with tempfile.TemporaryDirectory() as tmp:
+        os.chdir(tmp)  # the reference's CEM path writes a debug matrix file into the working directory
+        try:
+            u, npat = R.calculate_dipole(rho)
+        finally:
+            os.chdir(here)
     pats = dipole_patterns(data.abmn(), data.sensorCount())
     assert len(pats) == npat
     np.savez_compressed(
@@ -86,7 +98,8 @@ def case(name, mesh, data, seed, sr, numerical=False):
         dim=mesh.dim(), nodes=mesh.nodes, cells=mesh.cells, cell_markers=mesh.cell_markers,
         node_markers=mesh.node_markers, boundaries=mesh.boundaries, boundary_markers=mesh.boundary_markers,
         boundary_cells=mesh.boundary_cells, sensors=data.sensorPositions(), abmn=data.abmn(), k=k, w=w,
-        rho=rho, u=u, n_patterns=npat, patterns=pats, primary=prim, sr=int(bool(sr)))
+        rho=rho, u=u, n_patterns=npat, patterns=pats, primary=prim, sr=int(bool(sr)),
+        contact_impedance=np.zeros(0) if contact_impedance is None else contact_impedance)
     R.close()
     print(name, mesh, len(data), "k:", len(k), "patterns:", npat)
 
@@ -125,6 +138,14 @@ def main():
     d2 = createData(xs, "dd")
     case("ert2d_dipole_sr_small", m2, d2, seed=65, sr=True)
     case("ert2d_dipole_tp_small", m2, d2, seed=66, sr=False)
+    for src, name in (("ert2d_cem_small", "ert2d_dipole_cem_small"), ("ert3d_cem_small", "ert3d_dipole_cem_small"),
+                      ("ert2d_bypass_small", "ert2d_dipole_bypass_small")):
+        z = np.load(os.path.join(OUT, src + ".npz"))
+        mz = Mesh(int(z["dim"]), z["nodes"], z["cells"], z["cell_markers"], z["node_markers"], z["boundaries"],
+                  z["boundary_markers"], z["boundary_cells"], check=False)
+        zc = z["contact_impedance"]
+        case(name, mz, DataContainerERT(z["sensors"], z["abmn"]), seed=0, sr=False,
+             contact_impedance=zc if len(zc) else None, kw=(z["k"], z["w"]), rho=z["rho"])
 
 
 if __name__ == "__main__":

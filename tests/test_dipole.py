@@ -12,7 +12,8 @@ right-hand side linear in the source, and a singularity-removal potential
 that does not depend on the source resistivity at the free nodes.
 
 CPU: the oracle (pure poles, dipole=True) against the reference's dipole
-solves, voltages <= 1e-9 of the largest; the closed-domain
+solves, voltages <= 1e-9 of the largest (complete-electrode-model and
+bypass electrodes too; the bypass resistors' conditioning: 1e-8); the closed-domain
 singularity-removal primaries, which the reference takes per (a, b) pattern,
 equal the oracle's pole differences (<= 1e-8).  GPU: ``calculate`` in the
 dipole mode against the same fixtures (<= 1e-6), ``calculate`` of pole
@@ -35,6 +36,7 @@ from pygimli_gb300.mesh import Mesh  # noqa: E402
 
 CASES = ["ert3d_dipole_sr_small", "ert3d_dipole_tp_small", "ert3d_dipole_closed_tp_small",
          "ert3d_dipole_closed_sr_small", "ert2d_dipole_sr_small", "ert2d_dipole_tp_small"]
+CEM_CASES = ["ert2d_dipole_cem_small", "ert3d_dipole_cem_small", "ert2d_dipole_bypass_small"]
 TOL_ORACLE = 1e-9
 TOL_GPU = 1e-6
 
@@ -78,10 +80,22 @@ def test_oracle_matches_reference(golden_dir, name):
     assert rel(u, z["u"]) <= TOL_ORACLE
 
 
+@pytest.mark.parametrize("name", CEM_CASES)
+def test_oracle_cem_matches_reference(golden_dir, name):
+    """The dipole pattern with complete-electrode-model and bypass
+    electrodes (total potential, the reference's calculate with its CEM
+    potentials): the differences of the oracle's pure poles."""
+    z, mesh, data = load(golden_dir, name)
+    zc = z["contact_impedance"]
+    P = CO.TotalPotentialProblem(mesh, data.sensorPositions(), data.abmn(), data["k"], z["k"], z["w"],
+                                 contact_impedance=zc if len(zc) else None, dipole=True)
+    assert rel(P.calculate(z["rho"]), z["u"]) <= (1e-8 if "bypass" in name else TOL_ORACLE)
+
+
 def test_pattern_count_and_order(golden_dir):
     """The reference solved one pattern per distinct (a, b) pair, in the
     order of its pattern index (a + 1)(nSensors + 1) + b + 1."""
-    for name in CASES:
+    for name in CASES + CEM_CASES:
         z, _, data = load(golden_dir, name)
         ab = data.abmn()[:, :2].astype(np.int64)
         assert int(z["n_patterns"]) == len({tuple(p) for p in ab.tolist()})
